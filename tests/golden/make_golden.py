@@ -1,0 +1,274 @@
+"""Generate the golden fixtures in this folder.
+
+Runs only where the reference sources exist (the build host), never on the
+GPU host and never from the test suite.  Two kinds of fixture:
+
+1. ``ref_<case>.npz`` -- the reference's own ``MeasureIABox.measure_xi_w`` /
+   ``measure_xi_multipoles`` run on small seeded catalogues.  The reference
+   is imported from ``/root/reference/src`` with stand-ins for modules that
+   are absent here and unused by the box path (kmeans_radec, astropy,
+   pathos, pyccl), an in-memory replacement for h5py, and ``lpmn`` mapped to
+   ``scipy.special.assoc_legendre_p`` (scipy 1.18 removed ``lpmn``).  Each
+   file stores the inputs (``in/<key>``), the call parameters (``meta``) and
+   every dataset the reference wrote (``out/<hdf5 path>``).  Integer pair
+   counts come from a second reference run with unit weights
+   (``cnt/<path>`` = that run's DD datasets).
+
+2. ``tng300_mock_outputs.npz`` -- every dataset of the reference's golden
+   output files ``tests/data/processed/TNG300/mock_IA_TNG300*.hdf5``, read
+   with the minimal HDF5 reader in ``h5read.py``.
+
+Usage:  python tests/golden/make_golden.py
+"""
+
+from __future__ import annotations
+
+import json
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REF = "/root/reference"
+sys.path.insert(0, os.path.join(HERE, "..", ".."))
+
+
+# --------------------------------------------------------------------------
+# Import shims for the reference
+# --------------------------------------------------------------------------
+
+class _Group(dict):
+    def _walk(self, path, create=False):
+        node = self
+        for part in [p for p in path.split("/") if p]:
+            if part not in node:
+                if not create:
+                    raise KeyError(path)
+                dict.__setitem__(node, part, _Group())
+            node = dict.__getitem__(node, part)
+        return node
+
+    def __getitem__(self, k):
+        return self._walk(k)
+
+    def __delitem__(self, k):
+        parts = [p for p in k.split("/") if p]
+        dict.__delitem__(self._walk("/".join(parts[:-1])), parts[-1])
+
+    def create_group(self, k):
+        return self._walk(k, create=True)
+
+    def create_dataset(self, k, data=None, **kw):
+        parts = [p for p in k.split("/") if p]
+        g = self._walk("/".join(parts[:-1]), create=True)
+        dict.__setitem__(g, parts[-1], np.array(data))
+        return dict.__getitem__(g, parts[-1])
+
+    def keys(self):
+        return dict.keys(self)
+
+    def close(self):
+        pass
+
+
+_FILES: dict = {}
+
+
+class _File(_Group):
+    def __new__(cls, name, mode="r"):
+        if mode == "w" or name not in _FILES:
+            _FILES[name] = _Group()
+            open(name, "a").close()  # the reference deletes its temp file afterwards
+        return _FILES[name]
+
+    def __init__(self, *a, **k):
+        pass
+
+
+def install_shims():
+    sys.modules["kmeans_radec"] = types.SimpleNamespace(kmeans_sample=None)
+    astro = types.ModuleType("astropy")
+    cosmo = types.ModuleType("astropy.cosmology")
+    cosmo.LambdaCDM = lambda **k: None
+    astro.cosmology = cosmo
+    sys.modules["astropy"] = astro
+    sys.modules["astropy.cosmology"] = cosmo
+    pth = types.ModuleType("pathos")
+    pm = types.ModuleType("pathos.multiprocessing")
+    pm.ProcessingPool = None
+    pth.multiprocessing = pm
+    sys.modules["pathos"] = pth
+    sys.modules["pathos.multiprocessing"] = pm
+    sys.modules["pyccl"] = types.ModuleType("pyccl")
+    h5 = types.ModuleType("h5py")
+    h5.File = _File
+    sys.modules["h5py"] = h5
+    import scipy.special as ss
+    if not hasattr(ss, "lpmn"):
+        def lpmn(m, n, z):
+            out = np.zeros((m + 1, n + 1))
+            out[m, n] = float(np.squeeze(ss.assoc_legendre_p(n, m, z)))
+            return out, None
+        ss.lpmn = lpmn
+    sys.path.insert(0, os.path.join(REF, "src"))
+
+
+def walk(g, prefix=""):
+    for k in g.keys():
+        v = dict.__getitem__(g, k)
+        p = f"{prefix}/{k}" if prefix else k
+        if isinstance(v, _Group):
+            yield from walk(v, p)
+        else:
+            yield p, v
+
+
+# --------------------------------------------------------------------------
+# Cases
+# --------------------------------------------------------------------------
+
+def uniform_case(seed, n, L):
+    from measure_ia_gb300.catalogs import uniform_catalog
+    return uniform_catalog(n, L, seed)
+
+
+def clustered_case(seed, n_centres, L, n_shape, mean_children=10, sigma=1.0):
+    from measure_ia_gb300.catalogs import neyman_scott_catalog
+    return neyman_scott_catalog(n_centres, L, n_shape, seed, mean_children=mean_children, sigma=sigma)
+
+
+def edge_case(seed, L):
+    """Uniform points plus pairs placed exactly on r_min, r_max, r-bin edges,
+    Pi-bin edges and jackknife faces, and points at coordinate 0."""
+    from measure_ia_gb300.catalogs import uniform_catalog, inject_edge_pairs
+    d = uniform_catalog(1500, L, seed)
+    return inject_edge_pairs(d, L, seed + 1, r_edges=np.logspace(-1, np.log10(20.0), 11),
+                             pi_edges=np.linspace(-20.0, 20.0, 9), n_sub=3)
+
+
+CASES = {
+    # name: (catalogue builder, MeasureIABox kwargs, calls)
+    "w_jk27_mp": (lambda: uniform_case(11, 2500, 205.0),
+                  dict(simulation=None, snapshot=None, separation_limits=[0.1, 20.0], num_bins_r=10,
+                       num_bins_pi=8, pi_max=20.0, boxsize=205.0, num_nodes=2),
+                  [("w", "All", "both", 27, "tmp")]),
+    "m_jk27_mp": (lambda: uniform_case(12, 2500, 205.0),
+                  dict(simulation=None, snapshot=None, separation_limits=[0.1, 20.0], num_bins_r=10,
+                       num_bins_pi=20, pi_max=20.0, boxsize=205.0, num_nodes=2),
+                  [("m", "All", "both", 27, "tmp")]),
+    "w_clustered_jk27": (lambda: clustered_case(13, 300, 205.0, 1800),
+                         dict(simulation=None, snapshot=None, separation_limits=[0.1, 20.0], num_bins_r=10,
+                              num_bins_pi=8, pi_max=20.0, boxsize=205.0, num_nodes=2),
+                         [("w", "clu", "both", 27, "tmp")]),
+    "m_clustered_jk27": (lambda: clustered_case(14, 300, 205.0, 1800),
+                         dict(simulation=None, snapshot=None, separation_limits=[0.1, 20.0], num_bins_r=10,
+                              num_bins_pi=20, pi_max=20.0, boxsize=205.0, num_nodes=2),
+                         [("m", "clu", "both", 27, "tmp")]),
+    "w_tng_default_jk8": (lambda: uniform_case(15, 2000, 205.0),
+                          dict(simulation="TNG300", snapshot=99, separation_limits=[0.1, 20.0], num_bins_r=10,
+                               num_bins_pi=8, pi_max=None, num_nodes=1),
+                          [("w", "All", "both", 8, "tmp"), ("m", "All", "both", 8, "tmp")]),
+    "w_nojk_tree": (lambda: uniform_case(16, 2500, 150.0),
+                    dict(simulation=None, snapshot=3, separation_limits=[0.2, 15.0], num_bins_r=7,
+                         num_bins_pi=6, pi_max=15.0, boxsize=150.0, num_nodes=1),
+                    [("w", "nojk", "both", 0, "tmp"), ("m", "nojk", "g+", 0, "tmp")]),
+    "w_brute_jk8": (lambda: uniform_case(17, 1200, 100.0),
+                    dict(simulation=None, snapshot=None, separation_limits=[0.1, 20.0], num_bins_r=10,
+                         num_bins_pi=8, pi_max=20.0, boxsize=100.0, num_nodes=1),
+                    [("w", "br", "both", 8, False), ("m", "br", "gg", 8, False)]),
+    "edges_jk27": (lambda: edge_case(18, 205.0),
+                   dict(simulation=None, snapshot=None, separation_limits=[0.1, 20.0], num_bins_r=10,
+                        num_bins_pi=8, pi_max=20.0, boxsize=205.0, num_nodes=2),
+                   [("w", "edge", "both", 27, "tmp"), ("m", "edge", "both", 27, "tmp")]),
+    "los0_ellipticity": (lambda: clustered_case(19, 250, 120.0, 1500),
+                         dict(simulation=None, snapshot=None, separation_limits=[0.1, 20.0], num_bins_r=10,
+                              num_bins_pi=8, pi_max=20.0, boxsize=120.0, num_nodes=2),
+                         [("w", "l0", "both", 8, "tmp", dict(ellipticity="ellipticity", los=0)),
+                          ("m", "l0", "both", 8, "tmp", dict(ellipticity="ellipticity", los=0))]),
+    "masks_jk8": (lambda: clustered_case(20, 250, 205.0, 2000),
+                  dict(simulation=None, snapshot=None, separation_limits=[0.1, 20.0], num_bins_r=10,
+                       num_bins_pi=8, pi_max=20.0, boxsize=205.0, num_nodes=2),
+                  [("w", "msk", "both", 8, "tmp", dict(mask="quirk")),
+                   ("w", "mskw", "both", 8, "tmp", dict(mask="full"))]),
+}
+
+
+def _masks(data, kind):
+    rng = np.random.default_rng(99)
+    sel_p = rng.uniform(size=len(data["Position"])) < 0.6
+    sel_s = rng.uniform(size=len(data["Position_shape_sample"])) < 0.6
+    masks = {"Position": sel_p, "Position_shape_sample": sel_s, "Axis_Direction": sel_s, "q": sel_s}
+    if kind == "full":
+        masks["weight"] = sel_p
+        masks["weight_shape_sample"] = sel_s
+    return masks
+
+
+def run_case(name, builder, kw, calls):
+    from measureia import MeasureIABox
+    base = builder()
+    arrays = {}
+    meta = {"kwargs": kw, "calls": []}
+    for key in ("Position", "Position_shape_sample", "Axis_Direction", "q", "weight", "weight_shape_sample"):
+        if key in base:
+            arrays[f"in/{key}"] = np.asarray(base[key])
+    outfile = f"/tmp/golden_{name}.hdf5"
+    cntfile = f"/tmp/golden_{name}_cnt.hdf5"
+    _FILES.pop(outfile, None)
+    _FILES.pop(cntfile, None)
+    for call in calls:
+        kind, dname, corr, num_jk, tmp = call[:5]
+        extra = call[5] if len(call) > 5 else {}
+        los = extra.get("los", 2)
+        ell = extra.get("ellipticity", "distortion")
+        mkind = extra.get("mask")
+        meta["calls"].append(dict(kind=kind, dataset=dname, corr_type=corr, num_jk=num_jk,
+                                  temp=(tmp if tmp is False else "path"), los=los, ellipticity=ell, mask=mkind))
+        for weighted, fname in ((True, outfile), (False, cntfile)):
+            data = {k: np.array(v) for k, v in base.items()}
+            data["LOS"] = los
+            if not weighted:
+                data["weight"] = np.ones(len(data["Position"]))
+                data["weight_shape_sample"] = np.ones(len(data["Position_shape_sample"]))
+            masks = _masks(data, mkind) if mkind else None
+            box = MeasureIABox(data, fname, **kw)
+            tpath = "/tmp" if tmp == "tmp" else False
+            if kind == "w":
+                box.measure_xi_w(dname, corr, num_jk, temp_file_path=tpath, masks=masks, ellipticity=ell)
+            else:
+                box.measure_xi_multipoles(dname, corr, num_jk, temp_file_path=tpath, masks=masks, ellipticity=ell)
+    for p, v in walk(_FILES[outfile]):
+        arrays[f"out/{p}"] = np.asarray(v)
+    for p, v in walk(_FILES[cntfile]):
+        if p.endswith("_DD"):
+            arrays[f"cnt/{p}"] = np.rint(np.asarray(v)).astype(np.int64)
+    arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, f"ref_{name}.npz"), **arrays)
+    print(name, "datasets:", sum(1 for k in arrays if k.startswith("out/")))
+
+
+def extract_reference_golden_files():
+    from h5read import read_all
+    out = {}
+    for tag, fn in (("small", "mock_IA_TNG300.hdf5"), ("large", "mock_IA_TNG300_large.hdf5")):
+        for path, arr in read_all(os.path.join(REF, "tests/data/processed/TNG300", fn)).items():
+            out[f"{tag}/{path}"] = arr
+    np.savez_compressed(os.path.join(HERE, "tng300_mock_outputs.npz"), **out)
+    print("golden hdf5 datasets:", len(out))
+
+
+if __name__ == "__main__":
+    sys.path.insert(0, HERE)
+    install_shims()
+    import io, contextlib
+    only = sys.argv[1:]
+    if not only or "hdf5" in only:
+        extract_reference_golden_files()
+    for name, (builder, kw, calls) in CASES.items():
+        if only and name not in only:
+            continue
+        with contextlib.redirect_stdout(io.StringIO()):
+            run_case(name, builder, kw, calls)
+        print("done", name)
