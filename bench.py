@@ -1,0 +1,292 @@
+"""Benchmark: binned pairs/s of the w_gg + w_g+ measurement with 27 jackknife
+regions on the clustered 4M-galaxy catalogue, mixed form vs plain FP64 form.
+
+Workload (seeded synthetic, no dataset download): Neyman-Scott catalogue in a
+205 Mpc/h periodic box, 80,000 parents x Poisson(50) children with sigma = 1
+Mpc/h Gaussian offsets (~4.0M positions), shape sample a random 1M subset,
+axis towards the parent in the projected plane + von Mises(kappa=2) noise,
+q ~ Beta(4,2), lognormal weights (sigma 0.3), plus 2,000 injected pairs on
+bin edges.  Binning: 10 log r_p bins 0.1-20 Mpc/h, 8 linear Pi bins over
+|Pi| <= 20 Mpc/h, LOS = z, 27 jackknife sub-boxes.
+
+A step is one full measurement (cell-list build, pair counts with
+jackknife parts, FP64 edge re-test, analytic RR, realisations, w, covariance)
+on catalogues resident in HBM.  Binned pair: one (shape, position) pair that
+lands in an (r_p, Pi) bin, counted once.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "binned pairs/s, wg+&wgg 4M gal 27JK: mixed vs FP64 GPU form at <=1e-6 rel err"
+L_BOX = 205.0
+R_BINS = np.logspace(-1, np.log10(20.0), 11)
+PI_BINS = np.linspace(-20.0, 20.0, 9)
+LANE_OPS_PER_PAIR = 32          # FP32 lane-ops per binned (r_p, Pi) pair (fixed recipe)
+
+
+def make_catalog(seed=2026, n_centres=80000, n_shape=1_000_000, n_edge=2000):
+    from measure_ia_gb300.catalogs import neyman_scott_catalog, add_edge_pairs
+    d = neyman_scott_catalog(n_centres, L_BOX, n_shape, seed, mean_children=50, sigma=1.0, kappa=2.0)
+    return add_edge_pairs(d, L_BOX, seed + 1, R_BINS, PI_BINS, n_edge)
+
+
+def world():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+
+class ClockSampler:
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# CPU reference (the oracle's restatement of the reference's tree + Pool path)
+# ---------------------------------------------------------------------------
+
+def cpu_reference(data, n_sample_shapes, processes):
+    """Binned pairs/s of the reference algorithm (KD-tree pre-selection at
+    r_min and r_max, per-pair numpy binning with jackknife scatter, a process
+    pool over shape chunks of 1000) on the first ``n_sample_shapes`` shapes
+    against all positions."""
+    from oracle import ia_oracle as O
+    b = O.Binning(boxsize=L_BOX, r_min=0.1, r_max=20.0, num_bins_r=10, num_bins_pi=8, pi_max=20.0)
+    pos, spos = data["Position"], data["Position_shape_sample"]
+    axis = data["Axis_Direction"] / np.sqrt((data["Axis_Direction"] ** 2).sum(1))[:, None]
+    e = O.ellipticity_size(data["q"])
+    ws = data["weight_shape_sample"]
+    t0 = time.perf_counter()
+    R = O.responsivity(ws, e)
+    lab_p = O.jackknife_labels(pos, b.L_0p5, 3)
+    lab_s = O.jackknife_labels(spos, b.L_0p5, 3)
+    c = O.count_pairs_parallel("w", b, 2, pos, data["weight"], spos, axis, e, ws, R, lab_p, lab_s, 27,
+                               (0, n_sample_shapes), processes=processes, chunk=max(1, n_sample_shapes // (4 * processes)))
+    dt = time.perf_counter() - t0
+    return int(c.npairs.sum()), dt
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+
+def run_gpu(args, data, rank, ws, local):
+    import torch
+    from measure_ia_gb300.engine import PairCounter
+    from measure_ia_gb300 import MeasureIABox
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    keys = ("Position", "weight", "Position_shape_sample", "Axis_Direction", "q", "weight_shape_sample")
+    dcat = {k: torch.from_numpy(np.ascontiguousarray(data[k], dtype=np.float64)).to(dev) for k in keys}
+    n_pos, n_shape = dcat["Position"].shape[0], dcat["Position_shape_sample"].shape[0]
+    stream = torch.cuda.current_stream(dev)
+
+    def time_form(precision, steps, warmup):
+        pc = PairCounter("w", boxsize=L_BOX, r_bins=R_BINS, r_min=0.1, r_max=20.0, p_bins=PI_BINS, l_subboxes=3,
+                         precision=precision, device=local)
+        bufs = pc.allocate(n_pos, n_shape)
+        for _ in range(warmup):
+            pc.run(dcat, bufs, stream)
+        torch.cuda.synchronize()
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for _ in range(steps):
+            pc.run(dcat, bufs, stream)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1) / steps
+        m = pc.fetch(bufs)
+        return pc, bufs, m, ms
+
+    # plain FP64 form first (reference for the accuracy figures), then the mixed headline
+    fp_steps = max(1, min(args.steps, 2))
+    pc64, _, m64, ms64 = time_form("fp64", fp_steps, 1)
+    with ClockSampler(local) as clk:
+        pcm, bufm, mm, msm = time_form("mixed", args.steps, args.warmup)
+    clocks = clk.summary()
+
+    binned = mm.stats["binned_pairs"]
+    assert binned == m64.stats["binned_pairs"], "mixed and FP64 forms binned different pairs"
+    counts_exact = bool(np.array_equal(mm.npairs, m64.npairs))
+    err = {}
+    for k, name in (("proj_gp", "w_g+"), ("proj_gg", "w_gg"), ("cov_gp", "cov w_g+"), ("cov_gg", "cov w_gg")):
+        a, b = m64[k], mm[k]
+        err[name] = {"max_rel_per_bin": float(np.max(np.abs(b - a) / np.maximum(np.abs(a), 1e-300))),
+                     "max_rel_to_vector_scale": float(np.max(np.abs(b - a)) / np.max(np.abs(a)))}
+    err["w_g+ in jackknife sigma"] = float(np.max(np.abs(mm["proj_gp"] - m64["proj_gp"]) / m64["std_gp"]))
+
+    # end to end through the public API with host buffers
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    host = {k: data[k] for k in keys}
+    host["LOS"] = 2
+    h2d = sum(np.asarray(data[k]).nbytes for k in keys)
+    for _ in range(e2e_steps):
+        box = MeasureIABox(dict(host), None, None, None, [0.1, 20.0], 10, 8, 20.0, boxsize=L_BOX, num_nodes=2,
+                           precision="mixed", device=local)
+        box.measure_xi_w("bench", "both", 27, temp_file_path="/tmp")
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    d2h = pcm.layout.total * 8 + (1 + 27) * 80 * 8
+    return dict(binned=binned, ms=msm, ms64=ms64, clocks=clocks, counts_exact=counts_exact, err=err,
+                e2e_s=e2e_s, h2d=h2d, d2h=d2h, stats=mm.stats, stats64=m64.stats)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=500, help="shapes in the CPU-baseline sample")
+    args = ap.parse_args()
+    rank, ws, local = world()
+    data = make_catalog()
+    n_pos, n_shape = len(data["Position"]), len(data["Position_shape_sample"])
+    config = {"workload": "clustered 4M positions / 1M shapes, w_gg+w_g+, 27 jackknife regions (config 2)",
+              "n_positions": n_pos, "n_shapes": n_shape, "boxsize": L_BOX, "r_p_bins": "10 log 0.1-20",
+              "pi_bins": "8 linear |Pi|<=20", "membership": "kd-tree (r_min < r_p <= r_max)",
+              "l2": "inputs larger than L2 (sorted working set > 129 MB)"}
+    cores = os.cpu_count() or 1
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        results = []
+        for _ in range(args.warmup):
+            cpu_reference(data, max(100, args.cpu_sample // 4), cores)
+        for _ in range(args.steps):
+            results.append(cpu_reference(data, args.cpu_sample, cores))
+        pairs = sum(r[0] for r in results)
+        secs = sum(r[1] for r in results)
+        v = pairs / secs
+        line = {"metric": METRIC, "value": v, "unit": "binned pairs/s", "n_gpus": 0, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
+                "config": config,
+                "cpu_baseline": {"value": v, "unit": "binned pairs/s", "cores": cores, "kind": "port",
+                                 "sample": f"first {args.cpu_sample} shapes x all {n_pos} positions per step"},
+                "e2e": {"value": v, "unit": "binned pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    # CPU baseline first, before any CUDA context exists (the pool forks)
+    cpu = None
+    if rank == 0:
+        pairs, secs = cpu_reference(data, args.cpu_sample, cores)
+        cpu = {"value": pairs / secs, "unit": "binned pairs/s", "cores": cores, "kind": "port",
+               "sample": f"first {args.cpu_sample} shapes x all {n_pos} positions, {secs:.1f} s"}
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    r = run_gpu(args, data, rank, ws, local)
+    t_step = r["ms"] / 1e3
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([t_step], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_step = float(t.item())
+    value = r["binned"] * ws / t_step
+    import torch
+    props = torch.cuda.get_device_properties(local)
+    peak = props.multi_processor_count * 128 * 2070e6 / 1e12
+    achieved = LANE_OPS_PER_PAIR * r["binned"] / t_step / 1e12
+    if rank != 0:
+        return
+    launches_per_step = 18  # prep 15 (prep 2, scans 9, scatter 2, work units 2), pairs 1, edge re-test 1, post 1
+    line = {
+        "metric": METRIC, "value": value, "unit": "binned pairs/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 pair arithmetic, f64 edge re-test and reductions", "data": "synthetic",
+        "config": config,
+        "fp64_form": {"value": r["binned"] / (r["ms64"] / 1e3), "ms_per_step": r["ms64"]},
+        "mixed_over_fp64": r["ms64"] / r["ms"],
+        "accuracy_mixed_vs_fp64": r["err"], "counts_bit_exact_mixed_vs_fp64": r["counts_exact"],
+        "binned_pairs_per_step": r["binned"], "edge_pairs_retested": r["stats"]["edge_pairs"],
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "note": "32 FP32 lane-ops per binned pair over the whole step; peak = SMs x 128 x 2070 MHz"},
+        "cpu_baseline": cpu,
+        "e2e": {"value": r["binned"] / r["e2e_s"], "unit": "binned pairs/s", "h2d_bytes_per_step": r["h2d"],
+                "d2h_bytes_per_step": r["d2h"]},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": r["clocks"],
+    }
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,168 @@
+/*
+ * measure_ia_gb300 -- C ABI of the GB300 (sm_103a) periodic-box pair counter.
+ *
+ * One call, mia_measure(), does what MeasureIA's box backends do for one
+ * dataset: neighbour search, per-pair binning of DD, S+D and SxD (with the
+ * jackknife parts), analytic RR, jackknife realisations, Pi integration or
+ * Legendre multipoles, and the jackknife mean/std/covariance.  Inputs and
+ * outputs are device pointers; scratch memory is a caller-provided device
+ * buffer of mia_workspace_size() bytes.  The library allocates no memory.
+ *
+ * Reference interfaces replaced (MarloesvL/measure_IA, src/measureia/):
+ *   mia_measure, kind MIA_KIND_W
+ *     MeasureWBoxJackknife._measure_xi_rp_pi_box_jk_multiprocessing
+ *       (measure_w_box_jk.py:648-857), ..._jk_tree (:293-541),
+ *       ..._jk_brute (:69-291);
+ *     MeasureWBox._measure_xi_rp_pi_box_multiprocessing
+ *       (measure_w_box.py:493-656), ..._tree (:233-410), ..._brute (:65-231);
+ *     then MeasureIABase._measure_w_g_i (measure_IA_base.py:515-575) and
+ *       ._combine_jackknife_information (measure_IA_base.py:454-513).
+ *   mia_measure, kind MIA_KIND_MULTIPOLES
+ *     MeasureMBoxJackknife._measure_xi_r_mur_box_jk_multiprocessing
+ *       (measure_m_box_jk.py:684-898), ..._jk_tree (:306-568),
+ *       ..._jk_brute (:72-304);
+ *     MeasureMultipolesBox._measure_xi_r_mur_box_multiprocessing
+ *       (measure_m_box.py:719-890), ..._tree (:433-627), ..._brute (:255-431);
+ *     then MeasureIABase._measure_multipoles (measure_IA_base.py:577-668)
+ *       and ._combine_jackknife_information.
+ *   mia_workspace_size / mia_output_layout: sizing helpers with no
+ *     reference counterpart (the reference allocates numpy arrays inside
+ *     each backend, e.g. measure_w_box_jk.py:749-759).
+ *
+ * Every function returns MIA_OK (0) or a nonzero MIA_ERR_* code; the
+ * message of the last failure on a context is in mia_last_error().
+ * A context is not re-entrant: use one context per host thread / stream.
+ */
+#ifndef MEASURE_IA_GB300_H
+#define MEASURE_IA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define MIA_API __attribute__((visibility("default")))
+#else
+#define MIA_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MIA_OK 0
+#define MIA_ERR_ARG 1        /* invalid argument (maps to ValueError)            */
+#define MIA_ERR_CUDA 2       /* CUDA runtime error                               */
+#define MIA_ERR_RANGE 3      /* coordinate outside [0, L) or not finite          */
+#define MIA_ERR_OVERFLOW 4   /* edge re-test queue overflow in the mixed form    */
+#define MIA_ERR_WORKSPACE 5  /* workspace missing, misaligned or too small       */
+
+enum { MIA_KIND_W = 0, MIA_KIND_MULTIPOLES = 1 };
+/* neighbour membership: TREE = the KD-tree backends (r_min < d <= r_max),
+   BRUTE = temp_file_path=False (every pair inside the bin range). */
+enum { MIA_TREE = 0, MIA_BRUTE = 1 };
+enum { MIA_FP64 = 0, MIA_MIXED = 1 };
+enum { MIA_DISTORTION = 0, MIA_ELLIPTICITY = 1 };
+
+#define MIA_MAX_BINS_R 64
+#define MIA_MAX_BINS_P 128
+#define MIA_MAX_BREAKS 96
+
+/* A catalogue as MeasureIABox.data holds it after masking: device pointers
+   to float64 arrays in C order (measure_IA_base.py:81-95). */
+typedef struct {
+  const double* position;        /* (n_pos, 3)   'Position'                      */
+  const double* weight;          /* (n_pos)      'weight'                        */
+  const double* position_shape;  /* (n_shape, 3) 'Position_shape_sample'         */
+  const double* axis_direction;  /* (n_shape, 2) 'Axis_Direction' (normalised here) */
+  const double* q;               /* (n_shape)    'q'                             */
+  const double* weight_shape;    /* (n_shape)    'weight_shape_sample'           */
+  int64_t n_pos;
+  int64_t n_shape;
+} mia_catalog;
+
+/* Measurement settings.  Host pointers.  The breakpoint tables encode the
+   reference's exact bin assignment (see measure_ia_gb300/binning.py): for
+   q = d^2 (r_p^2 for w, r^2 for multipoles) the bin is
+   q_bin[#{k : q >= q_break[k]}] (-1 = not binned); likewise p_bin for the
+   line-of-sight separation Pi (w) or mu_r = Pi / r (multipoles). */
+typedef struct {
+  int kind;            /* MIA_KIND_*                                       */
+  int membership;      /* MIA_TREE | MIA_BRUTE                             */
+  int precision;       /* MIA_FP64 | MIA_MIXED                             */
+  int los;             /* line-of-sight axis 0, 1 or 2 ('LOS')             */
+  int l_subboxes;      /* jackknife sub-boxes per side; 0 = no jackknife   */
+  int ellipticity;     /* MIA_DISTORTION | MIA_ELLIPTICITY                 */
+  int want_variance;   /* accumulate the sum of squared S+D terms          */
+  int n_r;             /* num_bins_r                                       */
+  int n_p;             /* num_bins_pi (Pi bins or mu_r bins)               */
+  int n_qbreak;
+  int n_pbreak;
+  int shapes_per_unit; /* 0 = automatic                                    */
+  double boxsize;      /* L                                                */
+  double volume;       /* L**3 as the reference forms it                   */
+  double r_min, r_max; /* separation_limits                                */
+  double rp_cut;       /* multipoles: pairs need r_p > rp_cut              */
+  double cell_size;    /* target cell side; 0 = automatic                  */
+  const double* r_edges;   /* n_r + 1 : r_bins                             */
+  const double* p_edges;   /* n_p + 1 : pi_bins or mu_r_bins               */
+  const double* q_break;   /* n_qbreak ascending                           */
+  const int* q_bin;        /* n_qbreak + 1                                 */
+  const double* p_break;   /* n_pbreak ascending                           */
+  const int* p_bin;        /* n_pbreak + 1                                 */
+} mia_config;
+
+/* Offsets (in doubles) of every product inside the output buffer.
+   nb = n_r * n_p; J = number of jackknife regions (0 without jackknife).
+   Histograms hold raw sums (no 1/(2R) factor): [0] = all pairs,
+   [1 + i] = pairs with the shape or the position in region i. */
+typedef struct {
+  int64_t total;
+  int64_t dd;          /* (1+J) * nb                                         */
+  int64_t splus;       /* (1+J) * nb   sum w_p w_s e_+                        */
+  int64_t scross;      /* nb           sum w_p w_s e_x                        */
+  int64_t variance;    /* nb           sum (w_p w_s e_+ / 2R)^2               */
+  int64_t npos_jk;     /* J   positions outside region i                    */
+  int64_t nshape_jk;   /* J   shapes outside region i                       */
+  int64_t R;           /* 1   responsivity                                  */
+  int64_t R_jk;        /* J                                                 */
+  int64_t rr;          /* nb  analytic RR                                    */
+  int64_t rr_jk;       /* J * nb                                            */
+  int64_t xi_gp, xi_gx, xi_gg, splusd, scrossd, sigmasq; /* nb each         */
+  int64_t xi_gp_jk, splusd_jk, xi_gg_jk, dd_jk;          /* J * nb each     */
+  int64_t proj_gp, proj_gg;          /* n_r : w or multipole, full sample    */
+  int64_t proj_gp_jk, proj_gg_jk;    /* J * n_r                              */
+  int64_t mean_gp, std_gp, cov_gp;   /* n_r, n_r, n_r * n_r                  */
+  int64_t mean_gg, std_gg, cov_gg;
+  int64_t stats;       /* 8: n_pos, n_shape, binned pairs, edge pairs
+                          re-tested, work units, cells, pair launches, 0    */
+} mia_layout;
+
+typedef struct {
+  double* out;                  /* layout.total doubles (device)           */
+  unsigned long long* npairs;   /* (1+J) * nb integer pair counts (device) */
+} mia_result;
+
+/* Context on one device (the device must be current on the calling thread). */
+typedef struct mia_context mia_context;
+
+MIA_API int mia_create(int device, mia_context** ctx);
+MIA_API int mia_destroy(mia_context* ctx);
+MIA_API const char* mia_last_error(const mia_context* ctx);
+MIA_API int mia_version(void);
+
+/* Bytes of device scratch mia_measure needs for this configuration. */
+MIA_API int mia_workspace_size(const mia_config* cfg, int64_t n_pos, int64_t n_shape, size_t* bytes);
+
+/* Output offsets for this configuration. */
+MIA_API int mia_output_layout(const mia_config* cfg, mia_layout* layout);
+
+/* The whole measurement, enqueued on `stream` (a cudaStream_t, 0 = legacy
+   default stream).  Returns after the results are complete on the device;
+   the catalogue, workspace and result buffers must stay valid until then. */
+MIA_API int mia_measure(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat, void* workspace,
+                size_t workspace_bytes, const mia_result* res, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

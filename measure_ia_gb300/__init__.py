@@ -1,0 +1,12 @@
+"""GB300-native periodic-box pair counting for intrinsic-alignment measurements.
+
+Drop-in for MeasureIA's ``MeasureIABox`` (w_gg, w_g+, multipoles, jackknife
+covariance); the pair counts run in hand-written sm_103a CUDA kernels behind
+the C ABI of ``include/measure_ia_gb300.h``.
+"""
+
+from .measure_ia import MeasureIABox
+from .output import open_output, read_npz_mirror
+from .sim_info import SimInfo
+
+__all__ = ["MeasureIABox", "SimInfo", "open_output", "read_npz_mirror"]

@@ -104,3 +104,36 @@ def inject_edge_pairs(data, L, seed, r_edges, pi_edges, n_sub=3, n_each=6):
     n = len(pos)
     return {"Position": pos, "Position_shape_sample": pos.copy(), "Axis_Direction": np.c_[np.cos(ang), np.sin(ang)],
             "LOS": data.get("LOS", 2), "q": q, "weight": np.ones(n), "weight_shape_sample": np.ones(n)}
+
+
+def add_edge_pairs(data, L, seed, r_edges, pi_edges, n_pairs):
+    """Append ``n_pairs`` (shape, position) pairs whose projected separation
+    equals an r-bin edge, or whose line-of-sight separation equals a Pi-bin
+    edge, up to the rounding of the FP64 subtraction.  The new shapes go to
+    the shape sample, the new positions to the position sample (LOS = z)."""
+    rng = np.random.default_rng(seed)
+    edges = [("r", float(x)) for x in r_edges] + [("p", float(x)) for x in pi_edges]
+    s_new, p_new = [], []
+    for k in range(n_pairs):
+        kind, edge = edges[k % len(edges)]
+        s = rng.uniform(25.0, L - 25.0, 3)
+        if kind == "r":
+            th = rng.uniform(0.0, 2 * np.pi)
+            off = np.array([edge * np.cos(th), edge * np.sin(th), rng.uniform(-15.0, 15.0)])
+        else:
+            rp = rng.uniform(0.2, 15.0)
+            th = rng.uniform(0.0, 2 * np.pi)
+            off = np.array([rp * np.cos(th), rp * np.sin(th), edge])
+        s_new.append(s)
+        p_new.append(s - off)
+    s_new = _wrap(np.array(s_new), L)
+    p_new = _wrap(np.array(p_new), L)
+    ang = rng.uniform(0.0, np.pi, n_pairs)
+    out = dict(data)
+    out["Position"] = np.concatenate([data["Position"], p_new])
+    out["weight"] = np.concatenate([data["weight"], np.ones(n_pairs)])
+    out["Position_shape_sample"] = np.concatenate([data["Position_shape_sample"], s_new])
+    out["Axis_Direction"] = np.concatenate([data["Axis_Direction"], np.c_[np.cos(ang), np.sin(ang)]])
+    out["q"] = np.concatenate([data["q"], rng.beta(4.0, 2.0, n_pairs)])
+    out["weight_shape_sample"] = np.concatenate([data["weight_shape_sample"], np.ones(n_pairs)])
+    return out

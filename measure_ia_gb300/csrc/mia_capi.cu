@@ -1,0 +1,482 @@
+// C ABI: context, sizing helpers and the mia_measure driver that enqueues the
+// preparation, pair and post-processing stages.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+
+#include "mia_internal.cuh"
+
+struct mia_context {
+  int device;
+  int num_sms;
+  std::string err;
+};
+
+namespace mia {
+
+namespace {
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+}  // namespace
+
+bool make_plan(const mia_config* cfg, long long n_pos, long long n_shape, Plan* pl, const char** why) {
+  Plan& p = *pl;
+  memset(&p, 0, sizeof(p));
+  if (!cfg) { *why = "null config"; return false; }
+  if (cfg->kind != MIA_KIND_W && cfg->kind != MIA_KIND_MULTIPOLES) { *why = "kind"; return false; }
+  if (cfg->los < 0 || cfg->los > 2) { *why = "LOS must be 0, 1 or 2"; return false; }
+  if (cfg->n_r < 1 || cfg->n_r > MIA_MAX_BINS_R) { *why = "num_bins_r out of range"; return false; }
+  if (cfg->n_p < 1 || cfg->n_p > MIA_MAX_BINS_P) { *why = "num_bins_pi out of range"; return false; }
+  if (cfg->n_qbreak < 0 || cfg->n_qbreak > MIA_MAX_BREAKS || cfg->n_pbreak < 0 || cfg->n_pbreak > MIA_MAX_BREAKS) {
+    *why = "too many breakpoints";
+    return false;
+  }
+  if (!(cfg->boxsize > 0.0)) { *why = "boxsize must be positive"; return false; }
+  if (cfg->l_subboxes < 0 || cfg->l_subboxes > 10) { *why = "jackknife sub-boxes per side must be 0..10"; return false; }
+  if (n_pos < 0 || n_shape < 0 || n_pos > 0x7fffffffLL || n_shape > 0x7fffffffLL) { *why = "sample size"; return false; }
+  if (!cfg->r_edges || !cfg->p_edges || !cfg->q_bin || !cfg->p_bin) { *why = "missing tables"; return false; }
+  const double L = cfg->boxsize;
+  p.axis[0] = cfg->los == 0 ? 1 : 0;
+  p.axis[1] = cfg->los == 2 ? 1 : 2;
+  p.axis[2] = cfg->los;
+  p.n_sub = cfg->l_subboxes > 0 ? cfg->l_subboxes : 1;
+  p.J = cfg->l_subboxes > 0 ? cfg->l_subboxes * cfg->l_subboxes * cfg->l_subboxes : 0;
+  p.nb = cfg->n_r * cfg->n_p;
+  double rr = fmax(cfg->r_max, cfg->r_edges[cfg->n_r]);
+  p.range_proj = rr;
+  if (cfg->kind == MIA_KIND_W) p.range_los = fmax(fabs(cfg->p_edges[0]), fabs(cfg->p_edges[cfg->n_p]));
+  else p.range_los = rr;
+  double target[3];
+  double cs = cfg->cell_size > 0.0 ? cfg->cell_size : 0.0;
+  target[0] = target[1] = cs > 0.0 ? cs : p.range_proj / 2.0;
+  target[2] = cs > 0.0 ? cs : fmax(p.range_los / 2.0, 1e-300);
+  long long cells = 1;
+  for (int k = 0; k < 3; ++k) {
+    long long n = (long long)floor(L / target[k]);
+    if (n > 1024) n = 1024;
+    n = (n / p.n_sub) * p.n_sub;
+    if (n < p.n_sub) n = p.n_sub;
+    p.n[k] = (int)n;
+    cells *= n;
+  }
+  while (cells > (1LL << 25)) {  // keep the cell tables modest
+    cells = 1;
+    for (int k = 0; k < 3; ++k) {
+      long long n = p.n[k] / 2;
+      n = (n / p.n_sub) * p.n_sub;
+      if (n < p.n_sub) n = p.n_sub;
+      p.n[k] = (int)n;
+      cells *= n;
+    }
+  }
+  p.n_cells = cells;
+  for (int k = 0; k < 3; ++k) {
+    p.s[k] = L / p.n[k];
+    double range = k == 2 ? p.range_los : p.range_proj;
+    long long R = (long long)ceil(range / p.s[k] * (1.0 + 1e-9));
+    if (R < 1) R = 1;
+    if (2 * R + 1 >= p.n[k]) {
+      p.full[k] = 1;
+      R = p.n[k] / 2;
+    }
+    p.R[k] = (int)R;
+  }
+  p.shapes_per_unit = cfg->shapes_per_unit > 0 ? cfg->shapes_per_unit : 128;
+  if (p.shapes_per_unit > 512) p.shapes_per_unit = 512;
+  p.n_wu_max = p.n_cells + n_shape + 1;
+  p.edge_capacity = 0;
+  if (cfg->precision == MIA_MIXED) {
+    long long cap = n_shape * 64;
+    if (cap < (1LL << 20)) cap = 1LL << 20;
+    if (cap > (1LL << 24)) cap = 1LL << 24;
+    p.edge_capacity = cap;
+  }
+  const bool mixed = cfg->precision == MIA_MIXED;
+  size_t o = 0;
+  auto take = [&](size_t& off, size_t bytes) {
+    off = o;
+    o = align256(o + bytes);
+  };
+  const size_t C = (size_t)p.n_cells;
+  const size_t NP = (size_t)(n_pos > 0 ? n_pos : 1), NS = (size_t)(n_shape > 0 ? n_shape : 1);
+  take(p.off_status, sizeof(Status));
+  take(p.off_tables, sizeof(Tables));
+  take(p.off_pcount, 4 * C);
+  take(p.off_pstart, 4 * (C + 1));
+  take(p.off_pcur, 4 * C);
+  take(p.off_scount, 4 * C);
+  take(p.off_sstart, 4 * (C + 1));
+  take(p.off_scur_lo, 4 * C);
+  take(p.off_scur_hi, 4 * C);
+  take(p.off_wucount, 4 * C);
+  take(p.off_wustart, 4 * (C + 1));
+  take(p.off_tiles, 4 * (C / kScanTile + 2));
+  take(p.off_pcell, 4 * NP);
+  take(p.off_plab, 4 * NP);
+  take(p.off_scell, 4 * NS);
+  take(p.off_slab, 4 * NS);
+  take(p.off_p64, 8 * 4 * NP);
+  take(p.off_plab_s, 4 * NP);
+  take(p.off_p32, mixed ? 4 * 7 * NP : 0);
+  take(p.off_s64, 8 * 7 * NS);
+  take(p.off_slab_s, 4 * NS);
+  take(p.off_s32, mixed ? 4 * 10 * NS : 0);
+  take(p.off_wu, sizeof(WorkUnit) * (size_t)p.n_wu_max);
+  take(p.off_reg, (size_t)(p.J + 1) * 32 + 64);
+  take(p.off_edges, sizeof(int2) * (size_t)p.edge_capacity);
+  p.total = o;
+  return true;
+}
+
+void bind_work(const Plan& p, void* base, Work* w) {
+  unsigned char* b = static_cast<unsigned char*>(base);
+  const size_t NP = 0;  // unused
+  (void)NP;
+  w->status = reinterpret_cast<Status*>(b + p.off_status);
+  w->tables = reinterpret_cast<Tables*>(b + p.off_tables);
+  w->pcount = reinterpret_cast<int*>(b + p.off_pcount);
+  w->pstart = reinterpret_cast<int*>(b + p.off_pstart);
+  w->pcur = reinterpret_cast<int*>(b + p.off_pcur);
+  w->scount = reinterpret_cast<int*>(b + p.off_scount);
+  w->sstart = reinterpret_cast<int*>(b + p.off_sstart);
+  w->scur_lo = reinterpret_cast<int*>(b + p.off_scur_lo);
+  w->scur_hi = reinterpret_cast<int*>(b + p.off_scur_hi);
+  w->wucount = reinterpret_cast<int*>(b + p.off_wucount);
+  w->wustart = reinterpret_cast<int*>(b + p.off_wustart);
+  w->tiles = reinterpret_cast<int*>(b + p.off_tiles);
+  w->pcell = reinterpret_cast<int*>(b + p.off_pcell);
+  w->plab = reinterpret_cast<int*>(b + p.off_plab);
+  w->scell = reinterpret_cast<int*>(b + p.off_scell);
+  w->slab = reinterpret_cast<int*>(b + p.off_slab);
+  const size_t np_ = (p.off_plab_s - p.off_p64) / 32;  // capacity of the FP64 position block
+  (void)np_;
+  w->plab_s = reinterpret_cast<int*>(b + p.off_plab_s);
+  w->slab_s = reinterpret_cast<int*>(b + p.off_slab_s);
+  w->wu = reinterpret_cast<WorkUnit*>(b + p.off_wu);
+  w->edges = reinterpret_cast<int2*>(b + p.off_edges);
+  unsigned char* reg = b + p.off_reg;
+  const size_t J1 = (size_t)p.J + 1;
+  w->reg.npos = reinterpret_cast<unsigned long long*>(reg);
+  w->reg.nshape = reinterpret_cast<unsigned long long*>(reg + 8 * J1);
+  w->reg.s1 = reinterpret_cast<double*>(reg + 16 * J1);
+  w->reg.s2 = reinterpret_cast<double*>(reg + 24 * J1);
+}
+
+// Bind the per-galaxy arrays once the sample sizes are known.
+static void bind_arrays(const Plan& p, void* base, long long n_pos, long long n_shape, Work* w) {
+  unsigned char* b = static_cast<unsigned char*>(base);
+  const size_t NP = (size_t)(n_pos > 0 ? n_pos : 1), NS = (size_t)(n_shape > 0 ? n_shape : 1);
+  double* p64 = reinterpret_cast<double*>(b + p.off_p64);
+  w->px = p64;
+  w->py = p64 + NP;
+  w->pz = p64 + 2 * NP;
+  w->pw = p64 + 3 * NP;
+  float* p32 = reinterpret_cast<float*>(b + p.off_p32);
+  w->pxh = p32;
+  w->pxl = p32 + NP;
+  w->pyh = p32 + 2 * NP;
+  w->pyl = p32 + 3 * NP;
+  w->pzh = p32 + 4 * NP;
+  w->pzl = p32 + 5 * NP;
+  w->pwf = p32 + 6 * NP;
+  double* s64 = reinterpret_cast<double*>(b + p.off_s64);
+  w->sx = s64;
+  w->sy = s64 + NS;
+  w->sz = s64 + 2 * NS;
+  w->sax = s64 + 3 * NS;
+  w->say = s64 + 4 * NS;
+  w->se = s64 + 5 * NS;
+  w->sws = s64 + 6 * NS;
+  float* s32 = reinterpret_cast<float*>(b + p.off_s32);
+  w->sxh = s32;
+  w->sxl = s32 + NS;
+  w->syh = s32 + 2 * NS;
+  w->syl = s32 + 3 * NS;
+  w->szh = s32 + 4 * NS;
+  w->szl = s32 + 5 * NS;
+  w->saxf = s32 + 6 * NS;
+  w->sayf = s32 + 7 * NS;
+  w->swef = s32 + 8 * NS;
+  w->swsf = s32 + 9 * NS;
+}
+
+static float f32_down(double v) {
+  float f = (float)v;
+  if ((double)f > v) f = nextafterf(f, -INFINITY);
+  return f;
+}
+static float f32_up(double v) {
+  float f = (float)v;
+  if ((double)f < v) f = nextafterf(f, INFINITY);
+  return f;
+}
+
+// Host-side construction of the device tables from the configuration.
+static void build_tables(const mia_config* cfg, Tables* T, int* lut_base) {
+  memset(T, 0, sizeof(Tables));
+  const double g = 1.0 / 524288.0;  // 2^-19 relative guard band on q
+  for (int j = 0; j < MIA_MAX_BREAKS; ++j) {
+    if (j < cfg->n_qbreak) {
+      double B = cfg->q_break[j];
+      T->q_break[j] = B;
+      memcpy(&T->q_key[j], &B, 8);
+      T->q_lo32[j] = f32_down(B * (1.0 - g));
+      T->q_hi32[j] = f32_up(B * (1.0 + g));
+    } else {
+      T->q_key[j] = 0x7fffffffffffffffLL;
+      T->q_lo32[j] = INFINITY;
+      T->q_hi32[j] = INFINITY;
+    }
+    if (j < cfg->n_pbreak) {
+      T->p_break[j] = cfg->p_break[j];
+      T->p_key[j] = order_key(cfg->p_break[j]);
+    } else {
+      T->p_key[j] = 0x7fffffffffffffffLL;
+    }
+  }
+  for (int j = 0; j <= MIA_MAX_BREAKS; ++j) {
+    T->q_bin[j] = j <= cfg->n_qbreak ? cfg->q_bin[j] : -1;
+    T->p_bin[j] = j <= cfg->n_pbreak ? cfg->p_bin[j] : -1;
+  }
+  for (int i = 0; i <= cfg->n_r; ++i) T->r_edges[i] = cfg->r_edges[i];
+  for (int i = 0; i <= cfg->n_p; ++i) T->p_edges[i] = cfg->p_edges[i];
+  // logarithmic lookup over the float bit pattern of q: bucket = bits >> 17
+  int base = 0;
+  if (cfg->n_qbreak > 0) {
+    unsigned bits;
+    float lo = T->q_lo32[0] > 0.0f ? T->q_lo32[0] : 1e-30f;
+    memcpy(&bits, &lo, 4);
+    base = (int)(bits >> (23 - kLutMantBits)) - (1 << kLutMantBits);
+    if (base < 0) base = 0;
+  }
+  *lut_base = base;
+  const int n = cfg->n_qbreak;
+  for (int b = 0; b < kLut; ++b) {
+    unsigned lo_bits = (unsigned)(b + base) << (23 - kLutMantBits);
+    unsigned hi_bits = (unsigned)(b + base + 1) << (23 - kLutMantBits);
+    float lo, hi;
+    memcpy(&lo, &lo_bits, 4);
+    memcpy(&hi, &hi_bits, 4);
+    if (!(lo < INFINITY)) {  // beyond the float range: walk
+      T->lut32[b] = 0x8000;
+      continue;
+    }
+    int iv = 0;
+    while (iv < n && T->q_hi32[iv] <= lo) ++iv;
+    bool clean = iv == n || T->q_lo32[iv] >= hi;
+    T->lut32[b] = (unsigned short)(iv | (clean ? 0 : 0x8000));
+  }
+}
+
+}  // namespace mia
+
+using namespace mia;
+
+extern "C" {
+
+int mia_version(void) { return 1; }
+
+int mia_create(int device, mia_context** out) {
+  if (!out) return MIA_ERR_ARG;
+  *out = nullptr;
+  mia_context* c = new mia_context();
+  c->device = device;
+  c->num_sms = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (e != cudaSuccess) {
+    delete c;
+    return MIA_ERR_CUDA;
+  }
+  *out = c;
+  return MIA_OK;
+}
+
+int mia_destroy(mia_context* ctx) {
+  delete ctx;
+  return MIA_OK;
+}
+
+const char* mia_last_error(const mia_context* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int mia_workspace_size(const mia_config* cfg, int64_t n_pos, int64_t n_shape, size_t* bytes) {
+  if (!bytes) return MIA_ERR_ARG;
+  Plan p;
+  const char* why = nullptr;
+  if (!make_plan(cfg, n_pos, n_shape, &p, &why)) return MIA_ERR_ARG;
+  *bytes = p.total;
+  return MIA_OK;
+}
+
+int mia_output_layout(const mia_config* cfg, mia_layout* lay) {
+  if (!cfg || !lay) return MIA_ERR_ARG;
+  if (cfg->n_r < 1 || cfg->n_r > MIA_MAX_BINS_R || cfg->n_p < 1 || cfg->n_p > MIA_MAX_BINS_P || cfg->l_subboxes < 0)
+    return MIA_ERR_ARG;
+  const int64_t nb = (int64_t)cfg->n_r * cfg->n_p, nr = cfg->n_r;
+  const int64_t J = cfg->l_subboxes > 0 ? (int64_t)cfg->l_subboxes * cfg->l_subboxes * cfg->l_subboxes : 0;
+  int64_t o = 0;
+  auto take = [&](int64_t& f, int64_t n) {
+    f = o;
+    o += n;
+  };
+  take(lay->dd, (1 + J) * nb);
+  take(lay->splus, (1 + J) * nb);
+  take(lay->scross, nb);
+  take(lay->variance, nb);
+  take(lay->npos_jk, J);
+  take(lay->nshape_jk, J);
+  take(lay->R, 1);
+  take(lay->R_jk, J);
+  take(lay->rr, nb);
+  take(lay->rr_jk, J * nb);
+  take(lay->xi_gp, nb);
+  take(lay->xi_gx, nb);
+  take(lay->xi_gg, nb);
+  take(lay->splusd, nb);
+  take(lay->scrossd, nb);
+  take(lay->sigmasq, nb);
+  take(lay->xi_gp_jk, J * nb);
+  take(lay->splusd_jk, J * nb);
+  take(lay->xi_gg_jk, J * nb);
+  take(lay->dd_jk, J * nb);
+  take(lay->proj_gp, nr);
+  take(lay->proj_gg, nr);
+  take(lay->proj_gp_jk, J * nr);
+  take(lay->proj_gg_jk, J * nr);
+  take(lay->mean_gp, nr);
+  take(lay->std_gp, nr);
+  take(lay->cov_gp, nr * nr);
+  take(lay->mean_gg, nr);
+  take(lay->std_gg, nr);
+  take(lay->cov_gg, nr * nr);
+  take(lay->stats, 8);
+  lay->total = o;
+  return MIA_OK;
+}
+
+static int fail(mia_context* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+#define MIA_CUDA(call)                                                                             \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) return fail(ctx, MIA_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+int mia_measure(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat, void* workspace,
+                size_t workspace_bytes, const mia_result* res, void* stream) {
+  if (!ctx) return MIA_ERR_ARG;
+  if (!cfg || !cat || !res || !res->out || !res->npairs) return fail(ctx, MIA_ERR_ARG, "null argument");
+  if (cat->n_pos > 0 && (!cat->position || !cat->weight)) return fail(ctx, MIA_ERR_ARG, "missing position arrays");
+  if (cat->n_shape > 0 && (!cat->position_shape || !cat->axis_direction || !cat->q || !cat->weight_shape))
+    return fail(ctx, MIA_ERR_ARG, "missing shape arrays");
+  if (cat->n_pos < 1 || cat->n_shape < 1) return fail(ctx, MIA_ERR_ARG, "empty position or shape sample");
+  Plan plan;
+  const char* why = "";
+  if (!make_plan(cfg, cat->n_pos, cat->n_shape, &plan, &why)) return fail(ctx, MIA_ERR_ARG, why);
+  if (!workspace || workspace_bytes < plan.total || ((uintptr_t)workspace & 255))
+    return fail(ctx, MIA_ERR_WORKSPACE, "workspace missing, not 256-byte aligned, or smaller than mia_workspace_size()");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  MIA_CUDA(cudaSetDevice(ctx->device));
+  mia_layout lay;
+  mia_output_layout(cfg, &lay);
+  Work w;
+  bind_work(plan, workspace, &w);
+  bind_arrays(plan, workspace, cat->n_pos, cat->n_shape, &w);
+
+  // tables
+  static thread_local Tables host_tables;
+  int lut_base = 0;
+  build_tables(cfg, &host_tables, &lut_base);
+  MIA_CUDA(cudaMemcpyAsync(w.tables, &host_tables, sizeof(Tables), cudaMemcpyHostToDevice, st));
+
+  // zero the counters and the outputs
+  unsigned char* b = static_cast<unsigned char*>(workspace);
+  MIA_CUDA(cudaMemsetAsync(b + plan.off_status, 0, sizeof(Status), st));
+  {
+    Status init;
+    memset(&init, 0, sizeof(init));
+    init.bad_index = ~0ULL;
+    static thread_local Status staged;
+    staged = init;
+    MIA_CUDA(cudaMemcpyAsync(w.status, &staged, sizeof(Status), cudaMemcpyHostToDevice, st));
+  }
+  MIA_CUDA(cudaMemsetAsync(b + plan.off_pcount, 0, plan.off_tiles - plan.off_pcount, st));
+  MIA_CUDA(cudaMemsetAsync(b + plan.off_reg, 0, (size_t)(plan.J + 1) * 32 + 64, st));
+  const size_t nb = (size_t)plan.nb, J1 = (size_t)plan.J + 1;
+  MIA_CUDA(cudaMemsetAsync(res->out, 0, sizeof(double) * (size_t)lay.total, st));
+  MIA_CUDA(cudaMemsetAsync(res->npairs, 0, sizeof(unsigned long long) * J1 * nb, st));
+
+  Params P;
+  memset(&P, 0, sizeof(P));
+  P.kind = cfg->kind;
+  P.membership = cfg->membership;
+  P.precision = cfg->precision;
+  P.los = cfg->los;
+  P.ellipticity = cfg->ellipticity;
+  P.want_variance = cfg->want_variance ? 1 : 0;
+  P.n_r = cfg->n_r;
+  P.n_p = cfg->n_p;
+  P.nb = plan.nb;
+  P.J = plan.J;
+  P.n_sub = plan.n_sub;
+  P.n_qbreak = cfg->n_qbreak;
+  P.n_pbreak = cfg->n_pbreak;
+  P.L = cfg->boxsize;
+  P.halfL = cfg->boxsize / 2.0;
+  P.Lf_hi = (float)cfg->boxsize;
+  P.Lf_lo = (float)(cfg->boxsize - (double)P.Lf_hi);
+  P.halfLf = (float)(cfg->boxsize / 2.0);
+  P.rp_cut = cfg->rp_cut;
+  P.rp_cut2 = cfg->rp_cut * cfg->rp_cut;
+  for (int k = 0; k < 3; ++k) {
+    P.axis[k] = plan.axis[k];
+    P.n[k] = plan.n[k];
+    P.R[k] = plan.R[k];
+    P.full[k] = plan.full[k];
+    P.s[k] = plan.s[k];
+    P.inv_s[k] = (double)plan.n[k] / cfg->boxsize;
+  }
+  P.range_proj = plan.range_proj;
+  P.range_los = plan.range_los;
+  P.n_cells = plan.n_cells;
+  P.shapes_per_unit = plan.shapes_per_unit;
+  P.lut32_base = lut_base;
+  const double p0 = cfg->p_edges[0], p1 = cfg->p_edges[cfg->n_p];
+  P.p_lo32 = (float)p0;
+  P.p_inv32 = (float)((double)cfg->n_p / (p1 - p0));
+  P.p_guard = (float)fmax(1.0 / 32768.0, cfg->n_p * 4e-6);
+  P.c_guard = 1e-12f;
+  P.wrap_guard = (float)(cfg->boxsize * 1e-5);
+  P.edge_capacity = plan.edge_capacity;
+
+  Out o;
+  o.dd = res->out + lay.dd;
+  o.splus = res->out + lay.splus;
+  o.scross = res->out + lay.scross;
+  o.variance = res->out + lay.variance;
+  o.npairs = res->npairs;
+
+  MIA_CUDA(launch_prep(plan, P, *cat, w, st));
+  MIA_CUDA(launch_pairs(plan, P, w, o, st, ctx->num_sms));
+  MIA_CUDA(launch_post(P, w, lay, res->out, cfg->volume, cat->n_pos, cat->n_shape, st));
+
+  static thread_local Status hs;
+  MIA_CUDA(cudaMemcpyAsync(&hs, w.status, sizeof(Status), cudaMemcpyDeviceToHost, st));
+  MIA_CUDA(cudaStreamSynchronize(st));
+  if (hs.flags & kStatusRange) {
+    char buf[160];
+    snprintf(buf, sizeof(buf), "coordinate outside [0, boxsize) or not finite (first offending index %llu)",
+             (unsigned long long)hs.bad_index);
+    return fail(ctx, MIA_ERR_RANGE, buf);
+  }
+  if (hs.flags & kStatusOverflow)
+    return fail(ctx, MIA_ERR_OVERFLOW, "edge re-test queue overflow; rerun in the FP64 form");
+  ctx->err.clear();
+  return MIA_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,268 @@
+// Internal definitions shared by the measure_ia_gb300 CUDA translation units.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/measure_ia_gb300.h"
+
+namespace mia {
+
+// --------------------------------------------------------------------------
+// Sizes
+// --------------------------------------------------------------------------
+constexpr int kThreads = 256;            // pair-kernel block size
+constexpr int kLutBits = 12;             // 4096-bucket logarithmic lookup tables
+constexpr int kLut = 1 << kLutBits;
+constexpr int kLutMantBits = 6;          // 64 buckets per octave of q
+constexpr int kMaxSlots = 12;            // jackknife regions a work unit can touch in shared memory
+constexpr int kMaxRows = 1024;           // neighbour rows per pass of a work unit
+constexpr int kMaxSegs = 2 * kMaxRows;   // a row wraps into at most 2 contiguous segments
+constexpr int kScanTile = 2048;
+
+// status word bits
+constexpr unsigned kStatusRange = 1u;      // input coordinate outside [0, L) or NaN
+constexpr unsigned kStatusOverflow = 2u;   // edge queue overflow
+constexpr unsigned kStatusNoSlot = 4u;     // (informational) global-atomic fallback used
+
+// --------------------------------------------------------------------------
+// Device-visible status block (first bytes of the workspace)
+// --------------------------------------------------------------------------
+struct Status {
+  unsigned flags;
+  unsigned pad;
+  unsigned long long edge_count;       // pairs queued for the FP64 re-test
+  unsigned long long wu_next;          // persistent-kernel work counter
+  unsigned long long n_wu;             // number of work units
+  unsigned long long binned;           // binned pairs (all regions, once each)
+  unsigned long long bad_index;        // first offending input index (range check)
+  unsigned long long maxw_bits;        // max |w_p| (bit pattern; non-negative doubles order as integers)
+  unsigned long long maxws_bits;       // max(|w_s|, |w_s e|)
+};
+
+// Exact bin tables, built on the host from the reference's formulas.
+struct Tables {
+  // q = d^2 breakpoints (FP64) and their keys; bins of the intervals between them
+  double q_break[MIA_MAX_BREAKS];
+  long long q_key[MIA_MAX_BREAKS];     // bit pattern of q_break (q >= 0, so integer order = value order)
+  int q_bin[MIA_MAX_BREAKS + 1];
+  // FP32 guard band around each q breakpoint: q < q_lo32 -> surely below, q >= q_hi32 -> surely above
+  float q_lo32[MIA_MAX_BREAKS];
+  float q_hi32[MIA_MAX_BREAKS];
+  // Pi or mu breakpoints, keys in signed-order form
+  double p_break[MIA_MAX_BREAKS];
+  long long p_key[MIA_MAX_BREAKS];
+  int p_bin[MIA_MAX_BREAKS + 1];
+  // lookup tables: bucket -> interval index | 0x8000 (bucket holds a breakpoint)
+  unsigned short lut32[kLut];
+  // bin edges (r_bins; pi_bins or mu_r_bins)
+  double r_edges[MIA_MAX_BINS_R + 1];
+  double p_edges[MIA_MAX_BINS_P + 1];
+};
+
+// --------------------------------------------------------------------------
+// Plan: geometry of the cell grid and the workspace carve-up
+// --------------------------------------------------------------------------
+struct Plan {
+  // geometry, in cell-dimension order d0, d1 (projected plane), d2 (line of sight)
+  int axis[3];          // original axis of d0, d1, d2
+  int n[3];             // cells per dimension
+  double s[3];          // cell side
+  int R[3];             // neighbour reach in cells
+  int full[3];          // every cell of the dimension is visited (reach covers the box)
+  int n_sub;            // jackknife sub-boxes per side (1 when no jackknife)
+  int J;                // number of jackknife regions (0 when none)
+  long long n_cells;
+  double range_proj;    // largest binned projected separation (or 3-D for multipoles)
+  double range_los;     // largest binned |Pi| (w) or r (multipoles)
+  int shapes_per_unit;
+  long long n_wu_max;
+  long long edge_capacity;
+  int nb;
+  // workspace offsets in bytes
+  size_t off_status, off_tables;
+  size_t off_pcount, off_pstart, off_pcur, off_scount, off_sstart, off_scur_lo, off_scur_hi;
+  size_t off_wucount, off_wustart, off_tiles;
+  size_t off_pcell, off_plab, off_scell, off_slab;
+  size_t off_p64, off_plab_s, off_p32;
+  size_t off_s64, off_slab_s, off_s32;
+  size_t off_wu;
+  size_t off_reg;
+  size_t off_edges;
+  size_t total;
+};
+
+// Work unit: a run of shapes of one cell with one jackknife label.
+struct WorkUnit {
+  int cell;
+  int begin;   // first shape (sorted order)
+  int count;
+  int label;   // jackknife region of every shape in the unit
+};
+
+// Region accumulators (per jackknife region, plus the totals at index J).
+struct RegionStats {
+  unsigned long long* npos;     // J + 1
+  unsigned long long* nshape;   // J + 1
+  double* s1;                   // J + 1 : sum w_s (1 - e^2/2)
+  double* s2;                   // J + 1 : sum w_s
+};
+
+// Kernel parameters passed by value.
+struct Params {
+  int kind, membership, precision, los, ellipticity, want_variance;
+  int n_r, n_p, nb, J, n_sub;
+  int n_qbreak, n_pbreak;
+  double L, halfL;
+  float Lf_hi, Lf_lo, halfLf;
+  double rp_cut2;               // rp_cut^2 (multipoles), exact decision uses rp > rp_cut via q_p
+  double rp_cut;
+  // cell grid
+  int axis[3], n[3], R[3], full[3];
+  double s[3], inv_s[3];
+  double range_proj, range_los;
+  long long n_cells;
+  int shapes_per_unit;
+  // mixed-form guards and tables
+  int lut32_base;               // bucket of the first lut32 entry
+  float p_lo32, p_inv32;        // Pi/mu: t = (v - p_lo) * p_inv, bin = floor(t)
+  float p_guard;                // fraction of a bin treated as ambiguous at each edge
+  float c_guard;                // sin^2(phi) below which the exact FP64 cos(phi) decides
+  float wrap_guard;
+  long long edge_capacity;
+};
+
+// Workspace pointers, derived from a Plan and a base address.
+struct Work {
+  Status* status;
+  Tables* tables;
+  int *pcount, *pstart, *pcur, *scount, *sstart, *scur_lo, *scur_hi;
+  int *wucount, *wustart, *tiles;
+  int *pcell, *plab, *scell, *slab;
+  // sorted positions: FP64 coordinates in cell-dimension order and weights
+  double *px, *py, *pz, *pw;
+  int* plab_s;
+  // mixed form: FP32 hi/lo coordinates and weight
+  float *pxh, *pxl, *pyh, *pyl, *pzh, *pzl, *pwf;
+  // sorted shapes
+  double *sx, *sy, *sz, *sax, *say, *se, *sws;
+  int* slab_s;
+  float *sxh, *sxl, *syh, *syl, *szh, *szl, *saxf, *sayf, *swef, *swsf;
+  WorkUnit* wu;
+  RegionStats reg;
+  int2* edges;
+};
+
+// Output pointers (into the caller's result buffers).
+struct Out {
+  double* dd;        // (1+J) * nb
+  double* splus;     // (1+J) * nb
+  double* scross;    // nb
+  double* variance;  // nb
+  unsigned long long* npairs;   // (1+J) * nb
+};
+
+// --------------------------------------------------------------------------
+// Exact FP64 pair arithmetic: the reference's per-pair sequence of IEEE
+// operations (measure_w_box_jk.py:584-617, measure_m_box_jk.py:611-653),
+// written with explicit round-to-nearest intrinsics so that no operation is
+// fused into an FMA.
+// --------------------------------------------------------------------------
+
+// Signed doubles mapped to integers in value order.
+__host__ __device__ inline long long order_key(double v) {
+#ifdef __CUDA_ARCH__
+  long long b = __double_as_longlong(v);
+#else
+  long long b;
+  memcpy(&b, &v, 8);
+#endif
+  return b >= 0 ? b : (long long)(0x8000000000000000ULL - (unsigned long long)b) - 1;
+}
+
+__device__ __forceinline__ double wrap_exact(double d, double L, double halfL) {
+  // sep[sep > L/2] -= L ; sep[sep < -L/2] += L   (measure_w_box_jk.py:585-587)
+  if (d > halfL) d = __dsub_rn(d, L);
+  if (d < -halfL) d = __dadd_rn(d, L);
+  return d;
+}
+
+// Number of breakpoints <= key (binary search over an ascending key table).
+__device__ __forceinline__ int count_le(const long long* keys, int n, long long key) {
+  int lo = 0, hi = n;  // answer in [lo, hi]
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (keys[mid] <= key) lo = mid + 1; else hi = mid;
+  }
+  return lo;
+}
+
+struct PairResult {
+  int bin;      // -1 if not binned
+  double ep;    // e cos 2phi (0 under the reference's NaN rule)
+  double ex;    // e sin 2phi
+};
+
+// Shape s, position p: coordinates in cell-dimension order (d0, d1 projected,
+// d2 line of sight).  `perm_r2` selects the original-axis order of the 3-D sum.
+__device__ __forceinline__ PairResult pair_exact(const Params& P, const Tables& T, double sx, double sy,
+                                                 double sz, double ax, double ay, double e, double qx, double qy,
+                                                 double qz) {
+  PairResult res;
+  res.bin = -1;
+  res.ep = 0.0;
+  res.ex = 0.0;
+  double dx = wrap_exact(__dsub_rn(sx, qx), P.L, P.halfL);
+  double dy = wrap_exact(__dsub_rn(sy, qy), P.L, P.halfL);
+  double dz = wrap_exact(__dsub_rn(sz, qz), P.L, P.halfL);
+  double xx = __dmul_rn(dx, dx), yy = __dmul_rn(dy, dy), zz = __dmul_rn(dz, dz);
+  double qp = __dadd_rn(xx, yy);  // r_p^2 = sum over not-LOS axes in axis order
+  double q;
+  if (P.kind == MIA_KIND_W) {
+    q = qp;
+  } else {
+    // r^2 = (s_x^2 + s_y^2) + s_z^2 in ORIGINAL axis order; (d0, d1, d2) is
+    // (x, y, z) for LOS 2, (y, z, x) for LOS 0 and (x, z, y) for LOS 1
+    if (P.los == 2) q = __dadd_rn(__dadd_rn(xx, yy), zz);
+    else if (P.los == 0) q = __dadd_rn(__dadd_rn(zz, xx), yy);
+    else q = __dadd_rn(__dadd_rn(xx, zz), yy);
+  }
+  int ib = T.q_bin[count_le(T.q_key, P.n_qbreak, __double_as_longlong(q))];
+  if (ib < 0) return res;
+  int jb;
+  double rp = __dsqrt_rn(qp);
+  if (P.kind == MIA_KIND_W) {
+    jb = T.p_bin[count_le(T.p_key, P.n_pbreak, order_key(dz))];
+  } else {
+    if (!(rp > P.rp_cut)) return res;
+    double r = __dsqrt_rn(q);
+    double mu = __ddiv_rn(dz, r);
+    jb = T.p_bin[count_le(T.p_key, P.n_pbreak, order_key(mu))];
+  }
+  if (jb < 0) return res;
+  res.bin = ib * P.n_p + jb;
+  // phi = arccos(sdir . a) with sdir = proj / r_p (measure_w_box_jk.py:590-596)
+  double c = __dadd_rn(__dmul_rn(__ddiv_rn(dx, rp), ax), __dmul_rn(__ddiv_rn(dy, rp), ay));
+  if (c >= -1.0 && c <= 1.0) {  // arccos of |c| > 1 (or NaN) is NaN -> e_+ = e_x = 0
+    double c2 = __dmul_rn(c, c);
+    double cos2 = __dsub_rn(__dadd_rn(c2, c2), 1.0);
+    double s = __dsqrt_rn(__dmul_rn(__dsub_rn(1.0, c), __dadd_rn(1.0, c)));
+    double sin2 = __dmul_rn(__dadd_rn(c, c), s);
+    res.ep = __dmul_rn(e, cos2);
+    res.ex = __dmul_rn(e, sin2);
+  }
+  return res;
+}
+
+// Workspace carve-up (host); returns false on a bad configuration.
+bool make_plan(const mia_config* cfg, long long n_pos, long long n_shape, Plan* plan, const char** why);
+void bind_work(const Plan& plan, void* base, Work* w);
+
+// Stage launchers (mia_prep.cu, mia_pairs.cu, mia_post.cu)
+cudaError_t launch_prep(const Plan& plan, const Params& P, const mia_catalog& cat, const Work& w, cudaStream_t st);
+cudaError_t launch_pairs(const Plan& plan, const Params& P, const Work& w, const Out& o, cudaStream_t st,
+                         int num_sms);
+cudaError_t launch_post(const Params& P, const Work& w, const mia_layout& lay, double* out, double volume,
+                        long long n_pos, long long n_shape, cudaStream_t st);
+
+}  // namespace mia

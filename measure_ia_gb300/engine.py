@@ -1,0 +1,211 @@
+"""Host driver of the CUDA pair counter.
+
+``PairCounter`` holds one measurement configuration (binning, jackknife,
+precision) and runs ``mia_measure`` on device-resident catalogues.  PyTorch
+supplies the device buffers and the stream; all arithmetic happens in the
+CUDA library.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+from . import binning as B
+
+_CONTEXTS: dict[int, C.c_void_p] = {}
+
+
+def context(device: int) -> C.c_void_p:
+    lib = L.load()
+    if device not in _CONTEXTS:
+        h = C.c_void_p()
+        rc = lib.mia_create(device, C.byref(h))
+        if rc != L.MIA_OK:
+            raise L.MiaError(rc, "mia_create failed")
+        _CONTEXTS[device] = h
+    return _CONTEXTS[device]
+
+
+def _dptr(ptr):
+    return C.cast(ptr, C.POINTER(C.c_double))
+
+
+@dataclass
+class Measurement:
+    """Products of one measurement, as host arrays (layout of the reference's outputs)."""
+    kind: str
+    n_r: int
+    n_p: int
+    J: int
+    arrays: dict
+    npairs: np.ndarray          # (1+J, n_r, n_p) int64: [0] all pairs, [1+i] region i
+    stats: dict
+
+    def __getitem__(self, k):
+        return self.arrays[k]
+
+
+class PairCounter:
+    """One configuration of the box pair count (w or multipoles)."""
+
+    def __init__(self, kind, *, boxsize, r_bins, r_min, r_max, p_bins, los=2, l_subboxes=0, precision="fp64",
+                 membership="tree", ellipticity="distortion", want_variance=False, volume=None, rp_cut=0.0,
+                 cell_size=0.0, shapes_per_unit=0, device=0):
+        if kind not in ("w", "m"):
+            raise ValueError(kind)
+        self.kind = kind
+        self.device = device
+        self.n_r = len(r_bins) - 1
+        self.n_p = len(p_bins) - 1
+        if self.n_r > L.MAX_BINS_R or self.n_p > L.MAX_BINS_P:
+            raise ValueError(f"at most {L.MAX_BINS_R} r bins and {L.MAX_BINS_P} pi/mu bins are supported")
+        self.J = l_subboxes ** 3 if l_subboxes > 0 else 0
+        self._r_edges = np.ascontiguousarray(r_bins, dtype=np.float64)
+        self._p_edges = np.ascontiguousarray(p_bins, dtype=np.float64)
+        qt = B.r_table(kind, self._r_edges, r_min, r_max, self.n_r, membership, rp_cut)
+        pt = B.pi_table(self._p_edges, self.n_p) if kind == "w" else B.mu_table(self._p_edges, self.n_p)
+        self.q_table, self.p_table = qt, pt
+        self._qb = np.ascontiguousarray(qt.breaks, dtype=np.float64)
+        self._qn = np.ascontiguousarray(qt.bins, dtype=np.int32)
+        self._pb = np.ascontiguousarray(pt.breaks, dtype=np.float64)
+        self._pn = np.ascontiguousarray(pt.bins, dtype=np.int32)
+        cfg = L.Config()
+        cfg.kind = L.MIA_KIND_W if kind == "w" else L.MIA_KIND_MULTIPOLES
+        cfg.membership = L.MIA_TREE if membership == "tree" else L.MIA_BRUTE
+        cfg.precision = L.MIA_MIXED if precision == "mixed" else L.MIA_FP64
+        cfg.los = int(los)
+        cfg.l_subboxes = int(l_subboxes)
+        cfg.ellipticity = L.MIA_DISTORTION if ellipticity == "distortion" else L.MIA_ELLIPTICITY
+        cfg.want_variance = int(bool(want_variance))
+        cfg.n_r, cfg.n_p = self.n_r, self.n_p
+        cfg.n_qbreak, cfg.n_pbreak = len(self._qb), len(self._pb)
+        cfg.shapes_per_unit = int(shapes_per_unit)
+        cfg.boxsize = float(boxsize)
+        cfg.volume = float(boxsize ** 3 if volume is None else volume)
+        cfg.r_min, cfg.r_max = float(r_min), float(r_max)
+        cfg.rp_cut = float(rp_cut)
+        cfg.cell_size = float(cell_size)
+        cfg.r_edges = self._r_edges.ctypes.data_as(C.POINTER(C.c_double))
+        cfg.p_edges = self._p_edges.ctypes.data_as(C.POINTER(C.c_double))
+        cfg.q_break = self._qb.ctypes.data_as(C.POINTER(C.c_double))
+        cfg.q_bin = self._qn.ctypes.data_as(C.POINTER(C.c_int))
+        cfg.p_break = self._pb.ctypes.data_as(C.POINTER(C.c_double))
+        cfg.p_bin = self._pn.ctypes.data_as(C.POINTER(C.c_int))
+        self.cfg = cfg
+        self.precision = precision
+        lib = L.load()
+        lay = L.Layout()
+        rc = lib.mia_output_layout(C.byref(cfg), C.byref(lay))
+        if rc != L.MIA_OK:
+            raise L.MiaError(rc, "invalid configuration")
+        self.layout = lay
+
+    # ---- sizes ---------------------------------------------------------------
+    def workspace_bytes(self, n_pos, n_shape):
+        lib = L.load()
+        n = C.c_size_t()
+        rc = lib.mia_workspace_size(C.byref(self.cfg), int(n_pos), int(n_shape), C.byref(n))
+        if rc != L.MIA_OK:
+            raise L.MiaError(rc, "invalid configuration")
+        return n.value
+
+    def allocate(self, n_pos, n_shape):
+        """Device buffers for one run: (workspace, out, npairs) torch tensors."""
+        import torch
+        dev = torch.device("cuda", self.device)
+        ws = torch.empty(self.workspace_bytes(n_pos, n_shape), dtype=torch.uint8, device=dev)
+        out = torch.empty(self.layout.total, dtype=torch.float64, device=dev)
+        npairs = torch.empty((1 + self.J) * self.n_r * self.n_p, dtype=torch.int64, device=dev)
+        return ws, out, npairs
+
+    # ---- run -----------------------------------------------------------------
+    def run(self, cat, buffers, stream=None):
+        """Enqueue mia_measure on device tensors and wait for it.
+
+        ``cat``: dict with CUDA float64 contiguous tensors 'Position' (N,3),
+        'weight', 'Position_shape_sample' (M,3), 'Axis_Direction' (M,2), 'q',
+        'weight_shape_sample'."""
+        import torch
+        ws, out, npairs = buffers
+        c = L.Catalog()
+        c.position = cat["Position"].data_ptr()
+        c.weight = cat["weight"].data_ptr()
+        c.position_shape = cat["Position_shape_sample"].data_ptr()
+        c.axis_direction = cat["Axis_Direction"].data_ptr()
+        c.q = cat["q"].data_ptr()
+        c.weight_shape = cat["weight_shape_sample"].data_ptr()
+        c.n_pos = cat["Position"].shape[0]
+        c.n_shape = cat["Position_shape_sample"].shape[0]
+        r = L.Result()
+        r.out = out.data_ptr()
+        r.npairs = npairs.data_ptr()
+        if stream is None:
+            stream = torch.cuda.current_stream(self.device)
+        lib = L.load()
+        ctx = context(self.device)
+        rc = lib.mia_measure(ctx, C.byref(self.cfg), C.byref(c), C.c_void_p(ws.data_ptr()), ws.numel(),
+                             C.byref(r), C.c_void_p(stream.cuda_stream))
+        if rc != L.MIA_OK:
+            msg = lib.mia_last_error(ctx).decode()
+            if rc in (L.MIA_ERR_ARG, L.MIA_ERR_RANGE):
+                raise ValueError(msg)
+            raise L.MiaError(rc, msg)
+
+    def fetch(self, buffers):
+        """Copy the products to the host and slice them by the output layout."""
+        _, out, npairs = buffers
+        o = out.cpu().numpy()
+        cnt = npairs.cpu().numpy().reshape(1 + self.J, self.n_r, self.n_p)
+        lay = self.layout
+        nb, nr, npp, J = self.n_r * self.n_p, self.n_r, self.n_p, self.J
+
+        def grid(off, k=1):
+            return o[off:off + k * nb].reshape((k, nr, npp) if k > 1 or J else (nr, npp)) if k else None
+
+        a = {}
+        a["DD_all"] = o[lay.dd:lay.dd + (1 + J) * nb].reshape(1 + J, nr, npp)
+        a["Splus_all"] = o[lay.splus:lay.splus + (1 + J) * nb].reshape(1 + J, nr, npp)
+        for k in ("scross", "variance", "rr", "xi_gp", "xi_gx", "xi_gg", "splusd", "scrossd", "sigmasq"):
+            off = getattr(lay, k)
+            a[k] = o[off:off + nb].reshape(nr, npp)
+        a["DD"] = a["DD_all"][0]
+        for k in ("rr_jk", "xi_gp_jk", "splusd_jk", "xi_gg_jk", "dd_jk"):
+            off = getattr(lay, k)
+            a[k] = o[off:off + J * nb].reshape(J, nr, npp)
+        for k in ("proj_gp", "proj_gg", "mean_gp", "std_gp", "mean_gg", "std_gg"):
+            off = getattr(lay, k)
+            a[k] = o[off:off + nr]
+        for k in ("proj_gp_jk", "proj_gg_jk"):
+            off = getattr(lay, k)
+            a[k] = o[off:off + J * nr].reshape(J, nr)
+        for k in ("cov_gp", "cov_gg"):
+            off = getattr(lay, k)
+            a[k] = o[off:off + nr * nr].reshape(nr, nr)
+        a["R"] = o[lay.R]
+        a["R_jk"] = o[lay.R_jk:lay.R_jk + J]
+        a["npos_jk"] = o[lay.npos_jk:lay.npos_jk + J]
+        a["nshape_jk"] = o[lay.nshape_jk:lay.nshape_jk + J]
+        st = o[lay.stats:lay.stats + 8]
+        stats = dict(n_pos=int(st[0]), n_shape=int(st[1]), binned_pairs=int(st[2]), edge_pairs=int(st[3]),
+                     work_units=int(st[4]))
+        return Measurement(self.kind, nr, npp, J, a, cnt, stats)
+
+    def measure(self, cat, stream=None):
+        """Convenience: copy host arrays (numpy) or use device tensors, run, fetch."""
+        import torch
+        dev = torch.device("cuda", self.device)
+        dcat = {}
+        for k in ("Position", "weight", "Position_shape_sample", "Axis_Direction", "q", "weight_shape_sample"):
+            v = cat[k]
+            if isinstance(v, torch.Tensor):
+                t = v.to(device=dev, dtype=torch.float64).contiguous()
+            else:
+                t = torch.from_numpy(np.ascontiguousarray(v, dtype=np.float64)).to(dev)
+            dcat[k] = t
+        bufs = self.allocate(dcat["Position"].shape[0], dcat["Position_shape_sample"].shape[0])
+        self.run(dcat, bufs, stream)
+        return self.fetch(bufs)

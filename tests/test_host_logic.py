@@ -1,0 +1,142 @@
+"""Host-side logic that needs no GPU: the C ABI library and its exports, the
+exact bin tables against the reference's formulas, and the API's validation."""
+
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from measure_ia_gb300 import binning as B
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_library_exports_every_header_symbol():
+    from measure_ia_gb300 import _lib
+    lib = _lib.load()
+    hdr = open(os.path.join(ROOT, "include", "measure_ia_gb300.h")).read()
+    declared = set(re.findall(r"MIA_API\s+[\w\s\*]+?\b(mia_\w+)\s*\(", hdr))
+    assert declared == set(_lib.EXPORTED)
+    for name in declared:
+        assert hasattr(lib, name)
+    assert lib.mia_version() >= 1
+
+
+def test_layout_and_workspace_sizes():
+    from measure_ia_gb300.engine import PairCounter
+    pc = PairCounter("w", boxsize=205.0, r_bins=np.logspace(-1, np.log10(20), 11), r_min=0.1, r_max=20.0,
+                     p_bins=np.linspace(-20, 20, 9), l_subboxes=3)
+    lay = pc.layout
+    assert lay.dd == 0 and lay.splus == 28 * 80 and lay.total > lay.stats
+    assert pc.workspace_bytes(10000, 10000) > 10000 * 60
+    mixed = PairCounter("w", boxsize=205.0, r_bins=np.logspace(-1, np.log10(20), 11), r_min=0.1, r_max=20.0,
+                        p_bins=np.linspace(-20, 20, 9), l_subboxes=3, precision="mixed")
+    assert mixed.workspace_bytes(10000, 10000) > pc.workspace_bytes(10000, 10000)
+
+
+def _ref_r_bin(rp, r_bins, r_min, r_max, n):
+    dlog = (np.log10(r_max) - np.log10(r_min)) / n
+    mask = (rp >= r_bins[0]) * (rp < r_bins[-1])
+    ind = np.floor(np.log10(rp[mask]) / dlog - np.log10(r_bins[0]) / dlog).astype(int)
+    if np.any(ind == n):
+        ind[ind >= n] -= 1
+    out = np.full(len(rp), -1)
+    out[mask] = np.where(ind < 0, ind + n, ind)
+    return out
+
+
+@pytest.mark.parametrize("r_min,r_max,n", [(0.1, 20.0, 10), (0.2, 15.0, 7), (0.1, 60.0, 15)])
+def test_r_table_matches_reference_formula(r_min, r_max, n):
+    r_bins = np.logspace(np.log10(r_min), np.log10(r_max), n + 1)
+    t = B.r_table("w", r_bins, r_min, r_max, n, "brute")
+    rng = np.random.default_rng(5)
+    rp = np.concatenate([np.exp(rng.uniform(np.log(r_min / 2), np.log(r_max * 2), 200000)), r_bins,
+                         np.nextafter(r_bins, 0), np.nextafter(r_bins, 1)])
+    q = rp * rp
+    rp_exact = np.sqrt(q)
+    np.testing.assert_array_equal(t.lookup(q), _ref_r_bin(rp_exact, r_bins, r_min, r_max, n))
+
+
+def test_tree_membership_uses_squared_radii():
+    r_bins = np.logspace(-1, np.log10(20.0), 11)
+    t = B.r_table("w", r_bins, 0.1, 20.0, 10, "tree")
+    rmax2 = 20.0 * 20.0
+    assert t.lookup(np.array([rmax2]))[0] >= 0
+    assert t.lookup(np.array([np.nextafter(rmax2, np.inf)]))[0] == -1
+    assert t.lookup(np.array([0.1 * 0.1]))[0] == -1
+
+
+def test_pi_and_mu_tables_match_reference_formula():
+    pi_bins = np.linspace(-20.0, 20.0, 9)
+    t = B.pi_table(pi_bins, 8)
+    rng = np.random.default_rng(6)
+    x = np.concatenate([rng.uniform(-30, 30, 100000), pi_bins, np.nextafter(pi_bins, -1), np.nextafter(pi_bins, 1),
+                        [-1e-15, -1e-16, 0.0, -0.0]])
+    step = (pi_bins[-1] - pi_bins[0]) / 8
+    mask = (x >= pi_bins[0]) & (x < pi_bins[-1])
+    ind = np.floor(x[mask] / step - pi_bins[0] / step).astype(int)
+    ind[ind >= 8] -= 1
+    want = np.full(len(x), -1)
+    want[mask] = ind
+    np.testing.assert_array_equal(t.lookup(x), want)
+    mu_bins = np.linspace(-1, 1, 21)
+    tm = B.mu_table(mu_bins, 20)
+    mu = np.concatenate([rng.uniform(-1, 1, 100000), mu_bins])
+    ind = np.floor(mu / 0.1 - mu_bins[0] / 0.1).astype(int)
+    ind[ind >= 20] -= 1
+    np.testing.assert_array_equal(tm.lookup(mu), ind)
+
+
+def test_order_key_roundtrip_and_order():
+    x = np.array([-np.inf, -3.5, -1e-300, -0.0, 0.0, 1e-300, 2.0, np.inf])
+    k = B.order_key(x)
+    assert np.all(np.diff(k) > 0)
+    np.testing.assert_array_equal(B.from_key(k).view(np.int64), x.view(np.int64))
+
+
+def test_validation_errors_match_reference():
+    from measure_ia_gb300 import MeasureIABox
+    from measure_ia_gb300.catalogs import uniform_catalog
+    d = uniform_catalog(100, 50.0, 1)
+    box = MeasureIABox(d, None, None, None, [0.1, 5.0], 5, 4, 5.0, boxsize=50.0)
+    with pytest.raises(ValueError, match="x\\^3"):
+        box.measure_xi_w("x", "both", 10, temp_file_path="/tmp")
+    with pytest.raises(ValueError, match="temp_file_path"):
+        box.measure_xi_w("x", "both", 8, temp_file_path=None)
+    with pytest.raises(KeyError, match="corr_type"):
+        box.measure_xi_w("x", "bad", 8, temp_file_path="/tmp")
+    with pytest.raises(ValueError, match="ellipticity"):
+        box.measure_xi_multipoles("x", "both", 8, temp_file_path="/tmp", ellipticity="nope")
+    with pytest.raises(ValueError, match="pi_max"):
+        MeasureIABox(d, None, None, None)
+
+
+def test_default_weights_written_into_callers_dict_and_siminfo():
+    from measure_ia_gb300 import MeasureIABox
+    d = {"Position": np.zeros((3, 3)), "Position_shape_sample": np.zeros((2, 3))}
+    MeasureIABox(d, None, "TNG300", 99)
+    np.testing.assert_array_equal(d["weight"], np.ones(3))
+    np.testing.assert_array_equal(d["weight_shape_sample"], np.ones(2))
+    b = MeasureIABox(None, None, "TNG300", 30)
+    assert b.boxsize == 205.0 and b.snap_group == "Snapshot_30/" and b.L_0p5 == 102.5
+    b = MeasureIABox(None, None, None, None, boxsize=300.0)
+    assert b.snap_group == "" and b.boxsize == 300.0
+    assert MeasureIABox(None, None, pi_max=20.0).boxsize is None
+
+
+def test_mask_weight_quirk_mutates_masks():
+    """Without weight keys the first sum(mask) weights are selected
+    (measure_w_box_jk.py:701-712)."""
+    from measure_ia_gb300 import MeasureIABox
+    from measure_ia_gb300.catalogs import uniform_catalog
+    d = uniform_catalog(10, 50.0, 2)
+    d["weight"] = np.arange(10.0)
+    box = MeasureIABox(d, None, None, None, [0.1, 5.0], 5, 4, 5.0, boxsize=50.0)
+    sel = np.zeros(10, bool)
+    sel[[2, 5, 7]] = True
+    masks = {"Position": sel, "Position_shape_sample": sel, "Axis_Direction": sel, "q": sel}
+    got = box._select(masks)
+    np.testing.assert_array_equal(got["weight"], [0.0, 1.0, 2.0])
+    assert "weight" in masks and "weight_shape_sample" in masks
