@@ -187,6 +187,9 @@ def run_gpu(args, data, rank, ws, local):
     err["w_g+ in jackknife sigma"] = float(np.max(np.abs(mm["proj_gp"] - m64["proj_gp"]) / m64["std_gp"]))
 
     # end to end through the public API with host buffers
+    if args.no_e2e:
+        return dict(binned=binned, ms=msm, ms64=ms64, clocks=clocks, counts_exact=counts_exact, err=err,
+                    e2e_s=float("nan"), h2d=0, d2h=0, stats=mm.stats, stats64=m64.stats)
     t0 = time.perf_counter()
     e2e_steps = max(1, min(args.steps, 3))
     torch.cuda.synchronize()
@@ -211,6 +214,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--cpu-sample", type=int, default=500, help="shapes in the CPU-baseline sample")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     args = ap.parse_args()
     rank, ws, local = world()
     data = make_catalog()
@@ -244,7 +249,7 @@ def main():
 
     # CPU baseline first, before any CUDA context exists (the pool forks)
     cpu = None
-    if rank == 0:
+    if rank == 0 and not args.no_cpu:
         pairs, secs = cpu_reference(data, args.cpu_sample, cores)
         cpu = {"value": pairs / secs, "unit": "binned pairs/s", "cores": cores, "kind": "port",
                "sample": f"first {args.cpu_sample} shapes x all {n_pos} positions, {secs:.1f} s"}

