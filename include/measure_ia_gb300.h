@@ -162,6 +162,25 @@ MIA_API int mia_output_layout(const mia_config* cfg, mia_layout* layout);
 MIA_API int mia_measure(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat, void* workspace,
                 size_t workspace_bytes, const mia_result* res, void* stream);
 
+/* Size of the library's own device scratch used by mia_measure_static. */
+#define MIA_STATIC_SCRATCH_BYTES (64ull * 1024ull * 1024ull)
+
+/* mia_measure without a workspace argument, for callers that cannot allocate
+   device memory: code running under a host application or plugin framework
+   that owns the whole GPU memory budget and hands out no scratch, or a loop
+   that must not call cudaMalloc because it synchronises the device.  The
+   scratch is a 64 MiB array in the library's device module, held on every
+   GPU that loads the library until the process exits.  Measurements whose
+   scratch need (mia_workspace_size) exceeds MIA_STATIC_SCRATCH_BYTES are
+   rejected with MIA_ERR_WORKSPACE.  The first call on a device looks up the
+   array's device address (cudaGetSymbolAddress); make that first call before
+   any stream capture.  All calls share the one array, so calls that overlap
+   on the GPU (other streams, other host threads) race; every call clears what
+   must start at zero.  Inputs and outputs are still caller-provided device
+   buffers.  No counterpart in the reference. */
+MIA_API int mia_measure_static(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat,
+                               const mia_result* res, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

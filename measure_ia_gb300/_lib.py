@@ -20,7 +20,8 @@ MIA_DISTORTION, MIA_ELLIPTICITY = 0, 1
 MAX_BINS_R, MAX_BINS_P, MAX_BREAKS = 64, 128, 96
 
 EXPORTED = ("mia_create", "mia_destroy", "mia_last_error", "mia_version", "mia_workspace_size",
-            "mia_output_layout", "mia_measure")
+            "mia_output_layout", "mia_measure", "mia_measure_static")
+STATIC_SCRATCH_BYTES = 64 * 1024 * 1024
 
 
 class Catalog(C.Structure):
@@ -84,6 +85,9 @@ def load(path=LIB_PATH):
     lib.mia_measure.argtypes = [C.c_void_p, C.POINTER(Config), C.POINTER(Catalog), C.c_void_p, C.c_size_t,
                                 C.POINTER(Result), C.c_void_p]
     lib.mia_measure.restype = C.c_int
+    lib.mia_measure_static.argtypes = [C.c_void_p, C.POINTER(Config), C.POINTER(Catalog), C.POINTER(Result),
+                                       C.c_void_p]
+    lib.mia_measure_static.restype = C.c_int
     _lib = lib
     return lib
 

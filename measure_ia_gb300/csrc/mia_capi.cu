@@ -3,6 +3,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 
 #include "mia_internal.cuh"
@@ -477,6 +478,58 @@ int mia_measure(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat,
     return fail(ctx, MIA_ERR_OVERFLOW, "edge re-test queue overflow; rerun in the FP64 form");
   ctx->err.clear();
   return MIA_OK;
+}
+
+// ---- entry point without device allocation ---------------------------------
+//
+// For callers that cannot allocate device memory (a host framework owning the
+// whole GPU memory budget, or a loop where cudaMalloc's implicit device
+// synchronisation is not allowed), mia_measure_static runs mia_measure on a
+// scratch array compiled into this module.  In host code `g_static_scratch`
+// is only a host-side handle; its device address is looked up once per
+// device, with that device current, and then passed on as the workspace.
+// Every call shares the array: mia_measure zeroes what must start at zero,
+// and calls that overlap on the GPU race.
+
+static __device__ __align__(256) unsigned char g_static_scratch[MIA_STATIC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxStaticDevices = 64;
+void* g_static_ptr[kMaxStaticDevices] = {};
+std::mutex g_static_mutex;
+}  // namespace
+
+int mia_measure_static(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat, const mia_result* res,
+                       void* stream) {
+  if (!ctx) return MIA_ERR_ARG;
+  if (!cfg || !cat || !res) return fail(ctx, MIA_ERR_ARG, "null argument");
+  Plan plan;
+  const char* why = "";
+  if (!make_plan(cfg, cat->n_pos, cat->n_shape, &plan, &why)) return fail(ctx, MIA_ERR_ARG, why);
+  if (plan.total > (size_t)MIA_STATIC_SCRATCH_BYTES) {
+    char buf[256];
+    snprintf(buf, sizeof(buf),
+             "mia_measure_static: this measurement needs %zu bytes of scratch but the static scratch holds %llu; "
+             "use mia_measure with a caller-provided workspace",
+             plan.total, (unsigned long long)MIA_STATIC_SCRATCH_BYTES);
+    return fail(ctx, MIA_ERR_WORKSPACE, buf);
+  }
+  if (ctx->device < 0 || ctx->device >= kMaxStaticDevices)
+    return fail(ctx, MIA_ERR_ARG, "mia_measure_static: device index out of range");
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    base = g_static_ptr[ctx->device];
+    if (!base) {
+      cudaError_t e = cudaSetDevice(ctx->device);
+      if (e == cudaSuccess) e = cudaGetSymbolAddress(&base, g_static_scratch);
+      if (e != cudaSuccess || !base)
+        return fail(ctx, MIA_ERR_CUDA,
+                    std::string("mia_measure_static: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+      g_static_ptr[ctx->device] = base;
+    }
+  }
+  return mia_measure(ctx, cfg, cat, base, (size_t)MIA_STATIC_SCRATCH_BYTES, res, stream);
 }
 
 }  // extern "C"
