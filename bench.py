@@ -148,6 +148,8 @@ def run_gpu(args, data, rank, ws, local):
     n_pos, n_shape = dcat["Position"].shape[0], dcat["Position_shape_sample"].shape[0]
     stream = torch.cuda.current_stream(dev)
 
+    per_step = {}
+
     def time_form(precision, steps, warmup):
         pc = PairCounter("w", boxsize=L_BOX, r_bins=R_BINS, r_min=0.1, r_max=20.0, p_bins=PI_BINS, l_subboxes=3,
                          precision=precision, device=local)
@@ -158,23 +160,27 @@ def run_gpu(args, data, rank, ws, local):
         if ws > 1:
             import torch.distributed as dist
             dist.barrier()
-        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
         torch.cuda.synchronize()
-        ev0.record(stream)
-        for _ in range(steps):
+        evs[0].record(stream)
+        for i in range(steps):
             pc.run(dcat, bufs, stream)
-        ev1.record(stream)
+            evs[i + 1].record(stream)
         torch.cuda.synchronize()
-        ms = ev0.elapsed_time(ev1) / steps
+        ms = evs[0].elapsed_time(evs[-1]) / steps
+        per_step[precision] = [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
         m = pc.fetch(bufs)
         return pc, bufs, m, ms
 
     # plain FP64 form first (reference for the accuracy figures), then the mixed headline
-    fp_steps = max(1, min(args.steps, 2))
-    pc64, _, m64, ms64 = time_form("fp64", fp_steps, 1)
     with ClockSampler(local) as clk:
         pcm, bufm, mm, msm = time_form("mixed", args.steps, args.warmup)
     clocks = clk.summary()
+    if args.only_mixed:
+        m64, ms64 = mm, float("nan")
+    else:
+        fp_steps = max(1, min(args.steps, 2))
+        pc64, _, m64, ms64 = time_form("fp64", fp_steps, 1)
 
     binned = mm.stats["binned_pairs"]
     assert binned == m64.stats["binned_pairs"], "mixed and FP64 forms binned different pairs"
@@ -189,7 +195,7 @@ def run_gpu(args, data, rank, ws, local):
     # end to end through the public API with host buffers
     if args.no_e2e:
         return dict(binned=binned, ms=msm, ms64=ms64, clocks=clocks, counts_exact=counts_exact, err=err,
-                    e2e_s=float("nan"), h2d=0, d2h=0, stats=mm.stats, stats64=m64.stats)
+                    e2e_s=float("nan"), h2d=0, d2h=0, stats=mm.stats, stats64=m64.stats, per_step=per_step)
     t0 = time.perf_counter()
     e2e_steps = max(1, min(args.steps, 3))
     torch.cuda.synchronize()
@@ -204,7 +210,7 @@ def run_gpu(args, data, rank, ws, local):
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     d2h = pcm.layout.total * 8 + (1 + 27) * 80 * 8
     return dict(binned=binned, ms=msm, ms64=ms64, clocks=clocks, counts_exact=counts_exact, err=err,
-                e2e_s=e2e_s, h2d=h2d, d2h=d2h, stats=mm.stats, stats64=m64.stats)
+                e2e_s=e2e_s, h2d=h2d, d2h=d2h, stats=mm.stats, stats64=m64.stats, per_step=per_step)
 
 
 def main():
@@ -216,9 +222,12 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=500, help="shapes in the CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--only-mixed", action="store_true", help="time the mixed form only (profiling runs)")
+    ap.add_argument("--centres", type=int, default=80000, help="Neyman-Scott parents (profiling runs)")
+    ap.add_argument("--shapes", type=int, default=1_000_000, help="shape-sample size (profiling runs)")
     args = ap.parse_args()
     rank, ws, local = world()
-    data = make_catalog()
+    data = make_catalog(n_centres=args.centres, n_shape=args.shapes)
     n_pos, n_shape = len(data["Position"]), len(data["Position_shape_sample"])
     config = {"workload": "clustered 4M positions / 1M shapes, w_gg+w_g+, 27 jackknife regions (config 2)",
               "n_positions": n_pos, "n_shapes": n_shape, "boxsize": L_BOX, "r_p_bins": "10 log 0.1-20",
@@ -288,6 +297,7 @@ def main():
         "e2e": {"value": r["binned"] / r["e2e_s"], "unit": "binned pairs/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},
         "gpu_launches": launches_per_step * args.steps,
+        "step_ms": r["per_step"],
         "clocks": r["clocks"],
     }
     print(json.dumps(line))

@@ -58,11 +58,13 @@ class Result(C.Structure):
 _lib = None
 
 
-def load(path=LIB_PATH):
-    """The loaded library (built on first use if the sources are present)."""
+def load(path=None):
+    """The loaded library (built on first use if the sources are present).
+    ``MIA_LIB_PATH`` selects another build of the same sources."""
     global _lib
     if _lib is not None:
         return _lib
+    path = path or os.environ.get("MIA_LIB_PATH") or LIB_PATH
     if not os.path.exists(path):
         from . import build as _build
         try:

@@ -38,18 +38,23 @@ def _stale(lib, deps):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-def build(force=False, verbose=False):
-    """Compile if any source is newer than the library.  Returns the library path."""
+def build(force=False, verbose=False, defines=(), out=None):
+    """Compile if any source is newer than the library.  Returns the library path.
+
+    ``defines`` adds -D options and ``out`` names another output library
+    (tuning builds)."""
+    lib_path = out or LIB_PATH
+    build_dir = BUILD_DIR if not defines else os.path.join(BUILD_DIR, "_".join(d.replace("=", "") for d in defines))
     srcs = [os.path.join(CSRC, s) for s in SOURCES]
     hdrs = [os.path.join(CSRC, "mia_internal.cuh"), os.path.join(HERE, "..", "include", "measure_ia_gb300.h")]
-    if not force and not _stale(LIB_PATH, srcs + hdrs + [os.path.abspath(__file__)]):
-        return LIB_PATH
-    os.makedirs(BUILD_DIR, exist_ok=True)
+    if not force and not _stale(lib_path, srcs + hdrs + [os.path.abspath(__file__)]):
+        return lib_path
+    os.makedirs(build_dir, exist_ok=True)
     nvcc = nvcc_path()
 
     def compile_one(src):
-        obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
-        cmd = [nvcc, *ARCH, *FLAGS, "-c", src, "-o", obj]
+        obj = os.path.join(build_dir, os.path.basename(src) + ".o")
+        cmd = [nvcc, *ARCH, *FLAGS, *[f"-D{d}" for d in defines], "-c", src, "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed for {src}:\n{r.stderr}")
@@ -59,13 +64,13 @@ def build(force=False, verbose=False):
 
     with cf.ThreadPoolExecutor(max_workers=len(srcs)) as ex:
         objs = list(ex.map(compile_one, srcs))
-    tmp = LIB_PATH + ".tmp"
+    tmp = lib_path + ".tmp"
     cmd = [nvcc, *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")
-    os.replace(tmp, LIB_PATH)
-    return LIB_PATH
+    os.replace(tmp, lib_path)
+    return lib_path
 
 
 if __name__ == "__main__":

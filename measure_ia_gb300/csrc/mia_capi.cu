@@ -85,7 +85,7 @@ bool make_plan(const mia_config* cfg, long long n_pos, long long n_shape, Plan* 
     p.R[k] = (int)R;
   }
   p.shapes_per_unit = cfg->shapes_per_unit > 0 ? cfg->shapes_per_unit : 128;
-  if (p.shapes_per_unit > 512) p.shapes_per_unit = 512;
+  if (p.shapes_per_unit > kThreads) p.shapes_per_unit = kThreads;  // one staged shape per thread
   p.n_wu_max = p.n_cells + n_shape + 1;
   p.edge_capacity = 0;
   if (cfg->precision == MIA_MIXED) {
@@ -452,6 +452,12 @@ int mia_measure(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat,
   P.p_guard = (float)fmax(1.0 / 32768.0, cfg->n_p * 4e-6);
   P.c_guard = 1e-12f;
   P.wrap_guard = (float)(cfg->boxsize * 1e-5);
+  {
+    double pm = fmax(fabs(p0), fabs(p1));
+    P.los_cut = cfg->kind == MIA_KIND_W ? f32_up(pm * (1.0 + 1e-5) + 1e-30) : INFINITY;
+    const int nq = cfg->n_qbreak;
+    P.q_cut = (nq > 0 && cfg->q_bin[nq] < 0) ? host_tables.q_hi32[nq - 1] : INFINITY;
+  }
   P.edge_capacity = plan.edge_capacity;
 
   Out o;

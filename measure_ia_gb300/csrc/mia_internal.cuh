@@ -129,6 +129,8 @@ struct Params {
   float p_guard;                // fraction of a bin treated as ambiguous at each edge
   float c_guard;                // sin^2(phi) below which the exact FP64 cos(phi) decides
   float wrap_guard;
+  float los_cut;                // |Pi| above this is surely outside the Pi bins (w)
+  float q_cut;                  // q above this is surely beyond the last binned separation
   long long edge_capacity;
 };
 

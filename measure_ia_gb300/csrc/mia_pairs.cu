@@ -24,6 +24,10 @@ namespace mia {
 
 namespace {
 
+#ifndef MIA_BIN_CACHE
+#define MIA_BIN_CACHE 0  // per-thread two-entry cache of bin partials in front of the shared atomics
+#endif
+
 constexpr int kRowsPerPass = 512;
 constexpr int kSegsPerPass = 2 * kRowsPerPass;
 
@@ -60,7 +64,7 @@ __host__ __device__ inline SmemLayout smem_layout(int J, int spu, int K, int nb,
   L.slot_region = o;
   o = align16(o + sizeof(int) * kMaxSlots);
   L.shapes = o;
-  o = align16(o + (size_t)spu * (mixed ? 40 : 56));
+  o = align16(o + (size_t)spu * (mixed ? 44 : 56));
   L.seg_begin = o;
   o = align16(o + sizeof(int) * kSegsPerPass);
   L.seg_pref = o;
@@ -82,6 +86,15 @@ __device__ __forceinline__ void acc_fixed(unsigned* lo, int* hi, int idx, int v)
   unsigned nw = old + (unsigned)v;
   int d = (v < 0 ? -1 : 0) + (nw < old ? 1 : 0);
   if (d) atomicAdd(&hi[idx], d);
+}
+
+// Add a signed 64-bit fixed-point partial to a (low word, high word) pair.
+__device__ __forceinline__ void add64_shared(unsigned* lo, int* hi, int idx, long long v) {
+  const unsigned vlo = (unsigned)(unsigned long long)v;
+  int vhi = (int)(v >> 32);
+  const unsigned old = atomicAdd(&lo[idx], vlo);
+  vhi += (old + vlo < old) ? 1 : 0;
+  if (vhi) atomicAdd(&hi[idx], vhi);
 }
 
 __device__ __forceinline__ double fixed_value(const unsigned* lo, const int* hi, int idx, double inv) {
@@ -128,7 +141,7 @@ __device__ __forceinline__ void shift_hilo(float& h, float& l, int sh, float Lh,
 
 // ---- the persistent pair kernel ----------------------------------------------
 
-template <int MIXED, int VAR>
+template <int MIXED, int VAR, int KIND, int FULL>
 __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int K) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x;
@@ -280,14 +293,36 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
     // -- shapes of the unit -> shared
     const int S = u.count;
     if (MIXED) {
+      // stage the shapes ordered by line-of-sight coordinate: consecutive
+      // shapes then tend to share a (r_p, Pi) bin with a given position,
+      // which the per-thread accumulator cache below exploits
       float4* A = reinterpret_cast<float4*>(smem + SL.shapes);
       float4* B = A + P.shapes_per_unit;
       float2* C = reinterpret_cast<float2*>(B + P.shapes_per_unit);
-      for (int i = tid; i < S; i += blockDim.x) {
-        int g = u.begin + i;
-        A[i] = make_float4(w.sxh[g], w.syh[g], w.szh[g], w.swsf[g]);
-        B[i] = make_float4(w.sxl[g], w.syl[g], w.szl[g], w.swef[g]);
-        C[i] = make_float2(w.saxf[g], w.sayf[g]);
+      int* I = reinterpret_cast<int*>(C + P.shapes_per_unit);
+      float* zs = reinterpret_cast<float*>(seg_begin);  // free until the segments are built
+      float4 ra = make_float4(0.f, 0.f, 0.f, 0.f), rb = ra;
+      float2 rc = make_float2(0.f, 0.f);
+      float z = 0.f;
+      const int g = u.begin + tid;
+      if (tid < S) {
+        ra = make_float4(w.sxh[g], w.syh[g], w.szh[g], w.swsf[g]);
+        rb = make_float4(w.sxl[g], w.syl[g], w.szl[g], w.swef[g]);
+        rc = make_float2(w.saxf[g], w.sayf[g]);
+        z = ra.z + rb.z;
+        zs[tid] = z;
+      }
+      __syncthreads();
+      if (tid < S) {
+        int rank = 0;
+        for (int j = 0; j < S; ++j) {
+          const float zj = zs[j];
+          rank += (zj < z || (zj == z && j < tid)) ? 1 : 0;
+        }
+        A[rank] = ra;
+        B[rank] = rb;
+        C[rank] = rc;
+        I[rank] = g;
       }
     } else {
       double* D = reinterpret_cast<double*>(smem + SL.shapes);
@@ -317,7 +352,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
           double gap2 = g2 > 0 ? g2 * P.s[2] : 0.0;
           double rem;
           bool ok;
-          if (P.kind == MIA_KIND_W) {
+          if (KIND == MIA_KIND_W) {
             ok = gap1 * gap1 <= r2proj && gap2 * gap2 <= r2los;
             rem = r2proj - gap1 * gap1;
           } else {
@@ -413,6 +448,10 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
       }
       const int total = s_total;
       int seg = 0;
+      // two-entry cache of this thread's partial sums, keyed by histogram index
+      int ck0 = -1, ck1 = -1;
+      unsigned cn0 = 0, cn1 = 0;
+      long long cd0 = 0, cp0 = 0, cx0 = 0, cd1 = 0, cp1 = 0, cx1 = 0;
       for (int t = tid; t < total; t += blockDim.x) {
         while (t >= seg_pref[seg + 1]) ++seg;
         const int pidx = seg_begin[seg] + (t - seg_pref[seg]);
@@ -423,6 +462,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
           const float4* A = reinterpret_cast<const float4*>(smem + SL.shapes);
           const float4* B = A + P.shapes_per_unit;
           const float2* C = reinterpret_cast<const float2*>(B + P.shapes_per_unit);
+          const int* I = reinterpret_cast<const int*>(C + P.shapes_per_unit);
           float pxh = w.pxh[pidx], pxl = w.pxl[pidx];
           float pyh = w.pyh[pidx], pyl = w.pyl[pidx];
           float pzh = w.pzh[pidx], pzl = w.pzl[pidx];
@@ -434,25 +474,31 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
           for (int i = 0; i < S; ++i) {
             const float4 a = A[i];
             const float4 b = B[i];
-            float dx = (a.x - pxh) + (b.x - pxl);
-            float dy = (a.y - pyh) + (b.y - pyl);
             float dz = (a.z - pzh) + (b.z - pzl);
             bool edge = false;
-            if (P.full[0] | P.full[1] | P.full[2]) {
+            if (FULL) {
+              if (KIND == MIA_KIND_W) {
+                if (P.full[2]) {
+                  if (dz > P.halfLf) dz -= P.Lf_hi;
+                  else if (dz < -P.halfLf) dz += P.Lf_hi;
+                }
+              } else if (P.full[2] && fabsf(dz) >= P.halfLf - P.wrap_guard) {
+                edge = true;
+              }
+            }
+            // early rejection on the line of sight: surely outside [pi_bins[0], pi_bins[-1]]
+            if (KIND == MIA_KIND_W && fabsf(dz) > P.los_cut) continue;
+            float dx = (a.x - pxh) + (b.x - pxl);
+            float dy = (a.y - pyh) + (b.y - pyl);
+            if (FULL) {
               // pairs whose nearest image differs from the cell image: FP64 decides
               if (P.full[0] && fabsf(dx) >= P.halfLf - P.wrap_guard) edge = true;
               if (P.full[1] && fabsf(dy) >= P.halfLf - P.wrap_guard) edge = true;
-              if (P.full[2]) {
-                if (P.kind == MIA_KIND_W) {
-                  if (dz > P.halfLf) dz -= 2.0f * P.halfLf;
-                  else if (dz < -P.halfLf) dz += 2.0f * P.halfLf;
-                } else if (fabsf(dz) >= P.halfLf - P.wrap_guard) {
-                  edge = true;
-                }
-              }
             }
             const float qp = fmaf(dx, dx, dy * dy);
-            const float q = P.kind == MIA_KIND_W ? qp : fmaf(dz, dz, qp);
+            const float q = KIND == MIA_KIND_W ? qp : fmaf(dz, dz, qp);
+            // early rejection: surely beyond the last binned separation
+            if (q > P.q_cut) continue;
             // r bin: logarithmic bucket of q, exact FP64 breakpoints with a guard band
             int iv;
             {
@@ -471,11 +517,15 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
             int jb;
             {
               float v;
-              if (P.kind == MIA_KIND_W) {
+              if (KIND == MIA_KIND_W) {
                 v = dz;
               } else {
-                if (!(qp > (float)P.rp_cut2) && P.rp_cut2 == 0.0) {
-                  if (!edge) continue;
+                if (P.rp_cut2 == 0.0) {
+                  if (!(qp > 0.0f) && !edge) continue;  // r_p > rp_cut = 0 (measure_m_box_jk.py:637)
+                } else {
+                  const float rc2 = (float)P.rp_cut2;
+                  if (qp < rc2 * (1.0f - 1e-5f)) { if (!edge) continue; }
+                  else if (qp <= rc2 * (1.0f + 1e-5f)) edge = true;
                 }
                 v = dz * rsqrtf(q);
               }
@@ -493,7 +543,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
             if (crs * crs < P.c_guard * qp) edge = true;
             if (edge) {
               unsigned long long k = atomicAdd(&w.status->edge_count, 1ULL);
-              if (k < (unsigned long long)P.edge_capacity) w.edges[k] = make_int2(u.begin + i, pidx);
+              if (k < (unsigned long long)P.edge_capacity) w.edges[k] = make_int2(I[i], pidx);
               else atomicOr(&w.status->flags, kStatusOverflow);
               continue;
             }
@@ -506,13 +556,33 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
             ++my_binned;
             if (slot >= 0) {
               const int hi = base + bin;
-              atomicAdd(&h_cnt[hi], 1u);
-              acc_fixed(dd_lo, dd_hi, hi, __float2int_rn(ww * fixed_scale));
-              acc_fixed(sp_lo, sp_hi, hi, __float2int_rn(we * cos2 * fixed_scale));
-              acc_fixed(sx_lo, sx_hi, hi, __float2int_rn(we * sin2 * fixed_scale));
-              if (VAR) {
-                float tv = we * cos2 / (float)twoR;
-                acc_fixed(vr_lo, vr_hi, hi, __float2int_rn(tv * tv * fixed_scale));
+              const int vd = __float2int_rn(ww * fixed_scale);
+              const int vp = __float2int_rn(we * cos2 * fixed_scale);
+              const int vx = __float2int_rn(we * sin2 * fixed_scale);
+              if (VAR || !MIA_BIN_CACHE) {
+                atomicAdd(&h_cnt[hi], 1u);
+                acc_fixed(dd_lo, dd_hi, hi, vd);
+                acc_fixed(sp_lo, sp_hi, hi, vp);
+                acc_fixed(sx_lo, sx_hi, hi, vx);
+                if (VAR) {
+                  float tv = we * cos2 / (float)twoR;
+                  acc_fixed(vr_lo, vr_hi, hi, __float2int_rn(tv * tv * fixed_scale));
+                }
+              } else if (hi == ck0) {
+                ++cn0; cd0 += vd; cp0 += vp; cx0 += vx;
+              } else if (hi == ck1) {  // hit in the older entry: make it the newer one
+                const int tk = ck0; const unsigned tn = cn0; const long long td = cd0, tp = cp0, tx = cx0;
+                ck0 = ck1; cn0 = cn1 + 1; cd0 = cd1 + vd; cp0 = cp1 + vp; cx0 = cx1 + vx;
+                ck1 = tk; cn1 = tn; cd1 = td; cp1 = tp; cx1 = tx;
+              } else {  // miss: evict the older entry to shared memory
+                if (ck1 >= 0) {
+                  atomicAdd(&h_cnt[ck1], cn1);
+                  add64_shared(dd_lo, dd_hi, ck1, cd1);
+                  add64_shared(sp_lo, sp_hi, ck1, cp1);
+                  add64_shared(sx_lo, sx_hi, ck1, cx1);
+                }
+                ck1 = ck0; cn1 = cn0; cd1 = cd0; cp1 = cp0; cx1 = cx0;
+                ck0 = hi; cn0 = 1; cd0 = vd; cp0 = vp; cx0 = vx;
               }
             } else {
               double sp = (double)(we * cos2);
@@ -547,6 +617,20 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
               atomicOr(&w.status->flags, kStatusNoSlot);
             }
           }
+        }
+      }
+      if (MIXED && !VAR && MIA_BIN_CACHE) {
+        if (ck0 >= 0) {
+          atomicAdd(&h_cnt[ck0], cn0);
+          add64_shared(dd_lo, dd_hi, ck0, cd0);
+          add64_shared(sp_lo, sp_hi, ck0, cp0);
+          add64_shared(sx_lo, sx_hi, ck0, cx0);
+        }
+        if (ck1 >= 0) {
+          atomicAdd(&h_cnt[ck1], cn1);
+          add64_shared(dd_lo, dd_hi, ck1, cd1);
+          add64_shared(sp_lo, sp_hi, ck1, cp1);
+          add64_shared(sx_lo, sx_hi, ck1, cx1);
         }
       }
       __syncthreads();
@@ -621,20 +705,29 @@ __global__ void k_edge_retest(Params P, Work w, Out o) {
   if ((threadIdx.x & 31) == 0 && binned) atomicAdd(&w.status->binned, binned);
 }
 
-template <int MIXED, int VAR>
-cudaError_t launch_one(const Plan& plan, const Params& P, const Work& w, const Out& o, cudaStream_t st, int num_sms,
-                       int K) {
+template <int MIXED, int VAR, int KIND, int FULL>
+cudaError_t launch_one(const Params& P, const Work& w, const Out& o, cudaStream_t st, int num_sms, int K) {
   SmemLayout SL = smem_layout(P.J, P.shapes_per_unit, K, P.nb, MIXED, VAR);
   size_t smem = SL.total;
-  cudaError_t e = cudaFuncSetAttribute(k_pairs<MIXED, VAR>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  auto kern = k_pairs<MIXED, VAR, KIND, FULL>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairs<MIXED, VAR>, kThreads, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  int grid = num_sms * per_sm;
-  k_pairs<MIXED, VAR><<<grid, kThreads, smem, st>>>(P, w, o, K);
+  kern<<<num_sms * per_sm, kThreads, smem, st>>>(P, w, o, K);
   return cudaGetLastError();
+}
+
+template <int MIXED, int VAR>
+cudaError_t launch_kind(const Params& P, const Work& w, const Out& o, cudaStream_t st, int num_sms, int K) {
+  const bool full = P.full[0] || P.full[1] || P.full[2];
+  if (P.kind == MIA_KIND_W)
+    return full ? launch_one<MIXED, VAR, MIA_KIND_W, 1>(P, w, o, st, num_sms, K)
+                : launch_one<MIXED, VAR, MIA_KIND_W, 0>(P, w, o, st, num_sms, K);
+  return full ? launch_one<MIXED, VAR, MIA_KIND_MULTIPOLES, 1>(P, w, o, st, num_sms, K)
+              : launch_one<MIXED, VAR, MIA_KIND_MULTIPOLES, 0>(P, w, o, st, num_sms, K);
 }
 
 }  // namespace
@@ -668,12 +761,12 @@ cudaError_t launch_pairs(const Plan& plan, const Params& P, const Work& w, const
   }
   cudaError_t e;
   if (P.precision == MIA_MIXED) {
-    e = P.want_variance ? launch_one<1, 1>(plan, P, w, o, st, num_sms, K) : launch_one<1, 0>(plan, P, w, o, st, num_sms, K);
+    e = P.want_variance ? launch_kind<1, 1>(P, w, o, st, num_sms, K) : launch_kind<1, 0>(P, w, o, st, num_sms, K);
     if (e != cudaSuccess) return e;
     k_edge_retest<<<num_sms * 4, 256, 0, st>>>(P, w, o);
     e = cudaGetLastError();
   } else {
-    e = P.want_variance ? launch_one<0, 1>(plan, P, w, o, st, num_sms, K) : launch_one<0, 0>(plan, P, w, o, st, num_sms, K);
+    e = P.want_variance ? launch_kind<0, 1>(P, w, o, st, num_sms, K) : launch_kind<0, 0>(P, w, o, st, num_sms, K);
   }
   return e;
 }
