@@ -97,7 +97,8 @@ typedef struct {
   int n_p;             /* num_bins_pi (Pi bins or mu_r bins)               */
   int n_qbreak;
   int n_pbreak;
-  int shapes_per_unit; /* 0 = automatic                                    */
+  int shapes_per_unit; /* 0 = automatic (at most 256)                      */
+  int cell_refine;     /* position cells per shape cell side; 0 = automatic */
   double boxsize;      /* L                                                */
   double volume;       /* L**3 as the reference forms it                   */
   double r_min, r_max; /* separation_limits                                */

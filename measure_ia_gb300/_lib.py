@@ -34,7 +34,7 @@ class Config(C.Structure):
     _fields_ = [("kind", C.c_int), ("membership", C.c_int), ("precision", C.c_int), ("los", C.c_int),
                 ("l_subboxes", C.c_int), ("ellipticity", C.c_int), ("want_variance", C.c_int),
                 ("n_r", C.c_int), ("n_p", C.c_int), ("n_qbreak", C.c_int), ("n_pbreak", C.c_int),
-                ("shapes_per_unit", C.c_int), ("boxsize", C.c_double), ("volume", C.c_double),
+                ("shapes_per_unit", C.c_int), ("cell_refine", C.c_int), ("boxsize", C.c_double), ("volume", C.c_double),
                 ("r_min", C.c_double), ("r_max", C.c_double), ("rp_cut", C.c_double), ("cell_size", C.c_double),
                 ("r_edges", C.POINTER(C.c_double)), ("p_edges", C.POINTER(C.c_double)),
                 ("q_break", C.POINTER(C.c_double)), ("q_bin", C.POINTER(C.c_int)),

@@ -73,17 +73,49 @@ bool make_plan(const mia_config* cfg, long long n_pos, long long n_shape, Plan* 
     }
   }
   p.n_cells = cells;
+  long long fcells = 1;
   for (int k = 0; k < 3; ++k) {
     p.s[k] = L / p.n[k];
     double range = k == 2 ? p.range_los : p.range_proj;
     long long R = (long long)ceil(range / p.s[k] * (1.0 + 1e-9));
     if (R < 1) R = 1;
-    if (2 * R + 1 >= p.n[k]) {
-      p.full[k] = 1;
-      R = p.n[k] / 2;
-    }
+    if (2 * R + 1 >= p.n[k]) R = p.n[k] / 2;
     p.R[k] = (int)R;
+    // position grid: refine each shape cell m times (at most 1024 cells per side)
+    int m = cfg->cell_refine > 0 ? cfg->cell_refine : 3;
+    while (m > 1 && (long long)m * p.n[k] > 1024) --m;
+    p.m[k] = m;
+    p.nf[k] = m * p.n[k];
+    p.sf[k] = L / p.nf[k];
+    long long Rf = (long long)ceil(range / p.sf[k] * (1.0 + 1e-9));
+    if (Rf < 1) Rf = 1;
+    if (m + 2 * Rf >= p.nf[k]) {
+      p.full[k] = 1;
+      Rf = (p.nf[k] - m + 1) / 2;
+    }
+    p.Rf[k] = (int)Rf;
+    fcells *= p.nf[k];
   }
+  // keep the position-cell tables modest: coarsen the refinement if needed
+  while (fcells > (1LL << 26) && (p.m[0] > 1 || p.m[1] > 1 || p.m[2] > 1)) {
+    fcells = 1;
+    for (int k = 0; k < 3; ++k) {
+      if (p.m[k] > 1) --p.m[k];
+      p.nf[k] = p.m[k] * p.n[k];
+      p.sf[k] = L / p.nf[k];
+      double range = k == 2 ? p.range_los : p.range_proj;
+      long long Rf = (long long)ceil(range / p.sf[k] * (1.0 + 1e-9));
+      if (Rf < 1) Rf = 1;
+      p.full[k] = 0;
+      if (p.m[k] + 2 * Rf >= p.nf[k]) {
+        p.full[k] = 1;
+        Rf = (p.nf[k] - p.m[k] + 1) / 2;
+      }
+      p.Rf[k] = (int)Rf;
+      fcells *= p.nf[k];
+    }
+  }
+  p.n_fcells = fcells;
   p.shapes_per_unit = cfg->shapes_per_unit > 0 ? cfg->shapes_per_unit : 128;
   if (p.shapes_per_unit > kThreads) p.shapes_per_unit = kThreads;  // one staged shape per thread
   p.n_wu_max = p.n_cells + n_shape + 1;
@@ -101,19 +133,20 @@ bool make_plan(const mia_config* cfg, long long n_pos, long long n_shape, Plan* 
     o = align256(o + bytes);
   };
   const size_t C = (size_t)p.n_cells;
+  const size_t CF = (size_t)p.n_fcells;
   const size_t NP = (size_t)(n_pos > 0 ? n_pos : 1), NS = (size_t)(n_shape > 0 ? n_shape : 1);
   take(p.off_status, sizeof(Status));
   take(p.off_tables, sizeof(Tables));
-  take(p.off_pcount, 4 * C);
-  take(p.off_pstart, 4 * (C + 1));
-  take(p.off_pcur, 4 * C);
+  take(p.off_pcount, 4 * CF);
+  take(p.off_pstart, 4 * (CF + 1));
+  take(p.off_pcur, 4 * CF);
   take(p.off_scount, 4 * C);
   take(p.off_sstart, 4 * (C + 1));
   take(p.off_scur_lo, 4 * C);
   take(p.off_scur_hi, 4 * C);
   take(p.off_wucount, 4 * C);
   take(p.off_wustart, 4 * (C + 1));
-  take(p.off_tiles, 4 * (C / kScanTile + 2));
+  take(p.off_tiles, 4 * ((C > CF ? C : CF) / kScanTile + 2));
   take(p.off_pcell, 4 * NP);
   take(p.off_plab, 4 * NP);
   take(p.off_scell, 4 * NS);
@@ -267,7 +300,9 @@ static void build_tables(const mia_config* cfg, Tables* T, int* lut_base) {
     int iv = 0;
     while (iv < n && T->q_hi32[iv] <= lo) ++iv;
     bool clean = iv == n || T->q_lo32[iv] >= hi;
-    T->lut32[b] = (unsigned short)(iv | (clean ? 0 : 0x8000));
+    // clean bucket: the bin itself (+1, 0 = not binned); otherwise the first
+    // breakpoint to compare against, flagged
+    T->lut32[b] = clean ? (unsigned short)(T->q_bin[iv] + 1) : (unsigned short)(iv | 0x8000);
   }
 }
 
@@ -440,6 +475,10 @@ int mia_measure(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat,
     P.full[k] = plan.full[k];
     P.s[k] = plan.s[k];
     P.inv_s[k] = (double)plan.n[k] / cfg->boxsize;
+    P.m[k] = plan.m[k];
+    P.nf[k] = plan.nf[k];
+    P.Rf[k] = plan.Rf[k];
+    P.sf[k] = plan.sf[k];
   }
   P.range_proj = plan.range_proj;
   P.range_los = plan.range_los;
@@ -455,6 +494,7 @@ int mia_measure(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat,
   {
     double pm = fmax(fabs(p0), fabs(p1));
     P.los_cut = cfg->kind == MIA_KIND_W ? f32_up(pm * (1.0 + 1e-5) + 1e-30) : INFINITY;
+    P.zwin = f32_up(plan.range_los * (1.0 + 1e-5) + cfg->boxsize * 5e-7);
     const int nq = cfg->n_qbreak;
     P.q_cut = (nq > 0 && cfg->q_bin[nq] < 0) ? host_tables.q_hi32[nq - 1] : INFINITY;
   }

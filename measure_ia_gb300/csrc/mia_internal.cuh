@@ -12,7 +12,7 @@ namespace mia {
 // Sizes
 // --------------------------------------------------------------------------
 constexpr int kThreads = 256;            // pair-kernel block size
-constexpr int kLutBits = 12;             // 4096-bucket logarithmic lookup tables
+constexpr int kLutBits = 11;             // 2048-bucket logarithmic lookup table (32 octaves)
 constexpr int kLut = 1 << kLutBits;
 constexpr int kLutMantBits = 6;          // 64 buckets per octave of q
 constexpr int kMaxSlots = 12;            // jackknife regions a work unit can touch in shared memory
@@ -66,10 +66,15 @@ struct Tables {
 struct Plan {
   // geometry, in cell-dimension order d0, d1 (projected plane), d2 (line of sight)
   int axis[3];          // original axis of d0, d1, d2
-  int n[3];             // cells per dimension
-  double s[3];          // cell side
-  int R[3];             // neighbour reach in cells
-  int full[3];          // every cell of the dimension is visited (reach covers the box)
+  int n[3];             // shape cells per dimension (coarse grid)
+  double s[3];          // shape cell side
+  int R[3];             // neighbour reach in coarse cells
+  int m[3];             // position cells per shape cell along each dimension
+  int nf[3];            // position cells per dimension (fine grid, nf = m * n)
+  double sf[3];         // position cell side
+  int Rf[3];            // neighbour reach in position cells
+  int full[3];          // the reach covers the box: every position cell is visited, per-pair wrap
+  long long n_fcells;
   int n_sub;            // jackknife sub-boxes per side (1 when no jackknife)
   int J;                // number of jackknife regions (0 when none)
   long long n_cells;
@@ -117,9 +122,9 @@ struct Params {
   float Lf_hi, Lf_lo, halfLf;
   double rp_cut2;               // rp_cut^2 (multipoles), exact decision uses rp > rp_cut via q_p
   double rp_cut;
-  // cell grid
-  int axis[3], n[3], R[3], full[3];
-  double s[3], inv_s[3];
+  // cell grids: shapes on the coarse grid (n, s, R), positions on the fine grid (nf, sf, Rf)
+  int axis[3], n[3], R[3], full[3], m[3], nf[3], Rf[3];
+  double s[3], inv_s[3], sf[3];
   double range_proj, range_los;
   long long n_cells;
   int shapes_per_unit;
@@ -130,6 +135,7 @@ struct Params {
   float c_guard;                // sin^2(phi) below which the exact FP64 cos(phi) decides
   float wrap_guard;
   float los_cut;                // |Pi| above this is surely outside the Pi bins (w)
+  float zwin;                   // half-width of the line-of-sight window over the LOS-sorted shapes
   float q_cut;                  // q above this is surely beyond the last binned separation
   long long edge_capacity;
 };

@@ -28,7 +28,7 @@ namespace {
 #define MIA_BIN_CACHE 0  // per-thread two-entry cache of bin partials in front of the shared atomics
 #endif
 
-constexpr int kRowsPerPass = 512;
+constexpr int kRowsPerPass = 256;
 constexpr int kSegsPerPass = 2 * kRowsPerPass;
 
 struct SmemLayout {
@@ -64,13 +64,13 @@ __host__ __device__ inline SmemLayout smem_layout(int J, int spu, int K, int nb,
   L.slot_region = o;
   o = align16(o + sizeof(int) * kMaxSlots);
   L.shapes = o;
-  o = align16(o + (size_t)spu * (mixed ? 44 : 56));
+  o = align16(o + (size_t)spu * (mixed ? 48 : 56));
   L.seg_begin = o;
   o = align16(o + sizeof(int) * kSegsPerPass);
   L.seg_pref = o;
   o = align16(o + sizeof(int) * (kSegsPerPass + 1));
   L.seg_shift = o;
-  o = align16(o + sizeof(int) * kSegsPerPass);
+  o = align16(o + sizeof(unsigned char) * kSegsPerPass);
   L.hist = o;
   o = align16(o + sizeof(unsigned) * (size_t)K * nb * hist_words(mixed, var) + 16);
   L.total = o;
@@ -97,10 +97,10 @@ __device__ __forceinline__ void add64_shared(unsigned* lo, int* hi, int idx, lon
   if (vhi) atomicAdd(&hi[idx], vhi);
 }
 
-__device__ __forceinline__ double fixed_value(const unsigned* lo, const int* hi, int idx, double inv) {
-  long long v = ((long long)hi[idx] << 32) + (long long)lo[idx];
-  return (double)v * inv;
+__device__ __forceinline__ long long fixed_raw(const unsigned* lo, const int* hi, int idx) {
+  return ((long long)hi[idx] << 32) + (long long)lo[idx];
 }
+
 
 // Direct global accumulation (pairs whose position region has no slot, and the
 // FP64 edge re-test).
@@ -139,6 +139,217 @@ __device__ __forceinline__ void shift_hilo(float& h, float& l, int sh, float Lh,
   l = l + err + (sh > 0 ? Ll : -Ll);
 }
 
+// ---- mixed-form pair processing -----------------------------------------------
+
+struct HistView {
+  unsigned* cnt;
+  unsigned *dd_lo, *sp_lo, *sx_lo, *vr_lo;
+  int *dd_hi, *sp_hi, *sx_hi, *vr_hi;
+};
+
+// A thread's two most recent (histogram index -> exact fixed-point partial)
+// entries; a pair whose bin matches one of them adds in registers, otherwise
+// the older entry goes to the shared histogram.
+struct BinCache {
+  int k0 = -1, k1 = -1;
+  unsigned n0 = 0, n1 = 0;
+  long long d0 = 0, p0 = 0, x0 = 0, d1 = 0, p1 = 0, x1 = 0;
+
+  __device__ __forceinline__ static void flush(const HistView& h, int k, unsigned n, long long d, long long p,
+                                               long long x) {
+    atomicAdd(&h.cnt[k], n);
+    add64_shared(h.dd_lo, h.dd_hi, k, d);
+    add64_shared(h.sp_lo, h.sp_hi, k, p);
+    add64_shared(h.sx_lo, h.sx_hi, k, x);
+  }
+  __device__ __forceinline__ void add(const HistView& h, int k, int vd, int vp, int vx) {
+    if (k == k0) {
+      ++n0; d0 += vd; p0 += vp; x0 += vx;
+    } else if (k == k1) {  // hit in the older entry: it becomes the newer one
+      const int tk = k0; const unsigned tn = n0; const long long td = d0, tp = p0, tx = x0;
+      k0 = k1; n0 = n1 + 1; d0 = d1 + vd; p0 = p1 + vp; x0 = x1 + vx;
+      k1 = tk; n1 = tn; d1 = td; p1 = tp; x1 = tx;
+    } else {
+      if (k1 >= 0) flush(h, k1, n1, d1, p1, x1);
+      k1 = k0; n1 = n0; d1 = d0; p1 = p0; x1 = x0;
+      k0 = k; n0 = 1; d0 = vd; p0 = vp; x0 = vx;
+    }
+  }
+  __device__ __forceinline__ void flush_all(const HistView& h) {
+    if (k0 >= 0) flush(h, k0, n0, d0, p0, x0);
+    if (k1 >= 0) flush(h, k1, n1, d1, p1, x1);
+    k0 = k1 = -1;
+  }
+};
+
+// One position in FP32 hi/lo form, moved to the periodic image of its row.
+struct MixedPos {
+  float xh, xl, yh, yl, zh, zl, w;
+  int idx, lab, slot, base;
+  bool valid;
+};
+
+__device__ __forceinline__ void load_mixed_pos(const Params& P, const Work& w, const int* seg_begin,
+                                               const int* seg_pref, const unsigned char* seg_shift, const int* slot_of, int nb,
+                                               int t, int total, int& seg, MixedPos& p) {
+  p.valid = t < total;
+  int pidx = 0;
+  int code = 13;  // no shift
+  if (p.valid) {
+    while (t >= seg_pref[seg + 1]) ++seg;
+    pidx = seg_begin[seg] + (t - seg_pref[seg]);
+    code = seg_shift[seg];
+  }
+  p.idx = pidx;
+  p.lab = p.valid ? w.plab_s[pidx] : 0;
+  p.slot = slot_of[p.lab];
+  p.base = p.slot * nb;
+  p.xh = w.pxh[pidx]; p.xl = w.pxl[pidx];
+  p.yh = w.pyh[pidx]; p.yl = w.pyl[pidx];
+  p.zh = w.pzh[pidx]; p.zl = w.pzl[pidx];
+  p.w = w.pwf[pidx];
+  shift_hilo(p.xh, p.xl, code % 3 - 1, P.Lf_hi, P.Lf_lo);
+  shift_hilo(p.yh, p.yl, (code / 3) % 3 - 1, P.Lf_hi, P.Lf_lo);
+  shift_hilo(p.zh, p.zl, code / 9 - 1, P.Lf_hi, P.Lf_lo);
+}
+
+// Widen [lo, hi) by the shapes whose staged line-of-sight coordinate lies in
+// [z - win, z + win] (Z ascending).
+__device__ __forceinline__ void z_window(const float* Z, int S, float z, float win, int& lo_out, int& hi_out) {
+  const float zlo = z - win, zhi = z + win;
+  int lo = 0, hi = S;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (Z[mid] < zlo) lo = mid + 1; else hi = mid;
+  }
+  const int first = lo;
+  hi = S;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (Z[mid] <= zhi) lo = mid + 1; else hi = mid;
+  }
+  if (first < lo_out) lo_out = first;
+  if (lo > hi_out) hi_out = lo;
+}
+
+// Everything one (shape i, position p) pair contributes in the mixed form:
+// FP32 separations, guarded bin decisions, e+/ex, fixed-point accumulation; a
+// pair near any decision edge is queued for the FP64 re-test instead.
+template <int KIND, int FULL, int VAR>
+__device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T, const float4& a, const float4& b,
+                                           const float2* C, const int* I, int i, const MixedPos& p,
+                                           const HistView& h, BinCache& cache, const Work& w, const Out& o,
+                                           float fixed_scale, double twoR, int label_a,
+                                           unsigned long long& my_binned) {
+  float dz = (a.z - p.zh) + (b.z - p.zl);
+  bool edge = false;
+  if (FULL) {
+    if (KIND == MIA_KIND_W) {
+      if (P.full[2]) {
+        if (dz > P.halfLf) dz -= P.Lf_hi;
+        else if (dz < -P.halfLf) dz += P.Lf_hi;
+      }
+    } else if (P.full[2] && fabsf(dz) >= P.halfLf - P.wrap_guard) {
+      edge = true;
+    }
+  }
+  // early rejection on the line of sight: surely outside [pi_bins[0], pi_bins[-1]]
+  if (KIND == MIA_KIND_W && fabsf(dz) > P.los_cut) return;
+  const float dx = (a.x - p.xh) + (b.x - p.xl);
+  const float dy = (a.y - p.yh) + (b.y - p.yl);
+  if (FULL) {
+    // pairs whose nearest image differs from the cell image: FP64 decides
+    if (P.full[0] && fabsf(dx) >= P.halfLf - P.wrap_guard) edge = true;
+    if (P.full[1] && fabsf(dy) >= P.halfLf - P.wrap_guard) edge = true;
+  }
+  const float qp = fmaf(dx, dx, dy * dy);
+  const float q = KIND == MIA_KIND_W ? qp : fmaf(dz, dz, qp);
+  // early rejection: surely beyond the last binned separation
+  if (q > P.q_cut) return;
+  // r bin: logarithmic bucket of q; clean buckets hold the bin itself, buckets
+  // touching a guard band fall back to the exact FP64 breakpoints
+  int ib;
+  {
+    const int bucket = (int)(__float_as_uint(q) >> (23 - kLutMantBits)) - P.lut32_base;
+    const unsigned short e = (bucket >= 0 && bucket < kLut) ? T.lut32[bucket] : (unsigned short)0x8000;
+    if (!(e & 0x8000)) {
+      ib = (int)e - 1;
+    } else {
+      int iv = e & 0x7fff;
+      while (iv < P.n_qbreak && q >= T.q_hi32[iv]) ++iv;
+      if (iv < P.n_qbreak && q >= T.q_lo32[iv]) edge = true;
+      ib = T.q_bin[iv];
+    }
+  }
+  if (ib < 0 && !edge) return;
+  int jb;
+  {
+    float v;
+    if (KIND == MIA_KIND_W) {
+      v = dz;
+    } else {
+      if (P.rp_cut2 == 0.0) {
+        if (!(qp > 0.0f) && !edge) return;  // r_p > rp_cut = 0 (measure_m_box_jk.py:637)
+      } else {
+        const float rc2 = (float)P.rp_cut2;
+        if (qp < rc2 * (1.0f - 1e-5f)) {
+          if (!edge) return;
+        } else if (qp <= rc2 * (1.0f + 1e-5f)) {
+          edge = true;
+        }
+      }
+      v = dz * rsqrtf(q);
+    }
+    const float t2 = (v - P.p_lo32) * P.p_inv32;
+    const float fl = floorf(t2);
+    const float fr = t2 - fl;
+    jb = (int)fl;
+    if (fr < P.p_guard || fr > 1.0f - P.p_guard) edge = true;
+    if (jb < 0 || jb >= P.n_p) jb = -1;
+  }
+  if (!edge && jb < 0) return;
+  const float2 cxy = C[i];
+  const float dot = fmaf(dx, cxy.x, dy * cxy.y);
+  const float crs = fmaf(dx, cxy.y, -dy * cxy.x);
+  if (crs * crs < P.c_guard * qp) edge = true;
+  if (edge) {
+    const unsigned long long k = atomicAdd(&w.status->edge_count, 1ULL);
+    if (k < (unsigned long long)P.edge_capacity) w.edges[k] = make_int2(I[i], p.idx);
+    else atomicOr(&w.status->flags, kStatusOverflow);
+    return;
+  }
+  const int bin = ib * P.n_p + jb;
+  const float inv = __fdividef(1.0f, qp);
+  const float cos2 = (dot * dot - crs * crs) * inv;
+  const float sin2 = 2.0f * dot * fabsf(crs) * inv;
+  const float ww = p.w * a.w;
+  const float we = p.w * b.w;
+  ++my_binned;
+  if (p.slot >= 0) {
+    const int k = p.base + bin;
+    const int vd = __float2int_rn(ww * fixed_scale);
+    const int vp = __float2int_rn(we * cos2 * fixed_scale);
+    const int vx = __float2int_rn(we * sin2 * fixed_scale);
+    if (VAR || !MIA_BIN_CACHE) {
+      atomicAdd(&h.cnt[k], 1u);
+      acc_fixed(h.dd_lo, h.dd_hi, k, vd);
+      acc_fixed(h.sp_lo, h.sp_hi, k, vp);
+      acc_fixed(h.sx_lo, h.sx_hi, k, vx);
+      if (VAR) {
+        const float tv = we * cos2 / (float)twoR;
+        acc_fixed(h.vr_lo, h.vr_hi, k, __float2int_rn(tv * tv * fixed_scale));
+      }
+    } else {
+      cache.add(h, k, vd, vp, vx);
+    }
+  } else {
+    const double sp = (double)(we * cos2);
+    const double tv = sp / twoR;
+    acc_global(o, P.nb, P.J, label_a, p.lab, bin, (double)ww, sp, (double)(we * sin2), tv * tv, VAR);
+    atomicOr(&w.status->flags, kStatusNoSlot);
+  }
+}
+
 // ---- the persistent pair kernel ----------------------------------------------
 
 template <int MIXED, int VAR, int KIND, int FULL>
@@ -152,12 +363,14 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
   int* slot_region = reinterpret_cast<int*>(smem + SL.slot_region);
   int* seg_begin = reinterpret_cast<int*>(smem + SL.seg_begin);
   int* seg_pref = reinterpret_cast<int*>(smem + SL.seg_pref);
-  int* seg_shift = reinterpret_cast<int*>(smem + SL.seg_shift);
+  unsigned char* seg_shift = reinterpret_cast<unsigned char*>(smem + SL.seg_shift);
   unsigned* hist = reinterpret_cast<unsigned*>(smem + SL.hist);
   const int KB = K * nb;
 
   __shared__ int s_wu;
   __shared__ int s_nslots;
+  __shared__ int s_copies;
+  __shared__ int s_stride;
   __shared__ int s_scan[32];
   __shared__ int s_total;
 
@@ -222,11 +435,9 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
   }
   const int hist_u32 = MIXED ? KB * hist_words(1, VAR) : (int)(align16(sizeof(unsigned) * (size_t)KB) / 4) + KB * 2 * (3 + VAR);
 
-  // row enumeration extents (line-of-sight dimension d2 and projected d1)
-  int lo1 = P.full[1] ? -(P.n[1] / 2) : -P.R[1];
-  int N1 = P.full[1] ? P.n[1] : 2 * P.R[1] + 1;
-  int lo2 = P.full[2] ? -(P.n[2] / 2) : -P.R[2];
-  int N2 = P.full[2] ? P.n[2] : 2 * P.R[2] + 1;
+  // rows of position cells: fine-grid extents along d1 and d2 around a shape cell
+  const int N1 = P.full[1] ? P.nf[1] : P.m[1] + 2 * P.Rf[1];
+  const int N2 = P.full[2] ? P.nf[2] : P.m[2] + 2 * P.Rf[2];
   const int n_rows = N1 * N2;
   const double r2proj = P.range_proj * P.range_proj;
   const double r2los = P.range_los * P.range_los;
@@ -259,8 +470,9 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
         int sets[3][16];
         int cnt[3] = {0, 0, 0};
         for (int k = 0; k < 3; ++k) {
-          int lo = P.full[k] ? -(P.n[k] / 2) : -P.R[k];
-          int N = P.full[k] ? P.n[k] : 2 * P.R[k] + 1;
+          const bool all = P.full[k] || 2 * P.R[k] + 1 >= P.n[k];
+          int lo = all ? -(P.n[k] / 2) : -P.R[k];
+          int N = all ? P.n[k] : 2 * P.R[k] + 1;
           for (int d = 0; d < N && cnt[k] < 16; ++d) {
             int cc = wrapi(((c[k] + lo + d) % P.n[k] + P.n[k]) % P.n[k], P.n[k]);
             int sb = (int)((long long)cc * P.n_sub / P.n[k]);
@@ -288,6 +500,16 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
         }
       }
       s_nslots = ns;
+      // private copies of the unit's histograms (mixed form): lanes holding
+      // neighbouring positions hit the same bin against a shape, so lane l
+      // adds into copy l mod R; the odd stride puts the copies in distinct banks
+      int R = 1;
+      if (MIXED) {
+        const int cap = K * nb;  // words available per histogram array
+        while (R < 8 && (2 * R) * (ns * nb + 1) <= cap) R *= 2;
+      }
+      s_copies = R;
+      s_stride = R > 1 ? ns * nb + 1 : ns * nb;
     }
     for (int i = tid; i < hist_u32; i += blockDim.x) hist[i] = 0u;
     // -- shapes of the unit -> shared
@@ -300,6 +522,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
       float4* B = A + P.shapes_per_unit;
       float2* C = reinterpret_cast<float2*>(B + P.shapes_per_unit);
       int* I = reinterpret_cast<int*>(C + P.shapes_per_unit);
+      float* Z = reinterpret_cast<float*>(I + P.shapes_per_unit);
       float* zs = reinterpret_cast<float*>(seg_begin);  // free until the segments are built
       float4 ra = make_float4(0.f, 0.f, 0.f, 0.f), rb = ra;
       float2 rc = make_float2(0.f, 0.f);
@@ -323,6 +546,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
         B[rank] = rb;
         C[rank] = rc;
         I[rank] = g;
+        Z[rank] = z;
       }
     } else {
       double* D = reinterpret_cast<double*>(smem + SL.shapes);
@@ -346,10 +570,14 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
         int r = pass + rr;
         int len0 = 0, len1 = 0, b0 = 0, b1 = 0, sh0 = 0, sh1 = 0;
         if (r < n_rows) {
-          int d1 = lo1 + r % N1, d2 = lo2 + r / N1;
-          int g1 = abs(d1) - 1, g2 = abs(d2) - 1;
-          double gap1 = g1 > 0 ? g1 * P.s[1] : 0.0;
-          double gap2 = g2 > 0 ? g2 * P.s[2] : 0.0;
+          // unwrapped fine indices of the row and its distance to the shape cell
+          const int f1 = c[1] * P.m[1], f2 = c[2] * P.m[2];
+          const int lo1 = P.full[1] ? f1 - (P.nf[1] - P.m[1]) / 2 : f1 - P.Rf[1];
+          const int lo2 = P.full[2] ? f2 - (P.nf[2] - P.m[2]) / 2 : f2 - P.Rf[2];
+          const int u1 = lo1 + r % N1, u2 = lo2 + r / N1;
+          const int g1 = u1 > f1 + P.m[1] - 1 ? u1 - f1 - P.m[1] : (u1 < f1 ? f1 - u1 - 1 : 0);
+          const int g2 = u2 > f2 + P.m[2] - 1 ? u2 - f2 - P.m[2] : (u2 < f2 ? f2 - u2 - 1 : 0);
+          const double gap1 = g1 * P.sf[1], gap2 = g2 * P.sf[2];
           double rem;
           bool ok;
           if (KIND == MIA_KIND_W) {
@@ -360,40 +588,35 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
             ok = rem >= 0.0;
           }
           if (ok) {
-            int u1 = c[1] + d1, u2 = c[2] + d2;
-            int sh1d = u1 < 0 ? -1 : (u1 >= P.n[1] ? 1 : 0);
-            int sh2d = u2 < 0 ? -1 : (u2 >= P.n[2] ? 1 : 0);
-            int cc1 = wrapi(u1, P.n[1]), cc2 = wrapi(u2, P.n[2]);
-            int xlo, xhi;
+            const int sh1d = u1 < 0 ? -1 : (u1 >= P.nf[1] ? 1 : 0);
+            const int sh2d = u2 < 0 ? -1 : (u2 >= P.nf[2] ? 1 : 0);
+            const int cc1 = wrapi(u1, P.nf[1]), cc2 = wrapi(u2, P.nf[2]);
+            const int f0 = c[0] * P.m[0];
+            int a0, a1;
             if (P.full[0]) {
-              xlo = -(P.n[0] / 2);
-              xhi = P.n[0] - P.n[0] / 2 - 1;
+              a0 = f0 - (P.nf[0] - P.m[0]) / 2;
+              a1 = a0 + P.nf[0] - 1;
             } else {
-              double r0 = sqrt(rem > 0.0 ? rem : 0.0);
-              int R0 = (int)ceil(r0 / P.s[0] * (1.0 + 1e-9));
-              if (R0 > P.R[0]) R0 = P.R[0];
-              xlo = -R0;
-              xhi = R0;
+              int R0 = (int)ceil(sqrt(rem > 0.0 ? rem : 0.0) / P.sf[0] * (1.0 + 1e-9));
+              if (R0 > P.Rf[0]) R0 = P.Rf[0];
+              a0 = f0 - R0;
+              a1 = f0 + P.m[0] - 1 + R0;
             }
-            long long rowbase = ((long long)cc2 * P.n[1] + cc1) * P.n[0];
-            int a0 = c[0] + xlo, a1 = c[0] + xhi;
-            int code_yz = 3 * (sh1d + 1) + 9 * (sh2d + 1);
+            const long long rowbase = ((long long)cc2 * P.nf[1] + cc1) * P.nf[0];
+            const int code_yz = 3 * (sh1d + 1) + 9 * (sh2d + 1);
             if (a0 < 0) {
-              int lo_c = a0 + P.n[0];
-              b0 = w.pstart[rowbase + lo_c];
-              len0 = w.pstart[rowbase + P.n[0]] - b0;
+              b0 = w.pstart[rowbase + a0 + P.nf[0]];
+              len0 = w.pstart[rowbase + P.nf[0]] - b0;
               sh0 = code_yz + 0;  // d0 shift -1
-              int hi_c = a1;
               b1 = w.pstart[rowbase];
-              len1 = w.pstart[rowbase + hi_c + 1] - b1;
+              len1 = w.pstart[rowbase + a1 + 1] - b1;
               sh1 = code_yz + 1;
-            } else if (a1 >= P.n[0]) {
+            } else if (a1 >= P.nf[0]) {
               b0 = w.pstart[rowbase + a0];
-              len0 = w.pstart[rowbase + P.n[0]] - b0;
+              len0 = w.pstart[rowbase + P.nf[0]] - b0;
               sh0 = code_yz + 1;
-              int hi_c = a1 - P.n[0];
               b1 = w.pstart[rowbase];
-              len1 = w.pstart[rowbase + hi_c + 1] - b1;
+              len1 = w.pstart[rowbase + a1 - P.nf[0] + 1] - b1;
               sh1 = code_yz + 2;  // d0 shift +1
             } else {
               b0 = w.pstart[rowbase + a0];
@@ -404,8 +627,8 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
         }
         seg_begin[2 * rr] = b0;
         seg_begin[2 * rr + 1] = b1;
-        seg_shift[2 * rr] = sh0;
-        seg_shift[2 * rr + 1] = sh1;
+        seg_shift[2 * rr] = (unsigned char)sh0;
+        seg_shift[2 * rr + 1] = (unsigned char)sh1;
         seg_pref[2 * rr] = len0;
         seg_pref[2 * rr + 1] = len1;
       }
@@ -447,153 +670,61 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
         __syncthreads();
       }
       const int total = s_total;
-      int seg = 0;
-      // two-entry cache of this thread's partial sums, keyed by histogram index
-      int ck0 = -1, ck1 = -1;
-      unsigned cn0 = 0, cn1 = 0;
-      long long cd0 = 0, cp0 = 0, cx0 = 0, cd1 = 0, cp1 = 0, cx1 = 0;
-      for (int t = tid; t < total; t += blockDim.x) {
-        while (t >= seg_pref[seg + 1]) ++seg;
-        const int pidx = seg_begin[seg] + (t - seg_pref[seg]);
-        const int plab = w.plab_s[pidx];
-        const int slot = slot_of[plab];
-        const int base = slot * nb;
-        if (MIXED) {
-          const float4* A = reinterpret_cast<const float4*>(smem + SL.shapes);
-          const float4* B = A + P.shapes_per_unit;
-          const float2* C = reinterpret_cast<const float2*>(B + P.shapes_per_unit);
-          const int* I = reinterpret_cast<const int*>(C + P.shapes_per_unit);
-          float pxh = w.pxh[pidx], pxl = w.pxl[pidx];
-          float pyh = w.pyh[pidx], pyl = w.pyl[pidx];
-          float pzh = w.pzh[pidx], pzl = w.pzl[pidx];
-          const float pw = w.pwf[pidx];
-          const int code = seg_shift[seg];
-          shift_hilo(pxh, pxl, code % 3 - 1, P.Lf_hi, P.Lf_lo);
-          shift_hilo(pyh, pyl, (code / 3) % 3 - 1, P.Lf_hi, P.Lf_lo);
-          shift_hilo(pzh, pzl, code / 9 - 1, P.Lf_hi, P.Lf_lo);
-          for (int i = 0; i < S; ++i) {
-            const float4 a = A[i];
-            const float4 b = B[i];
-            float dz = (a.z - pzh) + (b.z - pzl);
-            bool edge = false;
-            if (FULL) {
-              if (KIND == MIA_KIND_W) {
-                if (P.full[2]) {
-                  if (dz > P.halfLf) dz -= P.Lf_hi;
-                  else if (dz < -P.halfLf) dz += P.Lf_hi;
-                }
-              } else if (P.full[2] && fabsf(dz) >= P.halfLf - P.wrap_guard) {
-                edge = true;
-              }
-            }
-            // early rejection on the line of sight: surely outside [pi_bins[0], pi_bins[-1]]
-            if (KIND == MIA_KIND_W && fabsf(dz) > P.los_cut) continue;
-            float dx = (a.x - pxh) + (b.x - pxl);
-            float dy = (a.y - pyh) + (b.y - pyl);
-            if (FULL) {
-              // pairs whose nearest image differs from the cell image: FP64 decides
-              if (P.full[0] && fabsf(dx) >= P.halfLf - P.wrap_guard) edge = true;
-              if (P.full[1] && fabsf(dy) >= P.halfLf - P.wrap_guard) edge = true;
-            }
-            const float qp = fmaf(dx, dx, dy * dy);
-            const float q = KIND == MIA_KIND_W ? qp : fmaf(dz, dz, qp);
-            // early rejection: surely beyond the last binned separation
-            if (q > P.q_cut) continue;
-            // r bin: logarithmic bucket of q, exact FP64 breakpoints with a guard band
-            int iv;
-            {
-              int bucket = (int)(__float_as_uint(q) >> (23 - kLutMantBits)) - P.lut32_base;
-              unsigned short e;
-              if (bucket >= 0 && bucket < kLut) e = T.lut32[bucket];
-              else e = 0x8000;
-              iv = e & 0x7fff;
-              if (e & 0x8000) {
-                while (iv < P.n_qbreak && q >= T.q_hi32[iv]) ++iv;
-                if (iv < P.n_qbreak && q >= T.q_lo32[iv]) edge = true;
-              }
-            }
-            const int ib = T.q_bin[iv];
-            if (ib < 0 && !edge) continue;
-            int jb;
-            {
-              float v;
-              if (KIND == MIA_KIND_W) {
-                v = dz;
-              } else {
-                if (P.rp_cut2 == 0.0) {
-                  if (!(qp > 0.0f) && !edge) continue;  // r_p > rp_cut = 0 (measure_m_box_jk.py:637)
-                } else {
-                  const float rc2 = (float)P.rp_cut2;
-                  if (qp < rc2 * (1.0f - 1e-5f)) { if (!edge) continue; }
-                  else if (qp <= rc2 * (1.0f + 1e-5f)) edge = true;
-                }
-                v = dz * rsqrtf(q);
-              }
-              float t2 = (v - P.p_lo32) * P.p_inv32;
-              float fl = floorf(t2);
-              float fr = t2 - fl;
-              jb = (int)fl;
-              if (fr < P.p_guard || fr > 1.0f - P.p_guard) edge = true;
-              if (jb < 0 || jb >= P.n_p) jb = -1;
-            }
-            if (!edge && jb < 0) continue;
-            const float cx = C[i].x, cy = C[i].y;
-            const float dot = fmaf(dx, cx, dy * cy);
-            const float crs = fmaf(dx, cy, -dy * cx);
-            if (crs * crs < P.c_guard * qp) edge = true;
-            if (edge) {
-              unsigned long long k = atomicAdd(&w.status->edge_count, 1ULL);
-              if (k < (unsigned long long)P.edge_capacity) w.edges[k] = make_int2(I[i], pidx);
-              else atomicOr(&w.status->flags, kStatusOverflow);
-              continue;
-            }
-            const int bin = ib * P.n_p + jb;
-            const float inv = __fdividef(1.0f, qp);
-            const float cos2 = (dot * dot - crs * crs) * inv;
-            const float sin2 = 2.0f * dot * fabsf(crs) * inv;
-            const float ww = pw * a.w;
-            const float we = pw * b.w;
-            ++my_binned;
-            if (slot >= 0) {
-              const int hi = base + bin;
-              const int vd = __float2int_rn(ww * fixed_scale);
-              const int vp = __float2int_rn(we * cos2 * fixed_scale);
-              const int vx = __float2int_rn(we * sin2 * fixed_scale);
-              if (VAR || !MIA_BIN_CACHE) {
-                atomicAdd(&h_cnt[hi], 1u);
-                acc_fixed(dd_lo, dd_hi, hi, vd);
-                acc_fixed(sp_lo, sp_hi, hi, vp);
-                acc_fixed(sx_lo, sx_hi, hi, vx);
-                if (VAR) {
-                  float tv = we * cos2 / (float)twoR;
-                  acc_fixed(vr_lo, vr_hi, hi, __float2int_rn(tv * tv * fixed_scale));
-                }
-              } else if (hi == ck0) {
-                ++cn0; cd0 += vd; cp0 += vp; cx0 += vx;
-              } else if (hi == ck1) {  // hit in the older entry: make it the newer one
-                const int tk = ck0; const unsigned tn = cn0; const long long td = cd0, tp = cp0, tx = cx0;
-                ck0 = ck1; cn0 = cn1 + 1; cd0 = cd1 + vd; cp0 = cp1 + vp; cx0 = cx1 + vx;
-                ck1 = tk; cn1 = tn; cd1 = td; cp1 = tp; cx1 = tx;
-              } else {  // miss: evict the older entry to shared memory
-                if (ck1 >= 0) {
-                  atomicAdd(&h_cnt[ck1], cn1);
-                  add64_shared(dd_lo, dd_hi, ck1, cd1);
-                  add64_shared(sp_lo, sp_hi, ck1, cp1);
-                  add64_shared(sx_lo, sx_hi, ck1, cx1);
-                }
-                ck1 = ck0; cn1 = cn0; cd1 = cd0; cp1 = cp0; cx1 = cx0;
-                ck0 = hi; cn0 = 1; cd0 = vd; cp0 = vp; cx0 = vx;
-              }
+      if (MIXED) {
+        const float4* A = reinterpret_cast<const float4*>(smem + SL.shapes);
+        const float4* B = A + P.shapes_per_unit;
+        const float2* C = reinterpret_cast<const float2*>(B + P.shapes_per_unit);
+        const int* I = reinterpret_cast<const int*>(C + P.shapes_per_unit);
+        const float* Z = reinterpret_cast<const float*>(I + P.shapes_per_unit);
+        const HistView hv{h_cnt, dd_lo, sp_lo, sx_lo, vr_lo, dd_hi, sp_hi, sx_hi, vr_hi};
+        BinCache cache;
+        int seg = 0;
+        const int copy_off = (tid & (s_copies - 1)) * s_stride;
+        // every warp runs the same number of iterations so that its lanes can
+        // agree on one shape range
+        for (int tb = 0; tb < total; tb += blockDim.x) {
+          MixedPos p0;
+          load_mixed_pos(P, w, seg_begin, seg_pref, seg_shift, slot_of, nb, tb + tid, total, seg, p0);
+          p0.base += copy_off;
+          int i_lo = S, i_hi = 0;
+          if (p0.valid) {
+            if (FULL && P.full[2]) {
+              i_lo = 0;
+              i_hi = S;
             } else {
-              double sp = (double)(we * cos2);
-              double tv = sp / twoR;
-              acc_global(o, nb, P.J, u.label, plab, bin, (double)ww, sp, (double)(we * sin2), tv * tv, VAR);
-              atomicOr(&w.status->flags, kStatusNoSlot);
+              // shapes are staged in line-of-sight order: only a window of them
+              // can be within range of this position (conservative float bounds)
+              z_window(Z, S, p0.zh + p0.zl, P.zwin, i_lo, i_hi);
             }
           }
-        } else {
-          const double* D = reinterpret_cast<const double*>(smem + SL.shapes);
-          const int M = P.shapes_per_unit;
+          // the union over the warp is barely wider (neighbouring positions),
+          // and every lane then reads the same staged shape in each iteration
+          const int wlo = __reduce_min_sync(0xffffffffu, i_lo);
+          const int whi = __reduce_max_sync(0xffffffffu, i_hi);
+          if (p0.valid && wlo < whi) {
+            float4 a = A[wlo], b = B[wlo];
+            for (int i = wlo; i < whi; ++i) {
+              // next shape in flight while this pair is processed (index S at most:
+              // still inside the staging area)
+              const float4 an = A[i + 1], bn = B[i + 1];
+              mixed_pair<KIND, FULL, VAR>(P, T, a, b, C, I, i, p0, hv, cache, w, o, fixed_scale, twoR, u.label,
+                                          my_binned);
+              a = an;
+              b = bn;
+            }
+          }
+        }
+        if (!VAR && MIA_BIN_CACHE) cache.flush_all(hv);
+      } else {
+        int seg = 0;
+        const double* D = reinterpret_cast<const double*>(smem + SL.shapes);
+        const int M = P.shapes_per_unit;
+        for (int t = tid; t < total; t += blockDim.x) {
+          while (t >= seg_pref[seg + 1]) ++seg;
+          const int pidx = seg_begin[seg] + (t - seg_pref[seg]);
+          const int plab = w.plab_s[pidx];
+          const int slot = slot_of[plab];
+          const int base = slot * nb;
           const double qx = w.px[pidx], qy = w.py[pidx], qz = w.pz[pidx], pw = w.pw[pidx];
           for (int i = 0; i < S; ++i) {
             PairResult r = pair_exact(P, *w.tables, D[i], D[M + i], D[2 * M + i], D[3 * M + i], D[4 * M + i],
@@ -619,36 +750,32 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
           }
         }
       }
-      if (MIXED && !VAR && MIA_BIN_CACHE) {
-        if (ck0 >= 0) {
-          atomicAdd(&h_cnt[ck0], cn0);
-          add64_shared(dd_lo, dd_hi, ck0, cd0);
-          add64_shared(sp_lo, sp_hi, ck0, cp0);
-          add64_shared(sx_lo, sx_hi, ck0, cx0);
-        }
-        if (ck1 >= 0) {
-          atomicAdd(&h_cnt[ck1], cn1);
-          add64_shared(dd_lo, dd_hi, ck1, cd1);
-          add64_shared(sp_lo, sp_hi, ck1, cp1);
-          add64_shared(sx_lo, sx_hi, ck1, cx1);
-        }
-      }
       __syncthreads();
     }
 
     // -- flush the unit's histograms
     const int ns = s_nslots;
     const int a = u.label;
+    const int copies = s_copies, stride = s_stride;
     for (int idx = tid; idx < ns * nb; idx += blockDim.x) {
       const int k = idx / nb, bin = idx - k * nb;
-      const unsigned cnt = h_cnt[idx];
+      unsigned cnt = 0;
+      for (int c = 0; c < copies; ++c) cnt += h_cnt[c * stride + idx];
       if (cnt == 0) continue;
       double dd, sp, sx, vr = 0.0;
       if (MIXED) {
-        dd = fixed_value(dd_lo, dd_hi, idx, fixed_inv);
-        sp = fixed_value(sp_lo, sp_hi, idx, fixed_inv);
-        sx = fixed_value(sx_lo, sx_hi, idx, fixed_inv);
-        if (VAR) vr = fixed_value(vr_lo, vr_hi, idx, fixed_inv);
+        long long vdd = 0, vsp = 0, vsx = 0, vvr = 0;
+        for (int c = 0; c < copies; ++c) {
+          const int j = c * stride + idx;
+          vdd += fixed_raw(dd_lo, dd_hi, j);
+          vsp += fixed_raw(sp_lo, sp_hi, j);
+          vsx += fixed_raw(sx_lo, sx_hi, j);
+          if (VAR) vvr += fixed_raw(vr_lo, vr_hi, j);
+        }
+        dd = (double)vdd * fixed_inv;
+        sp = (double)vsp * fixed_inv;
+        sx = (double)vsx * fixed_inv;
+        if (VAR) vr = (double)vvr * fixed_inv;
       } else {
         dd = dd_d[idx];
         sp = sp_d[idx];

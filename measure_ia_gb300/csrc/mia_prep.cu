@@ -22,6 +22,8 @@ struct PrepArgs {
   int axis[3];       // original axis of cell dimension k
   int n[3];
   double inv_s[3];
+  int nf[3];          // position (fine) grid
+  double inv_sf[3];
   int ellipticity;
 };
 
@@ -67,6 +69,15 @@ __device__ __forceinline__ int cell_of(const double c[3], const PrepArgs& A, int
   return (ci[2] * A.n[1] + ci[1]) * A.n[0] + ci[0];
 }
 
+__device__ __forceinline__ int fine_cell_of(const double c[3], const PrepArgs& A) {
+  int ci[3];
+  for (int k = 0; k < 3; ++k) {
+    int v = (int)floor(c[k] * A.inv_sf[k]);
+    ci[k] = v < 0 ? 0 : (v >= A.nf[k] ? A.nf[k] - 1 : v);
+  }
+  return (ci[2] * A.nf[1] + ci[1]) * A.nf[0] + ci[0];
+}
+
 // Region a cell lies in (cells refine the sub-box grid: n[k] is a multiple of n_sub).
 __device__ __forceinline__ int natural_region(const int ci[3], const PrepArgs& A) {
   if (A.n_sub <= 1) return 0;
@@ -81,8 +92,7 @@ __global__ void k_prep_positions(PrepArgs A, const double* __restrict__ pos, con
     double v[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
     if (!(in_box(v[0], A.L) && in_box(v[1], A.L) && in_box(v[2], A.L))) flag_range(w.status, i);
     double c[3] = {v[A.axis[0]], v[A.axis[1]], v[A.axis[2]]};
-    int ci[3];
-    int cell = cell_of(c, A, ci);
+    int cell = fine_cell_of(c, A);
     int lab = jk_label(v, A.L_sub, A.n_sub);
     w.pcell[i] = cell;
     w.plab[i] = lab;
@@ -357,6 +367,8 @@ cudaError_t launch_prep(const Plan& plan, const Params& P, const mia_catalog& ca
     A.axis[k] = plan.axis[k];
     A.n[k] = plan.n[k];
     A.inv_s[k] = (double)plan.n[k] / P.L;
+    A.nf[k] = plan.nf[k];
+    A.inv_sf[k] = (double)plan.nf[k] / P.L;
   }
   A.ellipticity = P.ellipticity;
   const int T = 256;
@@ -366,7 +378,7 @@ cudaError_t launch_prep(const Plan& plan, const Params& P, const mia_catalog& ca
                                                         w);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  if ((e = scan(w.pcount, plan.n_cells, w.pstart, w.tiles, nullptr, st)) != cudaSuccess) return e;
+  if ((e = scan(w.pcount, plan.n_fcells, w.pstart, w.tiles, nullptr, st)) != cudaSuccess) return e;
   if ((e = scan(w.scount, plan.n_cells, w.sstart, w.tiles, nullptr, st)) != cudaSuccess) return e;
   k_scatter_positions<<<grid_for(cat.n_pos, T), T, 0, st>>>(A, cat.position, cat.weight, cat.n_pos, w, mixed);
   k_scatter_shapes<<<grid_for(cat.n_shape, T), T, 0, st>>>(A, cat.position_shape, cat.axis_direction, cat.q,

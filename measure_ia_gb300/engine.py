@@ -54,7 +54,7 @@ class PairCounter:
 
     def __init__(self, kind, *, boxsize, r_bins, r_min, r_max, p_bins, los=2, l_subboxes=0, precision="fp64",
                  membership="tree", ellipticity="distortion", want_variance=False, volume=None, rp_cut=0.0,
-                 cell_size=0.0, shapes_per_unit=0, device=0):
+                 cell_size=0.0, shapes_per_unit=0, cell_refine=0, device=0):
         if kind not in ("w", "m"):
             raise ValueError(kind)
         self.kind = kind
@@ -84,6 +84,7 @@ class PairCounter:
         cfg.n_r, cfg.n_p = self.n_r, self.n_p
         cfg.n_qbreak, cfg.n_pbreak = len(self._qb), len(self._pb)
         cfg.shapes_per_unit = int(shapes_per_unit)
+        cfg.cell_refine = int(cell_refine)
         cfg.boxsize = float(boxsize)
         cfg.volume = float(boxsize ** 3 if volume is None else volume)
         cfg.r_min, cfg.r_max = float(r_min), float(r_max)
