@@ -163,6 +163,28 @@ MIA_API int mia_output_layout(const mia_config* cfg, mia_layout* layout);
 MIA_API int mia_measure(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat, void* workspace,
                 size_t workspace_bytes, const mia_result* res, void* stream);
 
+/* ---- batches: many catalogues, one binning, one persistent pair kernel ----
+   Many catalogues measured with the same configuration (e.g. mass or colour
+   subsamples of several snapshots) share one launch of the pair kernel: a
+   global work counter walks the work units of every catalogue, largest
+   workloads balance with the small ones.  Replaces repeated calls of the
+   backends above, one catalogue at a time (the reference's Pool.map covers
+   one catalogue, measure_w_box_jk.py:765-780).
+   mia_batch_prepare uploads tables and descriptors (synchronous, not
+   capturable); mia_batch_enqueue only enqueues memsets and kernels, so it can
+   be captured in a CUDA graph and replayed; mia_batch_status reads the
+   catalogues' error flags after the work completes.  results[i] receives
+   catalogue i's products in the layout of mia_output_layout. */
+MIA_API int mia_batch_workspace_size(const mia_config* cfg, int n, const int64_t* n_pos, const int64_t* n_shape,
+                                     size_t* bytes);
+MIA_API int mia_batch_prepare(mia_context* ctx, const mia_config* cfg, int n, const mia_catalog* cats,
+                              void* workspace, size_t workspace_bytes, const mia_result* results, void* stream);
+MIA_API int mia_batch_enqueue(mia_context* ctx, const mia_config* cfg, int n, const mia_catalog* cats,
+                              void* workspace, size_t workspace_bytes, const mia_result* results, void* stream);
+MIA_API int mia_batch_status(mia_context* ctx, int n, void* workspace, void* stream);
+MIA_API int mia_measure_batch(mia_context* ctx, const mia_config* cfg, int n, const mia_catalog* cats,
+                              void* workspace, size_t workspace_bytes, const mia_result* results, void* stream);
+
 /* Size of the library's own device scratch used by mia_measure_static. */
 #define MIA_STATIC_SCRATCH_BYTES (64ull * 1024ull * 1024ull)
 

@@ -20,7 +20,8 @@ MIA_DISTORTION, MIA_ELLIPTICITY = 0, 1
 MAX_BINS_R, MAX_BINS_P, MAX_BREAKS = 64, 128, 96
 
 EXPORTED = ("mia_create", "mia_destroy", "mia_last_error", "mia_version", "mia_workspace_size",
-            "mia_output_layout", "mia_measure", "mia_measure_static")
+            "mia_output_layout", "mia_measure", "mia_measure_static", "mia_batch_workspace_size",
+            "mia_batch_prepare", "mia_batch_enqueue", "mia_batch_status", "mia_measure_batch")
 STATIC_SCRATCH_BYTES = 64 * 1024 * 1024
 
 
@@ -90,6 +91,16 @@ def load(path=None):
     lib.mia_measure_static.argtypes = [C.c_void_p, C.POINTER(Config), C.POINTER(Catalog), C.POINTER(Result),
                                        C.c_void_p]
     lib.mia_measure_static.restype = C.c_int
+    lib.mia_batch_workspace_size.argtypes = [C.POINTER(Config), C.c_int, C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                             C.POINTER(C.c_size_t)]
+    lib.mia_batch_workspace_size.restype = C.c_int
+    for name in ("mia_batch_prepare", "mia_batch_enqueue", "mia_measure_batch"):
+        f = getattr(lib, name)
+        f.argtypes = [C.c_void_p, C.POINTER(Config), C.c_int, C.POINTER(Catalog), C.c_void_p, C.c_size_t,
+                      C.POINTER(Result), C.c_void_p]
+        f.restype = C.c_int
+    lib.mia_batch_status.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
+    lib.mia_batch_status.restype = C.c_int
     _lib = lib
     return lib
 

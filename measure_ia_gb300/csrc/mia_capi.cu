@@ -5,6 +5,7 @@
 #include <cstring>
 #include <mutex>
 #include <string>
+#include <vector>
 
 #include "mia_internal.cuh"
 
@@ -338,11 +339,7 @@ const char* mia_last_error(const mia_context* ctx) { return ctx ? ctx->err.c_str
 
 int mia_workspace_size(const mia_config* cfg, int64_t n_pos, int64_t n_shape, size_t* bytes) {
   if (!bytes) return MIA_ERR_ARG;
-  Plan p;
-  const char* why = nullptr;
-  if (!make_plan(cfg, n_pos, n_shape, &p, &why)) return MIA_ERR_ARG;
-  *bytes = p.total;
-  return MIA_OK;
+  return mia_batch_workspace_size(cfg, 1, &n_pos, &n_shape, bytes);
 }
 
 int mia_output_layout(const mia_config* cfg, mia_layout* lay) {
@@ -402,51 +399,71 @@ static int fail(mia_context* ctx, int code, const std::string& msg) {
     if (e_ != cudaSuccess) return fail(ctx, MIA_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
-int mia_measure(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat, void* workspace,
-                size_t workspace_bytes, const mia_result* res, void* stream) {
-  if (!ctx) return MIA_ERR_ARG;
-  if (!cfg || !cat || !res || !res->out || !res->npairs) return fail(ctx, MIA_ERR_ARG, "null argument");
-  if (cat->n_pos > 0 && (!cat->position || !cat->weight)) return fail(ctx, MIA_ERR_ARG, "missing position arrays");
-  if (cat->n_shape > 0 && (!cat->position_shape || !cat->axis_direction || !cat->q || !cat->weight_shape))
-    return fail(ctx, MIA_ERR_ARG, "missing shape arrays");
-  if (cat->n_pos < 1 || cat->n_shape < 1) return fail(ctx, MIA_ERR_ARG, "empty position or shape sample");
-  Plan plan;
-  const char* why = "";
-  if (!make_plan(cfg, cat->n_pos, cat->n_shape, &plan, &why)) return fail(ctx, MIA_ERR_ARG, why);
-  if (!workspace || workspace_bytes < plan.total || ((uintptr_t)workspace & 255))
-    return fail(ctx, MIA_ERR_WORKSPACE, "workspace missing, not 256-byte aligned, or smaller than mia_workspace_size()");
-  cudaStream_t st = static_cast<cudaStream_t>(stream);
-  MIA_CUDA(cudaSetDevice(ctx->device));
-  mia_layout lay;
-  mia_output_layout(cfg, &lay);
-  Work w;
-  bind_work(plan, workspace, &w);
-  bind_arrays(plan, workspace, cat->n_pos, cat->n_shape, &w);
+}  // extern "C"
 
-  // tables
-  static thread_local Tables host_tables;
-  int lut_base = 0;
-  build_tables(cfg, &host_tables, &lut_base);
-  MIA_CUDA(cudaMemcpyAsync(w.tables, &host_tables, sizeof(Tables), cudaMemcpyHostToDevice, st));
+namespace mia_batch {
 
-  // zero the counters and the outputs
-  unsigned char* b = static_cast<unsigned char*>(workspace);
-  MIA_CUDA(cudaMemsetAsync(b + plan.off_status, 0, sizeof(Status), st));
-  {
-    Status init;
-    memset(&init, 0, sizeof(init));
-    init.bad_index = ~0ULL;
-    static thread_local Status staged;
-    staged = init;
-    MIA_CUDA(cudaMemcpyAsync(w.status, &staged, sizeof(Status), cudaMemcpyHostToDevice, st));
+// Workspace of a batch: a header (work counter, dataset descriptors, prefix of
+// work-unit counts) followed by one dataset workspace per catalogue.
+struct BatchPlan {
+  std::vector<Plan> plans;
+  std::vector<size_t> off;
+  size_t ds_off = 0, prefix_off = 0, total = 0;
+};
+
+bool make_batch(const mia_config* cfg, int n, const mia_catalog* cats, BatchPlan* bp, std::string* why) {
+  if (n < 1) {
+    *why = "a batch needs at least one catalogue";
+    return false;
   }
-  MIA_CUDA(cudaMemsetAsync(b + plan.off_pcount, 0, plan.off_tiles - plan.off_pcount, st));
-  MIA_CUDA(cudaMemsetAsync(b + plan.off_reg, 0, (size_t)(plan.J + 1) * 32 + 64, st));
-  const size_t nb = (size_t)plan.nb, J1 = (size_t)plan.J + 1;
-  MIA_CUDA(cudaMemsetAsync(res->out, 0, sizeof(double) * (size_t)lay.total, st));
-  MIA_CUDA(cudaMemsetAsync(res->npairs, 0, sizeof(unsigned long long) * J1 * nb, st));
+  bp->plans.resize(n);
+  bp->off.resize(n);
+  size_t o = align256(sizeof(BatchHeader));
+  bp->ds_off = o;
+  o = align256(o + sizeof(Dataset) * (size_t)n);
+  bp->prefix_off = o;
+  o = align256(o + sizeof(unsigned long long) * (size_t)(n + 1));
+  for (int i = 0; i < n; ++i) {
+    const mia_catalog* c = &cats[i];
+    if (c->n_pos < 1 || c->n_shape < 1) {
+      *why = "empty position or shape sample";
+      return false;
+    }
+    if (!c->position || !c->weight || !c->position_shape || !c->axis_direction || !c->q || !c->weight_shape) {
+      *why = "missing catalogue arrays";
+      return false;
+    }
+    const char* w = "";
+    if (!make_plan(cfg, c->n_pos, c->n_shape, &bp->plans[i], &w)) {
+      *why = w;
+      return false;
+    }
+    bp->off[i] = o;
+    o = align256(o + bp->plans[i].total);
+  }
+  bp->total = o;
+  return true;
+}
 
-  Params P;
+size_t batch_bytes_for_sizes(const mia_config* cfg, int n, const int64_t* n_pos, const int64_t* n_shape, bool* ok) {
+  size_t o = align256(sizeof(BatchHeader));
+  o = align256(o + sizeof(Dataset) * (size_t)n);
+  o = align256(o + sizeof(unsigned long long) * (size_t)(n + 1));
+  *ok = true;
+  for (int i = 0; i < n; ++i) {
+    Plan p;
+    const char* w = "";
+    if (!make_plan(cfg, n_pos[i], n_shape[i], &p, &w)) {
+      *ok = false;
+      return 0;
+    }
+    o = align256(o + p.total);
+  }
+  return o;
+}
+
+void make_params(const mia_config* cfg, const Plan& plan, const Tables& T, int lut_base, Params* out) {
+  Params& P = *out;
   memset(&P, 0, sizeof(P));
   P.kind = cfg->kind;
   P.membership = cfg->membership;
@@ -491,39 +508,178 @@ int mia_measure(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat,
   P.p_guard = (float)fmax(1.0 / 32768.0, cfg->n_p * 4e-6);
   P.c_guard = 1e-12f;
   P.wrap_guard = (float)(cfg->boxsize * 1e-5);
-  {
-    double pm = fmax(fabs(p0), fabs(p1));
-    P.los_cut = cfg->kind == MIA_KIND_W ? f32_up(pm * (1.0 + 1e-5) + 1e-30) : INFINITY;
-    P.zwin = f32_up(plan.range_los * (1.0 + 1e-5) + cfg->boxsize * 5e-7);
-    const int nq = cfg->n_qbreak;
-    P.q_cut = (nq > 0 && cfg->q_bin[nq] < 0) ? host_tables.q_hi32[nq - 1] : INFINITY;
-  }
+  const double pm = fmax(fabs(p0), fabs(p1));
+  P.los_cut = cfg->kind == MIA_KIND_W ? f32_up(pm * (1.0 + 1e-5) + 1e-30) : INFINITY;
+  P.zwin = f32_up(plan.range_los * (1.0 + 1e-5) + cfg->boxsize * 5e-7);
+  const int nq = cfg->n_qbreak;
+  P.q_cut = (nq > 0 && cfg->q_bin[nq] < 0) ? T.q_hi32[nq - 1] : INFINITY;
   P.edge_capacity = plan.edge_capacity;
+}
 
-  Out o;
-  o.dd = res->out + lay.dd;
-  o.splus = res->out + lay.splus;
-  o.scross = res->out + lay.scross;
-  o.variance = res->out + lay.variance;
-  o.npairs = res->npairs;
+void make_dataset(const Plan& plan, void* base, const mia_catalog& cat, const mia_result& res, const mia_layout& lay,
+                  Dataset* d) {
+  bind_work(plan, base, &d->w);
+  bind_arrays(plan, base, cat.n_pos, cat.n_shape, &d->w);
+  d->w.edge_capacity = plan.edge_capacity;
+  d->o.dd = res.out + lay.dd;
+  d->o.splus = res.out + lay.splus;
+  d->o.scross = res.out + lay.scross;
+  d->o.variance = res.out + lay.variance;
+  d->o.npairs = res.npairs;
+}
 
-  MIA_CUDA(launch_prep(plan, P, *cat, w, st));
-  MIA_CUDA(launch_pairs(plan, P, w, o, st, ctx->num_sms));
-  MIA_CUDA(launch_post(P, w, lay, res->out, cfg->volume, cat->n_pos, cat->n_shape, st));
+__global__ void k_batch_status(const Dataset* ds, int n, BatchHeader* h) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  unsigned flags = 0;
+  int first = -1;
+  unsigned long long bad = ~0ULL;
+  for (int i = 0; i < n; ++i) {
+    const Status* st = ds[i].w.status;
+    flags |= st->flags;
+    if ((st->flags & kStatusRange) && first < 0) {
+      first = i;
+      bad = st->bad_index;
+    }
+  }
+  h->flags = flags;
+  h->first_bad = first;
+  h->bad_index = bad;
+}
 
-  static thread_local Status hs;
-  MIA_CUDA(cudaMemcpyAsync(&hs, w.status, sizeof(Status), cudaMemcpyDeviceToHost, st));
+}  // namespace mia_batch
+
+using namespace mia_batch;
+
+extern "C" {
+
+int mia_batch_workspace_size(const mia_config* cfg, int n, const int64_t* n_pos, const int64_t* n_shape,
+                             size_t* bytes) {
+  if (!cfg || !n_pos || !n_shape || !bytes || n < 1) return MIA_ERR_ARG;
+  bool ok = false;
+  size_t b = batch_bytes_for_sizes(cfg, n, n_pos, n_shape, &ok);
+  if (!ok) return MIA_ERR_ARG;
+  *bytes = b;
+  return MIA_OK;
+}
+
+int mia_batch_prepare(mia_context* ctx, const mia_config* cfg, int n, const mia_catalog* cats, void* workspace,
+                      size_t workspace_bytes, const mia_result* results, void* stream) {
+  if (!ctx) return MIA_ERR_ARG;
+  if (!cfg || !cats || !results) return fail(ctx, MIA_ERR_ARG, "null argument");
+  BatchPlan bp;
+  std::string why;
+  if (!make_batch(cfg, n, cats, &bp, &why)) return fail(ctx, MIA_ERR_ARG, why);
+  if (!workspace || workspace_bytes < bp.total || ((uintptr_t)workspace & 255))
+    return fail(ctx, MIA_ERR_WORKSPACE, "workspace missing, not 256-byte aligned, or smaller than the size query");
+  for (int i = 0; i < n; ++i)
+    if (!results[i].out || !results[i].npairs) return fail(ctx, MIA_ERR_ARG, "null result buffer");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  MIA_CUDA(cudaSetDevice(ctx->device));
+  mia_layout lay;
+  mia_output_layout(cfg, &lay);
+  unsigned char* b = static_cast<unsigned char*>(workspace);
+  static thread_local Tables host_tables;
+  static thread_local std::vector<Dataset> host_ds;
+  int lut_base = 0;
+  build_tables(cfg, &host_tables, &lut_base);
+  host_ds.resize(n);
+  for (int i = 0; i < n; ++i) {
+    make_dataset(bp.plans[i], b + bp.off[i], cats[i], results[i], lay, &host_ds[i]);
+    MIA_CUDA(cudaMemcpyAsync(host_ds[i].w.tables, &host_tables, sizeof(Tables), cudaMemcpyHostToDevice, st));
+  }
+  MIA_CUDA(cudaMemcpyAsync(b + bp.ds_off, host_ds.data(), sizeof(Dataset) * (size_t)n, cudaMemcpyHostToDevice, st));
   MIA_CUDA(cudaStreamSynchronize(st));
-  if (hs.flags & kStatusRange) {
-    char buf[160];
-    snprintf(buf, sizeof(buf), "coordinate outside [0, boxsize) or not finite (first offending index %llu)",
-             (unsigned long long)hs.bad_index);
+  ctx->err.clear();
+  return MIA_OK;
+}
+
+int mia_batch_enqueue(mia_context* ctx, const mia_config* cfg, int n, const mia_catalog* cats, void* workspace,
+                      size_t workspace_bytes, const mia_result* results, void* stream) {
+  if (!ctx) return MIA_ERR_ARG;
+  if (!cfg || !cats || !results) return fail(ctx, MIA_ERR_ARG, "null argument");
+  BatchPlan bp;
+  std::string why;
+  if (!make_batch(cfg, n, cats, &bp, &why)) return fail(ctx, MIA_ERR_ARG, why);
+  if (!workspace || workspace_bytes < bp.total || ((uintptr_t)workspace & 255))
+    return fail(ctx, MIA_ERR_WORKSPACE, "workspace missing, not 256-byte aligned, or smaller than the size query");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  mia_layout lay;
+  mia_output_layout(cfg, &lay);
+  unsigned char* b = static_cast<unsigned char*>(workspace);
+  int lut_base = 0;
+  static thread_local Tables tq;  // host copy: only the guard values enter the launch parameters
+  build_tables(cfg, &tq, &lut_base);
+  Params P;
+  make_params(cfg, bp.plans[0], tq, lut_base, &P);
+  BatchHeader* hdr = reinterpret_cast<BatchHeader*>(b);
+  const Dataset* ds_dev = reinterpret_cast<const Dataset*>(b + bp.ds_off);
+  unsigned long long* prefix = reinterpret_cast<unsigned long long*>(b + bp.prefix_off);
+  MIA_CUDA(cudaMemsetAsync(hdr, 0, sizeof(BatchHeader), st));
+  const size_t nb = (size_t)bp.plans[0].nb, J1 = (size_t)bp.plans[0].J + 1;
+  for (int i = 0; i < n; ++i) {
+    const Plan& pl = bp.plans[i];
+    unsigned char* base = b + bp.off[i];
+    Dataset d;
+    make_dataset(pl, base, cats[i], results[i], lay, &d);
+    MIA_CUDA(cudaMemsetAsync(base + pl.off_status, 0, sizeof(Status), st));
+    MIA_CUDA(cudaMemsetAsync(&d.w.status->bad_index, 0xFF, sizeof(unsigned long long), st));
+    MIA_CUDA(cudaMemsetAsync(base + pl.off_pcount, 0, pl.off_tiles - pl.off_pcount, st));
+    MIA_CUDA(cudaMemsetAsync(base + pl.off_reg, 0, (size_t)(pl.J + 1) * 32 + 64, st));
+    MIA_CUDA(cudaMemsetAsync(results[i].out, 0, sizeof(double) * (size_t)lay.total, st));
+    MIA_CUDA(cudaMemsetAsync(results[i].npairs, 0, sizeof(unsigned long long) * J1 * nb, st));
+    MIA_CUDA(launch_prep(pl, P, cats[i], d.w, st));
+  }
+  MIA_CUDA(launch_batch_prefix(ds_dev, n, prefix, st));
+  MIA_CUDA(launch_pairs(bp.plans[0], P, ds_dev, n, prefix, &hdr->wu_next, st, ctx->num_sms));
+  for (int i = 0; i < n; ++i) {
+    Dataset d;
+    make_dataset(bp.plans[i], b + bp.off[i], cats[i], results[i], lay, &d);
+    if (P.precision == MIA_MIXED) MIA_CUDA(launch_edge_retest(P, d.w, d.o, st, ctx->num_sms));
+    MIA_CUDA(launch_post(P, d.w, lay, results[i].out, cfg->volume, cats[i].n_pos, cats[i].n_shape, st));
+  }
+  ctx->err.clear();
+  return MIA_OK;
+}
+
+int mia_batch_status(mia_context* ctx, int n, void* workspace, void* stream) {
+  if (!ctx) return MIA_ERR_ARG;
+  if (!workspace || n < 1) return fail(ctx, MIA_ERR_ARG, "null argument");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  unsigned char* b = static_cast<unsigned char*>(workspace);
+  const Dataset* ds_dev = reinterpret_cast<const Dataset*>(b + align256(sizeof(BatchHeader)));
+  BatchHeader* hdr = reinterpret_cast<BatchHeader*>(b);
+  k_batch_status<<<1, 32, 0, st>>>(ds_dev, n, hdr);
+  MIA_CUDA(cudaGetLastError());
+  static thread_local BatchHeader hh;
+  MIA_CUDA(cudaMemcpyAsync(&hh, hdr, sizeof(BatchHeader), cudaMemcpyDeviceToHost, st));
+  MIA_CUDA(cudaStreamSynchronize(st));
+  if (hh.flags & kStatusRange) {
+    char buf[200];
+    snprintf(buf, sizeof(buf),
+             "coordinate outside [0, boxsize) or not finite (catalogue %d, first offending index %llu)",
+             hh.first_bad, (unsigned long long)hh.bad_index);
     return fail(ctx, MIA_ERR_RANGE, buf);
   }
-  if (hs.flags & kStatusOverflow)
+  if (hh.flags & kStatusOverflow)
     return fail(ctx, MIA_ERR_OVERFLOW, "edge re-test queue overflow; rerun in the FP64 form");
   ctx->err.clear();
   return MIA_OK;
+}
+
+int mia_measure_batch(mia_context* ctx, const mia_config* cfg, int n, const mia_catalog* cats, void* workspace,
+                      size_t workspace_bytes, const mia_result* results, void* stream) {
+  int rc = mia_batch_prepare(ctx, cfg, n, cats, workspace, workspace_bytes, results, stream);
+  if (rc != MIA_OK) return rc;
+  rc = mia_batch_enqueue(ctx, cfg, n, cats, workspace, workspace_bytes, results, stream);
+  if (rc != MIA_OK) return rc;
+  return mia_batch_status(ctx, n, workspace, stream);
+}
+
+int mia_measure(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat, void* workspace,
+                size_t workspace_bytes, const mia_result* res, void* stream) {
+  if (!ctx) return MIA_ERR_ARG;
+  if (!cfg || !cat || !res || !res->out || !res->npairs) return fail(ctx, MIA_ERR_ARG, "null argument");
+  return mia_measure_batch(ctx, cfg, 1, cat, workspace, workspace_bytes, res, stream);
 }
 
 // ---- entry point without device allocation ---------------------------------
@@ -549,15 +705,14 @@ int mia_measure_static(mia_context* ctx, const mia_config* cfg, const mia_catalo
                        void* stream) {
   if (!ctx) return MIA_ERR_ARG;
   if (!cfg || !cat || !res) return fail(ctx, MIA_ERR_ARG, "null argument");
-  Plan plan;
-  const char* why = "";
-  if (!make_plan(cfg, cat->n_pos, cat->n_shape, &plan, &why)) return fail(ctx, MIA_ERR_ARG, why);
-  if (plan.total > (size_t)MIA_STATIC_SCRATCH_BYTES) {
+  size_t need = 0;
+  if (mia_workspace_size(cfg, cat->n_pos, cat->n_shape, &need) != MIA_OK) return fail(ctx, MIA_ERR_ARG, "invalid configuration");
+  if (need > (size_t)MIA_STATIC_SCRATCH_BYTES) {
     char buf[256];
     snprintf(buf, sizeof(buf),
              "mia_measure_static: this measurement needs %zu bytes of scratch but the static scratch holds %llu; "
              "use mia_measure with a caller-provided workspace",
-             plan.total, (unsigned long long)MIA_STATIC_SCRATCH_BYTES);
+             need, (unsigned long long)MIA_STATIC_SCRATCH_BYTES);
     return fail(ctx, MIA_ERR_WORKSPACE, buf);
   }
   if (ctx->device < 0 || ctx->device >= kMaxStaticDevices)

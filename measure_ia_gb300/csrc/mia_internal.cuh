@@ -159,6 +159,7 @@ struct Work {
   WorkUnit* wu;
   RegionStats reg;
   int2* edges;
+  long long edge_capacity;
 };
 
 // Output pointers (into the caller's result buffers).
@@ -168,6 +169,21 @@ struct Out {
   double* scross;    // nb
   double* variance;  // nb
   unsigned long long* npairs;   // (1+J) * nb
+};
+
+// One dataset of a batch: its workspace and its outputs.
+struct Dataset {
+  Work w;
+  Out o;
+};
+
+// Batch header at the start of a (batch) workspace.
+struct BatchHeader {
+  unsigned long long wu_next;   // global work counter of the pair kernel
+  unsigned flags;               // OR of the datasets' status flags (after mia_batch_status)
+  int first_bad;                // first dataset with a range error
+  unsigned long long bad_index;
+  unsigned long long pad[5];
 };
 
 // --------------------------------------------------------------------------
@@ -268,8 +284,11 @@ void bind_work(const Plan& plan, void* base, Work* w);
 
 // Stage launchers (mia_prep.cu, mia_pairs.cu, mia_post.cu)
 cudaError_t launch_prep(const Plan& plan, const Params& P, const mia_catalog& cat, const Work& w, cudaStream_t st);
-cudaError_t launch_pairs(const Plan& plan, const Params& P, const Work& w, const Out& o, cudaStream_t st,
+cudaError_t launch_pairs(const Plan& plan, const Params& P, const Dataset* ds_dev, int n_ds,
+                         const unsigned long long* wu_prefix, unsigned long long* wu_next, cudaStream_t st,
                          int num_sms);
+cudaError_t launch_edge_retest(const Params& P, const Work& w, const Out& o, cudaStream_t st, int num_sms);
+cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, unsigned long long* wu_prefix, cudaStream_t st);
 cudaError_t launch_post(const Params& P, const Work& w, const mia_layout& lay, double* out, double volume,
                         long long n_pos, long long n_shape, cudaStream_t st);
 

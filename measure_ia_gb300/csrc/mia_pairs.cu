@@ -314,7 +314,7 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
   if (crs * crs < P.c_guard * qp) edge = true;
   if (edge) {
     const unsigned long long k = atomicAdd(&w.status->edge_count, 1ULL);
-    if (k < (unsigned long long)P.edge_capacity) w.edges[k] = make_int2(I[i], p.idx);
+    if (k < (unsigned long long)w.edge_capacity) w.edges[k] = make_int2(I[i], p.idx);
     else atomicOr(&w.status->flags, kStatusOverflow);
     return;
   }
@@ -353,7 +353,9 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
 // ---- the persistent pair kernel ----------------------------------------------
 
 template <int MIXED, int VAR, int KIND, int FULL>
-__global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int K) {
+__global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __restrict__ ds, int n_ds,
+                                                     const unsigned long long* __restrict__ wu_prefix,
+                                                     unsigned long long* wu_next, int K) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x;
   const int nb = P.nb;
@@ -368,15 +370,19 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
   const int KB = K * nb;
 
   __shared__ int s_wu;
+  __shared__ int s_ds;
+  __shared__ Dataset s_data;        // the current unit's dataset (workspace and outputs)
+  __shared__ double s_twoR, s_fixed_inv;
+  __shared__ float s_fixed_scale;
   __shared__ int s_nslots;
   __shared__ int s_copies;
   __shared__ int s_stride;
   __shared__ int s_scan[32];
   __shared__ int s_total;
 
-  // tables -> shared
+  // tables -> shared (the same binning for every dataset of a batch)
   {
-    const Tables& G = *w.tables;
+    const Tables& G = *ds[0].w.tables;
     for (int i = tid; i < MIA_MAX_BREAKS; i += blockDim.x) {
       T.q_key[i] = G.q_key[i];
       T.q_lo32[i] = G.q_lo32[i];
@@ -390,22 +396,12 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
     if (MIXED)
       for (int i = tid; i < kLut; i += blockDim.x) T.lut32[i] = G.lut32[i];
     for (int i = tid; i <= P.J; i += blockDim.x) slot_of[i] = -1;
-    if (tid == 0) s_nslots = 0;
+    if (tid == 0) {
+      s_nslots = 0;
+      s_ds = -1;
+    }
   }
-  const double twoR = 2.0 * (w.reg.s1[P.J] / w.reg.s2[P.J]);
-  const unsigned long long n_wu = w.status->n_wu;
-  // fixed-point scale 2^S with |term| * 2^S <= 2^30 for every pair term
-  float fixed_scale = 1.0f;
-  double fixed_inv = 1.0;
-  if (MIXED) {
-    double m = __longlong_as_double((long long)w.status->maxw_bits) *
-               __longlong_as_double((long long)w.status->maxws_bits);
-    if (!(m > 0.0) || !(m < 1e300)) m = 1.0;
-    int S = (int)floor(log2(1073741824.0 / m));
-    S = S > 40 ? 40 : (S < -60 ? -60 : S);
-    fixed_scale = ldexpf(1.0f, S);
-    fixed_inv = ldexp(1.0, -S);
-  }
+  const unsigned long long n_wu_all = wu_prefix[n_ds];
   __syncthreads();
 
   // views of the per-bin state
@@ -442,13 +438,44 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
   const double r2proj = P.range_proj * P.range_proj;
   const double r2los = P.range_los * P.range_los;
 
-  unsigned long long my_binned = 0;
-
   while (true) {
-    if (tid == 0) s_wu = (int)atomicAdd(&w.status->wu_next, 1ULL);
+    if (tid == 0) {
+      const unsigned long long g = atomicAdd(wu_next, 1ULL);
+      if (g >= n_wu_all) {
+        s_wu = -1;
+      } else {
+        // dataset of global unit g: largest d with wu_prefix[d] <= g
+        int lo = 0, hi = n_ds - 1;
+        while (lo < hi) {
+          const int mid = (lo + hi + 1) >> 1;
+          if (wu_prefix[mid] <= g) lo = mid; else hi = mid - 1;
+        }
+        s_wu = (int)(g - wu_prefix[lo]);
+        if (lo != s_ds) {
+          s_ds = lo;
+          s_data = ds[lo];
+          const Work& wd = ds[lo].w;
+          s_twoR = 2.0 * (wd.reg.s1[P.J] / wd.reg.s2[P.J]);
+          // fixed-point scale 2^S with |term| * 2^S <= 2^30 for every pair term of the dataset
+          double m = __longlong_as_double((long long)wd.status->maxw_bits) *
+                     __longlong_as_double((long long)wd.status->maxws_bits);
+          if (!(m > 0.0) || !(m < 1e300)) m = 1.0;
+          int S = (int)floor(log2(1073741824.0 / m));
+          S = S > 40 ? 40 : (S < -60 ? -60 : S);
+          s_fixed_scale = ldexpf(1.0f, S);
+          s_fixed_inv = ldexp(1.0, -S);
+        }
+      }
+    }
     __syncthreads();
     const int wi = s_wu;
-    if ((unsigned long long)wi >= n_wu) break;
+    if (wi < 0) break;
+    const Work& w = s_data.w;
+    const Out& o = s_data.o;
+    const double twoR = s_twoR;
+    const float fixed_scale = s_fixed_scale;
+    const double fixed_inv = s_fixed_inv;
+    unsigned long long my_binned = 0;
     const WorkUnit u = w.wu[wi];
     int c[3];
     {
@@ -801,17 +828,17 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, Work w, Out o, int
         }
       }
     }
+    // binned-pair total of the dataset, for the throughput figure
+    for (int of = 16; of > 0; of >>= 1) my_binned += __shfl_down_sync(0xffffffffu, my_binned, of);
+    if ((tid & 31) == 0 && my_binned) atomicAdd(&w.status->binned, my_binned);
     __syncthreads();
   }
-  // binned-pair total for the throughput figure
-  for (int of = 16; of > 0; of >>= 1) my_binned += __shfl_down_sync(0xffffffffu, my_binned, of);
-  if ((tid & 31) == 0 && my_binned) atomicAdd(&w.status->binned, my_binned);
 }
 
 // FP64 re-test of the pairs the mixed kernel could not decide in FP32.
 __global__ void k_edge_retest(Params P, Work w, Out o) {
   const unsigned long long n_raw = w.status->edge_count;
-  const unsigned long long n = n_raw < (unsigned long long)P.edge_capacity ? n_raw : (unsigned long long)P.edge_capacity;
+  const unsigned long long n = n_raw < (unsigned long long)w.edge_capacity ? n_raw : (unsigned long long)w.edge_capacity;
   const double twoR = 2.0 * (w.reg.s1[P.J] / w.reg.s2[P.J]);
   unsigned long long binned = 0;
   for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
@@ -833,7 +860,8 @@ __global__ void k_edge_retest(Params P, Work w, Out o) {
 }
 
 template <int MIXED, int VAR, int KIND, int FULL>
-cudaError_t launch_one(const Params& P, const Work& w, const Out& o, cudaStream_t st, int num_sms, int K) {
+cudaError_t launch_one(const Params& P, const Dataset* ds, int n_ds, const unsigned long long* wu_prefix,
+                       unsigned long long* wu_next, cudaStream_t st, int num_sms, int K) {
   SmemLayout SL = smem_layout(P.J, P.shapes_per_unit, K, P.nb, MIXED, VAR);
   size_t smem = SL.total;
   auto kern = k_pairs<MIXED, VAR, KIND, FULL>;
@@ -843,18 +871,30 @@ cudaError_t launch_one(const Params& P, const Work& w, const Out& o, cudaStream_
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  kern<<<num_sms * per_sm, kThreads, smem, st>>>(P, w, o, K);
+  kern<<<num_sms * per_sm, kThreads, smem, st>>>(P, ds, n_ds, wu_prefix, wu_next, K);
   return cudaGetLastError();
 }
 
 template <int MIXED, int VAR>
-cudaError_t launch_kind(const Params& P, const Work& w, const Out& o, cudaStream_t st, int num_sms, int K) {
+cudaError_t launch_kind(const Params& P, const Dataset* ds, int n_ds, const unsigned long long* wu_prefix,
+                        unsigned long long* wu_next, cudaStream_t st, int num_sms, int K) {
   const bool full = P.full[0] || P.full[1] || P.full[2];
   if (P.kind == MIA_KIND_W)
-    return full ? launch_one<MIXED, VAR, MIA_KIND_W, 1>(P, w, o, st, num_sms, K)
-                : launch_one<MIXED, VAR, MIA_KIND_W, 0>(P, w, o, st, num_sms, K);
-  return full ? launch_one<MIXED, VAR, MIA_KIND_MULTIPOLES, 1>(P, w, o, st, num_sms, K)
-              : launch_one<MIXED, VAR, MIA_KIND_MULTIPOLES, 0>(P, w, o, st, num_sms, K);
+    return full ? launch_one<MIXED, VAR, MIA_KIND_W, 1>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms, K)
+                : launch_one<MIXED, VAR, MIA_KIND_W, 0>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms, K);
+  return full ? launch_one<MIXED, VAR, MIA_KIND_MULTIPOLES, 1>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms, K)
+              : launch_one<MIXED, VAR, MIA_KIND_MULTIPOLES, 0>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms, K);
+}
+
+__global__ void k_batch_prefix(const Dataset* ds, int n, unsigned long long* prefix) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    unsigned long long acc = 0;
+    for (int i = 0; i < n; ++i) {
+      prefix[i] = acc;
+      acc += ds[i].w.status->n_wu;
+    }
+    prefix[n] = acc;
+  }
 }
 
 }  // namespace
@@ -863,7 +903,18 @@ size_t pair_smem_bytes(int J, int spu, int K, int nb, int mixed, int var) {
   return smem_layout(J, spu, K, nb, mixed, var).total;
 }
 
-cudaError_t launch_pairs(const Plan& plan, const Params& P, const Work& w, const Out& o, cudaStream_t st,
+cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, unsigned long long* wu_prefix, cudaStream_t st) {
+  k_batch_prefix<<<1, 32, 0, st>>>(ds_dev, n_ds, wu_prefix);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_edge_retest(const Params& P, const Work& w, const Out& o, cudaStream_t st, int num_sms) {
+  k_edge_retest<<<num_sms * 4, 256, 0, st>>>(P, w, o);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pairs(const Plan& plan, const Params& P, const Dataset* ds_dev, int n_ds,
+                         const unsigned long long* wu_prefix, unsigned long long* wu_next, cudaStream_t st,
                          int num_sms) {
   // slots: as many regions as a neighbourhood can touch, within the shared-memory budget
   int K = plan.J > 0 ? kMaxSlots : 1;
@@ -886,16 +937,11 @@ cudaError_t launch_pairs(const Plan& plan, const Params& P, const Work& w, const
                         budget)
       --K;
   }
-  cudaError_t e;
-  if (P.precision == MIA_MIXED) {
-    e = P.want_variance ? launch_kind<1, 1>(P, w, o, st, num_sms, K) : launch_kind<1, 0>(P, w, o, st, num_sms, K);
-    if (e != cudaSuccess) return e;
-    k_edge_retest<<<num_sms * 4, 256, 0, st>>>(P, w, o);
-    e = cudaGetLastError();
-  } else {
-    e = P.want_variance ? launch_kind<0, 1>(P, w, o, st, num_sms, K) : launch_kind<0, 0>(P, w, o, st, num_sms, K);
-  }
-  return e;
+  if (P.precision == MIA_MIXED)
+    return P.want_variance ? launch_kind<1, 1>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms, K)
+                           : launch_kind<1, 0>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms, K);
+  return P.want_variance ? launch_kind<0, 1>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms, K)
+                         : launch_kind<0, 0>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms, K);
 }
 
 }  // namespace mia

@@ -57,6 +57,11 @@ class PairCounter:
                  cell_size=0.0, shapes_per_unit=0, cell_refine=0, device=0):
         if kind not in ("w", "m"):
             raise ValueError(kind)
+        self._args = dict(boxsize=boxsize, r_bins=r_bins, r_min=r_min, r_max=r_max, p_bins=p_bins, los=los,
+                          l_subboxes=l_subboxes, precision=precision, membership=membership, ellipticity=ellipticity,
+                          want_variance=want_variance, volume=volume, rp_cut=rp_cut, device=device)
+        self.knobs = dict(cell_size=cell_size, cell_refine=cell_refine, shapes_per_unit=shapes_per_unit)
+        self.membership = membership
         self.kind = kind
         self.device = device
         self.n_r = len(r_bins) - 1
@@ -164,9 +169,6 @@ class PairCounter:
         lay = self.layout
         nb, nr, npp, J = self.n_r * self.n_p, self.n_r, self.n_p, self.J
 
-        def grid(off, k=1):
-            return o[off:off + k * nb].reshape((k, nr, npp) if k > 1 or J else (nr, npp)) if k else None
-
         a = {}
         a["DD_all"] = o[lay.dd:lay.dd + (1 + J) * nb].reshape(1 + J, nr, npp)
         a["Splus_all"] = o[lay.splus:lay.splus + (1 + J) * nb].reshape(1 + J, nr, npp)
@@ -195,6 +197,43 @@ class PairCounter:
                      work_units=int(st[4]))
         return Measurement(self.kind, nr, npp, J, a, cnt, stats)
 
+    def with_knobs(self, **knobs):
+        """The same measurement with other launch knobs (identical results)."""
+        return PairCounter(self.kind, **self._args, **{**self.knobs, **knobs})
+
+    def search_ranges(self):
+        r = max(float(self._args["r_max"]), float(self._r_edges[-1]))
+        if self.kind == "w":
+            return r, max(abs(float(self._p_edges[0])), abs(float(self._p_edges[-1])))
+        return r, r
+
+    def tuned(self, dcat, cache=True, log=None):
+        """A counter with autotuned launch knobs for this catalogue (see autotune.py)."""
+        import torch
+        from . import autotune
+        rp, rl = self.search_ranges()
+        key = None
+        if cache:
+            key = autotune.workload_key(self.kind, self.precision, dcat["Position"].shape[0],
+                                        dcat["Position_shape_sample"].shape[0], float(self._args["boxsize"]),
+                                        self.n_r, self.n_p, rp, rl, int(self._args["l_subboxes"]), self.membership,
+                                        torch.cuda.get_device_name(self.device))
+        best = autotune.tune(lambda **k: self.with_knobs(**k), dcat, rp, key=key, log=log)
+        return self.with_knobs(cell_size=best["cell_size"], cell_refine=best["cell_refine"],
+                               shapes_per_unit=best["shapes_per_unit"])
+
+    def to_device(self, cat):
+        import torch
+        dev = torch.device("cuda", self.device)
+        out = {}
+        for k in ("Position", "weight", "Position_shape_sample", "Axis_Direction", "q", "weight_shape_sample"):
+            v = cat[k]
+            if isinstance(v, torch.Tensor):
+                out[k] = v.to(device=dev, dtype=torch.float64).contiguous()
+            else:
+                out[k] = torch.from_numpy(np.ascontiguousarray(v, dtype=np.float64)).to(dev)
+        return out
+
     def measure(self, cat, stream=None):
         """Convenience: copy host arrays (numpy) or use device tensors, run, fetch."""
         import torch
@@ -210,3 +249,95 @@ class PairCounter:
         bufs = self.allocate(dcat["Position"].shape[0], dcat["Position_shape_sample"].shape[0])
         self.run(dcat, bufs, stream)
         return self.fetch(bufs)
+
+
+class BatchCounter:
+    """Many catalogues measured with one configuration in one persistent
+    pair-kernel launch (``mia_batch_*``).  ``prepare`` uploads tables once;
+    ``enqueue`` only enqueues memsets and kernels, so ``capture`` can record it
+    in a CUDA graph that ``replay`` re-runs."""
+
+    def __init__(self, counter: PairCounter, dcats):
+        import torch
+        self.pc = counter
+        self.dcats = list(dcats)
+        self.n = len(self.dcats)
+        lib = L.load()
+        n_pos = (C.c_int64 * self.n)(*[d["Position"].shape[0] for d in self.dcats])
+        n_shape = (C.c_int64 * self.n)(*[d["Position_shape_sample"].shape[0] for d in self.dcats])
+        nbytes = C.c_size_t()
+        rc = lib.mia_batch_workspace_size(C.byref(counter.cfg), self.n, n_pos, n_shape, C.byref(nbytes))
+        if rc != L.MIA_OK:
+            raise L.MiaError(rc, "invalid batch configuration")
+        dev = torch.device("cuda", counter.device)
+        self.ws = torch.empty(nbytes.value, dtype=torch.uint8, device=dev)
+        self.outs = [torch.empty(counter.layout.total, dtype=torch.float64, device=dev) for _ in range(self.n)]
+        self.cnts = [torch.empty((1 + counter.J) * counter.n_r * counter.n_p, dtype=torch.int64, device=dev)
+                     for _ in range(self.n)]
+        self.cats = (L.Catalog * self.n)()
+        self.res = (L.Result * self.n)()
+        for i, d in enumerate(self.dcats):
+            c = self.cats[i]
+            c.position, c.weight = d["Position"].data_ptr(), d["weight"].data_ptr()
+            c.position_shape = d["Position_shape_sample"].data_ptr()
+            c.axis_direction, c.q = d["Axis_Direction"].data_ptr(), d["q"].data_ptr()
+            c.weight_shape = d["weight_shape_sample"].data_ptr()
+            c.n_pos, c.n_shape = d["Position"].shape[0], d["Position_shape_sample"].shape[0]
+            self.res[i].out = self.outs[i].data_ptr()
+            self.res[i].npairs = self.cnts[i].data_ptr()
+        self.graph = None
+
+    def _call(self, name, stream):
+        import torch
+        lib = L.load()
+        ctx = context(self.pc.device)
+        if stream is None:
+            stream = torch.cuda.current_stream(self.pc.device)
+        rc = getattr(lib, name)(ctx, C.byref(self.pc.cfg), self.n, self.cats, C.c_void_p(self.ws.data_ptr()),
+                                self.ws.numel(), self.res, C.c_void_p(stream.cuda_stream))
+        if rc != L.MIA_OK:
+            raise L.MiaError(rc, lib.mia_last_error(ctx).decode())
+
+    def prepare(self, stream=None):
+        self._call("mia_batch_prepare", stream)
+
+    def enqueue(self, stream=None):
+        self._call("mia_batch_enqueue", stream)
+
+    def status(self, stream=None):
+        import torch
+        lib = L.load()
+        ctx = context(self.pc.device)
+        if stream is None:
+            stream = torch.cuda.current_stream(self.pc.device)
+        rc = lib.mia_batch_status(ctx, self.n, C.c_void_p(self.ws.data_ptr()), C.c_void_p(stream.cuda_stream))
+        if rc != L.MIA_OK:
+            msg = lib.mia_last_error(ctx).decode()
+            if rc in (L.MIA_ERR_ARG, L.MIA_ERR_RANGE):
+                raise ValueError(msg)
+            raise L.MiaError(rc, msg)
+
+    def run(self, stream=None):
+        self.enqueue(stream)
+        self.status(stream)
+
+    def capture(self):
+        """Record ``enqueue`` in a CUDA graph (after ``prepare``)."""
+        import torch
+        s = torch.cuda.Stream(self.pc.device)
+        s.wait_stream(torch.cuda.current_stream(self.pc.device))
+        with torch.cuda.stream(s):  # one eager run on the capture stream first
+            self.enqueue(s)
+        s.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s, capture_error_mode="relaxed"):
+            self.enqueue(s)
+        self.graph = g
+        return g
+
+    def replay(self):
+        self.graph.replay()
+        self.status()
+
+    def fetch(self, i):
+        return self.pc.fetch((None, self.outs[i], self.cnts[i]))

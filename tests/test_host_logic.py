@@ -140,3 +140,18 @@ def test_mask_weight_quirk_mutates_masks():
     got = box._select(masks)
     np.testing.assert_array_equal(got["weight"], [0.0, 1.0, 2.0])
     assert "weight" in masks and "weight_shape_sample" in masks
+
+
+def test_autotune_cache_roundtrip(tmp_path, monkeypatch):
+    from measure_ia_gb300 import autotune
+    path = str(tmp_path / "tune.json")
+    monkeypatch.setenv("MIA_TUNE_CACHE", path)
+    k1 = autotune.workload_key("w", "mixed", 4_000_000, 1_000_000, 205.0, 10, 8, 20.0, 20.0, 3, "tree", "GB300")
+    k2 = autotune.workload_key("w", "mixed", 4_100_000, 1_000_000, 205.0, 10, 8, 20.0, 20.0, 3, "tree", "GB300")
+    k3 = autotune.workload_key("w", "mixed", 8_000_000, 1_000_000, 205.0, 10, 8, 20.0, 20.0, 3, "tree", "GB300")
+    assert k1 == k2 and k1 != k3
+    assert autotune.load_cache() == {}
+    autotune.store(k1, {"cell_size": 11.4, "cell_refine": 3, "shapes_per_unit": 128, "ms": 1.0})
+    assert autotune.load_cache()[k1]["cell_refine"] == 3
+    sides, refines, units = autotune.candidates(20.0)
+    assert len(sides) == 5 and 3 in refines and 128 in units
