@@ -136,6 +136,47 @@ def cpu_reference(data, n_sample_shapes, processes):
 # GPU arm
 # ---------------------------------------------------------------------------
 
+def _errors(ref, got, keys):
+    out = {}
+    for k, name in keys:
+        a, b = ref[k], got[k]
+        out[name] = {"max_rel_per_bin": float(np.max(np.abs(b - a) / np.maximum(np.abs(a), 1e-300))),
+                     "max_rel_to_vector_scale": float(np.max(np.abs(b - a)) / np.max(np.abs(a)))}
+    return out
+
+
+def time_counter(pc, dcat, steps, warmup, stream, ws=1):
+    """ms per step (CUDA events on the launching stream), per-step list, products."""
+    import torch
+    n_pos, n_shape = dcat["Position"].shape[0], dcat["Position_shape_sample"].shape[0]
+    bufs = pc.allocate(n_pos, n_shape)
+    for _ in range(warmup):
+        pc.run(dcat, bufs, stream)
+    torch.cuda.synchronize()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    torch.cuda.synchronize()
+    evs[0].record(stream)
+    for i in range(steps):
+        pc.run(dcat, bufs, stream)
+        evs[i + 1].record(stream)
+    torch.cuda.synchronize()
+    ms = evs[0].elapsed_time(evs[-1]) / steps
+    per = [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
+    return ms, per, pc.fetch(bufs)
+
+
+def _pick(pc, dcat, args):
+    """Launch knobs: pinned by --knobs, else autotuned on this catalogue
+    (outside the timed region; cached per workload shape), else the defaults."""
+    if args.knobs:
+        cell, refine, spu = args.knobs.split(",")
+        return pc.with_knobs(cell_size=float(cell), cell_refine=int(refine), shapes_per_unit=int(spu))
+    return pc if args.no_tune else pc.tuned(dcat)
+
+
 def run_gpu(args, data, rank, ws, local):
     import torch
     from measure_ia_gb300.engine import PairCounter
@@ -145,72 +186,144 @@ def run_gpu(args, data, rank, ws, local):
     torch.cuda.set_device(dev)
     keys = ("Position", "weight", "Position_shape_sample", "Axis_Direction", "q", "weight_shape_sample")
     dcat = {k: torch.from_numpy(np.ascontiguousarray(data[k], dtype=np.float64)).to(dev) for k in keys}
-    n_pos, n_shape = dcat["Position"].shape[0], dcat["Position_shape_sample"].shape[0]
     stream = torch.cuda.current_stream(dev)
+    common = dict(boxsize=L_BOX, r_bins=R_BINS, r_min=0.1, r_max=20.0, p_bins=PI_BINS, l_subboxes=3, device=local)
 
-    per_step = {}
+    # launch knobs tuned on this catalogue (outside the timed region; cached per workload shape)
+    pcm = _pick(PairCounter("w", precision="mixed", **common), dcat, args)
+    knobs = dict(pcm.knobs)
 
-    def time_form(precision, steps, warmup):
-        pc = PairCounter("w", boxsize=L_BOX, r_bins=R_BINS, r_min=0.1, r_max=20.0, p_bins=PI_BINS, l_subboxes=3,
-                         precision=precision, device=local)
-        bufs = pc.allocate(n_pos, n_shape)
-        for _ in range(warmup):
-            pc.run(dcat, bufs, stream)
-        torch.cuda.synchronize()
-        if ws > 1:
-            import torch.distributed as dist
-            dist.barrier()
-        evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
-        torch.cuda.synchronize()
-        evs[0].record(stream)
-        for i in range(steps):
-            pc.run(dcat, bufs, stream)
-            evs[i + 1].record(stream)
-        torch.cuda.synchronize()
-        ms = evs[0].elapsed_time(evs[-1]) / steps
-        per_step[precision] = [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
-        m = pc.fetch(bufs)
-        return pc, bufs, m, ms
-
-    # plain FP64 form first (reference for the accuracy figures), then the mixed headline
     with ClockSampler(local) as clk:
-        pcm, bufm, mm, msm = time_form("mixed", args.steps, args.warmup)
+        msm, per_m, mm = time_counter(pcm, dcat, args.steps, args.warmup, stream, ws)
     clocks = clk.summary()
+    per_step = {"mixed": per_m}
     if args.only_mixed:
         m64, ms64 = mm, float("nan")
     else:
-        fp_steps = max(1, min(args.steps, 2))
-        pc64, _, m64, ms64 = time_form("fp64", fp_steps, 1)
+        pc64 = PairCounter("w", precision="fp64", **common, **knobs)
+        ms64, per_step["fp64"], m64 = time_counter(pc64, dcat, max(1, min(args.steps, 2)), 1, stream, ws)
 
     binned = mm.stats["binned_pairs"]
     assert binned == m64.stats["binned_pairs"], "mixed and FP64 forms binned different pairs"
     counts_exact = bool(np.array_equal(mm.npairs, m64.npairs))
-    err = {}
-    for k, name in (("proj_gp", "w_g+"), ("proj_gg", "w_gg"), ("cov_gp", "cov w_g+"), ("cov_gg", "cov w_gg")):
-        a, b = m64[k], mm[k]
-        err[name] = {"max_rel_per_bin": float(np.max(np.abs(b - a) / np.maximum(np.abs(a), 1e-300))),
-                     "max_rel_to_vector_scale": float(np.max(np.abs(b - a)) / np.max(np.abs(a)))}
+    err = _errors(m64, mm, (("proj_gp", "w_g+"), ("proj_gg", "w_gg"), ("cov_gp", "cov w_g+"), ("cov_gg", "cov w_gg")))
     err["w_g+ in jackknife sigma"] = float(np.max(np.abs(mm["proj_gp"] - m64["proj_gp"]) / m64["std_gp"]))
 
-    # end to end through the public API with host buffers
+    # multipoles on the same catalogue (10 log r bins 0.1-20, 20 mu bins over [-1, 1]): rate and accuracy
+    mult = None
+    if not args.only_mixed and not args.no_multipoles:
+        mc = dict(common, p_bins=np.linspace(-1.0, 1.0, 21))
+        pmm = PairCounter("m", precision="mixed", **mc)
+        pmm = _pick(pmm, dcat, args)
+        mms, _, mmm = time_counter(pmm, dcat, 2, 1, stream, ws)
+        pm64 = PairCounter("m", precision="fp64", **mc, **dict(pmm.knobs))
+        mms64, _, mm64 = time_counter(pm64, dcat, 1, 0, stream, ws)
+        mult = {"binned_pairs_per_step": mmm.stats["binned_pairs"],
+                "mixed": {"value": mmm.stats["binned_pairs"] / (mms / 1e3), "ms_per_step": mms},
+                "fp64": {"value": mm64.stats["binned_pairs"] / (mms64 / 1e3), "ms_per_step": mms64},
+                "counts_bit_exact_mixed_vs_fp64": bool(np.array_equal(mmm.npairs, mm64.npairs)),
+                "accuracy_mixed_vs_fp64": _errors(mm64, mmm, (("proj_gp", "multipole g+ (l=2)"),
+                                                              ("proj_gg", "multipole gg (l=0)"),
+                                                              ("cov_gp", "cov g+"), ("cov_gg", "cov gg")))}
+
+    res = dict(binned=binned, ms=msm, ms64=ms64, clocks=clocks, counts_exact=counts_exact, err=err,
+               stats=mm.stats, stats64=m64.stats, per_step=per_step, knobs=knobs, mult=mult,
+               e2e_s=float("nan"), h2d=0, d2h=0)
     if args.no_e2e:
-        return dict(binned=binned, ms=msm, ms64=ms64, clocks=clocks, counts_exact=counts_exact, err=err,
-                    e2e_s=float("nan"), h2d=0, d2h=0, stats=mm.stats, stats64=m64.stats, per_step=per_step)
-    t0 = time.perf_counter()
-    e2e_steps = max(1, min(args.steps, 3))
-    torch.cuda.synchronize()
+        return res
+    # end to end through the public API with host buffers: H2D copies, the
+    # measurement, D2H of every product and the dataset writes, every step
     host = {k: data[k] for k in keys}
     host["LOS"] = 2
-    h2d = sum(np.asarray(data[k]).nbytes for k in keys)
+    box = MeasureIABox(dict(host), None, None, None, [0.1, 20.0], 10, 8, 20.0, boxsize=L_BOX, num_nodes=2,
+                       precision="mixed", device=local, autotune=not args.no_tune)
+    box.measure_xi_w("bench", "both", 27, temp_file_path="/tmp")  # warm-up (tuner cache hit)
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        box = MeasureIABox(dict(host), None, None, None, [0.1, 20.0], 10, 8, 20.0, boxsize=L_BOX, num_nodes=2,
-                           precision="mixed", device=local)
         box.measure_xi_w("bench", "both", 27, temp_file_path="/tmp")
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
-    d2h = pcm.layout.total * 8 + (1 + 27) * 80 * 8
-    return dict(binned=binned, ms=msm, ms64=ms64, clocks=clocks, counts_exact=counts_exact, err=err,
-                e2e_s=e2e_s, h2d=h2d, d2h=d2h, stats=mm.stats, stats64=m64.stats, per_step=per_step)
+    res["e2e_s"] = (time.perf_counter() - t0) / e2e_steps
+    res["h2d"] = sum(np.asarray(data[k]).nbytes for k in keys)
+    res["d2h"] = pcm.layout.total * 8 + (1 + 27) * 80 * 8
+    return res
+
+
+def run_batch48(args, local):
+    """48 catalogues (12 mass bins x 4 snapshots), sizes log-uniform in
+    [5e3, 2e6] galaxies, each drawn with the clustered recipe (parents = N/50,
+    shapes = N/4, independent seeds), measured in one persistent pair-kernel
+    launch replayed from a CUDA graph, against the same catalogues measured
+    one after the other."""
+    import torch
+    from measure_ia_gb300.catalogs import neyman_scott_catalog
+    from measure_ia_gb300.engine import BatchCounter, PairCounter
+    rng = np.random.default_rng(48)
+    sizes = np.exp(rng.uniform(np.log(5e3), np.log(2e6), 48))
+    cats = [neyman_scott_catalog(max(2, int(n / 50)), L_BOX, max(100, int(n / 4)), 1000 + i, mean_children=50,
+                                 sigma=1.0) for i, n in enumerate(sizes)]
+    pc = PairCounter("w", boxsize=L_BOX, r_bins=R_BINS, r_min=0.1, r_max=20.0, p_bins=PI_BINS, l_subboxes=3,
+                     precision="mixed", device=local)
+    dcats = [pc.to_device(c) for c in cats]
+    stream = torch.cuda.current_stream(local)
+    # one after the other
+    bufs = [pc.allocate(d["Position"].shape[0], d["Position_shape_sample"].shape[0]) for d in dcats]
+    for d, b in zip(dcats, bufs):
+        pc.run(d, b, stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for d, b in zip(dcats, bufs):
+            pc.run(d, b, stream)
+    torch.cuda.synchronize()
+    seq_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+    binned = sum(pc.fetch(b).stats["binned_pairs"] for b in bufs)
+    # batched, replayed from a CUDA graph
+    batch = BatchCounter(pc, dcats)
+    batch.prepare()
+    batch.run()
+    batch.capture()
+    for _ in range(args.warmup):
+        batch.replay()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        batch.graph.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batch.status()
+    ms = e0.elapsed_time(e1) / args.steps
+    same = all(np.array_equal(batch.fetch(i).npairs, pc.fetch(b).npairs) for i, b in enumerate(bufs))
+    return {"metric": "binned pairs/s, 48 uneven catalogues, w_gg+w_g+ 27JK, mixed form", "value": binned / (ms / 1e3),
+            "unit": "binned pairs/s", "ms_per_step": ms, "one_after_the_other_ms": seq_ms,
+            "binned_pairs_per_step": binned, "counts_equal_to_one_by_one": bool(same),
+            "config": {"workload": "48 catalogues, sizes log-uniform 5e3-2e6 (config 3)",
+                       "n_positions_total": int(sum(len(c["Position"]) for c in cats)),
+                       "n_shapes_total": int(sum(len(c["Position_shape_sample"]) for c in cats))}}
+
+
+def run_large(args, local):
+    """1000 Mpc/h box, 500,000 parents x Poisson(50) (sigma 1.5 Mpc/h),
+    5M shapes, 15 log r_p bins 0.1-60, 20 Pi bins over |Pi| <= 60, 125
+    jackknife regions, mixed form."""
+    import torch
+    from measure_ia_gb300.catalogs import neyman_scott_catalog
+    from measure_ia_gb300.engine import PairCounter
+    data = neyman_scott_catalog(500_000, 1000.0, 5_000_000, 4, mean_children=50, sigma=1.5)
+    rb = np.logspace(-1, np.log10(60.0), 16)
+    pb = np.linspace(-60.0, 60.0, 21)
+    pc = PairCounter("w", boxsize=1000.0, r_bins=rb, r_min=0.1, r_max=60.0, p_bins=pb, l_subboxes=5,
+                     precision="mixed", device=local)
+    dcat = pc.to_device(data)
+    pc = _pick(pc, dcat, args)
+    ms, per, m = time_counter(pc, dcat, args.steps, max(1, args.warmup), torch.cuda.current_stream(local))
+    return {"metric": "binned pairs/s, w_gg+w_g+ 125JK, 1000 Mpc/h box, mixed form",
+            "value": m.stats["binned_pairs"] / (ms / 1e3), "unit": "binned pairs/s", "ms_per_step": ms,
+            "step_ms": per, "binned_pairs_per_step": m.stats["binned_pairs"], "knobs": pc.knobs,
+            "config": {"workload": "25M positions / 5M shapes, 1000 Mpc/h, 15x20 bins, 125 jackknife (config 4)",
+                       "n_positions": int(len(data["Position"])), "n_shapes": int(len(data["Position_shape_sample"]))}}
 
 
 def main():
@@ -223,10 +336,24 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--only-mixed", action="store_true", help="time the mixed form only (profiling runs)")
+    ap.add_argument("--no-tune", action="store_true", help="default launch knobs instead of the autotuner's")
+    ap.add_argument("--knobs", default="", help="CELL,REFINE,SPU launch knobs instead of tuning (profiling runs)")
+    ap.add_argument("--no-multipoles", action="store_true", help="skip the multipole rate and accuracy report")
+    ap.add_argument("--workload", default="config2", choices=["config2", "batch48", "large"],
+                    help="config2 = the headline line; batch48 and large print their own lines")
     ap.add_argument("--centres", type=int, default=80000, help="Neyman-Scott parents (profiling runs)")
     ap.add_argument("--shapes", type=int, default=1_000_000, help="shape-sample size (profiling runs)")
     args = ap.parse_args()
     rank, ws, local = world()
+    if args.workload != "config2":
+        import torch
+        torch.cuda.set_device(local)
+        line = run_batch48(args, local) if args.workload == "batch48" else run_large(args, local)
+        line.update({"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+                     "data": "synthetic"})
+        if rank == 0:
+            print(json.dumps(line))
+        return
     data = make_catalog(n_centres=args.centres, n_shape=args.shapes)
     n_pos, n_shape = len(data["Position"]), len(data["Position_shape_sample"])
     config = {"workload": "clustered 4M positions / 1M shapes, w_gg+w_g+, 27 jackknife regions (config 2)",
@@ -280,7 +407,7 @@ def main():
     achieved = LANE_OPS_PER_PAIR * r["binned"] / t_step / 1e12
     if rank != 0:
         return
-    launches_per_step = 18  # prep 15 (prep 2, scans 9, scatter 2, work units 2), pairs 1, edge re-test 1, post 1
+    launches_per_step = 20  # prep 15 (prep 2, scans 9, scatter 2, work units 2), work prefix 1, pairs 1, edge re-test 1, post 1, status 1
     line = {
         "metric": METRIC, "value": value, "unit": "binned pairs/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",
@@ -298,6 +425,8 @@ def main():
                 "d2h_bytes_per_step": r["d2h"]},
         "gpu_launches": launches_per_step * args.steps,
         "step_ms": r["per_step"],
+        "launch_knobs": r["knobs"],
+        "multipoles": r["mult"],
         "clocks": r["clocks"],
     }
     print(json.dumps(line))

@@ -68,6 +68,8 @@ def tune(make_counter, dcat, range_proj, key=None, path=None, log=None):
     the device-resident catalogue.  With ``key`` the result is cached."""
     import torch
 
+    from ._lib import MiaError
+
     if key is not None:
         hit = load_cache(path).get(key)
         if hit:
@@ -75,23 +77,33 @@ def tune(make_counter, dcat, range_proj, key=None, path=None, log=None):
     n_pos = dcat["Position"].shape[0]
     n_shape = dcat["Position_shape_sample"].shape[0]
     timings = {}
+    failures = []
 
     def time_one(knobs):
         tkey = (knobs["cell_size"], knobs["cell_refine"], knobs["shapes_per_unit"])
         if tkey in timings:
             return timings[tkey]
-        pc = make_counter(**knobs)
-        bufs = pc.allocate(n_pos, n_shape)
-        pc.run(dcat, bufs)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        torch.cuda.synchronize()
-        e0.record()
-        pc.run(dcat, bufs)
-        e1.record()
-        torch.cuda.synchronize()
-        ms = e0.elapsed_time(e1)
+        try:
+            pc = make_counter(**knobs)
+            bufs = pc.allocate(n_pos, n_shape)
+            pc.run(dcat, bufs)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record()
+            pc.run(dcat, bufs)
+            e1.record()
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1)
+        except (MiaError, torch.cuda.OutOfMemoryError) as exc:
+            # a candidate whose workspace does not fit or whose edge queue
+            # overflows is not a choice; the others still are
+            ms = math.inf
+            bufs = None
+            failures.append(exc)
+            if log:
+                log(f"autotune {knobs} -> skipped ({exc})")
         timings[tkey] = ms
-        if log:
+        if log and math.isfinite(ms):
             log(f"autotune {knobs} -> {ms:.3f} ms")
         del bufs
         return ms
@@ -100,6 +112,8 @@ def tune(make_counter, dcat, range_proj, key=None, path=None, log=None):
     best = min(({"cell_size": s, "cell_refine": 3, "shapes_per_unit": 128} for s in sides), key=time_one)
     best = min(({**best, "cell_refine": m} for m in refines), key=time_one)
     best = min(({**best, "shapes_per_unit": u} for u in units), key=time_one)
+    if not math.isfinite(timings[(best["cell_size"], best["cell_refine"], best["shapes_per_unit"])]):
+        raise failures[-1]
     best = {k: (float(v) if k == "cell_size" else int(v)) for k, v in best.items()}
     best["ms"] = timings[(best["cell_size"], best["cell_refine"], best["shapes_per_unit"])]
     if key is not None:

@@ -2,6 +2,7 @@
 // preparation, pair and post-processing stages.
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -122,9 +123,14 @@ bool make_plan(const mia_config* cfg, long long n_pos, long long n_shape, Plan* 
   p.n_wu_max = p.n_cells + n_shape + 1;
   p.edge_capacity = 0;
   if (cfg->precision == MIA_MIXED) {
-    long long cap = n_shape * 64;
+    long long cap = n_shape * 32;
     if (cap < (1LL << 20)) cap = 1LL << 20;
-    if (cap > (1LL << 24)) cap = 1LL << 24;
+    if (cap > (1LL << 28)) cap = 1LL << 28;
+    // MIA_EDGE_CAPACITY=<entries> replaces the default (workspace sizes follow)
+    if (const char* env = std::getenv("MIA_EDGE_CAPACITY")) {
+      const long long v = std::atoll(env);
+      if (v > 0) cap = v;
+    }
     p.edge_capacity = cap;
   }
   const bool mixed = cfg->precision == MIA_MIXED;
@@ -505,7 +511,17 @@ void make_params(const mia_config* cfg, const Plan& plan, const Tables& T, int l
   const double p0 = cfg->p_edges[0], p1 = cfg->p_edges[cfg->n_p];
   P.p_lo32 = (float)p0;
   P.p_inv32 = (float)((double)cfg->n_p / (p1 - p0));
-  P.p_guard = (float)fmax(1.0 / 32768.0, cfg->n_p * 4e-6);
+  {
+    // guard band on t = (v - p_lo) * n_p / (p_hi - p_lo), in bins: four times a
+    // bound on its FP32 error.  v = Pi carries the error of the hi/lo
+    // difference; v = mu = Pi * rsqrt(r^2) adds rsqrtf (2 ulp) and r^2 (4.5e-7)
+    const double u = 1.0 / 8388608.0;  // 2^-23
+    const double inv = (double)cfg->n_p / (p1 - p0);
+    const double vmax = cfg->kind == MIA_KIND_W ? plan.range_los : 1.0;
+    double ev = cfg->kind == MIA_KIND_W ? vmax * u : vmax * 6e-7;
+    double et = (ev + fabs(p0) * u * 0.5 + (vmax + fabs(p0)) * u * 0.5) * inv + cfg->n_p * u;
+    P.p_guard = (float)fmin(0.25, fmax(4.0 * et, 1.0 / 1048576.0));
+  }
   P.c_guard = 1e-12f;
   P.wrap_guard = (float)(cfg->boxsize * 1e-5);
   const double pm = fmax(fabs(p0), fabs(p1));

@@ -16,14 +16,18 @@ Backend choice mirrors the reference's dispatch (measure_IA.py:103-161):
 
 The temporary file the reference writes is not needed: catalogues stay in
 device memory.  Extra keyword arguments: ``precision`` ('fp64' for the plain
-FP64 form, 'mixed' for FP32 pair arithmetic with FP64 edge re-tests) and
-``device``.
+FP64 form, 'mixed' for FP32 pair arithmetic with FP64 edge re-tests),
+``device`` and ``autotune`` (search the launch knobs on first use of a
+workload shape; results are identical, only speed changes).
 """
 
 from __future__ import annotations
 
+import warnings
+
 import numpy as np
 
+from ._lib import MIA_ERR_OVERFLOW, MiaError
 from .engine import PairCounter
 from .output import norm_path, open_output
 from .sim_info import SimInfo
@@ -54,7 +58,7 @@ class MeasureIABox(SimInfo):
 
     def __init__(self, data, output_file_name, simulation=None, snapshot=None, separation_limits=[0.1, 20.0],
                  num_bins_r=8, num_bins_pi=20, pi_max=None, boxsize=None, periodicity=True, num_nodes=1,
-                 precision="fp64", device=0):
+                 precision="fp64", device=0, autotune=False):
         SimInfo.__init__(self, simulation, snapshot, boxsize)
         self.data = data
         self.output_file_name = output_file_name
@@ -62,6 +66,7 @@ class MeasureIABox(SimInfo):
         self.num_nodes = num_nodes
         self.precision = precision
         self.device = device
+        self.autotune = autotune
         try:
             self.Num_position = len(data["Position"])
             self.Num_shape = len(data["Position_shape_sample"])
@@ -150,13 +155,30 @@ class MeasureIABox(SimInfo):
         L_sub, layout = self._validate(corr_type, num_jk, temp_file_path)
         cat = self._select(masks)
         los = self.data["LOS"]
-        counter = PairCounter(kind, boxsize=self.boxsize, r_bins=self.r_bins, r_min=self.r_min, r_max=self.r_max,
-                              p_bins=self.pi_bins if kind == "w" else self.mu_r_bins, los=los, l_subboxes=L_sub,
-                              precision=self.precision, membership="brute" if layout == "brute" else "tree",
-                              ellipticity=ellipticity, want_variance=(layout == "brute" and L_sub > 0),
-                              volume=self.boxsize ** 3, rp_cut=0.0 if rp_cut is None else rp_cut,
-                              device=self.device)
-        meas = counter.measure(cat)
+        args = dict(boxsize=self.boxsize, r_bins=self.r_bins, r_min=self.r_min, r_max=self.r_max,
+                    p_bins=self.pi_bins if kind == "w" else self.mu_r_bins, los=los, l_subboxes=L_sub,
+                    precision=self.precision, membership="brute" if layout == "brute" else "tree",
+                    ellipticity=ellipticity, want_variance=(layout == "brute" and L_sub > 0),
+                    volume=self.boxsize ** 3, rp_cut=0.0 if rp_cut is None else rp_cut, device=self.device)
+        counter = PairCounter(kind, **args)
+        dcat = counter.to_device(cat)
+        if self.autotune:
+            counter = counter.tuned(dcat)
+        n_pos, n_shape = dcat["Position"].shape[0], dcat["Position_shape_sample"].shape[0]
+        bufs = counter.allocate(n_pos, n_shape)
+        try:
+            counter.run(dcat, bufs)
+        except MiaError as exc:
+            # more pairs near a bin edge than the FP64 re-test queue holds:
+            # the mixed form cannot finish exactly, the FP64 form always can
+            if exc.code != MIA_ERR_OVERFLOW or self.precision != "mixed":
+                raise
+            warnings.warn("mixed form: edge re-test queue overflow, measuring in the FP64 form", RuntimeWarning)
+            del bufs
+            counter = PairCounter(kind, **{**args, "precision": "fp64"})
+            bufs = counter.allocate(n_pos, n_shape)
+            counter.run(dcat, bufs)
+        meas = counter.fetch(bufs)
         self.last_measurement = meas
         self._write(kind, dataset_name, corr_type, num_jk, meas, layout)
         return meas

@@ -1,0 +1,90 @@
+"""Failure paths that must end in a clean error or a correct result, never a
+wrong one: the mixed form's FP64 edge re-test queue overflowing, and the
+autotuner meeting launch configurations that fail."""
+
+import math
+import warnings
+
+import numpy as np
+import pytest
+
+from golden_io import assert_close
+
+pytestmark = pytest.mark.gpu
+
+R_BINS = np.logspace(-1, np.log10(20.0), 11)
+PI_BINS = np.linspace(-20.0, 20.0, 9)
+
+
+def _edge_catalogue():
+    from measure_ia_gb300.catalogs import add_edge_pairs, neyman_scott_catalog
+    data = neyman_scott_catalog(300, 205.0, 6000, 11, mean_children=40, sigma=1.0)
+    return add_edge_pairs(data, 205.0, 5, R_BINS, PI_BINS, 400)
+
+
+def _counter(precision, **knobs):
+    from measure_ia_gb300.engine import PairCounter
+    return PairCounter("w", boxsize=205.0, r_bins=R_BINS, r_min=0.1, r_max=20.0, p_bins=PI_BINS, l_subboxes=3,
+                       precision=precision, **knobs)
+
+
+def test_edge_queue_overflow_is_an_error(monkeypatch):
+    """A queue of 16 entries cannot hold the re-tests of 400 planted edge
+    pairs: the run reports MIA_ERR_OVERFLOW instead of binning them in FP32."""
+    from measure_ia_gb300._lib import MIA_ERR_OVERFLOW, MiaError
+    data = _edge_catalogue()
+    monkeypatch.setenv("MIA_EDGE_CAPACITY", "16")
+    pc = _counter("mixed")
+    with pytest.raises(MiaError) as err:
+        pc.measure(data)
+    assert err.value.code == MIA_ERR_OVERFLOW
+    # the device and the library stay usable: the default capacity succeeds
+    monkeypatch.delenv("MIA_EDGE_CAPACITY")
+    ok = _counter("mixed").measure(data)
+    ref = _counter("fp64").measure(data)
+    np.testing.assert_array_equal(ok.npairs, ref.npairs)
+
+
+def test_box_falls_back_to_fp64_form_on_overflow(monkeypatch, tmp_path):
+    """MeasureIABox(precision='mixed') re-measures in the FP64 form when the
+    queue overflows, with a RuntimeWarning, and its products equal an FP64 run."""
+    from measure_ia_gb300 import MeasureIABox, open_output
+    data = _edge_catalogue()
+    kw = dict(separation_limits=[0.1, 20.0], num_bins_r=10, num_bins_pi=8, pi_max=20.0, boxsize=205.0)
+    ref = MeasureIABox(data, str(tmp_path / "fp64.hdf5"), **kw, precision="fp64")
+    ref.measure_xi_w("d", "both", 27, temp_file_path=str(tmp_path))
+    monkeypatch.setenv("MIA_EDGE_CAPACITY", "16")
+    box = MeasureIABox(data, str(tmp_path / "mixed.hdf5"), **kw, precision="mixed")
+    with warnings.catch_warnings(record=True) as caught:
+        warnings.simplefilter("always")
+        box.measure_xi_w("d", "both", 27, temp_file_path=str(tmp_path))
+    assert any("overflow" in str(w.message) for w in caught)
+    np.testing.assert_array_equal(box.last_measurement.npairs, ref.last_measurement.npairs)
+    a, b = open_output(str(tmp_path / "fp64.hdf5")), open_output(str(tmp_path / "mixed.hdf5"))
+    for path in a.keys():
+        assert_close(b.read(path), a.read(path), 1e-12, path)
+
+
+def test_autotune_skips_failing_candidates(tmp_path):
+    """Candidates that raise are timed as infinite; the choice is one that ran."""
+    from measure_ia_gb300 import autotune
+    from measure_ia_gb300._lib import MIA_ERR_WORKSPACE, MiaError
+    data = _edge_catalogue()
+    pc = _counter("mixed")
+    dcat = pc.to_device(data)
+    rp, _ = pc.search_ranges()
+
+    def make(**knobs):
+        if knobs["cell_refine"] != 2 or knobs["shapes_per_unit"] == 256:
+            raise MiaError(MIA_ERR_WORKSPACE, "candidate refused")
+        return pc.with_knobs(**knobs)
+
+    best = autotune.tune(make, dcat, rp)
+    assert best["cell_refine"] == 2 and best["shapes_per_unit"] != 256 and math.isfinite(best["ms"])
+
+    def refuse(**knobs):
+        raise MiaError(MIA_ERR_WORKSPACE, "candidate refused")
+
+    with pytest.raises(MiaError):
+        autotune.tune(refuse, dcat, rp, key="k", path=str(tmp_path / "t.json"))
+    assert autotune.load_cache(str(tmp_path / "t.json")) == {}
