@@ -24,9 +24,6 @@ namespace mia {
 
 namespace {
 
-#ifndef MIA_BIN_CACHE
-#define MIA_BIN_CACHE 0  // per-thread two-entry cache of bin partials in front of the shared atomics
-#endif
 
 constexpr int kRowsPerPass = 256;
 constexpr int kSegsPerPass = 2 * kRowsPerPass;
@@ -54,7 +51,8 @@ struct TablesSmem {
   unsigned short lut32[kLut];
 };
 
-__host__ __device__ inline SmemLayout smem_layout(int J, int spu, int K, int nb, int mixed, int var) {
+// hw: words per histogram array (slots x bins, times the private copies)
+__host__ __device__ inline SmemLayout smem_layout(int J, int spu, int hw, int mixed, int var) {
   SmemLayout L;
   size_t o = 0;
   L.tables = o;
@@ -72,7 +70,7 @@ __host__ __device__ inline SmemLayout smem_layout(int J, int spu, int K, int nb,
   L.seg_shift = o;
   o = align16(o + sizeof(unsigned char) * kSegsPerPass);
   L.hist = o;
-  o = align16(o + sizeof(unsigned) * (size_t)K * nb * hist_words(mixed, var) + 16);
+  o = align16(o + sizeof(unsigned) * (size_t)hw * hist_words(mixed, var) + 16);
   L.total = o;
   return L;
 }
@@ -147,41 +145,6 @@ struct HistView {
   int *dd_hi, *sp_hi, *sx_hi, *vr_hi;
 };
 
-// A thread's two most recent (histogram index -> exact fixed-point partial)
-// entries; a pair whose bin matches one of them adds in registers, otherwise
-// the older entry goes to the shared histogram.
-struct BinCache {
-  int k0 = -1, k1 = -1;
-  unsigned n0 = 0, n1 = 0;
-  long long d0 = 0, p0 = 0, x0 = 0, d1 = 0, p1 = 0, x1 = 0;
-
-  __device__ __forceinline__ static void flush(const HistView& h, int k, unsigned n, long long d, long long p,
-                                               long long x) {
-    atomicAdd(&h.cnt[k], n);
-    add64_shared(h.dd_lo, h.dd_hi, k, d);
-    add64_shared(h.sp_lo, h.sp_hi, k, p);
-    add64_shared(h.sx_lo, h.sx_hi, k, x);
-  }
-  __device__ __forceinline__ void add(const HistView& h, int k, int vd, int vp, int vx) {
-    if (k == k0) {
-      ++n0; d0 += vd; p0 += vp; x0 += vx;
-    } else if (k == k1) {  // hit in the older entry: it becomes the newer one
-      const int tk = k0; const unsigned tn = n0; const long long td = d0, tp = p0, tx = x0;
-      k0 = k1; n0 = n1 + 1; d0 = d1 + vd; p0 = p1 + vp; x0 = x1 + vx;
-      k1 = tk; n1 = tn; d1 = td; p1 = tp; x1 = tx;
-    } else {
-      if (k1 >= 0) flush(h, k1, n1, d1, p1, x1);
-      k1 = k0; n1 = n0; d1 = d0; p1 = p0; x1 = x0;
-      k0 = k; n0 = 1; d0 = vd; p0 = vp; x0 = vx;
-    }
-  }
-  __device__ __forceinline__ void flush_all(const HistView& h) {
-    if (k0 >= 0) flush(h, k0, n0, d0, p0, x0);
-    if (k1 >= 0) flush(h, k1, n1, d1, p1, x1);
-    k0 = k1 = -1;
-  }
-};
-
 // One position in FP32 hi/lo form, moved to the periodic image of its row.
 struct MixedPos {
   float xh, xl, yh, yl, zh, zl, w;
@@ -238,7 +201,7 @@ __device__ __forceinline__ void z_window(const float* Z, int S, float z, float w
 template <int KIND, int FULL, int VAR>
 __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T, const float4& a, const float4& b,
                                            const float2* C, const int* I, int i, const MixedPos& p,
-                                           const HistView& h, BinCache& cache, const Work& w, const Out& o,
+                                           const HistView& h, const Work& w, const Out& o,
                                            float fixed_scale, double twoR, int label_a,
                                            unsigned long long& my_binned) {
   float dz = (a.z - p.zh) + (b.z - p.zl);
@@ -330,18 +293,16 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
     const int vd = __float2int_rn(ww * fixed_scale);
     const int vp = __float2int_rn(we * cos2 * fixed_scale);
     const int vx = __float2int_rn(we * sin2 * fixed_scale);
-    if (VAR || !MIA_BIN_CACHE) {
-      atomicAdd(&h.cnt[k], 1u);
-      acc_fixed(h.dd_lo, h.dd_hi, k, vd);
-      acc_fixed(h.sp_lo, h.sp_hi, k, vp);
-      acc_fixed(h.sx_lo, h.sx_hi, k, vx);
-      if (VAR) {
-        const float tv = we * cos2 / (float)twoR;
-        acc_fixed(h.vr_lo, h.vr_hi, k, __float2int_rn(tv * tv * fixed_scale));
-      }
-    } else {
-      cache.add(h, k, vd, vp, vx);
+    int vv = 0;
+    if (VAR) {
+      const float tv = we * cos2 / (float)twoR;
+      vv = __float2int_rn(tv * tv * fixed_scale);
     }
+    atomicAdd(&h.cnt[k], 1u);
+    acc_fixed(h.dd_lo, h.dd_hi, k, vd);
+    acc_fixed(h.sp_lo, h.sp_hi, k, vp);
+    acc_fixed(h.sx_lo, h.sx_hi, k, vx);
+    if (VAR) acc_fixed(h.vr_lo, h.vr_hi, k, vv);
   } else {
     const double sp = (double)(we * cos2);
     const double tv = sp / twoR;
@@ -355,11 +316,11 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
 template <int MIXED, int VAR, int KIND, int FULL>
 __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __restrict__ ds, int n_ds,
                                                      const unsigned long long* __restrict__ wu_prefix,
-                                                     unsigned long long* wu_next, int K) {
+                                                     unsigned long long* wu_next, int K, int HW) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x;
   const int nb = P.nb;
-  const SmemLayout SL = smem_layout(P.J, P.shapes_per_unit, K, nb, MIXED, VAR);
+  const SmemLayout SL = smem_layout(P.J, P.shapes_per_unit, HW, MIXED, VAR);
   TablesSmem& T = *reinterpret_cast<TablesSmem*>(smem + SL.tables);
   int* slot_of = reinterpret_cast<int*>(smem + SL.slot_of);
   int* slot_region = reinterpret_cast<int*>(smem + SL.slot_region);
@@ -367,7 +328,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
   int* seg_pref = reinterpret_cast<int*>(smem + SL.seg_pref);
   unsigned char* seg_shift = reinterpret_cast<unsigned char*>(smem + SL.seg_shift);
   unsigned* hist = reinterpret_cast<unsigned*>(smem + SL.hist);
-  const int KB = K * nb;
+  const int KB = HW;  // >= K * nb
 
   __shared__ int s_wu;
   __shared__ int s_ds;
@@ -528,23 +489,22 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
       }
       s_nslots = ns;
       // private copies of the unit's histograms (mixed form): lanes holding
-      // neighbouring positions hit the same bin against a shape, so lane l
-      // adds into copy l mod R; the odd stride puts the copies in distinct banks
+      // neighbouring positions hit the same bin against a shape, and shared
+      // atomics on one address serialise, so lane l adds into copy l mod R;
+      // the odd stride puts the R copies of a bin in R distinct banks
       int R = 1;
-      if (MIXED) {
-        const int cap = K * nb;  // words available per histogram array
-        while (R < 8 && (2 * R) * (ns * nb + 1) <= cap) R *= 2;
-      }
+      const int stride = (ns * nb) | 1;
+      if (MIXED)
+        while (R < 32 && (2 * R) * stride <= HW) R *= 2;
       s_copies = R;
-      s_stride = R > 1 ? ns * nb + 1 : ns * nb;
+      s_stride = R > 1 ? stride : ns * nb;
     }
     for (int i = tid; i < hist_u32; i += blockDim.x) hist[i] = 0u;
     // -- shapes of the unit -> shared
     const int S = u.count;
     if (MIXED) {
-      // stage the shapes ordered by line-of-sight coordinate: consecutive
-      // shapes then tend to share a (r_p, Pi) bin with a given position,
-      // which the per-thread accumulator cache below exploits
+      // stage the shapes ordered by line-of-sight coordinate: a position then
+      // meets only a contiguous window of them within the Pi range
       float4* A = reinterpret_cast<float4*>(smem + SL.shapes);
       float4* B = A + P.shapes_per_unit;
       float2* C = reinterpret_cast<float2*>(B + P.shapes_per_unit);
@@ -704,7 +664,6 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
         const int* I = reinterpret_cast<const int*>(C + P.shapes_per_unit);
         const float* Z = reinterpret_cast<const float*>(I + P.shapes_per_unit);
         const HistView hv{h_cnt, dd_lo, sp_lo, sx_lo, vr_lo, dd_hi, sp_hi, sx_hi, vr_hi};
-        BinCache cache;
         int seg = 0;
         const int copy_off = (tid & (s_copies - 1)) * s_stride;
         // every warp runs the same number of iterations so that its lanes can
@@ -734,14 +693,12 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
               // next shape in flight while this pair is processed (index S at most:
               // still inside the staging area)
               const float4 an = A[i + 1], bn = B[i + 1];
-              mixed_pair<KIND, FULL, VAR>(P, T, a, b, C, I, i, p0, hv, cache, w, o, fixed_scale, twoR, u.label,
-                                          my_binned);
+              mixed_pair<KIND, FULL, VAR>(P, T, a, b, C, I, i, p0, hv, w, o, fixed_scale, twoR, u.label, my_binned);
               a = an;
               b = bn;
             }
           }
         }
-        if (!VAR && MIA_BIN_CACHE) cache.flush_all(hv);
       } else {
         int seg = 0;
         const double* D = reinterpret_cast<const double*>(smem + SL.shapes);
@@ -859,19 +816,73 @@ __global__ void k_edge_retest(Params P, Work w, Out o) {
   if ((threadIdx.x & 31) == 0 && binned) atomicAdd(&w.status->binned, binned);
 }
 
+// Histogram words per array for the mixed form: K slots of nb bins at least,
+// and as much more (for private copies, up to 32 copies of one slot) as fits
+// without lowering the blocks per SM that the registers allow.
+template <int MIXED, int VAR, int KIND, int FULL>
+cudaError_t hist_words_for(const Params& P, int K, int& hw) {
+  hw = K * P.nb;
+  if (!MIXED) return cudaSuccess;
+  auto kern = k_pairs<MIXED, VAR, KIND, FULL>;
+  int dev = 0, smem_sm = 0, smem_blk = 0, reserved = 0, b_reg = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_blk, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b_reg, kern, kThreads, 0);
+  cudaFuncAttributes fa;
+  if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kern);
+  if (e != cudaSuccess) return e;
+  if (b_reg < 1) return cudaSuccess;
+  long long room = (long long)smem_sm / b_reg - reserved - (long long)fa.sharedSizeBytes;
+  if (room > smem_blk - (long long)fa.sharedSizeBytes) room = smem_blk - (long long)fa.sharedSizeBytes;
+  const int hw_max = 32 * (P.nb | 1);
+  int best = hw;
+  for (int c = hw_max; c > hw; c -= 16)
+    if ((long long)smem_layout(P.J, P.shapes_per_unit, c, MIXED, VAR).total <= room) {
+      best = c;
+      break;
+    }
+  hw = best;
+  return cudaSuccess;
+}
+
 template <int MIXED, int VAR, int KIND, int FULL>
 cudaError_t launch_one(const Params& P, const Dataset* ds, int n_ds, const unsigned long long* wu_prefix,
                        unsigned long long* wu_next, cudaStream_t st, int num_sms, int K) {
-  SmemLayout SL = smem_layout(P.J, P.shapes_per_unit, K, P.nb, MIXED, VAR);
-  size_t smem = SL.total;
+  int hw = 0;
+  cudaError_t e = hist_words_for<MIXED, VAR, KIND, FULL>(P, K, hw);
+  if (e != cudaSuccess) return e;
   auto kern = k_pairs<MIXED, VAR, KIND, FULL>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int hw0 = K * P.nb;
+  int per_sm = 0, per_sm0 = 0;
+  size_t smem = smem_layout(P.J, P.shapes_per_unit, hw0, MIXED, VAR).total;
+  e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm0, kern, kThreads, smem);
   if (e != cudaSuccess) return e;
+  per_sm = per_sm0;
+  // the copies must not cost a block per SM
+  while (hw > hw0) {
+    const size_t s1 = smem_layout(P.J, P.shapes_per_unit, hw, MIXED, VAR).total;
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1);
+    if (e != cudaSuccess) return e;
+    int b = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kern, kThreads, s1);
+    if (e != cudaSuccess) return e;
+    if (b >= per_sm0) {
+      smem = s1;
+      per_sm = b;
+      break;
+    }
+    hw = hw - 16 > hw0 ? hw - 16 : hw0;
+  }
+  if (hw == hw0) {
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  kern<<<num_sms * per_sm, kThreads, smem, st>>>(P, ds, n_ds, wu_prefix, wu_next, K);
+  kern<<<num_sms * per_sm, kThreads, smem, st>>>(P, ds, n_ds, wu_prefix, wu_next, K, hw);
   return cudaGetLastError();
 }
 
@@ -900,7 +911,7 @@ __global__ void k_batch_prefix(const Dataset* ds, int n, unsigned long long* pre
 }  // namespace
 
 size_t pair_smem_bytes(int J, int spu, int K, int nb, int mixed, int var) {
-  return smem_layout(J, spu, K, nb, mixed, var).total;
+  return smem_layout(J, spu, K * nb, mixed, var).total;
 }
 
 cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, unsigned long long* wu_prefix, cudaStream_t st) {
