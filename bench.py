@@ -172,8 +172,11 @@ def _pick(pc, dcat, args):
     """Launch knobs: pinned by --knobs, else autotuned on this catalogue
     (outside the timed region; cached per workload shape), else the defaults."""
     if args.knobs:
-        cell, refine, spu = args.knobs.split(",")
-        return pc.with_knobs(cell_size=float(cell), cell_refine=int(refine), shapes_per_unit=int(spu))
+        v = args.knobs.split(",")
+        k = dict(cell_size=float(v[0]), cell_refine=int(v[1]), shapes_per_unit=int(v[2]))
+        if len(v) == 5:
+            k.update(cell_size_los=float(v[3]), cell_refine_los=int(v[4]))
+        return pc.with_knobs(**k)
     return pc if args.no_tune else pc.tuned(dcat)
 
 
@@ -337,7 +340,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--only-mixed", action="store_true", help="time the mixed form only (profiling runs)")
     ap.add_argument("--no-tune", action="store_true", help="default launch knobs instead of the autotuner's")
-    ap.add_argument("--knobs", default="", help="CELL,REFINE,SPU launch knobs instead of tuning (profiling runs)")
+    ap.add_argument("--knobs", default="", help="CELL,REFINE,SPU[,CELL_LOS,REFINE_LOS] launch knobs instead of tuning (profiling runs)")
     ap.add_argument("--no-multipoles", action="store_true", help="skip the multipole rate and accuracy report")
     ap.add_argument("--workload", default="config2", choices=["config2", "batch48", "large"],
                     help="config2 = the headline line; batch48 and large print their own lines")

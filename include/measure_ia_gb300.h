@@ -98,18 +98,29 @@ typedef struct {
   int n_qbreak;
   int n_pbreak;
   int shapes_per_unit; /* 0 = automatic (at most 256)                      */
-  int cell_refine;     /* position cells per shape cell side; 0 = automatic */
+  int cell_refine;     /* position cells per shape cell side in the projected
+                          plane (and along the line of sight unless
+                          cell_refine_los is set); 0 = automatic             */
   double boxsize;      /* L                                                */
   double volume;       /* L**3 as the reference forms it                   */
   double r_min, r_max; /* separation_limits                                */
   double rp_cut;       /* multipoles: pairs need r_p > rp_cut              */
-  double cell_size;    /* target cell side; 0 = automatic                  */
+  double cell_size;    /* target cell side in the projected plane (and along
+                          the line of sight unless cell_size_los is set);
+                          0 = automatic                                     */
   const double* r_edges;   /* n_r + 1 : r_bins                             */
   const double* p_edges;   /* n_p + 1 : pi_bins or mu_r_bins               */
   const double* q_break;   /* n_qbreak ascending                           */
   const int* q_bin;        /* n_qbreak + 1                                 */
   const double* p_break;   /* n_pbreak ascending                           */
   const int* p_bin;        /* n_pbreak + 1                                 */
+  /* Launch geometry along the line of sight.  Cells that are narrow in the
+     projected plane and long along the line of sight keep fewer out-of-range
+     candidates per binned pair at the same shapes per cell.  Results do not
+     depend on these (nor on cell_size, cell_refine, shapes_per_unit). */
+  double cell_size_los;    /* target cell side along the LOS; 0 = cell_size */
+  int cell_refine_los;     /* position cells per shape cell along the LOS;
+                              0 = cell_refine                               */
 } mia_config;
 
 /* Offsets (in doubles) of every product inside the output buffer.

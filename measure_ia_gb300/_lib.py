@@ -39,7 +39,8 @@ class Config(C.Structure):
                 ("r_min", C.c_double), ("r_max", C.c_double), ("rp_cut", C.c_double), ("cell_size", C.c_double),
                 ("r_edges", C.POINTER(C.c_double)), ("p_edges", C.POINTER(C.c_double)),
                 ("q_break", C.POINTER(C.c_double)), ("q_bin", C.POINTER(C.c_int)),
-                ("p_break", C.POINTER(C.c_double)), ("p_bin", C.POINTER(C.c_int))]
+                ("p_break", C.POINTER(C.c_double)), ("p_bin", C.POINTER(C.c_int)),
+                ("cell_size_los", C.c_double), ("cell_refine_los", C.c_int)]
 
 
 _LAYOUT_FIELDS = ["total", "dd", "splus", "scross", "variance", "npos_jk", "nshape_jk", "R", "R_jk", "rr", "rr_jk",

@@ -1,12 +1,22 @@
-"""Autotuner for the pair-count launch configuration.
+"""Autotuner for the pair-count launch geometry.
 
-Three knobs change speed but never results: the shape-cell side
-(``cell_size``), the number of position cells per shape cell along each
-axis (``cell_refine``) and the shapes staged per work unit
-(``shapes_per_unit``).  ``tune`` times candidates on the caller's own
-device-resident catalogue (CUDA events, one warm-up and one timed run each),
-keeps the fastest, and stores the choice in a JSON cache keyed by the
-workload shape, so later measurements of the same shape reuse it.
+Five knobs change speed but never results:
+
+* ``cell_size`` -- shape-cell side in the projected plane.  Narrow cells
+  leave fewer positions outside r_p <= r_max among the candidates of a shape;
+* ``cell_size_los`` -- shape-cell side along the line of sight (0 = equal to
+  ``cell_size``).  Long cells keep many shapes per cell when the projected
+  side is small; the line-of-sight window over the staged shapes removes the
+  out-of-range ones cheaply;
+* ``cell_refine`` / ``cell_refine_los`` -- position cells per shape cell in
+  the plane / along the line of sight (0 = equal to ``cell_refine``);
+* ``shapes_per_unit`` -- shapes staged per work unit.
+
+``tune`` times candidates on the caller's own device-resident catalogue
+(CUDA events, one warm-up and one timed run each) by coordinate descent from
+a cubic-cell start, keeps the fastest, and stores the choice in a JSON cache
+keyed by the workload shape, so later measurements of the same shape reuse it.
+A candidate that fails (workspace too large, edge queue overflow) is skipped.
 
 The cache file is ``$MIA_TUNE_CACHE`` or ``~/.cache/measure_ia_gb300/tune.json``.
 """
@@ -17,7 +27,9 @@ import json
 import math
 import os
 
-DEFAULT = {"cell_size": 0.0, "cell_refine": 0, "shapes_per_unit": 0}
+KNOBS = ("cell_size", "cell_refine", "shapes_per_unit", "cell_size_los", "cell_refine_los")
+DEFAULT = {"cell_size": 0.0, "cell_refine": 0, "shapes_per_unit": 0, "cell_size_los": 0.0, "cell_refine_los": 0}
+_VERSION = "g2"  # geometry search with separate line-of-sight cells
 
 
 def cache_path():
@@ -30,7 +42,7 @@ def workload_key(kind, precision, n_pos, n_shape, boxsize, n_r, n_p, range_proj,
     """Sizes enter as powers of two (a doubling of the catalogue is a new shape)."""
     lp = int(round(math.log2(max(n_pos, 1))))
     ls = int(round(math.log2(max(n_shape, 1))))
-    return "|".join(str(x) for x in (device_name, kind, precision, lp, ls, round(boxsize, 3), n_r, n_p,
+    return "|".join(str(x) for x in (_VERSION, device_name, kind, precision, lp, ls, round(boxsize, 3), n_r, n_p,
                                      round(range_proj, 4), round(range_los, 4), l_subboxes, membership))
 
 
@@ -54,15 +66,16 @@ def store(key, choice, path=None):
     os.replace(tmp, path)
 
 
-def candidates(range_proj):
-    """Shape-cell sides around range/2 first, then refinement and unit size
-    around the best side."""
-    sides = [range_proj / k for k in (1.5, 1.75, 2.0, 2.5, 3.0)]
-    return sides, (2, 3, 4), (64, 128, 256)
+def candidates(range_proj, range_los=None):
+    """Search axes: projected sides, line-of-sight sides, refinements, unit sizes."""
+    range_los = range_proj if range_los is None else range_los
+    sides = [range_proj / k for k in (2.0, 3.0, 4.0, 6.0, 8.0)]
+    los_sides = [range_los * f for f in (0.5, 1.0, 2.0)]
+    return sides, los_sides, (1, 2, 3), (64, 128, 256)
 
 
-def tune(make_counter, dcat, range_proj, key=None, path=None, log=None):
-    """Return the fastest {cell_size, cell_refine, shapes_per_unit}.
+def tune(make_counter, dcat, range_proj, range_los=None, key=None, path=None, log=None):
+    """Return the fastest knob set (a dict over KNOBS, plus its time in 'ms').
 
     ``make_counter(**knobs)`` builds a PairCounter for the knobs; ``dcat`` is
     the device-resident catalogue.  With ``key`` the result is cached."""
@@ -72,17 +85,21 @@ def tune(make_counter, dcat, range_proj, key=None, path=None, log=None):
 
     if key is not None:
         hit = load_cache(path).get(key)
-        if hit:
+        if hit and all(k in hit for k in KNOBS):
             return hit
     n_pos = dcat["Position"].shape[0]
     n_shape = dcat["Position_shape_sample"].shape[0]
     timings = {}
     failures = []
 
+    def norm(knobs):
+        return tuple((k, float(knobs[k]) if k.startswith("cell_size") else int(knobs[k])) for k in KNOBS)
+
     def time_one(knobs):
-        tkey = (knobs["cell_size"], knobs["cell_refine"], knobs["shapes_per_unit"])
+        tkey = norm(knobs)
         if tkey in timings:
             return timings[tkey]
+        bufs = None
         try:
             pc = make_counter(**knobs)
             bufs = pc.allocate(n_pos, n_shape)
@@ -94,28 +111,37 @@ def tune(make_counter, dcat, range_proj, key=None, path=None, log=None):
             e1.record()
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1)
+            if log:
+                log(f"autotune {dict(tkey)} -> {ms:.3f} ms")
         except (MiaError, torch.cuda.OutOfMemoryError) as exc:
             # a candidate whose workspace does not fit or whose edge queue
             # overflows is not a choice; the others still are
             ms = math.inf
-            bufs = None
             failures.append(exc)
             if log:
-                log(f"autotune {knobs} -> skipped ({exc})")
+                log(f"autotune {dict(tkey)} -> skipped ({exc})")
         timings[tkey] = ms
-        if log and math.isfinite(ms):
-            log(f"autotune {knobs} -> {ms:.3f} ms")
         del bufs
         return ms
 
-    sides, refines, units = candidates(range_proj)
-    best = min(({"cell_size": s, "cell_refine": 3, "shapes_per_unit": 128} for s in sides), key=time_one)
-    best = min(({**best, "cell_refine": m} for m in refines), key=time_one)
-    best = min(({**best, "shapes_per_unit": u} for u in units), key=time_one)
-    if not math.isfinite(timings[(best["cell_size"], best["cell_refine"], best["shapes_per_unit"])]):
+    sides, los_sides, refines, units = candidates(range_proj, range_los)
+    # cubic cells first, then narrow cells of one line-of-sight length, then
+    # the line-of-sight geometry, the plane refinement and the unit size
+    # around the best so far
+    cubic = {"cell_size": range_proj / 3.0, "cell_refine": 2, "shapes_per_unit": 128, "cell_size_los": 0.0,
+             "cell_refine_los": 0}
+    best = min(({**cubic, "cell_size": s} for s in sides[:3]), key=time_one)
+    best = min([best] + [{**best, "cell_size": s, "cell_size_los": los_sides[1], "cell_refine_los": 1} for s in sides],
+               key=time_one)
+    if best["cell_size_los"] > 0.0:
+        best = min([best] + [{**best, "cell_size_los": ls, "cell_refine_los": m} for ls in los_sides for m in (1, 2)],
+                   key=time_one)
+    best = min([best] + [{**best, "cell_refine": m} for m in refines], key=time_one)
+    best = min([best] + [{**best, "shapes_per_unit": u} for u in units], key=time_one)
+    if not math.isfinite(time_one(best)):
         raise failures[-1]
-    best = {k: (float(v) if k == "cell_size" else int(v)) for k, v in best.items()}
-    best["ms"] = timings[(best["cell_size"], best["cell_refine"], best["shapes_per_unit"])]
+    out = dict(norm(best))
+    out["ms"] = time_one(best)
     if key is not None:
-        store(key, best, path)
-    return best
+        store(key, out, path)
+    return out

@@ -54,7 +54,7 @@ bool make_plan(const mia_config* cfg, long long n_pos, long long n_shape, Plan* 
   double target[3];
   double cs = cfg->cell_size > 0.0 ? cfg->cell_size : 0.0;
   target[0] = target[1] = cs > 0.0 ? cs : p.range_proj / 2.0;
-  target[2] = cs > 0.0 ? cs : fmax(p.range_los / 2.0, 1e-300);
+  target[2] = cfg->cell_size_los > 0.0 ? cfg->cell_size_los : (cs > 0.0 ? cs : fmax(p.range_los / 2.0, 1e-300));
   long long cells = 1;
   for (int k = 0; k < 3; ++k) {
     long long n = (long long)floor(L / target[k]);
@@ -85,6 +85,7 @@ bool make_plan(const mia_config* cfg, long long n_pos, long long n_shape, Plan* 
     p.R[k] = (int)R;
     // position grid: refine each shape cell m times (at most 1024 cells per side)
     int m = cfg->cell_refine > 0 ? cfg->cell_refine : 3;
+    if (k == 2 && cfg->cell_refine_los > 0) m = cfg->cell_refine_los;
     while (m > 1 && (long long)m * p.n[k] > 1024) --m;
     p.m[k] = m;
     p.nf[k] = m * p.n[k];

@@ -53,7 +53,8 @@ struct Tables {
   double p_break[MIA_MAX_BREAKS];
   long long p_key[MIA_MAX_BREAKS];
   int p_bin[MIA_MAX_BREAKS + 1];
-  // lookup tables: bucket -> interval index | 0x8000 (bucket holds a breakpoint)
+  // lookup tables: bucket -> bin + 1, or first breakpoint index | 0x8000
+  // (the bucket touches a guard band)
   unsigned short lut32[kLut];
   // bin edges (r_bins; pi_bins or mu_r_bins)
   double r_edges[MIA_MAX_BINS_R + 1];

@@ -34,11 +34,15 @@ struct SmemLayout {
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
-// Words of histogram state per (slot, bin).
-__host__ __device__ inline int hist_words(int mixed, int var) {
-  // mixed: cnt, dd lo/hi, sp lo/hi, sx lo/hi (+ var lo/hi)  -- u32 words
-  // fp64 : cnt (u32) + dd, sp, sx (+ var) doubles -> counted in u32 words
-  return mixed ? (7 + (var ? 2 : 0)) : (1 + 6 + (var ? 2 : 0));
+// u32 words of histogram state.  hw: words per replicated array (slots x
+// bins x private copies); knb: slots x bins.
+//   mixed: cnt, dd lo, sp lo, sx lo (+ var lo) replicated; the high words of
+//          the 64-bit sums (dd, sp, sx (+ var)) once per (slot, bin): only
+//          carries reach them, so they need no copies
+//   fp64 : cnt (u32) + dd, sp, sx (+ var) doubles, hw = knb
+__host__ __device__ inline size_t hist_u32_words(int hw, int knb, int mixed, int var) {
+  if (mixed) return (size_t)hw * (4 + var) + (size_t)knb * (3 + var);
+  return (size_t)hw * (1 + 6 + 2 * var) + 4;
 }
 
 struct TablesSmem {
@@ -51,8 +55,7 @@ struct TablesSmem {
   unsigned short lut32[kLut];
 };
 
-// hw: words per histogram array (slots x bins, times the private copies)
-__host__ __device__ inline SmemLayout smem_layout(int J, int spu, int hw, int mixed, int var) {
+__host__ __device__ inline SmemLayout smem_layout(int J, int spu, int hw, int knb, int mixed, int var) {
   SmemLayout L;
   size_t o = 0;
   L.tables = o;
@@ -70,7 +73,7 @@ __host__ __device__ inline SmemLayout smem_layout(int J, int spu, int hw, int mi
   L.seg_shift = o;
   o = align16(o + sizeof(unsigned char) * kSegsPerPass);
   L.hist = o;
-  o = align16(o + sizeof(unsigned) * (size_t)hw * hist_words(mixed, var) + 16);
+  o = align16(o + sizeof(unsigned) * hist_u32_words(hw, knb, mixed, var) + 16);
   L.total = o;
   return L;
 }
@@ -78,25 +81,14 @@ __host__ __device__ inline SmemLayout smem_layout(int J, int spu, int hw, int mi
 // ---- accumulation helpers ---------------------------------------------------
 
 // 64-bit fixed-point add built from native 32-bit shared atomics: the low word
-// takes the value, a carry or borrow out of it goes to the high word.
-__device__ __forceinline__ void acc_fixed(unsigned* lo, int* hi, int idx, int v) {
+// (in a lane's private copy) takes the value, a carry or borrow out of it goes
+// to the bin's one high word.  The sum of a bin is then the sum over copies
+// of the low words plus 2^32 times the high word.
+__device__ __forceinline__ void acc_fixed(unsigned* lo, int* hi, int idx, int hidx, int v) {
   unsigned old = atomicAdd(&lo[idx], (unsigned)v);
   unsigned nw = old + (unsigned)v;
   int d = (v < 0 ? -1 : 0) + (nw < old ? 1 : 0);
-  if (d) atomicAdd(&hi[idx], d);
-}
-
-// Add a signed 64-bit fixed-point partial to a (low word, high word) pair.
-__device__ __forceinline__ void add64_shared(unsigned* lo, int* hi, int idx, long long v) {
-  const unsigned vlo = (unsigned)(unsigned long long)v;
-  int vhi = (int)(v >> 32);
-  const unsigned old = atomicAdd(&lo[idx], vlo);
-  vhi += (old + vlo < old) ? 1 : 0;
-  if (vhi) atomicAdd(&hi[idx], vhi);
-}
-
-__device__ __forceinline__ long long fixed_raw(const unsigned* lo, const int* hi, int idx) {
-  return ((long long)hi[idx] << 32) + (long long)lo[idx];
+  if (d) atomicAdd(&hi[hidx], d);
 }
 
 
@@ -148,7 +140,7 @@ struct HistView {
 // One position in FP32 hi/lo form, moved to the periodic image of its row.
 struct MixedPos {
   float xh, xl, yh, yl, zh, zl, w;
-  int idx, lab, slot, base;
+  int idx, lab, slot, base, hbase;
   bool valid;
 };
 
@@ -167,6 +159,7 @@ __device__ __forceinline__ void load_mixed_pos(const Params& P, const Work& w, c
   p.lab = p.valid ? w.plab_s[pidx] : 0;
   p.slot = slot_of[p.lab];
   p.base = p.slot * nb;
+  p.hbase = p.base;
   p.xh = w.pxh[pidx]; p.xl = w.pxl[pidx];
   p.yh = w.pyh[pidx]; p.yl = w.pyl[pidx];
   p.zh = w.pzh[pidx]; p.zl = w.pzl[pidx];
@@ -230,7 +223,7 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
   // early rejection: surely beyond the last binned separation
   if (q > P.q_cut) return;
   // r bin: logarithmic bucket of q; clean buckets hold the bin itself, buckets
-  // touching a guard band fall back to the exact FP64 breakpoints
+  // touching a guard band fall back to the FP32 guard bands of the breakpoints
   int ib;
   {
     const int bucket = (int)(__float_as_uint(q) >> (23 - kLutMantBits)) - P.lut32_base;
@@ -287,9 +280,9 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
   const float sin2 = 2.0f * dot * fabsf(crs) * inv;
   const float ww = p.w * a.w;
   const float we = p.w * b.w;
-  ++my_binned;
-  if (p.slot >= 0) {
+  if (p.slot >= 0) {  // (binned pairs in the shared histograms are counted at the flush)
     const int k = p.base + bin;
+    const int kh = p.hbase + bin;
     const int vd = __float2int_rn(ww * fixed_scale);
     const int vp = __float2int_rn(we * cos2 * fixed_scale);
     const int vx = __float2int_rn(we * sin2 * fixed_scale);
@@ -299,20 +292,23 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
       vv = __float2int_rn(tv * tv * fixed_scale);
     }
     atomicAdd(&h.cnt[k], 1u);
-    acc_fixed(h.dd_lo, h.dd_hi, k, vd);
-    acc_fixed(h.sp_lo, h.sp_hi, k, vp);
-    acc_fixed(h.sx_lo, h.sx_hi, k, vx);
-    if (VAR) acc_fixed(h.vr_lo, h.vr_hi, k, vv);
+    acc_fixed(h.dd_lo, h.dd_hi, k, kh, vd);
+    acc_fixed(h.sp_lo, h.sp_hi, k, kh, vp);
+    acc_fixed(h.sx_lo, h.sx_hi, k, kh, vx);
+    if (VAR) acc_fixed(h.vr_lo, h.vr_hi, k, kh, vv);
   } else {
     const double sp = (double)(we * cos2);
     const double tv = sp / twoR;
     acc_global(o, P.nb, P.J, label_a, p.lab, bin, (double)ww, sp, (double)(we * sin2), tv * tv, VAR);
     atomicOr(&w.status->flags, kStatusNoSlot);
+    ++my_binned;
   }
 }
 
 // ---- the persistent pair kernel ----------------------------------------------
 
+// (a minimum-blocks bound of 4 gives the same 61 registers but code that
+// runs 8% slower on the 4M/1M w step; the register count alone allows 4)
 template <int MIXED, int VAR, int KIND, int FULL>
 __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __restrict__ ds, int n_ds,
                                                      const unsigned long long* __restrict__ wu_prefix,
@@ -320,7 +316,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x;
   const int nb = P.nb;
-  const SmemLayout SL = smem_layout(P.J, P.shapes_per_unit, HW, MIXED, VAR);
+  const SmemLayout SL = smem_layout(P.J, P.shapes_per_unit, HW, K * P.nb, MIXED, VAR);
   TablesSmem& T = *reinterpret_cast<TablesSmem*>(smem + SL.tables);
   int* slot_of = reinterpret_cast<int*>(smem + SL.slot_of);
   int* slot_region = reinterpret_cast<int*>(smem + SL.slot_region);
@@ -372,15 +368,15 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
   double *dd_d = nullptr, *sp_d = nullptr, *sx_d = nullptr, *vr_d = nullptr;
   if (MIXED) {
     dd_lo = hist + KB;
-    dd_hi = reinterpret_cast<int*>(hist + 2 * KB);
-    sp_lo = hist + 3 * KB;
-    sp_hi = reinterpret_cast<int*>(hist + 4 * KB);
-    sx_lo = hist + 5 * KB;
-    sx_hi = reinterpret_cast<int*>(hist + 6 * KB);
-    if (VAR) {
-      vr_lo = hist + 7 * KB;
-      vr_hi = reinterpret_cast<int*>(hist + 8 * KB);
-    }
+    sp_lo = hist + 2 * KB;
+    sx_lo = hist + 3 * KB;
+    if (VAR) vr_lo = hist + 4 * KB;
+    int* hi = reinterpret_cast<int*>(hist + (4 + VAR) * KB);
+    const int knb = K * nb;
+    dd_hi = hi;
+    sp_hi = hi + knb;
+    sx_hi = hi + 2 * knb;
+    if (VAR) vr_hi = hi + 3 * knb;
   } else {
     // doubles start at an 8-byte boundary after the counts
     size_t off = align16(sizeof(unsigned) * (size_t)KB);
@@ -390,7 +386,8 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
     sx_d = base + 2 * KB;
     if (VAR) vr_d = base + 3 * KB;
   }
-  const int hist_u32 = MIXED ? KB * hist_words(1, VAR) : (int)(align16(sizeof(unsigned) * (size_t)KB) / 4) + KB * 2 * (3 + VAR);
+  const int hist_u32 = MIXED ? (int)hist_u32_words(KB, K * nb, 1, VAR)
+                             : (int)(align16(sizeof(unsigned) * (size_t)KB) / 4) + KB * 2 * (3 + VAR);
 
   // rows of position cells: fine-grid extents along d1 and d2 around a shape cell
   const int N1 = P.full[1] ? P.nf[1] : P.m[1] + 2 * P.Rf[1];
@@ -717,7 +714,6 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
             const double ww = __dmul_rn(pw, D[6 * M + i]);
             const double sp = __dmul_rn(ww, r.ep);
             const double sx = __dmul_rn(ww, r.ex);
-            ++my_binned;
             double tv = 0.0;
             if (VAR) tv = __ddiv_rn(sp, twoR);
             if (slot >= 0) {
@@ -730,6 +726,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
             } else {
               acc_global(o, nb, P.J, u.label, plab, r.bin, ww, sp, sx, __dmul_rn(tv, tv), VAR);
               atomicOr(&w.status->flags, kStatusNoSlot);
+              ++my_binned;
             }
           }
         }
@@ -746,15 +743,17 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
       unsigned cnt = 0;
       for (int c = 0; c < copies; ++c) cnt += h_cnt[c * stride + idx];
       if (cnt == 0) continue;
+      my_binned += cnt;
       double dd, sp, sx, vr = 0.0;
       if (MIXED) {
-        long long vdd = 0, vsp = 0, vsx = 0, vvr = 0;
+        long long vdd = (long long)dd_hi[idx] << 32, vsp = (long long)sp_hi[idx] << 32,
+                  vsx = (long long)sx_hi[idx] << 32, vvr = VAR ? (long long)vr_hi[idx] << 32 : 0;
         for (int c = 0; c < copies; ++c) {
           const int j = c * stride + idx;
-          vdd += fixed_raw(dd_lo, dd_hi, j);
-          vsp += fixed_raw(sp_lo, sp_hi, j);
-          vsx += fixed_raw(sx_lo, sx_hi, j);
-          if (VAR) vvr += fixed_raw(vr_lo, vr_hi, j);
+          vdd += (long long)dd_lo[j];
+          vsp += (long long)sp_lo[j];
+          vsx += (long long)sx_lo[j];
+          if (VAR) vvr += (long long)vr_lo[j];
         }
         dd = (double)vdd * fixed_inv;
         sp = (double)vsp * fixed_inv;
@@ -839,7 +838,7 @@ cudaError_t hist_words_for(const Params& P, int K, int& hw) {
   const int hw_max = 32 * (P.nb | 1);
   int best = hw;
   for (int c = hw_max; c > hw; c -= 16)
-    if ((long long)smem_layout(P.J, P.shapes_per_unit, c, MIXED, VAR).total <= room) {
+    if ((long long)smem_layout(P.J, P.shapes_per_unit, c, K * P.nb, MIXED, VAR).total <= room) {
       best = c;
       break;
     }
@@ -856,7 +855,7 @@ cudaError_t launch_one(const Params& P, const Dataset* ds, int n_ds, const unsig
   auto kern = k_pairs<MIXED, VAR, KIND, FULL>;
   const int hw0 = K * P.nb;
   int per_sm = 0, per_sm0 = 0;
-  size_t smem = smem_layout(P.J, P.shapes_per_unit, hw0, MIXED, VAR).total;
+  size_t smem = smem_layout(P.J, P.shapes_per_unit, hw0, hw0, MIXED, VAR).total;
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm0, kern, kThreads, smem);
@@ -864,7 +863,7 @@ cudaError_t launch_one(const Params& P, const Dataset* ds, int n_ds, const unsig
   per_sm = per_sm0;
   // the copies must not cost a block per SM
   while (hw > hw0) {
-    const size_t s1 = smem_layout(P.J, P.shapes_per_unit, hw, MIXED, VAR).total;
+    const size_t s1 = smem_layout(P.J, P.shapes_per_unit, hw, hw0, MIXED, VAR).total;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1);
     if (e != cudaSuccess) return e;
     int b = 0;
@@ -911,7 +910,7 @@ __global__ void k_batch_prefix(const Dataset* ds, int n, unsigned long long* pre
 }  // namespace
 
 size_t pair_smem_bytes(int J, int spu, int K, int nb, int mixed, int var) {
-  return smem_layout(J, spu, K * nb, mixed, var).total;
+  return smem_layout(J, spu, K * nb, K * nb, mixed, var).total;
 }
 
 cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, unsigned long long* wu_prefix, cudaStream_t st) {

@@ -54,13 +54,14 @@ class PairCounter:
 
     def __init__(self, kind, *, boxsize, r_bins, r_min, r_max, p_bins, los=2, l_subboxes=0, precision="fp64",
                  membership="tree", ellipticity="distortion", want_variance=False, volume=None, rp_cut=0.0,
-                 cell_size=0.0, shapes_per_unit=0, cell_refine=0, device=0):
+                 cell_size=0.0, shapes_per_unit=0, cell_refine=0, cell_size_los=0.0, cell_refine_los=0, device=0):
         if kind not in ("w", "m"):
             raise ValueError(kind)
         self._args = dict(boxsize=boxsize, r_bins=r_bins, r_min=r_min, r_max=r_max, p_bins=p_bins, los=los,
                           l_subboxes=l_subboxes, precision=precision, membership=membership, ellipticity=ellipticity,
                           want_variance=want_variance, volume=volume, rp_cut=rp_cut, device=device)
-        self.knobs = dict(cell_size=cell_size, cell_refine=cell_refine, shapes_per_unit=shapes_per_unit)
+        self.knobs = dict(cell_size=cell_size, cell_refine=cell_refine, shapes_per_unit=shapes_per_unit,
+                          cell_size_los=cell_size_los, cell_refine_los=cell_refine_los)
         self.membership = membership
         self.kind = kind
         self.device = device
@@ -95,6 +96,8 @@ class PairCounter:
         cfg.r_min, cfg.r_max = float(r_min), float(r_max)
         cfg.rp_cut = float(rp_cut)
         cfg.cell_size = float(cell_size)
+        cfg.cell_size_los = float(cell_size_los)
+        cfg.cell_refine_los = int(cell_refine_los)
         cfg.r_edges = self._r_edges.ctypes.data_as(C.POINTER(C.c_double))
         cfg.p_edges = self._p_edges.ctypes.data_as(C.POINTER(C.c_double))
         cfg.q_break = self._qb.ctypes.data_as(C.POINTER(C.c_double))
@@ -218,9 +221,8 @@ class PairCounter:
                                         dcat["Position_shape_sample"].shape[0], float(self._args["boxsize"]),
                                         self.n_r, self.n_p, rp, rl, int(self._args["l_subboxes"]), self.membership,
                                         torch.cuda.get_device_name(self.device))
-        best = autotune.tune(lambda **k: self.with_knobs(**k), dcat, rp, key=key, log=log)
-        return self.with_knobs(cell_size=best["cell_size"], cell_refine=best["cell_refine"],
-                               shapes_per_unit=best["shapes_per_unit"])
+        best = autotune.tune(lambda **k: self.with_knobs(**k), dcat, rp, rl, key=key, log=log)
+        return self.with_knobs(**{k: best[k] for k in autotune.KNOBS})
 
     def to_device(self, cat):
         import torch

@@ -151,7 +151,9 @@ def test_autotune_cache_roundtrip(tmp_path, monkeypatch):
     k3 = autotune.workload_key("w", "mixed", 8_000_000, 1_000_000, 205.0, 10, 8, 20.0, 20.0, 3, "tree", "GB300")
     assert k1 == k2 and k1 != k3
     assert autotune.load_cache() == {}
-    autotune.store(k1, {"cell_size": 11.4, "cell_refine": 3, "shapes_per_unit": 128, "ms": 1.0})
-    assert autotune.load_cache()[k1]["cell_refine"] == 3
-    sides, refines, units = autotune.candidates(20.0)
-    assert len(sides) == 5 and 3 in refines and 128 in units
+    autotune.store(k1, {"cell_size": 2.5, "cell_refine": 2, "shapes_per_unit": 128, "cell_size_los": 20.0,
+                        "cell_refine_los": 1, "ms": 1.0})
+    assert autotune.load_cache()[k1]["cell_refine"] == 2
+    assert set(autotune.KNOBS) <= set(autotune.load_cache()[k1])
+    sides, los_sides, refines, units = autotune.candidates(20.0, 40.0)
+    assert len(sides) == 5 and 40.0 in los_sides and 2 in refines and 128 in units
