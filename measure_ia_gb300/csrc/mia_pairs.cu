@@ -80,15 +80,13 @@ __host__ __device__ inline SmemLayout smem_layout(int J, int spu, int hw, int kn
 
 // ---- accumulation helpers ---------------------------------------------------
 
-// 64-bit fixed-point add built from native 32-bit shared atomics: the low word
-// (in a lane's private copy) takes the value, a carry or borrow out of it goes
-// to the bin's one high word.  The sum of a bin is then the sum over copies
-// of the low words plus 2^32 times the high word.
-__device__ __forceinline__ void acc_fixed(unsigned* lo, int* hi, int idx, int hidx, int v) {
-  unsigned old = atomicAdd(&lo[idx], (unsigned)v);
-  unsigned nw = old + (unsigned)v;
-  int d = (v < 0 ? -1 : 0) + (nw < old ? 1 : 0);
-  if (d) atomicAdd(&hi[hidx], d);
+// 64-bit fixed-point sums built from native 32-bit shared atomics: the low
+// word (in a lane's private copy) takes the value, a carry or borrow out of it
+// goes to the bin's one high word.  The sum of a bin is then the sum over
+// copies of the low words plus 2^32 times the high word.  carry_of: the
+// high-word change for adding v to a low word that held `old`.
+__device__ __forceinline__ int carry_of(unsigned old, int v) {
+  return (v >> 31) + ((old + (unsigned)v) < old ? 1 : 0);
 }
 
 
@@ -224,6 +222,7 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
   if (q > P.q_cut) return;
   // r bin: logarithmic bucket of q; clean buckets hold the bin itself, buckets
   // touching a guard band fall back to the FP32 guard bands of the breakpoints
+  // (a floor(a log2 q + b) form for logarithmic bins measured slower)
   int ib;
   {
     const int bucket = (int)(__float_as_uint(q) >> (23 - kLutMantBits)) - P.lut32_base;
@@ -291,11 +290,22 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
       const float tv = we * cos2 / (float)twoR;
       vv = __float2int_rn(tv * tv * fixed_scale);
     }
+    // low words first (independent atomics), then one rarely taken branch for
+    // the carries and borrows into the high words
+    const unsigned od = atomicAdd(&h.dd_lo[k], (unsigned)vd);
+    const unsigned op = atomicAdd(&h.sp_lo[k], (unsigned)vp);
+    const unsigned ox = atomicAdd(&h.sx_lo[k], (unsigned)vx);
+    unsigned ov = 0;
+    if (VAR) ov = atomicAdd(&h.vr_lo[k], (unsigned)vv);
     atomicAdd(&h.cnt[k], 1u);
-    acc_fixed(h.dd_lo, h.dd_hi, k, kh, vd);
-    acc_fixed(h.sp_lo, h.sp_hi, k, kh, vp);
-    acc_fixed(h.sx_lo, h.sx_hi, k, kh, vx);
-    if (VAR) acc_fixed(h.vr_lo, h.vr_hi, k, kh, vv);
+    const int cd = carry_of(od, vd), cp = carry_of(op, vp), cx = carry_of(ox, vx);
+    const int cv = VAR ? carry_of(ov, vv) : 0;
+    if ((cd | cp | cx | cv) != 0) {
+      if (cd) atomicAdd(&h.dd_hi[kh], cd);
+      if (cp) atomicAdd(&h.sp_hi[kh], cp);
+      if (cx) atomicAdd(&h.sx_hi[kh], cx);
+      if (VAR && cv) atomicAdd(&h.vr_hi[kh], cv);
+    }
   } else {
     const double sp = (double)(we * cos2);
     const double tv = sp / twoR;
