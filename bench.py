@@ -163,9 +163,26 @@ def time_counter(pc, dcat, steps, warmup, stream, ws=1):
         pc.run(dcat, bufs, stream)
         evs[i + 1].record(stream)
     torch.cuda.synchronize()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
     ms = evs[0].elapsed_time(evs[-1]) / steps
     per = [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
     return ms, per, pc.fetch(bufs)
+
+
+def aggregate_ranks(t_step, binned, ws, device="cuda"):
+    """Whole-job figures of ws replicas: the slowest rank's step time and the
+    binned pairs of all ranks together (one all-reduce each; no data path)."""
+    if ws == 1:
+        return t_step, binned
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(t_step)], dtype=torch.float64, device=device)
+    b = torch.tensor([float(binned)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(b, op=dist.ReduceOp.SUM)
+    return float(t.item()), int(round(b.item()))
 
 
 def _pick(pc, dcat, args):
@@ -348,6 +365,8 @@ def main():
     ap.add_argument("--shapes", type=int, default=1_000_000, help="shape-sample size (profiling runs)")
     args = ap.parse_args()
     rank, ws, local = world()
+    if args.impl == "reference" and rank != 0:
+        return  # the CPU reference arm runs on rank 0 only
     if args.workload != "config2":
         import torch
         torch.cuda.set_device(local)
@@ -366,8 +385,6 @@ def main():
     cores = os.cpu_count() or 1
 
     if args.impl == "reference":
-        if rank != 0:
-            return
         results = []
         for _ in range(args.warmup):
             cpu_reference(data, max(100, args.cpu_sample // 4), cores)
@@ -396,14 +413,8 @@ def main():
         import torch.distributed as dist
         dist.init_process_group("nccl")
     r = run_gpu(args, data, rank, ws, local)
-    t_step = r["ms"] / 1e3
-    if ws > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([t_step], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_step = float(t.item())
-    value = r["binned"] * ws / t_step
+    t_step, binned_all = aggregate_ranks(r["ms"] / 1e3, r["binned"], ws)
+    value = binned_all / t_step
     import torch
     props = torch.cuda.get_device_properties(local)
     peak = props.multi_processor_count * 128 * 2070e6 / 1e12

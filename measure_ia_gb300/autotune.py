@@ -29,7 +29,7 @@ import os
 
 KNOBS = ("cell_size", "cell_refine", "shapes_per_unit", "cell_size_los", "cell_refine_los")
 DEFAULT = {"cell_size": 0.0, "cell_refine": 0, "shapes_per_unit": 0, "cell_size_los": 0.0, "cell_refine_los": 0}
-_VERSION = "g2"  # geometry search with separate line-of-sight cells
+_VERSION = "g3"  # geometry search with separate line-of-sight cells
 
 
 def cache_path():
@@ -69,7 +69,7 @@ def store(key, choice, path=None):
 def candidates(range_proj, range_los=None):
     """Search axes: projected sides, line-of-sight sides, refinements, unit sizes."""
     range_los = range_proj if range_los is None else range_los
-    sides = [range_proj / k for k in (2.0, 3.0, 4.0, 6.0, 8.0)]
+    sides = [range_proj / k for k in (2.0, 3.0, 4.0, 5.0, 6.0, 8.0)]
     los_sides = [range_los * f for f in (0.5, 1.0, 2.0)]
     return sides, los_sides, (1, 2, 3), (64, 128, 256)
 
@@ -125,17 +125,25 @@ def tune(make_counter, dcat, range_proj, range_los=None, key=None, path=None, lo
         return ms
 
     sides, los_sides, refines, units = candidates(range_proj, range_los)
-    # cubic cells first, then narrow cells of one line-of-sight length, then
+    rl = range_proj if range_los is None else range_los
+
+    def los_refine(ls, depth):
+        # position cells about rl / depth deep along the line of sight: the
+        # positions a warp holds then span a short stretch of it, so their
+        # line-of-sight windows over the staged shapes nearly coincide
+        return max(1, int(round(depth * ls / rl)))
+
+    # cubic cells first, then narrow cells one line-of-sight range long, then
     # the line-of-sight geometry, the plane refinement and the unit size
     # around the best so far
     cubic = {"cell_size": range_proj / 3.0, "cell_refine": 2, "shapes_per_unit": 128, "cell_size_los": 0.0,
              "cell_refine_los": 0}
     best = min(({**cubic, "cell_size": s} for s in sides[:3]), key=time_one)
-    best = min([best] + [{**best, "cell_size": s, "cell_size_los": los_sides[1], "cell_refine_los": 1} for s in sides],
-               key=time_one)
+    best = min([best] + [{**best, "cell_size": s, "cell_size_los": rl, "cell_refine_los": los_refine(rl, 6)}
+                         for s in sides[1:]], key=time_one)
     if best["cell_size_los"] > 0.0:
-        best = min([best] + [{**best, "cell_size_los": ls, "cell_refine_los": m} for ls in los_sides for m in (1, 2)],
-                   key=time_one)
+        best = min([best] + [{**best, "cell_size_los": ls, "cell_refine_los": los_refine(ls, d)}
+                             for ls in los_sides for d in (3, 6)], key=time_one)
     best = min([best] + [{**best, "cell_refine": m} for m in refines], key=time_one)
     best = min([best] + [{**best, "shapes_per_unit": u} for u in units], key=time_one)
     if not math.isfinite(time_one(best)):

@@ -86,8 +86,26 @@ __device__ __forceinline__ int natural_region(const int ci[3], const PrepArgs& A
   return (sub[0] * A.n_sub + sub[1]) * A.n_sub + sub[2];
 }
 
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_xor_sync(0xffffffffu, v, o);
+    v = x > v ? x : v;
+  }
+  return v;
+}
+
+// Per-galaxy labels and cells.  Region counts and sums go to per-block shared
+// histograms (J entries, dynamic shared memory) flushed once per block, and
+// the largest |weight| (bit pattern of a non-negative double: integer order =
+// value order) to one atomic per warp: a few hundred blocks then touch the
+// J + 2 global words instead of every galaxy.
 __global__ void k_prep_positions(PrepArgs A, const double* __restrict__ pos, const double* __restrict__ w_in,
                                  long long n, Work w) {
+  extern __shared__ __align__(8) unsigned char prep_smem[];
+  unsigned* s_np = reinterpret_cast<unsigned*>(prep_smem);
+  for (int j = threadIdx.x; j < A.J; j += blockDim.x) s_np[j] = 0u;
+  __syncthreads();
+  unsigned long long mx = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     double v[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
     if (!(in_box(v[0], A.L) && in_box(v[1], A.L) && in_box(v[2], A.L))) flag_range(w.status, i);
@@ -97,14 +115,31 @@ __global__ void k_prep_positions(PrepArgs A, const double* __restrict__ pos, con
     w.pcell[i] = cell;
     w.plab[i] = lab;
     atomicAdd(&w.pcount[cell], 1);
-    if (A.J > 0) atomicAdd(&w.reg.npos[lab], 1ULL);
-    atomicMax(&w.status->maxw_bits, (unsigned long long)__double_as_longlong(fabs(w_in[i])));
+    if (A.J > 0) atomicAdd(&s_np[lab], 1u);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(w_in[i]));
+    mx = b > mx ? b : mx;
   }
+  mx = warp_max_u64(mx);
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(&w.status->maxw_bits, mx);
+  __syncthreads();
+  for (int j = threadIdx.x; j < A.J; j += blockDim.x)
+    if (s_np[j]) atomicAdd(&w.reg.npos[j], (unsigned long long)s_np[j]);
 }
 
 __global__ void k_prep_shapes(PrepArgs A, const double* __restrict__ spos, const double* __restrict__ q,
                               const double* __restrict__ ws, long long n, Work w) {
+  extern __shared__ __align__(8) unsigned char prep_smem[];
+  double* s_s1 = reinterpret_cast<double*>(prep_smem);
+  double* s_s2 = s_s1 + A.J;
+  unsigned* s_ns = reinterpret_cast<unsigned*>(s_s2 + A.J);
+  for (int j = threadIdx.x; j < A.J; j += blockDim.x) {
+    s_s1[j] = 0.0;
+    s_s2[j] = 0.0;
+    s_ns[j] = 0u;
+  }
+  __syncthreads();
   double s1 = 0.0, s2 = 0.0;
+  unsigned long long mx = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     double v[3] = {spos[3 * i], spos[3 * i + 1], spos[3 * i + 2]};
     if (!(in_box(v[0], A.L) && in_box(v[1], A.L) && in_box(v[2], A.L))) flag_range(w.status, i);
@@ -126,14 +161,25 @@ __global__ void k_prep_shapes(PrepArgs A, const double* __restrict__ spos, const
     double wsi = ws[i];
     double t1 = __dmul_rn(wsi, __dsub_rn(1.0, __dmul_rn(__dmul_rn(e, e), 0.5)));
     if (A.J > 0) {
-      atomicAdd(&w.reg.nshape[lab], 1ULL);
-      atomicAdd(&w.reg.s1[lab], t1);
-      atomicAdd(&w.reg.s2[lab], wsi);
+      atomicAdd(&s_ns[lab], 1u);
+      atomicAdd(&s_s1[lab], t1);
+      atomicAdd(&s_s2[lab], wsi);
     }
     s1 += t1;
     s2 += wsi;
-    double mws = fmax(fabs(wsi), fabs(wsi * e));
-    atomicMax(&w.status->maxws_bits, (unsigned long long)__double_as_longlong(mws));
+    const double mws = fmax(fabs(wsi), fabs(wsi * e));
+    const unsigned long long b = (unsigned long long)__double_as_longlong(mws);
+    mx = b > mx ? b : mx;
+  }
+  mx = warp_max_u64(mx);
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(&w.status->maxws_bits, mx);
+  __syncthreads();
+  for (int j = threadIdx.x; j < A.J; j += blockDim.x) {
+    if (s_ns[j]) {
+      atomicAdd(&w.reg.nshape[j], (unsigned long long)s_ns[j]);
+      atomicAdd(&w.reg.s1[j], s_s1[j]);
+      atomicAdd(&w.reg.s2[j], s_s2[j]);
+    }
   }
   // block totals
   for (int o = 16; o > 0; o >>= 1) {
@@ -373,9 +419,13 @@ cudaError_t launch_prep(const Plan& plan, const Params& P, const mia_catalog& ca
   A.ellipticity = P.ellipticity;
   const int T = 256;
   int mixed = P.precision == MIA_MIXED;
-  k_prep_positions<<<grid_for(cat.n_pos, T), T, 0, st>>>(A, cat.position, cat.weight, cat.n_pos, w);
-  k_prep_shapes<<<grid_for(cat.n_shape, T), T, 0, st>>>(A, cat.position_shape, cat.q, cat.weight_shape, cat.n_shape,
-                                                        w);
+  // at most 1024 blocks, so that the per-block region histograms are flushed
+  // a bounded number of times
+  const int gp = grid_for(cat.n_pos, T) < 1024 ? grid_for(cat.n_pos, T) : 1024;
+  const int gs = grid_for(cat.n_shape, T) < 1024 ? grid_for(cat.n_shape, T) : 1024;
+  k_prep_positions<<<gp, T, sizeof(unsigned) * (size_t)plan.J, st>>>(A, cat.position, cat.weight, cat.n_pos, w);
+  k_prep_shapes<<<gs, T, (2 * sizeof(double) + sizeof(unsigned)) * (size_t)plan.J, st>>>(
+      A, cat.position_shape, cat.q, cat.weight_shape, cat.n_shape, w);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if ((e = scan(w.pcount, plan.n_fcells, w.pstart, w.tiles, nullptr, st)) != cudaSuccess) return e;
