@@ -145,9 +145,13 @@ def _errors(ref, got, keys):
     return out
 
 
-def time_counter(pc, dcat, steps, warmup, stream, ws=1):
-    """ms per step (CUDA events on the launching stream), per-step list, products."""
+def time_counter(pc, dcat, steps, warmup, stream, ws=1, kernel_ms=None):
+    """ms per step (CUDA events on the launching stream), per-step list, products.
+    With a list ``kernel_ms``, the pair kernel's own launch durations in the
+    timed steps (CUDA events the library records around that launch, on the
+    same stream) are appended to it."""
     import torch
+    from measure_ia_gb300 import engine
     n_pos, n_shape = dcat["Position"].shape[0], dcat["Position_shape_sample"].shape[0]
     bufs = pc.allocate(n_pos, n_shape)
     for _ in range(warmup):
@@ -157,6 +161,8 @@ def time_counter(pc, dcat, steps, warmup, stream, ws=1):
         import torch.distributed as dist
         dist.barrier()
     evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    if kernel_ms is not None:
+        engine.profile_pairs(pc.device, steps)
     torch.cuda.synchronize()
     evs[0].record(stream)
     for i in range(steps):
@@ -168,7 +174,22 @@ def time_counter(pc, dcat, steps, warmup, stream, ws=1):
         dist.barrier()
     ms = evs[0].elapsed_time(evs[-1]) / steps
     per = [evs[i].elapsed_time(evs[i + 1]) for i in range(steps)]
+    if kernel_ms is not None:
+        kernel_ms.extend(engine.pair_kernel_ms(pc.device, steps))
+        engine.profile_pairs(pc.device, 0)
     return ms, per, pc.fetch(bufs)
+
+
+def profiled_traffic():
+    """DRAM bytes (read + write) per pair-kernel launch on this workload, from
+    the committed ncu summary, or None."""
+    import re
+    try:
+        with open(os.path.join(ROOT, "profiles", "pairs_config2_w_jk27.md")) as f:
+            m = re.search(r"^dram_bytes_per_launch:\s*(\d+)", f.read(), re.M)
+        return int(m.group(1)) if m else None
+    except OSError:
+        return None
 
 
 def aggregate_ranks(t_step, binned, ws, device="cuda"):
@@ -214,7 +235,8 @@ def run_gpu(args, data, rank, ws, local):
     knobs = dict(pcm.knobs)
 
     with ClockSampler(local) as clk:
-        msm, per_m, mm = time_counter(pcm, dcat, args.steps, args.warmup, stream, ws)
+        kms = []
+        msm, per_m, mm = time_counter(pcm, dcat, args.steps, args.warmup, stream, ws, kernel_ms=kms)
     clocks = clk.summary()
     per_step = {"mixed": per_m}
     if args.only_mixed:
@@ -246,7 +268,7 @@ def run_gpu(args, data, rank, ws, local):
                                                               ("proj_gg", "multipole gg (l=0)"),
                                                               ("cov_gp", "cov g+"), ("cov_gg", "cov gg")))}
 
-    res = dict(binned=binned, ms=msm, ms64=ms64, clocks=clocks, counts_exact=counts_exact, err=err,
+    res = dict(binned=binned, ms=msm, kernel_ms=kms, ms64=ms64, clocks=clocks, counts_exact=counts_exact, err=err,
                stats=mm.stats, stats64=m64.stats, per_step=per_step, knobs=knobs, mult=mult,
                e2e_s=float("nan"), h2d=0, d2h=0)
     if args.no_e2e:
@@ -418,7 +440,11 @@ def main():
     import torch
     props = torch.cuda.get_device_properties(local)
     peak = props.multi_processor_count * 128 * 2070e6 / 1e12
-    achieved = LANE_OPS_PER_PAIR * r["binned"] / t_step / 1e12
+    # the pair kernel's own average launch time in the timed steps (its share
+    # of the step is the rest of the device time: preparation, re-test, post)
+    k_ms = float(np.mean(r["kernel_ms"])) if r["kernel_ms"] else r["ms"]
+    achieved = LANE_OPS_PER_PAIR * r["binned"] / (k_ms / 1e3) / 1e12
+    traffic = profiled_traffic()
     if rank != 0:
         return
     launches_per_step = 20  # prep 15 (prep 2, scans 9, scatter 2, work units 2), work prefix 1, pairs 1, edge re-test 1, post 1, status 1
@@ -432,8 +458,13 @@ def main():
         "accuracy_mixed_vs_fp64": r["err"], "counts_bit_exact_mixed_vs_fp64": r["counts_exact"],
         "binned_pairs_per_step": r["binned"], "edge_pairs_retested": r["stats"]["edge_pairs"],
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": None,
-                     "note": "32 FP32 lane-ops per binned pair over the whole step; peak = SMs x 128 x 2070 MHz"},
+                     "frac": achieved / peak, "traffic": traffic,
+                     "kernel": "k_pairs (persistent pair kernel)", "kernel_ms": k_ms,
+                     "kernel_share_of_step": k_ms / r["ms"],
+                     "note": "achieved = 32 FP32 lane-ops per binned pair / the pair kernel's mean launch time "
+                             "(CUDA events on the launching stream, timed steps); peak = nominal SMs x 128 x "
+                             "2070 MHz (no FP32 figure in MEASURED_PEAKS.json); traffic = DRAM bytes per "
+                             "launch from profiles/pairs_config2_w_jk27.md (ncu)"},
         "cpu_baseline": cpu,
         "e2e": {"value": r["binned"] / r["e2e_s"], "unit": "binned pairs/s", "h2d_bytes_per_step": r["h2d"],
                 "d2h_bytes_per_step": r["d2h"]},

@@ -196,6 +196,17 @@ MIA_API int mia_batch_status(mia_context* ctx, int n, void* workspace, void* str
 MIA_API int mia_measure_batch(mia_context* ctx, const mia_config* cfg, int n, const mia_catalog* cats,
                               void* workspace, size_t workspace_bytes, const mia_result* results, void* stream);
 
+
+/* Opt-in timing of the pair kernel (the dominant stage), for profiling: with
+   n_slots > 0 every later mia_measure / mia_batch_enqueue on this context
+   records a CUDA event pair around its pair-kernel launch, on the caller's
+   stream, into a ring of n_slots entries; n_slots = 0 switches it off.
+   mia_profile_read waits for and returns the durations (ms) of the last
+   min(n, recorded, n_slots) launches, oldest first, in *n_out.  No counterpart
+   in the reference (its Pool has no device stage to time). */
+MIA_API int mia_profile_pairs(mia_context* ctx, int n_slots);
+MIA_API int mia_profile_read(mia_context* ctx, float* ms, int n, int* n_out);
+
 /* Size of the library's own device scratch used by mia_measure_static. */
 #define MIA_STATIC_SCRATCH_BYTES (64ull * 1024ull * 1024ull)
 

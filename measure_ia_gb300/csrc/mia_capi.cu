@@ -14,7 +14,18 @@ struct mia_context {
   int device;
   int num_sms;
   std::string err;
+  // pair-kernel launch timing (mia_profile_pairs): a ring of event pairs
+  std::vector<cudaEvent_t> prof_start, prof_stop;
+  long long prof_count = 0;  // launches recorded since enabling
 };
+
+static void free_profile_events(mia_context* c) {
+  for (cudaEvent_t e : c->prof_start) cudaEventDestroy(e);
+  for (cudaEvent_t e : c->prof_stop) cudaEventDestroy(e);
+  c->prof_start.clear();
+  c->prof_stop.clear();
+  c->prof_count = 0;
+}
 
 namespace mia {
 
@@ -320,6 +331,12 @@ using namespace mia;
 
 extern "C" {
 
+static int fail(mia_context* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+
 int mia_version(void) { return 1; }
 
 int mia_create(int device, mia_context** out) {
@@ -338,7 +355,39 @@ int mia_create(int device, mia_context** out) {
 }
 
 int mia_destroy(mia_context* ctx) {
+  if (ctx) free_profile_events(ctx);
   delete ctx;
+  return MIA_OK;
+}
+
+int mia_profile_pairs(mia_context* ctx, int n_slots) {
+  if (!ctx || n_slots < 0) return MIA_ERR_ARG;
+  free_profile_events(ctx);
+  for (int i = 0; i < n_slots; ++i) {
+    cudaEvent_t a, b;
+    if (cudaEventCreate(&a) != cudaSuccess) return fail(ctx, MIA_ERR_CUDA, "cudaEventCreate");
+    if (cudaEventCreate(&b) != cudaSuccess) {
+      cudaEventDestroy(a);
+      return fail(ctx, MIA_ERR_CUDA, "cudaEventCreate");
+    }
+    ctx->prof_start.push_back(a);
+    ctx->prof_stop.push_back(b);
+  }
+  return MIA_OK;
+}
+
+int mia_profile_read(mia_context* ctx, float* ms, int n, int* n_out) {
+  if (!ctx || !ms || !n_out || n < 0) return MIA_ERR_ARG;
+  const long long slots = (long long)ctx->prof_start.size();
+  long long have = ctx->prof_count < slots ? ctx->prof_count : slots;
+  if (have > n) have = n;
+  for (long long k = 0; k < have; ++k) {  // oldest first among the last `have`
+    const long long j = (ctx->prof_count - have + k) % slots;
+    if (cudaEventSynchronize(ctx->prof_stop[j]) != cudaSuccess ||
+        cudaEventElapsedTime(&ms[k], ctx->prof_start[j], ctx->prof_stop[j]) != cudaSuccess)
+      return fail(ctx, MIA_ERR_CUDA, "pair-kernel timing events");
+  }
+  *n_out = (int)have;
   return MIA_OK;
 }
 
@@ -393,11 +442,6 @@ int mia_output_layout(const mia_config* cfg, mia_layout* lay) {
   take(lay->stats, 8);
   lay->total = o;
   return MIA_OK;
-}
-
-static int fail(mia_context* ctx, int code, const std::string& msg) {
-  if (ctx) ctx->err = msg;
-  return code;
 }
 
 #define MIA_CUDA(call)                                                                             \
@@ -647,7 +691,13 @@ int mia_batch_enqueue(mia_context* ctx, const mia_config* cfg, int n, const mia_
     MIA_CUDA(launch_prep(pl, P, cats[i], d.w, st));
   }
   MIA_CUDA(launch_batch_prefix(ds_dev, n, prefix, st));
+  const long long slot = ctx->prof_start.empty() ? -1 : ctx->prof_count % (long long)ctx->prof_start.size();
+  if (slot >= 0) MIA_CUDA(cudaEventRecord(ctx->prof_start[slot], st));
   MIA_CUDA(launch_pairs(bp.plans[0], P, ds_dev, n, prefix, &hdr->wu_next, st, ctx->num_sms));
+  if (slot >= 0) {
+    MIA_CUDA(cudaEventRecord(ctx->prof_stop[slot], st));
+    ++ctx->prof_count;
+  }
   for (int i = 0; i < n; ++i) {
     Dataset d;
     make_dataset(bp.plans[i], b + bp.off[i], cats[i], results[i], lay, &d);

@@ -30,6 +30,28 @@ def context(device: int) -> C.c_void_p:
     return _CONTEXTS[device]
 
 
+def profile_pairs(device: int, n_slots: int) -> None:
+    """Record CUDA events around the next pair-kernel launches of this device's
+    context (a ring of n_slots; 0 switches recording off)."""
+    lib = L.load()
+    ctx = context(device)
+    rc = lib.mia_profile_pairs(ctx, int(n_slots))
+    if rc != L.MIA_OK:
+        raise L.MiaError(rc, lib.mia_last_error(ctx).decode())
+
+
+def pair_kernel_ms(device: int, n: int) -> list:
+    """Durations (ms) of the last n recorded pair-kernel launches, oldest first."""
+    lib = L.load()
+    ctx = context(device)
+    buf = (C.c_float * max(int(n), 1))()
+    got = C.c_int()
+    rc = lib.mia_profile_read(ctx, buf, int(n), C.byref(got))
+    if rc != L.MIA_OK:
+        raise L.MiaError(rc, lib.mia_last_error(ctx).decode())
+    return [float(buf[i]) for i in range(got.value)]
+
+
 def _dptr(ptr):
     return C.cast(ptr, C.POINTER(C.c_double))
 
