@@ -81,13 +81,29 @@ __host__ __device__ inline SmemLayout smem_layout(int J, int spu, int hw, int kn
 // ---- accumulation helpers ---------------------------------------------------
 
 // 64-bit fixed-point sums built from native 32-bit shared atomics: the low
-// word (in a lane's private copy) takes the value, a carry or borrow out of it
-// goes to the bin's one high word.  The sum of a bin is then the sum over
-// copies of the low words plus 2^32 times the high word.  carry_of: the
-// high-word change for adding v to a low word that held `old`.
-__device__ __forceinline__ int carry_of(unsigned old, int v) {
-  return (v >> 31) + ((old + (unsigned)v) < old ? 1 : 0);
+// word (in a lane's private copy) is a signed 32-bit partial that takes the
+// value; when adding v overflows it (it wraps by 2^32) the bin's one high word
+// takes +1 or -1.  The sum of a bin is the sum over copies of the signed low
+// words plus 2^32 times the high word.  overflow_of is negative exactly when
+// adding v to a low word that held `old` overflowed.
+__device__ __forceinline__ int overflow_of(unsigned old, int v) {
+  const unsigned nw = old + (unsigned)v;
+  return (int)((old ^ nw) & ((unsigned)v ^ nw));
 }
+
+// Fixed-point scales of one dataset (powers of two).  The staged shape weights
+// carry sc_dd (w_s) and sc_sp (w_s e), so a pair's terms come out scaled.
+//   S+D, SxD : |term| <= 2^30 -- signed terms, typically a few per cent of
+//              the largest, so the partial of one (copy, bin) random-walks
+//              inside 2^31 over a work unit; the rounding is far below the
+//              FP32 error of a term, which the cancelling bins of w_g+ need
+//   w        : |term| <= 2^24 -- a positive sum that only grows: it wraps the
+//              low word once per ~10^3 adds
+//   var      : |term| <= 2^22 (squares, likewise positive)
+struct Scales {
+  float sc_dd, sc_sp, c_vr;   // c_vr: (S+D term scaled)^2 -> variance term scaled
+  double inv_dd, inv_sp, inv_vr;
+};
 
 
 // Direct global accumulation (pairs whose position region has no slot, and the
@@ -193,7 +209,7 @@ template <int KIND, int FULL, int VAR>
 __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T, const float4& a, const float4& b,
                                            const float2* C, const int* I, int i, const MixedPos& p,
                                            const HistView& h, const Work& w, const Out& o,
-                                           float fixed_scale, double twoR, int label_a,
+                                           const Scales& sc, double twoR, int label_a,
                                            unsigned long long& my_binned) {
   float dz = (a.z - p.zh) + (b.z - p.zl);
   bool edge = false;
@@ -277,39 +293,38 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
   const float inv = __fdividef(1.0f, qp);
   const float cos2 = (dot * dot - crs * crs) * inv;
   const float sin2 = 2.0f * dot * fabsf(crs) * inv;
-  const float ww = p.w * a.w;
-  const float we = p.w * b.w;
+  const float ww = p.w * a.w;   // scaled by sc_dd
+  const float we = p.w * b.w;   // scaled by sc_sp
+  const float tp = we * cos2, tx = we * sin2;
   if (p.slot >= 0) {  // (binned pairs in the shared histograms are counted at the flush)
     const int k = p.base + bin;
     const int kh = p.hbase + bin;
-    const int vd = __float2int_rn(ww * fixed_scale);
-    const int vp = __float2int_rn(we * cos2 * fixed_scale);
-    const int vx = __float2int_rn(we * sin2 * fixed_scale);
+    const int vd = __float2int_rn(ww);
+    const int vp = __float2int_rn(tp);
+    const int vx = __float2int_rn(tx);
     int vv = 0;
-    if (VAR) {
-      const float tv = we * cos2 / (float)twoR;
-      vv = __float2int_rn(tv * tv * fixed_scale);
-    }
+    if (VAR) vv = __float2int_rn(tp * tp * sc.c_vr);
     // low words first (independent atomics), then one rarely taken branch for
-    // the carries and borrows into the high words
+    // the overflows into the high words
     const unsigned od = atomicAdd(&h.dd_lo[k], (unsigned)vd);
     const unsigned op = atomicAdd(&h.sp_lo[k], (unsigned)vp);
     const unsigned ox = atomicAdd(&h.sx_lo[k], (unsigned)vx);
     unsigned ov = 0;
     if (VAR) ov = atomicAdd(&h.vr_lo[k], (unsigned)vv);
     atomicAdd(&h.cnt[k], 1u);
-    const int cd = carry_of(od, vd), cp = carry_of(op, vp), cx = carry_of(ox, vx);
-    const int cv = VAR ? carry_of(ov, vv) : 0;
-    if ((cd | cp | cx | cv) != 0) {
-      if (cd) atomicAdd(&h.dd_hi[kh], cd);
-      if (cp) atomicAdd(&h.sp_hi[kh], cp);
-      if (cx) atomicAdd(&h.sx_hi[kh], cx);
-      if (VAR && cv) atomicAdd(&h.vr_hi[kh], cv);
+    const int fd = overflow_of(od, vd), fp = overflow_of(op, vp), fx = overflow_of(ox, vx);
+    const int fv = VAR ? overflow_of(ov, vv) : 0;
+    if ((fd | fp | fx | fv) < 0) {
+      if (fd < 0) atomicAdd(&h.dd_hi[kh], (vd >> 31) | 1);
+      if (fp < 0) atomicAdd(&h.sp_hi[kh], (vp >> 31) | 1);
+      if (fx < 0) atomicAdd(&h.sx_hi[kh], (vx >> 31) | 1);
+      if (VAR && fv < 0) atomicAdd(&h.vr_hi[kh], (vv >> 31) | 1);
     }
   } else {
-    const double sp = (double)(we * cos2);
+    const double sp = (double)tp * sc.inv_sp;
     const double tv = sp / twoR;
-    acc_global(o, P.nb, P.J, label_a, p.lab, bin, (double)ww, sp, (double)(we * sin2), tv * tv, VAR);
+    acc_global(o, P.nb, P.J, label_a, p.lab, bin, (double)ww * sc.inv_dd, sp, (double)tx * sc.inv_sp, tv * tv,
+               VAR);
     atomicOr(&w.status->flags, kStatusNoSlot);
     ++my_binned;
   }
@@ -339,8 +354,8 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
   __shared__ int s_wu;
   __shared__ int s_ds;
   __shared__ Dataset s_data;        // the current unit's dataset (workspace and outputs)
-  __shared__ double s_twoR, s_fixed_inv;
-  __shared__ float s_fixed_scale;
+  __shared__ double s_twoR;
+  __shared__ Scales s_sc;
   __shared__ int s_nslots;
   __shared__ int s_copies;
   __shared__ int s_stride;
@@ -424,14 +439,26 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
           s_data = ds[lo];
           const Work& wd = ds[lo].w;
           s_twoR = 2.0 * (wd.reg.s1[P.J] / wd.reg.s2[P.J]);
-          // fixed-point scale 2^S with |term| * 2^S <= 2^30 for every pair term of the dataset
+          // fixed-point scales 2^S with m * 2^S within each sum's bound, m the
+          // largest |w_p| * max(|w_s|, |w_s e|) of the dataset (ilogb: exact floor(log2))
           double m = __longlong_as_double((long long)wd.status->maxw_bits) *
                      __longlong_as_double((long long)wd.status->maxws_bits);
           if (!(m > 0.0) || !(m < 1e300)) m = 1.0;
-          int S = (int)floor(log2(1073741824.0 / m));
-          S = S > 40 ? 40 : (S < -60 ? -60 : S);
-          s_fixed_scale = ldexpf(1.0f, S);
-          s_fixed_inv = ldexp(1.0, -S);
+          double mv = m / fabs(s_twoR);
+          mv = mv * mv;
+          if (!(mv > 0.0) || !(mv < 1e300)) mv = 1.0;
+          auto expo = [](double room) {
+            const int e = ilogb(room);
+            return e > 60 ? 60 : (e < -100 ? -100 : e);
+          };
+          const int Ssp = expo(1073741824.0 / m), Sdd = expo(16777216.0 / m), Svr = expo(4194304.0 / mv);
+          s_sc.sc_dd = (float)ldexp(1.0, Sdd);
+          s_sc.sc_sp = (float)ldexp(1.0, Ssp);
+          // (tp / 2^Ssp / twoR)^2 * 2^Svr = tp^2 * c_vr
+          s_sc.c_vr = (float)(ldexp(1.0, Svr - 2 * Ssp) / (s_twoR * s_twoR));
+          s_sc.inv_dd = ldexp(1.0, -Sdd);
+          s_sc.inv_sp = ldexp(1.0, -Ssp);
+          s_sc.inv_vr = ldexp(1.0, -Svr);
         }
       }
     }
@@ -441,8 +468,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
     const Work& w = s_data.w;
     const Out& o = s_data.o;
     const double twoR = s_twoR;
-    const float fixed_scale = s_fixed_scale;
-    const double fixed_inv = s_fixed_inv;
+    const Scales& sc = s_sc;
     unsigned long long my_binned = 0;
     const WorkUnit u = w.wu[wi];
     int c[3];
@@ -523,8 +549,9 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
       float z = 0.f;
       const int g = u.begin + tid;
       if (tid < S) {
-        ra = make_float4(w.sxh[g], w.syh[g], w.szh[g], w.swsf[g]);
-        rb = make_float4(w.sxl[g], w.syl[g], w.szl[g], w.swef[g]);
+        // weights times the (power-of-two) fixed-point scales: exact
+        ra = make_float4(w.sxh[g], w.syh[g], w.szh[g], w.swsf[g] * sc.sc_dd);
+        rb = make_float4(w.sxl[g], w.syl[g], w.szl[g], w.swef[g] * sc.sc_sp);
         rc = make_float2(w.saxf[g], w.sayf[g]);
         z = ra.z + rb.z;
         zs[tid] = z;
@@ -700,7 +727,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
               // next shape in flight while this pair is processed (index S at most:
               // still inside the staging area)
               const float4 an = A[i + 1], bn = B[i + 1];
-              mixed_pair<KIND, FULL, VAR>(P, T, a, b, C, I, i, p0, hv, w, o, fixed_scale, twoR, u.label, my_binned);
+              mixed_pair<KIND, FULL, VAR>(P, T, a, b, C, I, i, p0, hv, w, o, sc, twoR, u.label, my_binned);
               a = an;
               b = bn;
             }
@@ -758,17 +785,17 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
       if (MIXED) {
         long long vdd = (long long)dd_hi[idx] << 32, vsp = (long long)sp_hi[idx] << 32,
                   vsx = (long long)sx_hi[idx] << 32, vvr = VAR ? (long long)vr_hi[idx] << 32 : 0;
-        for (int c = 0; c < copies; ++c) {
+        for (int c = 0; c < copies; ++c) {  // low words are signed partials
           const int j = c * stride + idx;
-          vdd += (long long)dd_lo[j];
-          vsp += (long long)sp_lo[j];
-          vsx += (long long)sx_lo[j];
-          if (VAR) vvr += (long long)vr_lo[j];
+          vdd += (long long)(int)dd_lo[j];
+          vsp += (long long)(int)sp_lo[j];
+          vsx += (long long)(int)sx_lo[j];
+          if (VAR) vvr += (long long)(int)vr_lo[j];
         }
-        dd = (double)vdd * fixed_inv;
-        sp = (double)vsp * fixed_inv;
-        sx = (double)vsx * fixed_inv;
-        if (VAR) vr = (double)vvr * fixed_inv;
+        dd = (double)vdd * sc.inv_dd;
+        sp = (double)vsp * sc.inv_sp;
+        sx = (double)vsx * sc.inv_sp;
+        if (VAR) vr = (double)vvr * sc.inv_vr;
       } else {
         dd = dd_d[idx];
         sp = sp_d[idx];
