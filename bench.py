@@ -274,8 +274,15 @@ def run_gpu(args, data, rank, ws, local):
     if args.no_e2e:
         return res
     # end to end through the public API with host buffers: H2D copies, the
-    # measurement, D2H of every product and the dataset writes, every step
-    host = {k: data[k] for k in keys}
+    # measurement, D2H of every product and the dataset writes, every step.
+    # The catalogue sits in pinned (page-locked) host memory, handed over as
+    # numpy arrays like the reference's inputs.
+    host = {}
+    for k in keys:
+        a = np.ascontiguousarray(data[k], dtype=np.float64)
+        pinned = torch.empty(a.shape, dtype=torch.float64, pin_memory=True)
+        pinned.numpy()[...] = a
+        host[k] = pinned.numpy()
     host["LOS"] = 2
     box = MeasureIABox(dict(host), None, None, None, [0.1, 20.0], 10, 8, 20.0, boxsize=L_BOX, num_nodes=2,
                        precision="mixed", device=local, autotune=not args.no_tune)

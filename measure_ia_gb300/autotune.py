@@ -29,7 +29,7 @@ import os
 
 KNOBS = ("cell_size", "cell_refine", "shapes_per_unit", "cell_size_los", "cell_refine_los")
 DEFAULT = {"cell_size": 0.0, "cell_refine": 0, "shapes_per_unit": 0, "cell_size_los": 0.0, "cell_refine_los": 0}
-_VERSION = "g3"  # geometry search with separate line-of-sight cells
+_VERSION = "g4"  # geometry search with separate line-of-sight cells
 
 
 def cache_path():
@@ -143,7 +143,7 @@ def tune(make_counter, dcat, range_proj, range_los=None, key=None, path=None, lo
                          for s in sides[1:]], key=time_one)
     if best["cell_size_los"] > 0.0:
         best = min([best] + [{**best, "cell_size_los": ls, "cell_refine_los": los_refine(ls, d)}
-                             for ls in los_sides for d in (3, 6)], key=time_one)
+                             for ls in los_sides for d in (3, 6, 10)], key=time_one)
     best = min([best] + [{**best, "cell_refine": m} for m in refines], key=time_one)
     best = min([best] + [{**best, "shapes_per_unit": u} for u in units], key=time_one)
     if not math.isfinite(time_one(best)):

@@ -23,6 +23,7 @@ r_min and r_max, then their set difference, measure_w_box_jk.py:577-580).
 
 from __future__ import annotations
 
+import functools
 from dataclasses import dataclass
 
 import numpy as np
@@ -137,6 +138,34 @@ def _wrap_index(ind, n):
     return np.where(ind < 0, ind + n, ind)
 
 
+_TABLES = {}
+
+
+def _memo(fn):
+    """Tables depend only on their arguments and this host's numpy: build each
+    once per process (a table takes ~10 ms of bisection) and share it
+    read-only."""
+
+    def key(a):
+        if isinstance(a, (np.ndarray, list, tuple)):
+            return ("edges",) + tuple(float(x) for x in np.asarray(a, dtype=np.float64).ravel())
+        return a
+
+    @functools.wraps(fn)
+    def cached(*args, **kw):
+        k = (fn.__name__,) + tuple(key(a) for a in args) + tuple(sorted((n, key(v)) for n, v in kw.items()))
+        tab = _TABLES.get(k)
+        if tab is None:
+            tab = fn(*args, **kw)
+            tab.breaks.setflags(write=False)
+            tab.bins.setflags(write=False)
+            _TABLES[k] = tab
+        return tab
+
+    return cached
+
+
+@_memo
 def r_table(kind, r_bins, r_min, r_max, num_bins_r, membership="tree", rp_cut=0.0):
     """Bin of q = d^2 (w: r_p^2; multipoles: r^2), -1 if the pair is not binned.
 
@@ -167,6 +196,7 @@ def r_table(kind, r_bins, r_min, r_max, num_bins_r, membership="tree", rp_cut=0.
     return _table(f, bottom, top, seeds)
 
 
+@_memo
 def pi_table(pi_bins, num_bins_pi):
     """Bin of Pi (line-of-sight separation), -1 outside [pi_bins[0], pi_bins[-1])
     (measure_w_box_jk.py:603-617)."""
@@ -186,6 +216,7 @@ def pi_table(pi_bins, num_bins_pi):
     return _table(f, pi_bins[0] - span, pi_bins[-1] + span, list(pi_bins))
 
 
+@_memo
 def mu_table(mu_r_bins, num_bins_pi):
     """Bin of mu_r = Pi / r over [-1, 1] (measure_m_box_jk.py:646-653)."""
     mu_r_bins = np.asarray(mu_r_bins, dtype=np.float64)
