@@ -315,6 +315,7 @@ def run_batch48(args, local):
     pc = PairCounter("w", boxsize=L_BOX, r_bins=R_BINS, r_min=0.1, r_max=20.0, p_bins=PI_BINS, l_subboxes=3,
                      precision="mixed", device=local)
     dcats = [pc.to_device(c) for c in cats]
+    pc = _pick(pc, dcats[int(np.argmax(sizes))], args)  # launch knobs of the largest catalogue
     stream = torch.cuda.current_stream(local)
     # one after the other
     bufs = [pc.allocate(d["Position"].shape[0], d["Position_shape_sample"].shape[0]) for d in dcats]
@@ -345,12 +346,66 @@ def run_batch48(args, local):
     batch.status()
     ms = e0.elapsed_time(e1) / args.steps
     same = all(np.array_equal(batch.fetch(i).npairs, pc.fetch(b).npairs) for i, b in enumerate(bufs))
+    fp64 = None
+    if args.fp64:  # the plain FP64 form, one catalogue after the other, one step
+        pc64 = PairCounter("w", boxsize=L_BOX, r_bins=R_BINS, r_min=0.1, r_max=20.0, p_bins=PI_BINS, l_subboxes=3,
+                           precision="fp64", device=local, **pc.knobs)
+        ms64, exact, errs = 0.0, True, []
+        for i, d in enumerate(dcats):
+            t, _, m64 = time_counter(pc64, d, 1, 0, stream)
+            ms64 += t
+            exact &= bool(np.array_equal(m64.npairs, batch.fetch(i).npairs))
+            errs.append(_errors(m64, batch.fetch(i), (("proj_gp", "w_g+"), ("proj_gg", "w_gg"))))
+        worst = {k: max(e[k]["max_rel_to_vector_scale"] for e in errs) for k in ("w_g+", "w_gg")}
+        fp64 = {"value": binned / (ms64 / 1e3), "ms_per_step": ms64, "counts_bit_exact_mixed_vs_fp64": exact,
+                "max_rel_to_vector_scale_over_catalogues": worst}
     return {"metric": "binned pairs/s, 48 uneven catalogues, w_gg+w_g+ 27JK, mixed form", "value": binned / (ms / 1e3),
             "unit": "binned pairs/s", "ms_per_step": ms, "one_after_the_other_ms": seq_ms,
-            "binned_pairs_per_step": binned, "counts_equal_to_one_by_one": bool(same),
+            "binned_pairs_per_step": binned, "counts_equal_to_one_by_one": bool(same), "fp64_form": fp64,
+            "knobs": pc.knobs,
             "config": {"workload": "48 catalogues, sizes log-uniform 5e3-2e6 (config 3)",
                        "n_positions_total": int(sum(len(c["Position"]) for c in cats)),
                        "n_shapes_total": int(sum(len(c["Position_shape_sample"]) for c in cats))}}
+
+
+def run_small(args, local, which):
+    """Config 0 (10,000 uniform galaxies, shape = position sample, weights 1,
+    w only) or config 1 (clustered, 20,000 parents x Poisson(50), 200k shapes,
+    w and multipoles with 20 mu bins over [-1, 1]); 27 jackknife regions;
+    both forms, autotuned knobs."""
+    import torch
+    from measure_ia_gb300.catalogs import neyman_scott_catalog, uniform_catalog
+    from measure_ia_gb300.engine import PairCounter
+    if which == "config0":
+        data = uniform_catalog(10000, L_BOX, 2024)
+        kinds = [("w", PI_BINS)]
+    else:
+        data = neyman_scott_catalog(20000, L_BOX, 200_000, 11, mean_children=50, sigma=1.0, kappa=2.0)
+        kinds = [("w", PI_BINS), ("m", np.linspace(-1.0, 1.0, 21))]
+    stream = torch.cuda.current_stream(local)
+    out = {}
+    for kind, pbins in kinds:
+        common = dict(boxsize=L_BOX, r_bins=R_BINS, r_min=0.1, r_max=20.0, p_bins=pbins, l_subboxes=3, device=local)
+        pcm = PairCounter(kind, precision="mixed", **common)
+        dcat = pcm.to_device(data)
+        pcm = _pick(pcm, dcat, args)
+        ms, _, mm = time_counter(pcm, dcat, args.steps, args.warmup, stream)
+        pc64 = PairCounter(kind, precision="fp64", **common, **pcm.knobs)
+        ms64, _, m64 = time_counter(pc64, dcat, max(1, min(args.steps, 3)), 1, stream)
+        b = mm.stats["binned_pairs"]
+        label = "w" if kind == "w" else "multipoles"
+        out[label] = {"binned_pairs_per_step": b, "mixed": {"value": b / (ms / 1e3), "ms_per_step": ms},
+                      "fp64": {"value": b / (ms64 / 1e3), "ms_per_step": ms64},
+                      "counts_bit_exact_mixed_vs_fp64": bool(np.array_equal(mm.npairs, m64.npairs)),
+                      "accuracy_mixed_vs_fp64": _errors(m64, mm, (("proj_gp", "g+"), ("proj_gg", "gg"))),
+                      "knobs": pcm.knobs}
+    first = out["w"]
+    desc = ("10,000 uniform galaxies, w_gg+w_g+ 27JK (config 0)" if which == "config0" else
+            "clustered 1M positions / 200k shapes, w and multipoles, 27JK (config 1)")
+    return {"metric": f"binned pairs/s, {desc}, mixed form", "value": first["mixed"]["value"],
+            "unit": "binned pairs/s", "ms_per_step": first["mixed"]["ms_per_step"], "forms": out,
+            "config": {"workload": desc, "n_positions": int(len(data["Position"])),
+                       "n_shapes": int(len(data["Position_shape_sample"]))}}
 
 
 def run_large(args, local):
@@ -368,9 +423,17 @@ def run_large(args, local):
     dcat = pc.to_device(data)
     pc = _pick(pc, dcat, args)
     ms, per, m = time_counter(pc, dcat, args.steps, max(1, args.warmup), torch.cuda.current_stream(local))
+    fp64 = None
+    if args.fp64:  # the plain FP64 form, one step
+        pc64 = PairCounter("w", boxsize=1000.0, r_bins=rb, r_min=0.1, r_max=60.0, p_bins=pb, l_subboxes=5,
+                           precision="fp64", device=local, **pc.knobs)
+        ms64, _, m64 = time_counter(pc64, dcat, 1, 0, torch.cuda.current_stream(local))
+        fp64 = {"value": m.stats["binned_pairs"] / (ms64 / 1e3), "ms_per_step": ms64,
+                "counts_bit_exact_mixed_vs_fp64": bool(np.array_equal(m64.npairs, m.npairs)),
+                "accuracy_mixed_vs_fp64": _errors(m64, m, (("proj_gp", "w_g+"), ("proj_gg", "w_gg")))}
     return {"metric": "binned pairs/s, w_gg+w_g+ 125JK, 1000 Mpc/h box, mixed form",
             "value": m.stats["binned_pairs"] / (ms / 1e3), "unit": "binned pairs/s", "ms_per_step": ms,
-            "step_ms": per, "binned_pairs_per_step": m.stats["binned_pairs"], "knobs": pc.knobs,
+            "step_ms": per, "binned_pairs_per_step": m.stats["binned_pairs"], "knobs": pc.knobs, "fp64_form": fp64,
             "config": {"workload": "25M positions / 5M shapes, 1000 Mpc/h, 15x20 bins, 125 jackknife (config 4)",
                        "n_positions": int(len(data["Position"])), "n_shapes": int(len(data["Position_shape_sample"]))}}
 
@@ -388,7 +451,8 @@ def main():
     ap.add_argument("--no-tune", action="store_true", help="default launch knobs instead of the autotuner's")
     ap.add_argument("--knobs", default="", help="CELL,REFINE,SPU[,CELL_LOS,REFINE_LOS] launch knobs instead of tuning (profiling runs)")
     ap.add_argument("--no-multipoles", action="store_true", help="skip the multipole rate and accuracy report")
-    ap.add_argument("--workload", default="config2", choices=["config2", "batch48", "large"],
+    ap.add_argument("--fp64", action="store_true", help="batch48 / large: also time the plain FP64 form")
+    ap.add_argument("--workload", default="config2", choices=["config2", "batch48", "large", "config0", "config1"],
                     help="config2 = the headline line; batch48 and large print their own lines")
     ap.add_argument("--centres", type=int, default=80000, help="Neyman-Scott parents (profiling runs)")
     ap.add_argument("--shapes", type=int, default=1_000_000, help="shape-sample size (profiling runs)")
@@ -399,7 +463,12 @@ def main():
     if args.workload != "config2":
         import torch
         torch.cuda.set_device(local)
-        line = run_batch48(args, local) if args.workload == "batch48" else run_large(args, local)
+        if args.workload == "batch48":
+            line = run_batch48(args, local)
+        elif args.workload == "large":
+            line = run_large(args, local)
+        else:
+            line = run_small(args, local, args.workload)
         line.update({"n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
                      "data": "synthetic"})
         if rank == 0:

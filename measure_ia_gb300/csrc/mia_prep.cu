@@ -18,6 +18,7 @@ namespace {
 struct PrepArgs {
   double L;
   double L_sub;      // L_0p5 * 2.0 / L_subboxes, as the reference forms it
+  double inv_L_sub;  // 1 / L_sub: a first guess of the sub-box index only
   int n_sub, J;
   int axis[3];       // original axis of cell dimension k
   int n[3];
@@ -29,12 +30,15 @@ struct PrepArgs {
 
 // Jackknife label of a point (original axes): i*n^2 + j*n + k for the sub-box
 // it lies strictly inside, 0 on any face or outside (measure_IA_base.py:428-451).
-__device__ __forceinline__ int jk_label(const double v[3], double L_sub, int n_sub) {
+// x * (1 / L_sub) guesses the index to within one (no FP64 division, slow on
+// this part); the exact products k * L_sub, as the reference forms its bounds,
+// then move it to the sub-box that strictly contains x, if any.
+__device__ __forceinline__ int jk_label(const double v[3], double L_sub, double inv_L_sub, int n_sub) {
   if (n_sub <= 1) return 0;
   int idx[3];
   for (int a = 0; a < 3; ++a) {
     double x = v[a];
-    int k = (int)floor(x / L_sub);
+    int k = (int)floor(x * inv_L_sub);
     k = k < 0 ? 0 : (k >= n_sub ? n_sub - 1 : k);
     double lo = __dmul_rn((double)k, L_sub);
     double hi = __dmul_rn((double)(k + 1), L_sub);
@@ -111,7 +115,7 @@ __global__ void k_prep_positions(PrepArgs A, const double* __restrict__ pos, con
     if (!(in_box(v[0], A.L) && in_box(v[1], A.L) && in_box(v[2], A.L))) flag_range(w.status, i);
     double c[3] = {v[A.axis[0]], v[A.axis[1]], v[A.axis[2]]};
     int cell = fine_cell_of(c, A);
-    int lab = jk_label(v, A.L_sub, A.n_sub);
+    int lab = jk_label(v, A.L_sub, A.inv_L_sub, A.n_sub);
     w.pcell[i] = cell;
     w.plab[i] = lab;
     atomicAdd(&w.pcount[cell], 1);
@@ -146,7 +150,7 @@ __global__ void k_prep_shapes(PrepArgs A, const double* __restrict__ spos, const
     double c[3] = {v[A.axis[0]], v[A.axis[1]], v[A.axis[2]]};
     int ci[3];
     int cell = cell_of(c, A, ci);
-    int lab = jk_label(v, A.L_sub, A.n_sub);
+    int lab = jk_label(v, A.L_sub, A.inv_L_sub, A.n_sub);
     w.scell[i] = cell;
     w.slab[i] = lab;
     atomicAdd(&w.scount[cell], 1);
@@ -408,6 +412,7 @@ cudaError_t launch_prep(const Plan& plan, const Params& P, const mia_catalog& ca
   A.L = P.L;
   A.n_sub = plan.n_sub;
   A.L_sub = (P.L / 2.0) * 2.0 / (double)(plan.n_sub > 0 ? plan.n_sub : 1);
+  A.inv_L_sub = 1.0 / A.L_sub;
   A.J = plan.J;
   for (int k = 0; k < 3; ++k) {
     A.axis[k] = plan.axis[k];
