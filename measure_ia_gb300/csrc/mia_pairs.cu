@@ -298,7 +298,6 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
   const float tp = we * cos2, tx = we * sin2;
   if (p.slot >= 0) {  // (binned pairs in the shared histograms are counted at the flush)
     const int k = p.base + bin;
-    const int kh = p.hbase + bin;
     const int vd = __float2int_rn(ww);
     const int vp = __float2int_rn(tp);
     const int vx = __float2int_rn(tx);
@@ -315,6 +314,7 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
     const int fd = overflow_of(od, vd), fp = overflow_of(op, vp), fx = overflow_of(ox, vx);
     const int fv = VAR ? overflow_of(ov, vv) : 0;
     if ((fd | fp | fx | fv) < 0) {
+      const int kh = p.hbase + bin;
       if (fd < 0) atomicAdd(&h.dd_hi[kh], (vd >> 31) | 1);
       if (fp < 0) atomicAdd(&h.sp_hi[kh], (vp >> 31) | 1);
       if (fx < 0) atomicAdd(&h.sx_hi[kh], (vx >> 31) | 1);
@@ -722,14 +722,18 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
           const int wlo = __reduce_min_sync(0xffffffffu, i_lo);
           const int whi = __reduce_max_sync(0xffffffffu, i_hi);
           if (p0.valid && wlo < whi) {
-            float4 a = A[wlo], b = B[wlo];
-            for (int i = wlo; i < whi; ++i) {
-              // next shape in flight while this pair is processed (index S at most:
-              // still inside the staging area)
-              const float4 an = A[i + 1], bn = B[i + 1];
-              mixed_pair<KIND, FULL, VAR>(P, T, a, b, C, I, i, p0, hv, w, o, sc, twoR, u.label, my_binned);
-              a = an;
-              b = bn;
+            // the next shape is in flight while this pair is processed (index S
+            // at most: still inside the staging area); two register sets take
+            // turns, so the prefetched shape is never copied
+            float4 a0 = A[wlo], b0 = B[wlo];
+            for (int i = wlo;;) {
+              const float4 a1 = A[i + 1], b1 = B[i + 1];
+              mixed_pair<KIND, FULL, VAR>(P, T, a0, b0, C, I, i, p0, hv, w, o, sc, twoR, u.label, my_binned);
+              if (++i >= whi) break;
+              a0 = A[i + 1];
+              b0 = B[i + 1];
+              mixed_pair<KIND, FULL, VAR>(P, T, a1, b1, C, I, i, p0, hv, w, o, sc, twoR, u.label, my_binned);
+              if (++i >= whi) break;
             }
           }
         }
