@@ -197,6 +197,20 @@ MIA_API int mia_measure_batch(mia_context* ctx, const mia_config* cfg, int n, co
                               void* workspace, size_t workspace_bytes, const mia_result* results, void* stream);
 
 
+/* Jackknife covariance of two datasets (or of one with itself: pass the same
+   pointer twice), on device, from their realisations: real_a and real_b hold
+   n_real rows of n_bins doubles (row starts stride_a / stride_b doubles
+   apart; e.g. the proj_gp_jk block of two mia_measure outputs).  Writes
+   cov (n_bins x n_bins, row-major, cov[j][i] pairs a's bin j with b's bin i)
+   and std (n_bins) as the reference forms them: f = (n_real - 1) / n_real,
+   cov = f * sum_r (a_r - mean_a)(b_r - mean_b)^T, std = sqrt(f * sum_r
+   (a_r - mean_a)(b_r - mean_b)) elementwise (NaN where that is negative).
+   All pointers are device memory; enqueued on `stream`.  Replaces
+   MeasureJackknife.measure_covariance_multiple_datasets
+   (measure_jackknife.py:485-571) without the HDF5 round trip. */
+MIA_API int mia_jackknife_cross_cov(mia_context* ctx, int n_real, int n_bins, const double* real_a, int64_t stride_a,
+                                    const double* real_b, int64_t stride_b, double* cov, double* std, void* stream);
+
 /* Opt-in timing of the pair kernel (the dominant stage), for profiling: with
    n_slots > 0 every later mia_measure / mia_batch_enqueue on this context
    records a CUDA event pair around its pair-kernel launch, on the caller's

@@ -22,7 +22,7 @@ MAX_BINS_R, MAX_BINS_P, MAX_BREAKS = 64, 128, 96
 EXPORTED = ("mia_create", "mia_destroy", "mia_last_error", "mia_version", "mia_workspace_size",
             "mia_output_layout", "mia_measure", "mia_measure_static", "mia_batch_workspace_size",
             "mia_batch_prepare", "mia_batch_enqueue", "mia_batch_status", "mia_measure_batch",
-            "mia_profile_pairs", "mia_profile_read")
+            "mia_profile_pairs", "mia_profile_read", "mia_jackknife_cross_cov")
 STATIC_SCRATCH_BYTES = 64 * 1024 * 1024
 
 
@@ -103,6 +103,9 @@ def load(path=None):
         f.restype = C.c_int
     lib.mia_batch_status.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p]
     lib.mia_batch_status.restype = C.c_int
+    lib.mia_jackknife_cross_cov.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_void_p, C.c_int64, C.c_void_p,
+                                            C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.mia_jackknife_cross_cov.restype = C.c_int
     lib.mia_profile_pairs.argtypes = [C.c_void_p, C.c_int]
     lib.mia_profile_pairs.restype = C.c_int
     lib.mia_profile_read.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]

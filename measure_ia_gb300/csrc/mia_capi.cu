@@ -360,6 +360,19 @@ int mia_destroy(mia_context* ctx) {
   return MIA_OK;
 }
 
+int mia_jackknife_cross_cov(mia_context* ctx, int n_real, int n_bins, const double* real_a, int64_t stride_a,
+                            const double* real_b, int64_t stride_b, double* cov, double* std, void* stream) {
+  if (!ctx) return MIA_ERR_ARG;
+  if (n_real < 1 || n_bins < 1 || n_bins > 4096 || !real_a || !real_b || !cov || !std || stride_a < n_bins ||
+      stride_b < n_bins)
+    return fail(ctx, MIA_ERR_ARG, "cross covariance: need n_real >= 1, 1 <= n_bins <= 4096, strides >= n_bins");
+  const cudaError_t e = launch_cross_cov(n_real, n_bins, real_a, stride_a, real_b, stride_b, cov, std,
+                                         static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return fail(ctx, MIA_ERR_CUDA, std::string("cross covariance: ") + cudaGetErrorString(e));
+  ctx->err.clear();
+  return MIA_OK;
+}
+
 int mia_profile_pairs(mia_context* ctx, int n_slots) {
   if (!ctx || n_slots < 0) return MIA_ERR_ARG;
   free_profile_events(ctx);

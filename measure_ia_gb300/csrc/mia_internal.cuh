@@ -292,5 +292,7 @@ cudaError_t launch_edge_retest(const Params& P, const Work& w, const Out& o, cud
 cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, unsigned long long* wu_prefix, cudaStream_t st);
 cudaError_t launch_post(const Params& P, const Work& w, const mia_layout& lay, double* out, double volume,
                         long long n_pos, long long n_shape, cudaStream_t st);
+cudaError_t launch_cross_cov(int n_real, int n_bins, const double* a, long long sa, const double* b, long long sb,
+                             double* cov, double* std, cudaStream_t st);
 
 }  // namespace mia

@@ -178,7 +178,50 @@ __global__ void k_post(PostArgs A, Work w, mia_layout lay, double* out) {
   }
 }
 
+// Jackknife covariance of two datasets' realisations (measure_jackknife.py:
+// 519-555): realisation means, cov[j][i] = f * sum_b (a_b[j] - ma[j]) *
+// (b_b[i] - mb[i]) and std[j] = sqrt(f * sum_b (a_b[j] - ma[j]) *
+// (b_b[j] - mb[j])), f = (n - 1) / n, every sum in realisation order and
+// every product rounded before its add, as numpy forms them.  One block:
+// the inputs are (1 + J) x n_r values.
+__global__ void k_cross_cov(int n_real, int n_bins, const double* __restrict__ a, long long sa,
+                            const double* __restrict__ b, long long sb, double* cov, double* std) {
+  extern __shared__ double means[];
+  double* ma = means;
+  double* mb = means + n_bins;
+  for (int j = threadIdx.x; j < n_bins; j += blockDim.x) {
+    double s = 0.0, t = 0.0;
+    for (int r = 0; r < n_real; ++r) {
+      s = __dadd_rn(s, a[r * sa + j]);
+      t = __dadd_rn(t, b[r * sb + j]);
+    }
+    ma[j] = __ddiv_rn(s, (double)n_real);
+    mb[j] = __ddiv_rn(t, (double)n_real);
+  }
+  __syncthreads();
+  const double f = __ddiv_rn((double)(n_real - 1), (double)n_real);
+  for (int e = threadIdx.x; e < n_bins * n_bins; e += blockDim.x) {
+    const int j = e / n_bins, i = e - j * n_bins;
+    double s = 0.0;
+    for (int r = 0; r < n_real; ++r)
+      s = __dadd_rn(s, __dmul_rn(__dsub_rn(a[r * sa + j], ma[j]), __dsub_rn(b[r * sb + i], mb[i])));
+    cov[e] = __dmul_rn(s, f);
+  }
+  for (int j = threadIdx.x; j < n_bins; j += blockDim.x) {
+    double s = 0.0;
+    for (int r = 0; r < n_real; ++r)
+      s = __dadd_rn(s, __dmul_rn(__dsub_rn(a[r * sa + j], ma[j]), __dsub_rn(b[r * sb + j], mb[j])));
+    std[j] = __dsqrt_rn(__dmul_rn(s, f));
+  }
+}
+
 }  // namespace
+
+cudaError_t launch_cross_cov(int n_real, int n_bins, const double* a, long long sa, const double* b, long long sb,
+                             double* cov, double* std, cudaStream_t st) {
+  k_cross_cov<<<1, 256, 2 * sizeof(double) * (size_t)n_bins, st>>>(n_real, n_bins, a, sa, b, sb, cov, std);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_post(const Params& P, const Work& w, const mia_layout& lay, double* out, double volume,
                         long long n_pos, long long n_shape, cudaStream_t st) {

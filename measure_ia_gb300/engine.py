@@ -52,6 +52,40 @@ def pair_kernel_ms(device: int, n: int) -> list:
     return [float(buf[i]) for i in range(got.value)]
 
 
+def jackknife_cross_cov(real_a, real_b=None, device: int = 0, stream=None):
+    """Jackknife covariance and std of two datasets' realisations (n_real x
+    n_bins each; ``real_b=None`` = ``real_a`` with itself), computed on the
+    device by ``mia_jackknife_cross_cov`` (measure_jackknife.py:485-571).
+    Inputs are CUDA tensors (rows may be strided) or host arrays; returns
+    (cov, std) as CUDA tensors."""
+    import torch
+    dev = torch.device("cuda", device)
+
+    def dev2d(x):
+        t = x if isinstance(x, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(x, dtype=np.float64))
+        t = t.to(device=dev, dtype=torch.float64)
+        if t.dim() != 2 or t.stride(1) != 1:
+            t = t.reshape(t.shape[0], -1).contiguous()
+        return t
+
+    a = dev2d(real_a)
+    b = a if real_b is None else dev2d(real_b)
+    if a.shape != b.shape:
+        raise ValueError(f"realisation shapes differ: {tuple(a.shape)} vs {tuple(b.shape)}")
+    n_real, n_bins = a.shape
+    cov = torch.empty((n_bins, n_bins), dtype=torch.float64, device=dev)
+    std = torch.empty(n_bins, dtype=torch.float64, device=dev)
+    st = stream if stream is not None else torch.cuda.current_stream(dev)
+    lib = L.load()
+    ctx = context(device)
+    rc = lib.mia_jackknife_cross_cov(ctx, int(n_real), int(n_bins), C.c_void_p(a.data_ptr()), int(a.stride(0)),
+                                     C.c_void_p(b.data_ptr()), int(b.stride(0)), C.c_void_p(cov.data_ptr()),
+                                     C.c_void_p(std.data_ptr()), C.c_void_p(st.cuda_stream))
+    if rc != L.MIA_OK:
+        raise L.MiaError(rc, lib.mia_last_error(ctx).decode())
+    return cov, std
+
+
 def _dptr(ptr):
     return C.cast(ptr, C.POINTER(C.c_double))
 
@@ -365,3 +399,17 @@ class BatchCounter:
 
     def fetch(self, i):
         return self.pc.fetch((None, self.outs[i], self.cnts[i]))
+
+    def realisations(self, i, key="gp"):
+        """Catalogue i's jackknife realisations of w (or the multipoles),
+        key 'gp' or 'gg': a (J, n_r) view of its device output."""
+        off = getattr(self.pc.layout, f"proj_{key}_jk")
+        J, nr = self.pc.J, self.pc.n_r
+        return self.outs[i][off:off + J * nr].view(J, nr)
+
+    def cross_covariance(self, i, j=None, key="gp"):
+        """Jackknife covariance between catalogues i and j (i with itself
+        when j is None) straight from the device outputs: (cov, std) CUDA
+        tensors."""
+        b = None if j is None else self.realisations(j, key)
+        return jackknife_cross_cov(self.realisations(i, key), b, device=self.pc.device)

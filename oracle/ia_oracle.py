@@ -406,6 +406,58 @@ def combine_jackknife(realisations):
     return mean, std, cov
 
 
+def jackknife_cross_cov(real_a, real_b):
+    """Jackknife covariance of two datasets' realisations (n_box, n_r) each
+    (``MeasureJackknife.measure_covariance_multiple_datasets``,
+    measure_jackknife.py:519-555): means in realisation order, then
+    cov[:, i] += (a_b - mean_a) * (b_b[i] - mean_b[i]) and
+    std += (a_b - mean_a) * (b_b - mean_b), both times (n - 1) / n, std
+    square-rooted (NaN where the cross sum is negative).  With real_a is
+    real_b it is the single-dataset branch (:533-539)."""
+    real_a = np.asarray(real_a, dtype=np.float64)
+    real_b = np.asarray(real_b, dtype=np.float64)
+    n_box, nr = real_a.shape
+    ma = np.zeros(nr)
+    mb = np.zeros(nr)
+    for x in real_a:
+        ma += x
+    ma /= n_box
+    for x in real_b:
+        mb += x
+    mb /= n_box
+    cov = np.zeros((nr, nr))
+    std = np.zeros(nr)
+    for xa, xb in zip(real_a, real_b):
+        std += (xa - ma) * (xb - mb)
+        for i in range(nr):
+            cov[:, i] += (xa - ma) * (xb[i] - mb[i])
+    std *= (n_box - 1) / n_box
+    with np.errstate(invalid="ignore"):
+        std = np.sqrt(std)
+    cov *= (n_box - 1) / n_box
+    return cov, std
+
+
+def full_projection_cov(cov_00, cov_11, cov_22, cov_01, cov_02, cov_12):
+    """The combined covariances of three projections
+    (``create_full_cov_matrix_projections``, measure_jackknife.py:604-635):
+    returns (cov3, cov2 of 0-1, cov2 of 0-2, cov2 of 1-2).  The reference
+    reads its 'cov_yz' from the (0, 2) pair dataset and its 'cov_xz' from the
+    (1, 2) one (:611-612) and assembles with those names; this follows it."""
+    cov_xx, cov_yy, cov_zz, cov_xy = cov_00, cov_11, cov_22, cov_01
+    cov_yz, cov_xz = cov_02, cov_12
+    cov3 = np.concatenate((np.concatenate((cov_xx, cov_xy, cov_xz), axis=1),
+                           np.concatenate((cov_xy.T, cov_yy, cov_yz), axis=1),
+                           np.concatenate((cov_xz.T, cov_yz.T, cov_zz), axis=1)), axis=0)
+    cov2xy = np.concatenate((np.concatenate((cov_xx, cov_xy), axis=1),
+                             np.concatenate((cov_xy.T, cov_yy), axis=1)), axis=0)
+    cov2xz = np.concatenate((np.concatenate((cov_xx, cov_xz), axis=1),
+                             np.concatenate((cov_xz.T, cov_zz), axis=1)), axis=0)
+    cov2yz = np.concatenate((np.concatenate((cov_yy, cov_yz), axis=1),
+                             np.concatenate((cov_yz.T, cov_zz), axis=1)), axis=0)
+    return cov3, cov2xy, cov2xz, cov2yz
+
+
 def _sub(a, b):
     return "/".join(x for x in (a + "/" + b).split("/") if x)
 

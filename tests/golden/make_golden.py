@@ -18,6 +18,10 @@ GPU host and never from the test suite.  Two kinds of fixture:
    output files ``tests/data/processed/TNG300/mock_IA_TNG300*.hdf5``, read
    with the minimal HDF5 reader in ``h5read.py``.
 
+3. ``crosscov_los3.npz`` -- three line-of-sight projections of one catalogue
+   measured by the reference, then its cross-dataset jackknife covariance
+   functions on that output (``run_crosscov``).
+
 Usage:  python tests/golden/make_golden.py
 """
 
@@ -249,6 +253,51 @@ def run_case(name, builder, kw, calls):
     print(name, "datasets:", sum(1 for k in arrays if k.startswith("out/")))
 
 
+def run_crosscov():
+    """Cross-dataset jackknife covariance: three projections (LOS = 0, 1, 2) of
+    one clustered catalogue measured by the reference (w, jk8, multiprocessing
+    backend), then the reference's own
+    ``MeasureJackknife.measure_covariance_multiple_datasets`` and
+    ``create_full_cov_matrix_projections`` (measure_jackknife.py:485-652) on
+    that output, called on the box object (they use only the output file,
+    ``snap_group`` and ``num_bins_r``).  Returned arrays go to ``res/...``."""
+    from measureia import MeasureIABox
+    from measureia.measure_jackknife import MeasureJackknife
+    base = clustered_case(21, 250, 205.0, 2000)
+    kw = dict(simulation=None, snapshot=None, separation_limits=[0.1, 20.0], num_bins_r=10, num_bins_pi=8,
+              pi_max=20.0, boxsize=205.0, num_nodes=2)
+    outfile = "/tmp/golden_crosscov.hdf5"
+    _FILES.pop(outfile, None)
+    names = ["LOS_x", "LOS_y", "LOS_z"]
+    arrays = {f"in/{k}": np.asarray(v) for k, v in base.items() if k != "LOS"}
+    box = None
+    for los, dname in enumerate(names):
+        data = {k: np.array(v) for k, v in base.items()}
+        data["LOS"] = los
+        box = MeasureIABox(data, outfile, **kw)
+        box.measure_xi_w(dname, "both", 8, temp_file_path="/tmp")
+    # the reference's methods, bound to the box (create_full_cov_matrix_projections calls the other on self)
+    box.measure_covariance_multiple_datasets = types.MethodType(
+        MeasureJackknife.measure_covariance_multiple_datasets, box)
+    for ct in ("w_g_plus", "w_gg"):
+        c, sd = MeasureJackknife.measure_covariance_multiple_datasets(box, ct, ["LOS_y"], num_box=8, return_output=True)
+        arrays[f"res/{ct}/single_cov"], arrays[f"res/{ct}/single_std"] = c, sd
+        c, sd = MeasureJackknife.measure_covariance_multiple_datasets(box, ct, ["LOS_x", "LOS_z"], num_box=8,
+                                                                      return_output=True)
+        arrays[f"res/{ct}/pair_cov"], arrays[f"res/{ct}/pair_std"] = c, sd
+        MeasureJackknife.measure_covariance_multiple_datasets(box, ct, ["LOS_z"], num_box=8)
+        full = MeasureJackknife.create_full_cov_matrix_projections(box, ct, names, num_box=8, return_output=True)
+        for tag, m in zip(("cov3", "cov2xy", "cov2xz", "cov2yz"), full):
+            arrays[f"res/{ct}/{tag}"] = m
+        MeasureJackknife.create_full_cov_matrix_projections(box, ct, names, num_box=8)
+    for p, v in walk(_FILES[outfile]):
+        arrays[f"out/{p}"] = np.asarray(v)
+    meta = {"kwargs": kw, "names": names, "num_jk": 8, "seed": 21}
+    arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, "crosscov_los3.npz"), **arrays)
+    print("crosscov datasets:", sum(1 for k in arrays if k.startswith("out/")))
+
+
 def extract_reference_golden_files():
     from h5read import read_all
     out = {}
@@ -272,3 +321,7 @@ if __name__ == "__main__":
         with contextlib.redirect_stdout(io.StringIO()):
             run_case(name, builder, kw, calls)
         print("done", name)
+    if not only or "crosscov" in only:
+        with contextlib.redirect_stdout(io.StringIO()):
+            run_crosscov()
+        print("done crosscov")

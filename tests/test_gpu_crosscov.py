@@ -1,0 +1,104 @@
+"""Cross-dataset jackknife covariance on the device: the kernel against the
+reference's outputs, MeasureIABox's two methods end to end on the fixture's
+catalogue, and a batch's covariance read straight from its device outputs."""
+
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from golden_io import assert_close
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "..", "oracle"))
+import ia_oracle as O  # noqa: E402
+
+FIX = os.path.join(HERE, "golden", "crosscov_los3.npz")
+NAMES = ["LOS_x", "LOS_y", "LOS_z"]
+
+
+def realisations(z, ct, d, n=8):
+    return np.array([z[f"out/{ct}/{d}_jk{n}/{d}_{b}"] for b in range(n)])
+
+
+@pytest.mark.parametrize("ct", ["w_g_plus", "w_gg"])
+def test_kernel_matches_reference(ct):
+    from measure_ia_gb300.engine import jackknife_cross_cov
+    z = np.load(FIX)
+    cov, std = jackknife_cross_cov(realisations(z, ct, "LOS_x"), realisations(z, ct, "LOS_z"))
+    np.testing.assert_array_equal(cov.cpu().numpy(), z[f"res/{ct}/pair_cov"])   # same IEEE sequence
+    np.testing.assert_array_equal(std.cpu().numpy(), z[f"res/{ct}/pair_std"])
+    cov, std = jackknife_cross_cov(realisations(z, ct, "LOS_y"))
+    np.testing.assert_array_equal(cov.cpu().numpy(), z[f"res/{ct}/single_cov"])
+    np.testing.assert_array_equal(std.cpu().numpy(), z[f"res/{ct}/single_std"])
+
+
+def test_box_methods_end_to_end(tmp_path):
+    """The three projections measured here (FP64 form), then the covariance
+    methods: every dataset the reference wrote, to the FP64-form tolerance."""
+    from measure_ia_gb300 import MeasureIABox, open_output
+    z = np.load(FIX)
+    meta = json.loads(bytes(z["meta"]).decode())
+    base = {k[3:]: z[k] for k in z.files if k.startswith("in/")}
+    out = str(tmp_path / "xcov.hdf5")
+    box = None
+    for los, name in enumerate(NAMES):
+        data = {k: np.array(v) for k, v in base.items()}
+        data["LOS"] = los
+        box = MeasureIABox(data, out, **meta["kwargs"])
+        box.measure_xi_w(name, "both", 8, temp_file_path=str(tmp_path))
+    for ct in ("w_g_plus", "w_gg"):
+        c, s = box.measure_covariance_multiple_datasets(ct, ["LOS_x", "LOS_z"], num_box=8, return_output=True)
+        assert_close(c, z[f"res/{ct}/pair_cov"], 1e-9, f"{ct} pair cov")
+        box.measure_covariance_multiple_datasets(ct, ["LOS_z"], num_box=8)
+        full = box.create_full_cov_matrix_projections(ct, NAMES, num_box=8, return_output=True)
+        for m, tag in zip(full, ("cov3", "cov2xy", "cov2xz", "cov2yz")):
+            assert_close(m, z[f"res/{ct}/{tag}"], 1e-9, f"{ct} {tag}")
+        box.create_full_cov_matrix_projections(ct, NAMES, num_box=8)
+    st = open_output(out)
+    for key in z.files:
+        if key.startswith("out/") and ("jackknife_cov" in key or key.endswith("_jackknife_8")):
+            got, want = st.read(key[4:]), z[key]
+            ok = np.isfinite(want)
+            assert np.array_equal(np.isfinite(got), ok), key
+            assert_close(got[ok], want[ok], 1e-9, key)
+
+
+def test_errors_like_the_reference(tmp_path):
+    from measure_ia_gb300 import MeasureIABox
+    from measure_ia_gb300.catalogs import uniform_catalog
+    box = MeasureIABox(uniform_catalog(500, 100.0, 3), str(tmp_path / "e.hdf5"), None, None, [0.1, 20.0], 5, 4,
+                       20.0, boxsize=100.0, num_nodes=2)
+    with pytest.raises(ValueError):
+        box.measure_covariance_multiple_datasets("xi_gg", ["a"], num_box=8)
+    box.measure_xi_w("a", "both", 8, temp_file_path=str(tmp_path))
+    box.measure_xi_w("b", "both", 8, temp_file_path=str(tmp_path))
+    with pytest.raises(KeyError):
+        box.measure_covariance_multiple_datasets("w_gg", ["a", "b", "a"], num_box=8)
+    with pytest.raises(KeyError):
+        box.measure_covariance_multiple_datasets("w_gg", ["missing"], num_box=8)
+
+
+def test_batch_cross_covariance_from_device_outputs():
+    from measure_ia_gb300.catalogs import neyman_scott_catalog
+    from measure_ia_gb300.engine import BatchCounter, PairCounter
+    pc = PairCounter("w", boxsize=205.0, r_bins=np.logspace(-1, np.log10(20.0), 11), r_min=0.1, r_max=20.0,
+                     p_bins=np.linspace(-20.0, 20.0, 9), l_subboxes=3, precision="mixed")
+    cats = [neyman_scott_catalog(300, 205.0, 4000, s, mean_children=40, sigma=1.0) for s in (5, 6)]
+    batch = BatchCounter(pc, [pc.to_device(c) for c in cats])
+    batch.prepare()
+    batch.run()
+    for key, name in (("gp", "proj_gp_jk"), ("gg", "proj_gg_jk")):
+        ra, rb = batch.fetch(0)[name], batch.fetch(1)[name]
+        cov, std = batch.cross_covariance(0, 1, key)
+        c0, s0 = O.jackknife_cross_cov(ra, rb)
+        np.testing.assert_array_equal(cov.cpu().numpy(), c0)
+        np.testing.assert_array_equal(std.cpu().numpy(), s0)
+        cov, _ = batch.cross_covariance(1, key=key)
+        np.testing.assert_array_equal(cov.cpu().numpy(), O.jackknife_cross_cov(rb, rb)[0])
+        # the single-catalogue covariance of the measurement itself
+        assert_close(cov.cpu().numpy(), batch.fetch(1)[f"cov_{key}"], 1e-12, "own covariance")
