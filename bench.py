@@ -346,6 +346,26 @@ def run_batch48(args, local):
     batch.status()
     ms = e0.elapsed_time(e1) / args.steps
     same = all(np.array_equal(batch.fetch(i).npairs, pc.fetch(b).npairs) for i, b in enumerate(bufs))
+    # every pairwise jackknife cross-covariance of the 48 catalogues' w_g+,
+    # on the device from the batch outputs, against the oracle's numpy loop
+    # on the host (on rank 0's host cores, for the record)
+    from measure_ia_gb300.engine import jackknife_cross_cov
+    pairs = [(i, j) for i in range(len(dcats)) for j in range(i + 1, len(dcats))]
+    for i, j in pairs[:4]:
+        batch.cross_covariance(i, j)
+    torch.cuda.synchronize()
+    x0, x1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    x0.record(stream)
+    res = [batch.cross_covariance(i, j) for i, j in pairs]
+    x1.record(stream)
+    torch.cuda.synchronize()
+    xcov_ms = x0.elapsed_time(x1)
+    from oracle import ia_oracle  # the checker and the host baseline
+    reals = [batch.realisations(i).cpu().numpy() for i in range(len(dcats))]
+    t0 = time.perf_counter()
+    host = [ia_oracle.jackknife_cross_cov(reals[i], reals[j]) for i, j in pairs]
+    host_ms = (time.perf_counter() - t0) * 1e3
+    xcov_exact = all(np.array_equal(r[0].cpu().numpy(), h[0]) for r, h in zip(res, host))
     fp64 = None
     if args.fp64:  # the plain FP64 form, one catalogue after the other, one step
         pc64 = PairCounter("w", boxsize=L_BOX, r_bins=R_BINS, r_min=0.1, r_max=20.0, p_bins=PI_BINS, l_subboxes=3,
@@ -362,6 +382,8 @@ def run_batch48(args, local):
     return {"metric": "binned pairs/s, 48 uneven catalogues, w_gg+w_g+ 27JK, mixed form", "value": binned / (ms / 1e3),
             "unit": "binned pairs/s", "ms_per_step": ms, "one_after_the_other_ms": seq_ms,
             "binned_pairs_per_step": binned, "counts_equal_to_one_by_one": bool(same), "fp64_form": fp64,
+            "cross_covariances": {"pairs": len(pairs), "device_ms": xcov_ms, "host_oracle_ms": host_ms,
+                                  "bit_exact_vs_oracle": bool(xcov_exact)},
             "knobs": pc.knobs,
             "config": {"workload": "48 catalogues, sizes log-uniform 5e3-2e6 (config 3)",
                        "n_positions_total": int(sum(len(c["Position"]) for c in cats)),

@@ -585,6 +585,7 @@ void make_params(const mia_config* cfg, const Plan& plan, const Tables& T, int l
   const double pm = fmax(fabs(p0), fabs(p1));
   P.los_cut = cfg->kind == MIA_KIND_W ? f32_up(pm * (1.0 + 1e-5) + 1e-30) : INFINITY;
   P.zwin = f32_up(plan.range_los * (1.0 + 1e-5) + cfg->boxsize * 5e-7);
+  P.range_los32 = f32_down(plan.range_los);
   const int nq = cfg->n_qbreak;
   P.q_cut = (nq > 0 && cfg->q_bin[nq] < 0) ? T.q_hi32[nq - 1] : INFINITY;
   P.edge_capacity = plan.edge_capacity;

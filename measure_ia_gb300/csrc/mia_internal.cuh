@@ -137,6 +137,7 @@ struct Params {
   float wrap_guard;
   float los_cut;                // |Pi| above this is surely outside the Pi bins (w)
   float zwin;                   // half-width of the line-of-sight window over the LOS-sorted shapes
+  float range_los32;            // range_los in FP32: zwin - range_los32 is the window's slack
   float q_cut;                  // q above this is surely beyond the last binned separation
   long long edge_capacity;
 };

@@ -361,6 +361,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
   __shared__ int s_stride;
   __shared__ int s_scan[32];
   __shared__ int s_total;
+  __shared__ float s_box[4];  // the unit's shape cell in d0, d1, widened (see the window below)
 
   // tables -> shared (the same binning for every dataset of a batch)
   {
@@ -478,6 +479,16 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
       t /= P.n[0];
       c[1] = (int)(t % P.n[1]);
       c[2] = (int)(t / P.n[1]);
+    }
+    // -- the shape cell's projected box, widened by 1e-3 r_max + 1e-5 L: more
+    // than the FP32 error of a position's coordinates, so a gap measured to
+    // it never exceeds the true gap to any of the cell's shapes
+    if (tid == 0) {
+      const double m = 1e-3 * P.range_proj + 1e-5 * P.L;
+      s_box[0] = (float)(c[0] * P.s[0] - m);
+      s_box[1] = (float)((c[0] + 1) * P.s[0] + m);
+      s_box[2] = (float)(c[1] * P.s[1] - m);
+      s_box[3] = (float)((c[1] + 1) * P.s[1] + m);
     }
     // -- slot map for the jackknife regions around this cell
     if (tid == 0) {
@@ -713,8 +724,25 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
               i_hi = S;
             } else {
               // shapes are staged in line-of-sight order: only a window of them
-              // can be within range of this position (conservative float bounds)
-              z_window(Z, S, p0.zh + p0.zl, P.zwin, i_lo, i_hi);
+              // can be within range of this position (conservative float bounds).
+              // With a local neighbourhood the position sits in the cell's
+              // periodic image, and its projected gap g to the cell bounds every
+              // pair: g^2 beyond q_cut leaves nothing to bin, and for multipoles
+              // |Pi| <= sqrt(q_cut - g^2) (plus 1e-4 q_cut under the root for
+              // the FP32 rounding of the difference)
+              float win = P.zwin;
+              if (!FULL) {
+                const float px = p0.xh + p0.xl, py = p0.yh + p0.yl;
+                const float gx = fmaxf(0.0f, fmaxf(s_box[0] - px, px - s_box[1]));
+                const float gy = fmaxf(0.0f, fmaxf(s_box[2] - py, py - s_box[3]));
+                const float g2 = fmaf(gx, gx, gy * gy);
+                if (g2 > P.q_cut) {
+                  win = -1.0f;
+                } else if (KIND == MIA_KIND_MULTIPOLES) {
+                  win = fminf(win, sqrtf(fmaxf(P.q_cut - g2, 0.0f) + 1e-4f * P.q_cut) + P.zwin - P.range_los32);
+                }
+              }
+              if (win >= 0.0f) z_window(Z, S, p0.zh + p0.zl, win, i_lo, i_hi);
             }
           }
           // the union over the warp is barely wider (neighbouring positions),
