@@ -179,39 +179,44 @@ __global__ void k_post(PostArgs A, Work w, mia_layout lay, double* out) {
 }
 
 // Jackknife covariance of two datasets' realisations (measure_jackknife.py:
-// 519-555): realisation means, cov[j][i] = f * sum_b (a_b[j] - ma[j]) *
-// (b_b[i] - mb[i]) and std[j] = sqrt(f * sum_b (a_b[j] - ma[j]) *
-// (b_b[j] - mb[j])), f = (n - 1) / n, every sum in realisation order and
-// every product rounded before its add, as numpy forms them.  One block:
-// the inputs are (1 + J) x n_r values.
+// 519-555): realisation means, cov[j][i] = f * sum_r (a_r[j] - ma[j]) *
+// (b_r[i] - mb[i]) and std[j] = sqrt(f * sum_r (a_r[j] - ma[j]) *
+// (b_r[j] - mb[j])), f = (n - 1) / n, every sum in realisation order and
+// every product rounded before its add, as numpy forms them.  A block owns a
+// 32 x 32 tile of cov (rows j, columns i) and first forms the means of its 32
+// a-columns and 32 b-columns; the tiles on the diagonal also write std.
+constexpr int kCovTile = 32;
+
 __global__ void k_cross_cov(int n_real, int n_bins, const double* __restrict__ a, long long sa,
                             const double* __restrict__ b, long long sb, double* cov, double* std) {
-  extern __shared__ double means[];
-  double* ma = means;
-  double* mb = means + n_bins;
-  for (int j = threadIdx.x; j < n_bins; j += blockDim.x) {
-    double s = 0.0, t = 0.0;
-    for (int r = 0; r < n_real; ++r) {
-      s = __dadd_rn(s, a[r * sa + j]);
-      t = __dadd_rn(t, b[r * sb + j]);
+  __shared__ double ma[kCovTile], mb[kCovTile];
+  const int j0 = blockIdx.y * kCovTile, i0 = blockIdx.x * kCovTile;
+  const int t = threadIdx.x;
+  if (t < 2 * kCovTile) {
+    const bool rows = t < kCovTile;
+    const int col = (rows ? j0 : i0) + (t & (kCovTile - 1));
+    double s = 0.0;
+    if (col < n_bins) {
+      const double* x = rows ? a : b;
+      const long long sx = rows ? sa : sb;
+      for (int r = 0; r < n_real; ++r) s = __dadd_rn(s, x[r * sx + col]);
+      s = __ddiv_rn(s, (double)n_real);
     }
-    ma[j] = __ddiv_rn(s, (double)n_real);
-    mb[j] = __ddiv_rn(t, (double)n_real);
+    (rows ? ma : mb)[t & (kCovTile - 1)] = s;
   }
   __syncthreads();
   const double f = __ddiv_rn((double)(n_real - 1), (double)n_real);
-  for (int e = threadIdx.x; e < n_bins * n_bins; e += blockDim.x) {
-    const int j = e / n_bins, i = e - j * n_bins;
+  const int ti = t & (kCovTile - 1);
+  const int i = i0 + ti;
+  for (int tj = t / kCovTile; tj < kCovTile; tj += blockDim.x / kCovTile) {
+    const int j = j0 + tj;
+    if (j >= n_bins || i >= n_bins) continue;
     double s = 0.0;
     for (int r = 0; r < n_real; ++r)
-      s = __dadd_rn(s, __dmul_rn(__dsub_rn(a[r * sa + j], ma[j]), __dsub_rn(b[r * sb + i], mb[i])));
-    cov[e] = __dmul_rn(s, f);
-  }
-  for (int j = threadIdx.x; j < n_bins; j += blockDim.x) {
-    double s = 0.0;
-    for (int r = 0; r < n_real; ++r)
-      s = __dadd_rn(s, __dmul_rn(__dsub_rn(a[r * sa + j], ma[j]), __dsub_rn(b[r * sb + j], mb[j])));
-    std[j] = __dsqrt_rn(__dmul_rn(s, f));
+      s = __dadd_rn(s, __dmul_rn(__dsub_rn(a[r * sa + j], ma[tj]), __dsub_rn(b[r * sb + i], mb[ti])));
+    const double v = __dmul_rn(s, f);
+    cov[(long long)j * n_bins + i] = v;
+    if (i == j) std[j] = __dsqrt_rn(v);
   }
 }
 
@@ -219,7 +224,8 @@ __global__ void k_cross_cov(int n_real, int n_bins, const double* __restrict__ a
 
 cudaError_t launch_cross_cov(int n_real, int n_bins, const double* a, long long sa, const double* b, long long sb,
                              double* cov, double* std, cudaStream_t st) {
-  k_cross_cov<<<1, 256, 2 * sizeof(double) * (size_t)n_bins, st>>>(n_real, n_bins, a, sa, b, sb, cov, std);
+  const int tiles = (n_bins + kCovTile - 1) / kCovTile;
+  k_cross_cov<<<dim3(tiles, tiles), 256, 0, st>>>(n_real, n_bins, a, sa, b, sb, cov, std);
   return cudaGetLastError();
 }
 

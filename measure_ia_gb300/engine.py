@@ -413,3 +413,11 @@ class BatchCounter:
         tensors."""
         b = None if j is None else self.realisations(j, key)
         return jackknife_cross_cov(self.realisations(i, key), b, device=self.pc.device)
+
+    def full_covariance(self, key="gp"):
+        """Jackknife covariance of all catalogues' realisations at once, in one
+        launch: an (n n_r) x (n n_r) matrix whose (i, j) block of n_r x n_r is
+        cross_covariance(i, j), and std its diagonal's root."""
+        import torch
+        reals = torch.cat([self.realisations(i, key) for i in range(self.n)], dim=1)
+        return jackknife_cross_cov(reals, None, device=self.pc.device)

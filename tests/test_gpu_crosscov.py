@@ -102,3 +102,25 @@ def test_batch_cross_covariance_from_device_outputs():
         np.testing.assert_array_equal(cov.cpu().numpy(), O.jackknife_cross_cov(rb, rb)[0])
         # the single-catalogue covariance of the measurement itself
         assert_close(cov.cpu().numpy(), batch.fetch(1)[f"cov_{key}"], 1e-12, "own covariance")
+        # all catalogues in one launch: its blocks are the pairwise results
+        full, fstd = batch.full_covariance(key)
+        full = full.cpu().numpy()
+        nr = ra.shape[1]
+        np.testing.assert_array_equal(full[:nr, nr:], c0)
+        np.testing.assert_array_equal(full[nr:, nr:], O.jackknife_cross_cov(rb, rb)[0])
+        np.testing.assert_array_equal(fstd.cpu().numpy()[:nr], O.jackknife_cross_cov(ra, ra)[1])
+
+
+def test_tiled_kernel_on_many_bins():
+    """More bins than one 32 x 32 tile, uneven edge tiles, rows with a stride."""
+    import torch
+    from measure_ia_gb300.engine import jackknife_cross_cov
+    rng = np.random.default_rng(7)
+    a = rng.normal(size=(27, 77))
+    b = rng.normal(size=(27, 77)) + 0.3 * a
+    wide = torch.zeros((27, 100), dtype=torch.float64, device="cuda")
+    wide[:, :77] = torch.from_numpy(a).cuda()
+    cov, std = jackknife_cross_cov(wide[:, :77], b)
+    c0, s0 = O.jackknife_cross_cov(a, b)
+    np.testing.assert_array_equal(cov.cpu().numpy(), c0)
+    np.testing.assert_array_equal(std.cpu().numpy(), s0)
