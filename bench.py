@@ -555,7 +555,7 @@ def main():
     traffic = profiled_traffic()
     if rank != 0:
         return
-    launches_per_step = 20  # prep 15 (prep 2, scans 9, scatter 2, work units 2), work prefix 1, pairs 1, edge re-test 1, post 1, status 1
+    launches_per_step = 22  # prep 16 (prep 2, scans 9, scatter 2, responsivity sums 1, work units 2), work prefix 1, pairs 1, edge re-test 1, fixed-point sums 1, post 1, status 1
     line = {
         "metric": METRIC, "value": value, "unit": "binned pairs/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": r["ms"], "higher_is_better": True, "scaling": "weak",

@@ -95,6 +95,7 @@ struct Plan {
   size_t off_wu;
   size_t off_reg;
   size_t off_edges;
+  size_t off_acc;
   size_t total;
 };
 
@@ -112,7 +113,64 @@ struct RegionStats {
   unsigned long long* nshape;   // J + 1
   double* s1;                   // J + 1 : sum w_s (1 - e^2/2)
   double* s2;                   // J + 1 : sum w_s
+  long long* r1;                // J + 1 : s1 and s2 as exact fixed-point sums (scale
+  long long* r2;                //         region_scale), converted into s1, s2
 };
+
+// Fixed-point scale of the responsivity sums: 2^S with n * max|w_s| * 2^S <=
+// 2^62, so no total of n shapes can overflow and a term keeps ~62 - log2(n)
+// bits.  Integer sums make R independent of the order of the adds.
+__device__ inline double region_scale(unsigned long long maxws_bits, long long n_shape) {
+  double m = __longlong_as_double((long long)maxws_bits) * (double)(n_shape > 0 ? n_shape : 1);
+  if (!(m > 0.0) || !(m < 1e300)) m = 1.0;
+  int e = ilogb(4611686018427387904.0 / m);  // 2^62
+  e = e > 200 ? 200 : (e < -200 ? -200 : e);
+  return ldexp(1.0, e);
+}
+
+// Fixed-point scales of one dataset (powers of two), from its largest weight
+// product m = max|w_p| * max(|w_s|, |w_s e|) and responsivity R:
+//   S+D, SxD : |term| * 2^S <= 2^30 -- signed terms, typically a few per cent
+//              of the largest, so a work unit's partial of one (copy, bin)
+//              random-walks inside 2^31; the rounding is far below the FP32
+//              error of a term, which the cancelling bins of w_g+ need
+//   w        : |term| * 2^S <= 2^24 -- a positive sum that only grows: it wraps
+//              a 32-bit partial once per ~10^3 adds
+//   var      : (|term| / 2R)^2 * 2^S <= 2^22 (squares, likewise positive)
+// The staged shape weights carry sc_dd (w_s) and sc_sp (w_s e), so a pair's
+// terms come out scaled; c_vr maps a scaled S+D term to its variance term.
+struct Scales {
+  float sc_dd, sc_sp, c_vr;
+  double inv_dd, inv_sp, inv_vr;
+  double sd_dd, sd_sp, sd_vr;   // the scales as doubles (edge re-test)
+};
+
+__device__ inline Scales dataset_scales(const Status* st, double twoR) {
+  double m = __longlong_as_double((long long)st->maxw_bits) * __longlong_as_double((long long)st->maxws_bits);
+  if (!(m > 0.0) || !(m < 1e300)) m = 1.0;
+  double mv = m / fabs(twoR);
+  mv = mv * mv;
+  if (!(mv > 0.0) || !(mv < 1e300)) mv = 1.0;
+  auto expo = [](double room) {  // ilogb: the exact floor(log2(room))
+    const int e = ilogb(room);
+    return e > 60 ? 60 : (e < -100 ? -100 : e);
+  };
+  const int Ssp = expo(1073741824.0 / m), Sdd = expo(16777216.0 / m), Svr = expo(4194304.0 / mv);
+  Scales sc;
+  sc.sd_dd = ldexp(1.0, Sdd);
+  sc.sd_sp = ldexp(1.0, Ssp);
+  sc.sd_vr = ldexp(1.0, Svr);
+  sc.sc_dd = (float)sc.sd_dd;
+  sc.sc_sp = (float)sc.sd_sp;
+  sc.c_vr = (float)(ldexp(1.0, Svr - 2 * Ssp) / (twoR * twoR));  // (tp / 2^Ssp / twoR)^2 * 2^Svr = tp^2 * c_vr
+  sc.inv_dd = ldexp(1.0, -Sdd);
+  sc.inv_sp = ldexp(1.0, -Ssp);
+  sc.inv_vr = ldexp(1.0, -Svr);
+  return sc;
+}
+
+// 2R of a dataset (twice its responsivity, measure_w_box_jk.py:744).
+__device__ inline double dataset_twoR(const RegionStats& reg, int J) { return 2.0 * (reg.s1[J] / reg.s2[J]); }
 
 // Kernel parameters passed by value.
 struct Params {
@@ -161,6 +219,10 @@ struct Work {
   WorkUnit* wu;
   RegionStats reg;
   int2* edges;
+  // mixed form: exact 64-bit fixed-point sums of every pair's terms, in the
+  // dataset's scales (dataset_scales): w and S+D for all pairs and each
+  // jackknife region ((1+J) * nb), SxD and the variance terms (nb)
+  long long *acc_dd, *acc_sp, *acc_sx, *acc_vr;
   long long edge_capacity;
 };
 
@@ -293,6 +355,7 @@ cudaError_t launch_edge_retest(const Params& P, const Work& w, const Out& o, cud
 cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, unsigned long long* wu_prefix, cudaStream_t st);
 cudaError_t launch_post(const Params& P, const Work& w, const mia_layout& lay, double* out, double volume,
                         long long n_pos, long long n_shape, cudaStream_t st);
+cudaError_t launch_fixed_out(const Params& P, const Work& w, const Out& o, cudaStream_t st);
 cudaError_t launch_cross_cov(int n_real, int n_bins, const double* a, long long sa, const double* b, long long sb,
                              double* cov, double* std, cudaStream_t st);
 

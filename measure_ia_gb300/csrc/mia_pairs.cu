@@ -91,23 +91,36 @@ __device__ __forceinline__ int overflow_of(unsigned old, int v) {
   return (int)((old ^ nw) & ((unsigned)v ^ nw));
 }
 
-// Fixed-point scales of one dataset (powers of two).  The staged shape weights
-// carry sc_dd (w_s) and sc_sp (w_s e), so a pair's terms come out scaled.
-//   S+D, SxD : |term| <= 2^30 -- signed terms, typically a few per cent of
-//              the largest, so the partial of one (copy, bin) random-walks
-//              inside 2^31 over a work unit; the rounding is far below the
-//              FP32 error of a term, which the cancelling bins of w_g+ need
-//   w        : |term| <= 2^24 -- a positive sum that only grows: it wraps the
-//              low word once per ~10^3 adds
-//   var      : |term| <= 2^22 (squares, likewise positive)
-struct Scales {
-  float sc_dd, sc_sp, c_vr;   // c_vr: (S+D term scaled)^2 -> variance term scaled
-  double inv_dd, inv_sp, inv_vr;
-};
 
 
-// Direct global accumulation (pairs whose position region has no slot, and the
-// FP64 edge re-test).
+// Global accumulation of one pair in the mixed form (no slot for its position
+// region, or decided by the FP64 re-test): count plus fixed-point terms into
+// the dataset's 64-bit sums, for all pairs, region a and region b != a.
+__device__ __forceinline__ void acc_global_fixed(const Work& w, const Out& o, int nb, int J, int a, int b, int bin,
+                                                 long long vd, long long vp, long long vx, long long vv,
+                                                 int want_var) {
+  typedef unsigned long long u64;
+  atomicAdd(&o.npairs[bin], 1ULL);
+  atomicAdd(reinterpret_cast<u64*>(&w.acc_dd[bin]), (u64)vd);
+  atomicAdd(reinterpret_cast<u64*>(&w.acc_sp[bin]), (u64)vp);
+  atomicAdd(reinterpret_cast<u64*>(&w.acc_sx[bin]), (u64)vx);
+  if (want_var) atomicAdd(reinterpret_cast<u64*>(&w.acc_vr[bin]), (u64)vv);
+  if (J > 0) {
+    const size_t ia = (size_t)(1 + a) * nb + bin;
+    atomicAdd(&o.npairs[ia], 1ULL);
+    atomicAdd(reinterpret_cast<u64*>(&w.acc_dd[ia]), (u64)vd);
+    atomicAdd(reinterpret_cast<u64*>(&w.acc_sp[ia]), (u64)vp);
+    if (b != a) {
+      const size_t ib = (size_t)(1 + b) * nb + bin;
+      atomicAdd(&o.npairs[ib], 1ULL);
+      atomicAdd(reinterpret_cast<u64*>(&w.acc_dd[ib]), (u64)vd);
+      atomicAdd(reinterpret_cast<u64*>(&w.acc_sp[ib]), (u64)vp);
+    }
+  }
+}
+
+// Direct global accumulation in the plain FP64 form (pairs whose position
+// region has no slot).
 __device__ __forceinline__ void acc_global(const Out& o, int nb, int J, int a, int b, int bin, double dd, double sp,
                                            double sx, double var, int want_var) {
   atomicAdd(&o.npairs[bin], 1ULL);
@@ -321,10 +334,8 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
       if (VAR && fv < 0) atomicAdd(&h.vr_hi[kh], (vv >> 31) | 1);
     }
   } else {
-    const double sp = (double)tp * sc.inv_sp;
-    const double tv = sp / twoR;
-    acc_global(o, P.nb, P.J, label_a, p.lab, bin, (double)ww * sc.inv_dd, sp, (double)tx * sc.inv_sp, tv * tv,
-               VAR);
+    acc_global_fixed(w, o, P.nb, P.J, label_a, p.lab, bin, __float2ll_rn(ww), __float2ll_rn(tp), __float2ll_rn(tx),
+                     VAR ? __float2ll_rn(tp * tp * sc.c_vr) : 0, VAR);
     atomicOr(&w.status->flags, kStatusNoSlot);
     ++my_binned;
   }
@@ -439,27 +450,8 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
           s_ds = lo;
           s_data = ds[lo];
           const Work& wd = ds[lo].w;
-          s_twoR = 2.0 * (wd.reg.s1[P.J] / wd.reg.s2[P.J]);
-          // fixed-point scales 2^S with m * 2^S within each sum's bound, m the
-          // largest |w_p| * max(|w_s|, |w_s e|) of the dataset (ilogb: exact floor(log2))
-          double m = __longlong_as_double((long long)wd.status->maxw_bits) *
-                     __longlong_as_double((long long)wd.status->maxws_bits);
-          if (!(m > 0.0) || !(m < 1e300)) m = 1.0;
-          double mv = m / fabs(s_twoR);
-          mv = mv * mv;
-          if (!(mv > 0.0) || !(mv < 1e300)) mv = 1.0;
-          auto expo = [](double room) {
-            const int e = ilogb(room);
-            return e > 60 ? 60 : (e < -100 ? -100 : e);
-          };
-          const int Ssp = expo(1073741824.0 / m), Sdd = expo(16777216.0 / m), Svr = expo(4194304.0 / mv);
-          s_sc.sc_dd = (float)ldexp(1.0, Sdd);
-          s_sc.sc_sp = (float)ldexp(1.0, Ssp);
-          // (tp / 2^Ssp / twoR)^2 * 2^Svr = tp^2 * c_vr
-          s_sc.c_vr = (float)(ldexp(1.0, Svr - 2 * Ssp) / (s_twoR * s_twoR));
-          s_sc.inv_dd = ldexp(1.0, -Sdd);
-          s_sc.inv_sp = ldexp(1.0, -Ssp);
-          s_sc.inv_vr = ldexp(1.0, -Svr);
+          s_twoR = dataset_twoR(wd.reg, P.J);
+          s_sc = dataset_scales(wd.status, s_twoR);
         }
       }
     }
@@ -813,43 +805,56 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
       for (int c = 0; c < copies; ++c) cnt += h_cnt[c * stride + idx];
       if (cnt == 0) continue;
       my_binned += cnt;
-      double dd, sp, sx, vr = 0.0;
+      const int b = slot_region[k];
       if (MIXED) {
+        // the unit's exact partial of this (slot, bin): the high word plus the
+        // copies' signed low words, added to the dataset's 64-bit sums
+        // (integer adds: the totals do not depend on the order of the units)
+        typedef unsigned long long u64;
         long long vdd = (long long)dd_hi[idx] << 32, vsp = (long long)sp_hi[idx] << 32,
                   vsx = (long long)sx_hi[idx] << 32, vvr = VAR ? (long long)vr_hi[idx] << 32 : 0;
-        for (int c = 0; c < copies; ++c) {  // low words are signed partials
+        for (int c = 0; c < copies; ++c) {
           const int j = c * stride + idx;
           vdd += (long long)(int)dd_lo[j];
           vsp += (long long)(int)sp_lo[j];
           vsx += (long long)(int)sx_lo[j];
           if (VAR) vvr += (long long)(int)vr_lo[j];
         }
-        dd = (double)vdd * sc.inv_dd;
-        sp = (double)vsp * sc.inv_sp;
-        sx = (double)vsx * sc.inv_sp;
-        if (VAR) vr = (double)vvr * sc.inv_vr;
+        atomicAdd(&o.npairs[bin], (u64)cnt);
+        atomicAdd(reinterpret_cast<u64*>(&w.acc_dd[bin]), (u64)vdd);
+        atomicAdd(reinterpret_cast<u64*>(&w.acc_sp[bin]), (u64)vsp);
+        atomicAdd(reinterpret_cast<u64*>(&w.acc_sx[bin]), (u64)vsx);
+        if (VAR) atomicAdd(reinterpret_cast<u64*>(&w.acc_vr[bin]), (u64)vvr);
+        if (P.J > 0) {
+          const size_t ia = (size_t)(1 + a) * nb + bin;
+          atomicAdd(&o.npairs[ia], (u64)cnt);
+          atomicAdd(reinterpret_cast<u64*>(&w.acc_dd[ia]), (u64)vdd);
+          atomicAdd(reinterpret_cast<u64*>(&w.acc_sp[ia]), (u64)vsp);
+          if (b != a) {
+            const size_t ibb = (size_t)(1 + b) * nb + bin;
+            atomicAdd(&o.npairs[ibb], (u64)cnt);
+            atomicAdd(reinterpret_cast<u64*>(&w.acc_dd[ibb]), (u64)vdd);
+            atomicAdd(reinterpret_cast<u64*>(&w.acc_sp[ibb]), (u64)vsp);
+          }
+        }
       } else {
-        dd = dd_d[idx];
-        sp = sp_d[idx];
-        sx = sx_d[idx];
-        if (VAR) vr = vr_d[idx];
-      }
-      const int b = slot_region[k];
-      atomicAdd(&o.npairs[bin], (unsigned long long)cnt);
-      atomicAdd(&o.dd[bin], dd);
-      atomicAdd(&o.splus[bin], sp);
-      atomicAdd(&o.scross[bin], sx);
-      if (VAR) atomicAdd(&o.variance[bin], vr);
-      if (P.J > 0) {
-        size_t ia = (size_t)(1 + a) * nb + bin;
-        atomicAdd(&o.npairs[ia], (unsigned long long)cnt);
-        atomicAdd(&o.dd[ia], dd);
-        atomicAdd(&o.splus[ia], sp);
-        if (b != a) {
-          size_t ibb = (size_t)(1 + b) * nb + bin;
-          atomicAdd(&o.npairs[ibb], (unsigned long long)cnt);
-          atomicAdd(&o.dd[ibb], dd);
-          atomicAdd(&o.splus[ibb], sp);
+        const double dd = dd_d[idx], sp = sp_d[idx], sx = sx_d[idx], vr = VAR ? vr_d[idx] : 0.0;
+        atomicAdd(&o.npairs[bin], (unsigned long long)cnt);
+        atomicAdd(&o.dd[bin], dd);
+        atomicAdd(&o.splus[bin], sp);
+        atomicAdd(&o.scross[bin], sx);
+        if (VAR) atomicAdd(&o.variance[bin], vr);
+        if (P.J > 0) {
+          size_t ia = (size_t)(1 + a) * nb + bin;
+          atomicAdd(&o.npairs[ia], (unsigned long long)cnt);
+          atomicAdd(&o.dd[ia], dd);
+          atomicAdd(&o.splus[ia], sp);
+          if (b != a) {
+            size_t ibb = (size_t)(1 + b) * nb + bin;
+            atomicAdd(&o.npairs[ibb], (unsigned long long)cnt);
+            atomicAdd(&o.dd[ibb], dd);
+            atomicAdd(&o.splus[ibb], sp);
+          }
         }
       }
     }
@@ -860,11 +865,13 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
   }
 }
 
-// FP64 re-test of the pairs the mixed kernel could not decide in FP32.
+// FP64 re-test of the pairs the mixed kernel could not decide in FP32; their
+// FP64 terms join the dataset's fixed-point sums at the same scales.
 __global__ void k_edge_retest(Params P, Work w, Out o) {
   const unsigned long long n_raw = w.status->edge_count;
   const unsigned long long n = n_raw < (unsigned long long)w.edge_capacity ? n_raw : (unsigned long long)w.edge_capacity;
-  const double twoR = 2.0 * (w.reg.s1[P.J] / w.reg.s2[P.J]);
+  const double twoR = dataset_twoR(w.reg, P.J);
+  const Scales sc = dataset_scales(w.status, twoR);
   unsigned long long binned = 0;
   for (unsigned long long k = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; k < n;
        k += (unsigned long long)gridDim.x * blockDim.x) {
@@ -877,11 +884,28 @@ __global__ void k_edge_retest(Params P, Work w, Out o) {
     const double sp = __dmul_rn(ww, r.ep);
     const double sx = __dmul_rn(ww, r.ex);
     const double tv = __ddiv_rn(sp, twoR);
-    acc_global(o, P.nb, P.J, w.slab_s[si], w.plab_s[pi], r.bin, ww, sp, sx, __dmul_rn(tv, tv), P.want_variance);
+    acc_global_fixed(w, o, P.nb, P.J, w.slab_s[si], w.plab_s[pi], r.bin, __double2ll_rn(ww * sc.sd_dd),
+                     __double2ll_rn(sp * sc.sd_sp), __double2ll_rn(sx * sc.sd_sp),
+                     P.want_variance ? __double2ll_rn(tv * tv * sc.sd_vr) : 0, P.want_variance);
     ++binned;
   }
   for (int of = 16; of > 0; of >>= 1) binned += __shfl_down_sync(0xffffffffu, binned, of);
   if ((threadIdx.x & 31) == 0 && binned) atomicAdd(&w.status->binned, binned);
+}
+
+// Mixed form: the dataset's exact fixed-point sums into the output doubles
+// (w and S+D per region, SxD and the variance terms), before post-processing.
+__global__ void k_fixed_out(Params P, Work w, Out o) {
+  const Scales sc = dataset_scales(w.status, dataset_twoR(w.reg, P.J));
+  const int n1 = (1 + P.J) * P.nb;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1; i += gridDim.x * blockDim.x) {
+    o.dd[i] = (double)w.acc_dd[i] * sc.inv_dd;
+    o.splus[i] = (double)w.acc_sp[i] * sc.inv_sp;
+    if (i < P.nb) {
+      o.scross[i] = (double)w.acc_sx[i] * sc.inv_sp;
+      if (P.want_variance) o.variance[i] = (double)w.acc_vr[i] * sc.inv_vr;
+    }
+  }
 }
 
 // Histogram words per array for the mixed form: K slots of nb bins at least,
@@ -984,6 +1008,13 @@ size_t pair_smem_bytes(int J, int spu, int K, int nb, int mixed, int var) {
 
 cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, unsigned long long* wu_prefix, cudaStream_t st) {
   k_batch_prefix<<<1, 32, 0, st>>>(ds_dev, n_ds, wu_prefix);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fixed_out(const Params& P, const Work& w, const Out& o, cudaStream_t st) {
+  const int n1 = (1 + P.J) * P.nb;
+  const int blocks = (n1 + 255) / 256;
+  k_fixed_out<<<blocks < 1024 ? blocks : 1024, 256, 0, st>>>(P, w, o);
   return cudaGetLastError();
 }
 

@@ -133,16 +133,9 @@ __global__ void k_prep_positions(PrepArgs A, const double* __restrict__ pos, con
 __global__ void k_prep_shapes(PrepArgs A, const double* __restrict__ spos, const double* __restrict__ q,
                               const double* __restrict__ ws, long long n, Work w) {
   extern __shared__ __align__(8) unsigned char prep_smem[];
-  double* s_s1 = reinterpret_cast<double*>(prep_smem);
-  double* s_s2 = s_s1 + A.J;
-  unsigned* s_ns = reinterpret_cast<unsigned*>(s_s2 + A.J);
-  for (int j = threadIdx.x; j < A.J; j += blockDim.x) {
-    s_s1[j] = 0.0;
-    s_s2[j] = 0.0;
-    s_ns[j] = 0u;
-  }
+  unsigned* s_ns = reinterpret_cast<unsigned*>(prep_smem);
+  for (int j = threadIdx.x; j < A.J; j += blockDim.x) s_ns[j] = 0u;
   __syncthreads();
-  double s1 = 0.0, s2 = 0.0;
   unsigned long long mx = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     double v[3] = {spos[3 * i], spos[3 * i + 1], spos[3 * i + 2]};
@@ -162,15 +155,8 @@ __global__ void k_prep_shapes(PrepArgs A, const double* __restrict__ spos, const
     } else {
       e = __ddiv_rn(__dsub_rn(1.0, qq), __dadd_rn(1.0, qq));
     }
-    double wsi = ws[i];
-    double t1 = __dmul_rn(wsi, __dsub_rn(1.0, __dmul_rn(__dmul_rn(e, e), 0.5)));
-    if (A.J > 0) {
-      atomicAdd(&s_ns[lab], 1u);
-      atomicAdd(&s_s1[lab], t1);
-      atomicAdd(&s_s2[lab], wsi);
-    }
-    s1 += t1;
-    s2 += wsi;
+    const double wsi = ws[i];
+    if (A.J > 0) atomicAdd(&s_ns[lab], 1u);
     const double mws = fmax(fabs(wsi), fabs(wsi * e));
     const unsigned long long b = (unsigned long long)__double_as_longlong(mws);
     mx = b > mx ? b : mx;
@@ -178,21 +164,29 @@ __global__ void k_prep_shapes(PrepArgs A, const double* __restrict__ spos, const
   mx = warp_max_u64(mx);
   if ((threadIdx.x & 31) == 0 && mx) atomicMax(&w.status->maxws_bits, mx);
   __syncthreads();
-  for (int j = threadIdx.x; j < A.J; j += blockDim.x) {
-    if (s_ns[j]) {
-      atomicAdd(&w.reg.nshape[j], (unsigned long long)s_ns[j]);
-      atomicAdd(&w.reg.s1[j], s_s1[j]);
-      atomicAdd(&w.reg.s2[j], s_s2[j]);
-    }
+  for (int j = threadIdx.x; j < A.J; j += blockDim.x)
+    if (s_ns[j]) atomicAdd(&w.reg.nshape[j], (unsigned long long)s_ns[j]);
+}
+
+// The responsivity sums s1 = sum w_s (1 - e^2/2) and s2 = sum w_s, per region
+// and in total (measure_w_box_jk.py:744, :782-785), as exact fixed-point sums
+// at region_scale: one int64 per term, per-block shared totals, then global
+// totals.  Runs after k_prep_shapes has fixed the largest |w_s|.
+__device__ __forceinline__ void add_region_terms(long long* s_r1, long long* s_r2, int lab, int J, long long v1,
+                                                 long long v2, long long& t1, long long& t2) {
+  if (J > 0) {
+    atomicAdd(reinterpret_cast<unsigned long long*>(&s_r1[lab]), (unsigned long long)v1);
+    atomicAdd(reinterpret_cast<unsigned long long*>(&s_r2[lab]), (unsigned long long)v2);
   }
-  // block totals
-  for (int o = 16; o > 0; o >>= 1) {
-    s1 += __shfl_down_sync(0xffffffffu, s1, o);
-    s2 += __shfl_down_sync(0xffffffffu, s2, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    atomicAdd(&w.reg.s1[A.J], s1);
-    atomicAdd(&w.reg.s2[A.J], s2);
+  t1 += v1;
+  t2 += v2;
+}
+
+__global__ void k_region_sums(Work w, int J, long long n_shape) {
+  const double inv = 1.0 / region_scale(w.status->maxws_bits, n_shape);
+  for (int j = threadIdx.x; j <= J; j += blockDim.x) {
+    w.reg.s1[j] = (double)w.reg.r1[j] * inv;
+    w.reg.s2[j] = (double)w.reg.r2[j] * inv;
   }
 }
 
@@ -225,6 +219,13 @@ __global__ void k_scatter_positions(PrepArgs A, const double* __restrict__ pos, 
 __global__ void k_scatter_shapes(PrepArgs A, const double* __restrict__ spos, const double* __restrict__ axis,
                                  const double* __restrict__ q, const double* __restrict__ ws, long long n, Work w,
                                  int mixed) {
+  extern __shared__ __align__(8) unsigned char prep_smem[];
+  long long* s_r1 = reinterpret_cast<long long*>(prep_smem);
+  long long* s_r2 = s_r1 + A.J;
+  for (int j = threadIdx.x; j < A.J; j += blockDim.x) s_r1[j] = s_r2[j] = 0;
+  __syncthreads();
+  const double sr = region_scale(w.status->maxws_bits, n);
+  long long t1 = 0, t2 = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     int cell = w.scell[i];
     int lab = w.slab[i];
@@ -246,6 +247,8 @@ __global__ void k_scatter_shapes(PrepArgs A, const double* __restrict__ spos, co
       e = __ddiv_rn(__dsub_rn(1.0, qq), __dadd_rn(1.0, qq));
     }
     double wsi = ws[i];
+    const double r1 = __dmul_rn(wsi, __dsub_rn(1.0, __dmul_rn(__dmul_rn(e, e), 0.5)));
+    add_region_terms(s_r1, s_r2, lab, A.J, __double2ll_rn(r1 * sr), __double2ll_rn(wsi * sr), t1, t2);
     w.sx[slot] = c[0];
     w.sy[slot] = c[1];
     w.sz[slot] = c[2];
@@ -263,6 +266,20 @@ __global__ void k_scatter_shapes(PrepArgs A, const double* __restrict__ spos, co
       w.swef[slot] = __double2float_rn(wsi * e);
       w.swsf[slot] = __double2float_rn(wsi);
     }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    t1 += __shfl_down_sync(0xffffffffu, t1, o);
+    t2 += __shfl_down_sync(0xffffffffu, t2, o);
+  }
+  typedef unsigned long long u64;
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(reinterpret_cast<u64*>(&w.reg.r1[A.J]), (u64)t1);
+    atomicAdd(reinterpret_cast<u64*>(&w.reg.r2[A.J]), (u64)t2);
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < A.J; j += blockDim.x) {
+    atomicAdd(reinterpret_cast<u64*>(&w.reg.r1[j]), (u64)s_r1[j]);
+    atomicAdd(reinterpret_cast<u64*>(&w.reg.r2[j]), (u64)s_r2[j]);
   }
 }
 
@@ -429,15 +446,16 @@ cudaError_t launch_prep(const Plan& plan, const Params& P, const mia_catalog& ca
   const int gp = grid_for(cat.n_pos, T) < 1024 ? grid_for(cat.n_pos, T) : 1024;
   const int gs = grid_for(cat.n_shape, T) < 1024 ? grid_for(cat.n_shape, T) : 1024;
   k_prep_positions<<<gp, T, sizeof(unsigned) * (size_t)plan.J, st>>>(A, cat.position, cat.weight, cat.n_pos, w);
-  k_prep_shapes<<<gs, T, (2 * sizeof(double) + sizeof(unsigned)) * (size_t)plan.J, st>>>(
+  k_prep_shapes<<<gs, T, sizeof(unsigned) * (size_t)plan.J, st>>>(
       A, cat.position_shape, cat.q, cat.weight_shape, cat.n_shape, w);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if ((e = scan(w.pcount, plan.n_fcells, w.pstart, w.tiles, nullptr, st)) != cudaSuccess) return e;
   if ((e = scan(w.scount, plan.n_cells, w.sstart, w.tiles, nullptr, st)) != cudaSuccess) return e;
   k_scatter_positions<<<grid_for(cat.n_pos, T), T, 0, st>>>(A, cat.position, cat.weight, cat.n_pos, w, mixed);
-  k_scatter_shapes<<<grid_for(cat.n_shape, T), T, 0, st>>>(A, cat.position_shape, cat.axis_direction, cat.q,
-                                                           cat.weight_shape, cat.n_shape, w, mixed);
+  k_scatter_shapes<<<gs, T, 2 * sizeof(long long) * (size_t)plan.J, st>>>(
+      A, cat.position_shape, cat.axis_direction, cat.q, cat.weight_shape, cat.n_shape, w, mixed);
+  k_region_sums<<<1, 256, 0, st>>>(w, plan.J, cat.n_shape);
   k_wu_count<<<grid_for(plan.n_cells, T), T, 0, st>>>(plan.n_cells, plan.shapes_per_unit, w);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if ((e = scan(w.wucount, plan.n_cells, w.wustart, w.tiles, &w.status->n_wu, st)) != cudaSuccess) return e;

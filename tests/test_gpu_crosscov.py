@@ -58,6 +58,16 @@ def test_box_methods_end_to_end(tmp_path):
         full = box.create_full_cov_matrix_projections(ct, NAMES, num_box=8, return_output=True)
         for m, tag in zip(full, ("cov3", "cov2xy", "cov2xz", "cov2yz")):
             assert_close(m, z[f"res/{ct}/{tag}"], 1e-9, f"{ct} {tag}")
+        # the block relations the reference's own (disabled) projection test
+        # asserts (test_full_cov_matrix_projections.py), here with 10 bins
+        cov3, c12, c13, c23 = full
+        n = 10
+        np.testing.assert_array_equal(cov3[0:2 * n, 0:2 * n], c12)
+        np.testing.assert_array_equal(cov3[n:3 * n, n:3 * n], c23)
+        np.testing.assert_array_equal(cov3[0:n, 0:n], c13[0:n, 0:n])
+        np.testing.assert_array_equal(cov3[2 * n:3 * n, 0:n], c13[n:2 * n, 0:n])
+        np.testing.assert_array_equal(cov3[2 * n:3 * n, 2 * n:3 * n], c13[n:2 * n, n:2 * n])
+        np.testing.assert_array_equal(cov3[0:n, 2 * n:3 * n], c13[0:n, n:2 * n])
         box.create_full_cov_matrix_projections(ct, NAMES, num_box=8)
     st = open_output(out)
     for key in z.files:

@@ -88,3 +88,17 @@ def test_autotune_skips_failing_candidates(tmp_path):
     with pytest.raises(MiaError):
         autotune.tune(refuse, dcat, rp, key="k", path=str(tmp_path / "t.json"))
     assert autotune.load_cache(str(tmp_path / "t.json")) == {}
+
+
+def test_mixed_form_is_bitwise_reproducible():
+    """Every product of the mixed form comes from integer sums (the block
+    partials and the dataset's 64-bit totals), so two runs agree exactly
+    whatever order the work units and atomics took."""
+    from measure_ia_gb300.catalogs import neyman_scott_catalog
+    data = neyman_scott_catalog(600, 205.0, 12000, 21, mean_children=40, sigma=1.0)
+    pc = _counter("mixed")
+    dcat = pc.to_device(data)
+    a, b = pc.measure(dcat), pc.measure(dcat)
+    np.testing.assert_array_equal(a.npairs, b.npairs)
+    for k in a.arrays:
+        np.testing.assert_array_equal(a[k], b[k], err_msg=k)
