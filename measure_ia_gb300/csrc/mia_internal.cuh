@@ -136,7 +136,10 @@ __device__ inline double region_scale(unsigned long long maxws_bits, long long n
 //              error of a term, which the cancelling bins of w_g+ need
 //   w        : |term| * 2^S <= 2^24 -- a positive sum that only grows: it wraps
 //              a 32-bit partial once per ~10^3 adds
-//   var      : (|term| / 2R)^2 * 2^S <= 2^22 (squares, likewise positive)
+//   var      : (|term| / 2R)^2 * 2^S <= 2^30 -- positive squares, but only the
+//              brute layout with jackknife regions accumulates them, and there
+//              each one is divided by RR^2: a one-pair bin of a small term at
+//              small r needs the finer unit (2^22 left 5e-5 relative errors)
 // The staged shape weights carry sc_dd (w_s) and sc_sp (w_s e), so a pair's
 // terms come out scaled; c_vr maps a scaled S+D term to its variance term.
 struct Scales {
@@ -155,7 +158,7 @@ __device__ inline Scales dataset_scales(const Status* st, double twoR) {
     const int e = ilogb(room);
     return e > 60 ? 60 : (e < -100 ? -100 : e);
   };
-  const int Ssp = expo(1073741824.0 / m), Sdd = expo(16777216.0 / m), Svr = expo(4194304.0 / mv);
+  const int Ssp = expo(1073741824.0 / m), Sdd = expo(16777216.0 / m), Svr = expo(1073741824.0 / mv);
   Scales sc;
   sc.sd_dd = ldexp(1.0, Sdd);
   sc.sd_sp = ldexp(1.0, Ssp);
