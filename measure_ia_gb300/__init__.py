@@ -6,7 +6,7 @@ the C ABI of ``include/measure_ia_gb300.h``.
 """
 
 from .measure_ia import MeasureIABox
-from .output import open_output, read_npz_mirror
+from .output import open_output, read_output
 from .sim_info import SimInfo
 
-__all__ = ["MeasureIABox", "SimInfo", "open_output", "read_npz_mirror"]
+__all__ = ["MeasureIABox", "SimInfo", "open_output", "read_output"]

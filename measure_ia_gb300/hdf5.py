@@ -1,0 +1,339 @@
+"""HDF5 files without h5py: a writer and a reader for the subset of the
+format that the measurement products need.
+
+The reference writes its products with h5py (``write_data.py:1-56``), whose
+default ('earliest') file layout is what this module produces: superblock
+version 0 (offsets and lengths of 8 bytes, group leaf node K = 4, group
+internal node K = 16), version-1 object headers, groups as symbol tables (a
+version-1 B-tree of symbol-table nodes, names in a local heap; group entries
+cache the B-tree and heap addresses), and datasets with a version-1
+dataspace (current = maximum dimensions), an IEEE float or two's-complement
+integer datatype, a version-2 fill-value message and contiguous storage
+(layout message version 3).  Every structure follows the public HDF5 file
+format specification; the conventions h5py leaves in such files (the local
+heap's trailing free block, B-tree nodes allocated for 2K children, the
+datatype and fill messages marked constant) are kept so that the files look
+like h5py's.
+
+The reader covers the same layout plus what h5py writes into it:
+continuation messages, B-trees of several levels, compact storage and
+version-2 dataspaces.  Anything else raises ``NotImplementedError``.
+"""
+
+from __future__ import annotations
+
+import os
+import struct
+
+import numpy as np
+
+UNDEF = 0xFFFFFFFFFFFFFFFF
+SIGNATURE = b"\x89HDF\r\n\x1a\n"
+LEAF_K = 4                       # symbols per symbol-table node: 2 * LEAF_K
+NODE_K = 16                      # children per group B-tree node: 2 * NODE_K
+SNOD_BYTES = 8 + 2 * LEAF_K * 40
+BTREE_BYTES = 24 + (2 * NODE_K + 1) * 8 + 2 * NODE_K * 8
+FREE_NULL = 1                    # end of a local heap's free list
+SUPERBLOCK_BYTES = 96
+
+_MSG_DATASPACE, _MSG_DATATYPE, _MSG_FILL, _MSG_LAYOUT = 0x0001, 0x0003, 0x0005, 0x0008
+_MSG_CONTINUATION, _MSG_SYMBOL_TABLE = 0x0010, 0x0011
+
+
+def _pad8(n):
+    return (n + 7) & ~7
+
+
+# ----------------------------------------------------------------------------
+# writer
+# ----------------------------------------------------------------------------
+
+def _datatype(dt: np.dtype) -> bytes:
+    if dt.kind == "f" and dt.itemsize in (4, 8):
+        if dt.itemsize == 8:
+            props = struct.pack("<HHBBBBI", 0, 64, 52, 11, 0, 52, 1023)
+            sign = 63
+        else:
+            props = struct.pack("<HHBBBBI", 0, 32, 23, 8, 0, 23, 127)
+            sign = 31
+        # class 1 (floating point), version 1; little endian, mantissa msb implied
+        return bytes([0x11, 0x20, sign, 0x00]) + struct.pack("<I", dt.itemsize) + props
+    if dt.kind in "iu" and dt.itemsize in (1, 2, 4, 8):
+        bits = 0x08 if dt.kind == "i" else 0x00
+        return bytes([0x10, bits, 0x00, 0x00]) + struct.pack("<IHH", dt.itemsize, 0, 8 * dt.itemsize)
+    raise TypeError(f"dtype {dt} is not supported by the HDF5 writer")
+
+
+def _dataspace(shape) -> bytes:
+    rank = len(shape)
+    head = struct.pack("<BBBBI", 1, rank, 1 if rank else 0, 0, 0)
+    dims = b"".join(struct.pack("<Q", int(d)) for d in shape)
+    return head + dims + dims
+
+
+def _message(mtype, data, flags=0) -> bytes:
+    body = data + b"\0" * (_pad8(len(data)) - len(data))
+    return struct.pack("<HHB3x", mtype, len(body), flags) + body
+
+
+def _object_header(messages) -> bytes:
+    body = b"".join(messages)
+    return struct.pack("<BBHII4x", 1, 0, len(messages), 1, len(body)) + body
+
+
+class _Image:
+    """The file as a growing byte array; every allocation is 8-byte aligned."""
+
+    def __init__(self):
+        self.b = bytearray(SUPERBLOCK_BYTES)
+
+    def alloc(self, n):
+        a = len(self.b)
+        self.b += b"\0" * _pad8(n)
+        return a
+
+    def put(self, addr, data):
+        self.b[addr:addr + len(data)] = data
+
+
+def _entry(name_off, header, scratch=None) -> bytes:
+    if scratch is None:
+        return struct.pack("<QQII16x", name_off, header, 0, 0)
+    return struct.pack("<QQIIQQ", name_off, header, 1, 0, *scratch)
+
+
+def _write_dataset(img: _Image, value: np.ndarray) -> int:
+    v = np.asarray(value)
+    if v.dtype.kind == "b":
+        raise TypeError("boolean datasets are not supported by the HDF5 writer")
+    dt = v.dtype.newbyteorder("<") if v.dtype.byteorder != "|" else v.dtype
+    raw = np.ascontiguousarray(v, dtype=dt).tobytes()
+
+    def header(data_at):
+        return _object_header([
+            _message(_MSG_DATASPACE, _dataspace(v.shape)),
+            _message(_MSG_DATATYPE, _datatype(np.dtype(dt)), flags=1),
+            _message(_MSG_FILL, bytes([2, 2, 2, 1]) + struct.pack("<I", 0), flags=1),
+            _message(_MSG_LAYOUT, struct.pack("<BBQQ", 3, 1, data_at, len(raw)))])
+
+    addr = img.alloc(len(header(UNDEF)))
+    data_at = img.alloc(len(raw)) if raw else UNDEF   # an empty dataset has no storage
+    img.put(addr, header(data_at))
+    if raw:
+        img.put(data_at, raw)
+    return addr
+
+
+def _write_group(img: _Image, children: dict) -> tuple[int, int, int]:
+    """Writes a group and (recursively) its members; returns the addresses
+    of its object header, B-tree root and local heap."""
+    names = sorted(children, key=lambda s: s.encode())
+    # member objects first, so that their entries can be filled in
+    entries = {}
+    for n in names:
+        c = children[n]
+        if isinstance(c, dict):
+            h, bt, hp = _write_group(img, c)
+            entries[n] = (h, (bt, hp))
+        else:
+            entries[n] = (_write_dataset(img, c), None)
+    # local heap: "" at offset 0, the names, then one free block
+    heap_data = bytearray(b"\0" * 8)
+    offs = {}
+    for n in names:
+        offs[n] = len(heap_data)
+        enc = n.encode() + b"\0"
+        heap_data += enc + b"\0" * (_pad8(len(enc)) - len(enc))
+    free_at = len(heap_data)
+    heap_data += struct.pack("<QQ", FREE_NULL, 16)
+    heap = img.alloc(32)
+    heap_seg = img.alloc(len(heap_data))
+    img.put(heap, b"HEAP" + bytes([0, 0, 0, 0]) + struct.pack("<QQQ", len(heap_data), free_at, heap_seg))
+    img.put(heap_seg, bytes(heap_data))
+    # symbol-table nodes of up to 2 * LEAF_K entries each, in name order
+    per = 2 * LEAF_K
+    leaves = []
+    for i in range(0, len(names), per):
+        chunk = names[i:i + per]
+        at = img.alloc(SNOD_BYTES)
+        body = b"".join(_entry(offs[n], entries[n][0], entries[n][1]) for n in chunk)
+        img.put(at, b"SNOD" + struct.pack("<BBH", 1, 0, len(chunk)) + body)
+        leaves.append((at, offs[chunk[-1]]))          # (address, heap offset of its largest name)
+    # B-tree levels of up to 2 * NODE_K children until one root remains
+    level = 0
+    nodes = leaves
+    while True:
+        groups = [nodes[i:i + 2 * NODE_K] for i in range(0, len(nodes), 2 * NODE_K)] or [[]]
+        addrs = [img.alloc(BTREE_BYTES) for _ in groups]
+        parents = []
+        left_key = 0
+        for j, g in enumerate(groups):
+            left = addrs[j - 1] if j > 0 else UNDEF
+            right = addrs[j + 1] if j + 1 < len(groups) else UNDEF
+            body = struct.pack("<Q", left_key)
+            for child, key in g:
+                body += struct.pack("<QQ", child, key)
+            img.put(addrs[j], b"TREE" + struct.pack("<BBHQQ", 0, level, len(g), left, right) + body)
+            top_key = g[-1][1] if g else 0
+            parents.append((addrs[j], top_key))
+            left_key = top_key
+        if len(parents) == 1:
+            btree = parents[0][0]
+            break
+        nodes = parents
+        level += 1
+    hdr = _object_header([_message(_MSG_SYMBOL_TABLE, struct.pack("<QQ", btree, heap))])
+    h = img.alloc(len(hdr))
+    img.put(h, hdr)
+    return h, btree, heap
+
+
+def _tree(datasets: dict) -> dict:
+    root: dict = {}
+    for path, value in datasets.items():
+        parts = [p for p in path.split("/") if p]
+        if not parts:
+            raise ValueError("empty dataset path")
+        node = root
+        for p in parts[:-1]:
+            nxt = node.setdefault(p, {})
+            if not isinstance(nxt, dict):
+                raise ValueError(f"'{p}' in '{path}' is a dataset, not a group")
+            node = nxt
+        if isinstance(node.get(parts[-1]), dict):
+            raise ValueError(f"'{path}' is a group")
+        node[parts[-1]] = np.asarray(value)
+    return root
+
+
+def write_file(path, datasets: dict) -> None:
+    """Writes ``{'group/sub/name': array}`` as a new HDF5 file at ``path``
+    (replacing it atomically: the file appears complete or not at all)."""
+    img = _Image()
+    h, bt, hp = _write_group(img, _tree(datasets))
+    sb = SIGNATURE + bytes([0, 0, 0, 0, 0, 8, 8, 0]) + struct.pack("<HHI", LEAF_K, NODE_K, 0)
+    sb += struct.pack("<QQQQ", 0, UNDEF, len(img.b), UNDEF) + _entry(0, h, (bt, hp))
+    img.put(0, sb)
+    tmp = f"{path}.tmp{os.getpid()}"
+    with open(tmp, "wb") as f:
+        f.write(bytes(img.b))
+    os.replace(tmp, path)
+
+
+# ----------------------------------------------------------------------------
+# reader
+# ----------------------------------------------------------------------------
+
+class _Reader:
+    def __init__(self, data: bytes):
+        self.b = data
+        if data[:8] != SIGNATURE:
+            raise ValueError("not an HDF5 file")
+        ver = data[8]
+        if ver not in (0, 1):
+            raise NotImplementedError(f"superblock version {ver}")
+        if data[13] != 8 or data[14] != 8:
+            raise NotImplementedError("offsets or lengths other than 8 bytes")
+        root = 24 + (4 if ver == 1 else 0) + 32
+        self.root = self.u("Q", root + 8)[0]
+
+    def u(self, fmt, off):
+        return struct.unpack_from("<" + fmt, self.b, off)
+
+    def messages(self, addr):
+        if self.b[addr] != 1:
+            raise NotImplementedError(f"object header version {self.b[addr]}")
+        nmsg, = self.u("H", addr + 2)
+        size, = self.u("I", addr + 8)
+        blocks, out = [(addr + 16, size)], []
+        while blocks and len(out) < nmsg:
+            start, length = blocks.pop(0)
+            p = start
+            while p + 8 <= start + length and len(out) < nmsg:
+                mtype, msize = self.u("HH", p)
+                if mtype == _MSG_CONTINUATION:
+                    blocks.append(self.u("QQ", p + 8))
+                out.append((mtype, p + 8, msize))
+                p += 8 + msize
+        return out
+
+    def name(self, heap, off):
+        if self.b[heap:heap + 4] != b"HEAP":
+            raise ValueError("bad local heap")
+        seg, = self.u("Q", heap + 24)
+        s = seg + off
+        return self.b[s:self.b.index(b"\0", s)].decode()
+
+    def members(self, btree, heap):
+        out, stack = {}, [btree]
+        while stack:
+            node = stack.pop()
+            if self.b[node:node + 4] != b"TREE" or self.b[node + 4] != 0:
+                raise ValueError("bad group B-tree node")
+            level, used = self.b[node + 5], self.u("H", node + 6)[0]
+            for k in range(used):
+                child, = self.u("Q", node + 32 + 16 * k)
+                if level > 0:
+                    stack.append(child)
+                    continue
+                if self.b[child:child + 4] != b"SNOD":
+                    raise ValueError("bad symbol-table node")
+                for s in range(self.u("H", child + 6)[0]):
+                    e = child + 8 + 40 * s
+                    name_off, hdr = self.u("QQ", e)
+                    out[self.name(heap, name_off)] = hdr
+        return out
+
+    def dataset(self, msgs):
+        t = {m[0]: m for m in msgs}
+        _, d, _ = t[_MSG_DATASPACE]
+        ver, rank = self.b[d], self.b[d + 1]
+        if ver == 2 and self.b[d + 3] == 2:
+            return np.zeros(0)                      # null dataspace
+        dims_at = d + (8 if ver == 1 else 4)
+        shape = tuple(self.u("Q", dims_at + 8 * i)[0] for i in range(rank))
+        _, a, _ = t[_MSG_DATATYPE]
+        cls, bits, size = self.b[a] & 0x0F, self.b[a + 1], self.u("I", a + 4)[0]
+        order = ">" if bits & 1 else "<"
+        if cls == 1:
+            dt = np.dtype(f"{order}f{size}")
+        elif cls == 0:
+            dt = np.dtype(f"{order}{'i' if bits & 0x08 else 'u'}{size}")
+        else:
+            raise NotImplementedError(f"datatype class {cls}")
+        _, lay, _ = t[_MSG_LAYOUT]
+        if self.b[lay] != 3:
+            raise NotImplementedError(f"layout message version {self.b[lay]}")
+        n = int(np.prod(shape)) if rank else 1
+        if self.b[lay + 1] == 1:
+            addr, _ = self.u("QQ", lay + 2)
+            raw = b"" if addr == UNDEF else self.b[addr:addr + n * size]
+            if addr == UNDEF:
+                return np.zeros(shape, dt.newbyteorder("="))
+        elif self.b[lay + 1] == 0:
+            nbytes, = self.u("H", lay + 2)
+            raw = self.b[lay + 4:lay + 4 + nbytes]
+        else:
+            raise NotImplementedError("chunked storage")
+        return np.frombuffer(raw, dtype=dt, count=n).reshape(shape).astype(dt.newbyteorder("="))
+
+
+def read_file(path) -> dict:
+    """``{'group/sub/name': array}`` for every dataset in an HDF5 file."""
+    with open(path, "rb") as f:
+        r = _Reader(f.read())
+    out, stack, seen = {}, [("", r.root)], set()
+    while stack:
+        prefix, addr = stack.pop()
+        if addr in seen:
+            continue
+        seen.add(addr)
+        msgs = r.messages(addr)
+        st = [m for m in msgs if m[0] == _MSG_SYMBOL_TABLE]
+        if st:
+            btree, heap = r.u("QQ", st[0][1])
+            for n, hdr in r.members(btree, heap).items():
+                stack.append((f"{prefix}/{n}" if prefix else n, hdr))
+        elif any(m[0] == _MSG_LAYOUT for m in msgs):
+            out[prefix] = r.dataset(msgs)
+    return out

@@ -126,7 +126,7 @@ def _oracle(i):
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("i", range(N_CASES))
 def test_random_configuration(i, precision, tmp_path):
-    from measure_ia_gb300 import MeasureIABox, open_output
+    from measure_ia_gb300 import MeasureIABox, open_output, read_output
     case, data, masks = draw_case(i)
     ref = dict(_oracle(i))
     c = ref.pop("__counts__")
@@ -146,6 +146,10 @@ def test_random_configuration(i, precision, tmp_path):
     rtol = FP64_RTOL if precision == "fp64" else MIXED_RTOL
     for path, v in ref.items():
         _close(store.read(path), v, rtol, f"{path} {case}")
+    on_disk = read_output(out)                    # the HDF5 file holds exactly the store
+    assert set(on_disk) == set(ref)
+    for path in ref:
+        np.testing.assert_array_equal(on_disk[path], store.read(path))
 
 
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
