@@ -22,6 +22,14 @@ GPU host and never from the test suite.  Two kinds of fixture:
    measured by the reference, then its cross-dataset jackknife covariance
    functions on that output (``run_crosscov``).
 
+4. ``lc_<case>.npz`` -- the reference's ``MeasureIALightcone.measure_xi_w`` /
+   ``measure_xi_multipoles`` on small seeded lightcone catalogues with
+   randoms and jackknife patches (``run_lightcone``).  pyccl is replaced by a
+   module whose ``comoving_radial_distance`` is the package's ``FlatLCDM``;
+   the distances it returned are stored (``chi/z``, ``chi/chi``) so that tests
+   replay them exactly.  pathos's pool is replaced by a serial map (the
+   pooled realisation driver runs unchanged, one patch after another).
+
 Usage:  python tests/golden/make_golden.py
 """
 
@@ -42,6 +50,28 @@ sys.path.insert(0, os.path.join(HERE, "..", ".."))
 # --------------------------------------------------------------------------
 # Import shims for the reference
 # --------------------------------------------------------------------------
+
+class _Dataset:
+    """A stored array; like h5py, reading it (``ds[:]``, ``np.asarray(ds)``)
+    returns a copy, so in-place arithmetic on what was read leaves the file
+    unchanged."""
+
+    def __init__(self, v):
+        self.v = np.array(v)
+
+    def __getitem__(self, key):
+        return np.array(self.v[key])
+
+    def __array__(self, dtype=None, copy=None):
+        return np.array(self.v, dtype=dtype)
+
+    def __len__(self):
+        return len(self.v)
+
+    @property
+    def shape(self):
+        return self.v.shape
+
 
 class _Group(dict):
     def _walk(self, path, create=False):
@@ -67,7 +97,7 @@ class _Group(dict):
     def create_dataset(self, k, data=None, **kw):
         parts = [p for p in k.split("/") if p]
         g = self._walk("/".join(parts[:-1]), create=True)
-        dict.__setitem__(g, parts[-1], np.array(data))
+        dict.__setitem__(g, parts[-1], _Dataset(np.asarray(data)))
         return dict.__getitem__(g, parts[-1])
 
     def keys(self):
@@ -91,6 +121,29 @@ class _File(_Group):
         pass
 
 
+class _SerialPool:
+    def __init__(self, nodes=1):
+        pass
+
+    def map(self, f, *its):
+        return list(map(f, *its))
+
+
+_CHI_SEEN: dict = {}
+
+
+def _ccl_cosmology(Omega_c=0.225, Omega_b=0.045, h=0.7, **_):
+    from measure_ia_gb300.cosmology import FlatLCDM
+    return FlatLCDM(Omega_c=Omega_c, Omega_b=Omega_b, h=h)
+
+
+def _ccl_distance(cosmo, a):
+    chi = cosmo.comoving_radial_distance(a)
+    for x, c in zip(np.ravel(a), np.ravel(chi)):
+        _CHI_SEEN[float(x)] = float(c)
+    return chi
+
+
 def install_shims():
     sys.modules["kmeans_radec"] = types.SimpleNamespace(kmeans_sample=None)
     astro = types.ModuleType("astropy")
@@ -101,11 +154,14 @@ def install_shims():
     sys.modules["astropy.cosmology"] = cosmo
     pth = types.ModuleType("pathos")
     pm = types.ModuleType("pathos.multiprocessing")
-    pm.ProcessingPool = None
+    pm.ProcessingPool = _SerialPool
     pth.multiprocessing = pm
     sys.modules["pathos"] = pth
     sys.modules["pathos.multiprocessing"] = pm
-    sys.modules["pyccl"] = types.ModuleType("pyccl")
+    ccl = types.ModuleType("pyccl")
+    ccl.Cosmology = _ccl_cosmology
+    ccl.comoving_radial_distance = _ccl_distance
+    sys.modules["pyccl"] = ccl
     h5 = types.ModuleType("h5py")
     h5.File = _File
     sys.modules["h5py"] = h5
@@ -126,7 +182,7 @@ def walk(g, prefix=""):
         if isinstance(v, _Group):
             yield from walk(v, p)
         else:
-            yield p, v
+            yield p, np.asarray(v)
 
 
 # --------------------------------------------------------------------------
@@ -298,6 +354,101 @@ def run_crosscov():
     print("crosscov datasets:", sum(1 for k in arrays if k.startswith("out/")))
 
 
+def lightcone_catalogue(seed, n_pos, n_shape, n_rand, n_rand_shape=None, ra=(10.0, 40.0), dec=(-10.0, 10.0),
+                        z=(0.1, 0.3), weights=False):
+    """Clustered points in an RA/DEC/z window, shapes a subset of the
+    positions, uniform randoms (one sample, or separate position and shape
+    randoms), and RA-stripe jackknife patches 0..3."""
+    rng = np.random.default_rng(seed)
+    n_par = max(4, n_pos // 20)
+    cen = np.c_[rng.uniform(*ra, n_par), rng.uniform(*dec, n_par), rng.uniform(*z, n_par)]
+    pick = rng.integers(0, n_par, n_pos)
+    RA = cen[pick, 0] + rng.normal(0.0, 0.15, n_pos)
+    DEC = cen[pick, 1] + rng.normal(0.0, 0.15, n_pos)
+    Z = np.abs(cen[pick, 2] + rng.normal(0.0, 0.002, n_pos))
+    sh = np.sort(rng.choice(n_pos, n_shape, replace=False))
+    eps = rng.uniform(0.0, 0.6, n_shape)
+    ang = rng.uniform(0.0, np.pi, n_shape)
+    data = {"RA": RA, "DEC": DEC, "Redshift": Z, "RA_shape_sample": RA[sh], "DEC_shape_sample": DEC[sh],
+            "Redshift_shape_sample": Z[sh], "e1": eps * np.cos(2 * ang), "e2": eps * np.sin(2 * ang)}
+    if weights:
+        data["weight"] = np.exp(rng.normal(0.0, 0.3, n_pos))
+        data["weight_shape_sample"] = data["weight"][sh]
+    rnd = {"RA": rng.uniform(*ra, n_rand), "DEC": rng.uniform(*dec, n_rand), "Redshift": rng.uniform(*z, n_rand)}
+    if n_rand_shape:
+        rnd.update(RA_shape_sample=rng.uniform(*ra, n_rand_shape), DEC_shape_sample=rng.uniform(*dec, n_rand_shape),
+                   Redshift_shape_sample=rng.uniform(*z, n_rand_shape))
+    stripe = lambda x: np.clip(np.floor((x - ra[0]) / ((ra[1] - ra[0]) / 4)), 0, 3).astype(int)
+    patches = {"position": stripe(data["RA"]), "shape": stripe(data["RA_shape_sample"])}
+    if n_rand_shape:
+        patches.update(randoms_position=stripe(rnd["RA"]), randoms_shape=stripe(rnd["RA_shape_sample"]))
+    else:
+        patches["randoms"] = stripe(rnd["RA"])
+    return data, rnd, patches
+
+
+LC_CASES = {
+    # name: (kind, estimator, corr_type, catalogue kwargs, call kwargs, binning)
+    "w_clusters_both": ("w", "clusters", "both", dict(seed=31, n_pos=500, n_shape=300, n_rand=900), {},
+                        dict(separation_limits=[0.3, 25.0], num_bins_r=6, num_bins_pi=5, pi_max=30.0)),
+    "w_galaxies_gplus_overh": ("w", "galaxies", "g+", dict(seed=32, n_pos=450, n_shape=250, n_rand=700,
+                                                           n_rand_shape=500, weights=True),
+                               dict(over_h=True, cosmology=dict(Omega_c=0.25, Omega_b=0.05, h=0.68)),
+                               dict(separation_limits=[0.2, 15.0], num_bins_r=5, num_bins_pi=4, pi_max=20.0)),
+    "w_clusters_gg": ("w", "clusters", "gg", dict(seed=33, n_pos=400, n_shape=400, n_rand=800),
+                      dict(measure_cov=False),
+                      dict(separation_limits=[0.5, 30.0], num_bins_r=7, num_bins_pi=6, pi_max=40.0)),
+    "w_galaxies_both_nocov": ("w", "galaxies", "both", dict(seed=34, n_pos=400, n_shape=300, n_rand=600),
+                              dict(measure_cov=False),
+                              dict(separation_limits=[0.3, 20.0], num_bins_r=6, num_bins_pi=6, pi_max=25.0)),
+    "m_clusters_both": ("m", "clusters", "both", dict(seed=35, n_pos=500, n_shape=300, n_rand=900), {},
+                        dict(separation_limits=[0.3, 25.0], num_bins_r=6, num_bins_pi=8, pi_max=30.0)),
+    "m_galaxies_gg_rpcut": ("m", "galaxies", "gg", dict(seed=36, n_pos=450, n_shape=350, n_rand=800,
+                                                        n_rand_shape=600, weights=True),
+                            dict(rp_cut=1.0, over_h=True, measure_cov=False),
+                            dict(separation_limits=[0.4, 20.0], num_bins_r=5, num_bins_pi=6, pi_max=20.0)),
+    "m_galaxies_gplus": ("m", "galaxies", "g+", dict(seed=37, n_pos=400, n_shape=250, n_rand=700), {},
+                         dict(separation_limits=[0.3, 18.0], num_bins_r=6, num_bins_pi=10, pi_max=20.0)),
+}
+
+
+def run_lightcone(name):
+    """One lightcone case through the reference's MeasureIALightcone with
+    num_nodes = 2 (the pooled realisation driver; the serial one,
+    num_nodes = 1, passes its arguments out of order and raises)."""
+    from measureia.measure_IA import MeasureIALightcone
+    kind, est, corr, ckw, call, bkw = LC_CASES[name]
+    data, rnd, patches = lightcone_catalogue(**ckw)
+    arrays = {f"in/{k}": np.asarray(v) for k, v in data.items()}
+    arrays.update({f"rnd/{k}": np.asarray(v) for k, v in rnd.items()})
+    arrays.update({f"jk/{k}": np.asarray(v) for k, v in patches.items()})
+    outfile = f"/tmp/golden_lc_{name}.hdf5"
+    _FILES.pop(outfile, None)
+    _CHI_SEEN.clear()
+    call = dict(call)
+    cosmo_kw = call.pop("cosmology", None)
+    cosmology = _ccl_cosmology(**cosmo_kw) if cosmo_kw else None
+    measure_cov = call.pop("measure_cov", True)
+    lc = MeasureIALightcone({k: np.array(v) for k, v in data.items()}, {k: np.array(v) for k, v in rnd.items()},
+                            outfile, num_nodes=2, **bkw)
+    jk = {k: np.array(v) for k, v in patches.items()} if measure_cov else None
+    if kind == "w":
+        lc.measure_xi_w(est, "lc", corr, jk_patches=jk, measure_cov=measure_cov, cosmology=cosmology, **call)
+    else:
+        lc.measure_xi_multipoles(est, "lc", corr, jk_patches=jk, calc_errors=measure_cov, cosmology=cosmology,
+                                 **call)
+    for p, v in walk(_FILES[outfile]):
+        arrays[f"out/{p}"] = np.asarray(v)
+    zs = np.array(sorted(_CHI_SEEN))
+    arrays["chi/a"] = zs
+    arrays["chi/chi"] = np.array([_CHI_SEEN[a] for a in zs])
+    meta = {"kind": kind, "estimator": est, "corr_type": corr, "binning": bkw, "call": LC_CASES[name][4],
+            "measure_cov": measure_cov}
+    arrays["meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
+    np.savez_compressed(os.path.join(HERE, f"lc_{name}.npz"), **arrays)
+    print("lightcone", name, "datasets:", sum(1 for k in arrays if k.startswith("out/")))
+
+
 def extract_reference_golden_files():
     from h5read import read_all
     out = {}
@@ -325,3 +476,9 @@ if __name__ == "__main__":
         with contextlib.redirect_stdout(io.StringIO()):
             run_crosscov()
         print("done crosscov")
+    for name in LC_CASES:
+        if only and name not in only and "lightcone" not in only:
+            continue
+        with contextlib.redirect_stdout(io.StringIO()):
+            run_lightcone(name)
+        print("done", name)

@@ -60,3 +60,39 @@ def assert_close(a, b, rtol, what=""):
     lim = rtol * np.abs(b) + rtol * scale
     bad = err > lim
     assert not np.any(bad), f"{what}: max err {err.max():.3e} (scale {scale:.3e}) at {np.argwhere(bad)[:3].tolist()}"
+
+
+# ---- lightcone fixtures (lc_<case>.npz) ----------------------------------------
+
+def lc_case_names():
+    return sorted(os.path.basename(p)[3:-4] for p in glob.glob(os.path.join(GOLDEN, "lc_*.npz")))
+
+
+class TableCosmology:
+    """Replays the distances a fixture's reference run saw: chi(a) looked up
+    by the exact float64 scale factor, h as given."""
+
+    def __init__(self, a, chi, h):
+        self.table = dict(zip(np.asarray(a, dtype=np.float64).tolist(), np.asarray(chi, dtype=np.float64).tolist()))
+        self.h = h
+
+    def __getitem__(self, key):
+        if key == "h":
+            return self.h
+        raise KeyError(key)
+
+    def comoving_radial_distance(self, a):
+        a = np.asarray(a, dtype=np.float64)
+        return np.array([self.table[x] for x in a.ravel().tolist()]).reshape(a.shape)
+
+
+def load_lc_case(name):
+    z = np.load(os.path.join(GOLDEN, f"lc_{name}.npz"))
+    meta = json.loads(bytes(z["meta"]).decode())
+    data = {k[3:]: z[k] for k in z.files if k.startswith("in/")}
+    rnd = {k[4:]: z[k] for k in z.files if k.startswith("rnd/")}
+    jk = {k[3:]: z[k] for k in z.files if k.startswith("jk/")}
+    outs = {k[4:]: z[k] for k in z.files if k.startswith("out/")}
+    ckw = meta["call"].get("cosmology")
+    h = ckw["h"] if ckw else 0.7
+    return meta, data, rnd, jk, outs, TableCosmology(z["chi/a"], z["chi/chi"], h)
