@@ -240,6 +240,72 @@ MIA_API int mia_profile_read(mia_context* ctx, float* ms, int n, int* n_out);
 MIA_API int mia_measure_static(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat,
                                const mia_result* res, void* stream);
 
+/* ---- lightcone pair counts -------------------------------------------------
+
+   One brute-force lightcone counter of MeasureIALightcone, for one pair of
+   samples ("positions" = the outer loop of the reference, "shapes" = the
+   inner one), and all of its jackknife realisations in the same pass:
+
+     with_shapes = 1, w : _measure_xi_rp_pi_lightcone_brute  (measure_w_lightcone.py:45-214)
+     with_shapes = 0, w : _count_pairs_xi_rp_pi_lightcone_brute (measure_w_lightcone.py:216-343)
+     with_shapes = 1, m : _measure_xi_r_mur_lightcone_brute  (measure_m_lightcone.py:45-219)
+     with_shapes = 0, m : _count_pairs_xi_r_mur_lightcone_brute (measure_m_lightcone.py:221-363)
+
+   and the per-patch re-counts of the pooled jackknife driver
+   (measure_jackknife.py:265-484), which drop every pair with either member in
+   the patch.  Per pair the separations are the reference's flat-sky ones in
+   the position's frame, computed in FP64 in the reference's operation order:
+     dx = ((ra_s - ra_p) / 180 * pi) * chi_p * cos_dec_p,  dy = ((dec_s - dec_p) / 180 * pi) * chi_p,
+     Pi = chi_s - chi_p,  w: q = (h_extra dx)^2 + (h_extra dy)^2,
+     m: q = (dx^2 + dy^2) + Pi^2, r_p^2 = (h_extra dx)^2 + (h_extra dy)^2, mu = Pi / sqrt(q).
+   Bins come from breakpoint tables: q_bin over q (w: r_p^2, m: r^2) and p_bin
+   over Pi (w) or mu (m), each -1 for "not binned" and -2 for an index past the
+   last bin (where the reference's np.add.at raises IndexError; such pairs set
+   MIA_LC_INDEX_ERROR in *status and are not counted).  S+D / SxD use
+   e+ = -e cos 2(phi_a - phi_s), ex = -e sin 2(phi_a - phi_s) from the shape's
+   cos 2 phi_a, sin 2 phi_a and the separation direction (0 where r_p = 0).
+
+   Outputs (device): out[q][k][bin] for q = DD, S+D, SxD (S+D and SxD only
+   with with_shapes) and k = 0 (all pairs) or 1 + i (pairs with neither member
+   in patch i), bin = r * n_p + p; counts[k][bin] = pair counts (int64).  Sums
+   are raw: the reference's "DD == 0 -> 1" and the estimators are host work. */
+
+#define MIA_LC_INDEX_ERROR 1u
+#define MIA_LC_BAD_PATCH 2u       /* a position label outside 0..n_patch-1 (position skipped),
+                                     or a shape label >= n_patch (treated as -1) */
+
+typedef struct {
+  int kind;                 /* MIA_KIND_W or MIA_KIND_MULTIPOLES */
+  int with_shapes;          /* 1: DD, S+D, SxD; 0: DD only */
+  int n_r, n_p;
+  int n_patch;              /* jackknife patches 0..n_patch-1; 0 = no realisations */
+  int n_qbreak, n_pbreak;
+  const double* q_break;    /* host arrays, as in mia_config */
+  const int* q_bin;
+  const double* p_break;
+  const int* p_bin;
+  double h_extra;           /* factor on the projected separation (h with over_h, else 1) */
+  double rp_cut;            /* multipoles: a pair needs r_p > rp_cut */
+  double r_lim;             /* r_bins[-1]: no pair at or beyond it is binned */
+  double pi_lo, pi_hi;      /* w: binned Pi range [pi_lo, pi_hi) */
+  /* cell grid over the shapes (host-chosen; objects outside go to the edge cells) */
+  double ra0, ra_cell, dec0, dec_cell, chi0, chi_cell;
+  int n_ra, n_dec, n_chi;
+} mia_lc_config;
+
+typedef struct {            /* device arrays of n entries */
+  int64_t n;
+  const double *ra, *dec, *chi, *w;
+  const double* cos_dec;    /* positions: cos(dec / 180 * pi) as numpy forms it */
+  const double *e, *c2a, *s2a;  /* shapes with with_shapes: |e|, cos 2 phi_a, sin 2 phi_a */
+  const int32_t* patch;     /* 0..n_patch-1, or -1 (in no realisation's patch); NULL when n_patch = 0 */
+} mia_lc_sample;
+
+MIA_API int mia_lc_workspace_size(const mia_lc_config* cfg, int64_t n_pos, int64_t n_shape, size_t* bytes);
+MIA_API int mia_lc_count(mia_context* ctx, const mia_lc_config* cfg, const mia_lc_sample* pos,
+                         const mia_lc_sample* shape, void* workspace, size_t workspace_bytes, double* out,
+                         int64_t* counts, uint32_t* status, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

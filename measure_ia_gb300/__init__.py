@@ -5,8 +5,9 @@ covariance); the pair counts run in hand-written sm_103a CUDA kernels behind
 the C ABI of ``include/measure_ia_gb300.h``.
 """
 
+from .lightcone import MeasureIALightcone
 from .measure_ia import MeasureIABox
 from .output import open_output, read_output
 from .sim_info import SimInfo
 
-__all__ = ["MeasureIABox", "SimInfo", "open_output", "read_output"]
+__all__ = ["MeasureIABox", "MeasureIALightcone", "SimInfo", "open_output", "read_output"]

@@ -22,7 +22,9 @@ MAX_BINS_R, MAX_BINS_P, MAX_BREAKS = 64, 128, 96
 EXPORTED = ("mia_create", "mia_destroy", "mia_last_error", "mia_version", "mia_workspace_size",
             "mia_output_layout", "mia_measure", "mia_measure_static", "mia_batch_workspace_size",
             "mia_batch_prepare", "mia_batch_enqueue", "mia_batch_status", "mia_measure_batch",
-            "mia_profile_pairs", "mia_profile_read", "mia_jackknife_cross_cov")
+            "mia_profile_pairs", "mia_profile_read", "mia_jackknife_cross_cov", "mia_lc_workspace_size",
+            "mia_lc_count")
+MIA_LC_INDEX_ERROR, MIA_LC_BAD_PATCH = 1, 2
 STATIC_SCRATCH_BYTES = 64 * 1024 * 1024
 
 
@@ -59,6 +61,23 @@ class Result(C.Structure):
 
 
 _lib = None
+
+
+class LcConfig(C.Structure):
+    _fields_ = [("kind", C.c_int), ("with_shapes", C.c_int), ("n_r", C.c_int), ("n_p", C.c_int),
+                ("n_patch", C.c_int), ("n_qbreak", C.c_int), ("n_pbreak", C.c_int),
+                ("q_break", C.POINTER(C.c_double)), ("q_bin", C.POINTER(C.c_int)),
+                ("p_break", C.POINTER(C.c_double)), ("p_bin", C.POINTER(C.c_int)),
+                ("h_extra", C.c_double), ("rp_cut", C.c_double), ("r_lim", C.c_double), ("pi_lo", C.c_double),
+                ("pi_hi", C.c_double), ("ra0", C.c_double), ("ra_cell", C.c_double), ("dec0", C.c_double),
+                ("dec_cell", C.c_double), ("chi0", C.c_double), ("chi_cell", C.c_double), ("n_ra", C.c_int),
+                ("n_dec", C.c_int), ("n_chi", C.c_int)]
+
+
+class LcSample(C.Structure):
+    _fields_ = [("n", C.c_int64), ("ra", C.c_void_p), ("dec", C.c_void_p), ("chi", C.c_void_p), ("w", C.c_void_p),
+                ("cos_dec", C.c_void_p), ("e", C.c_void_p), ("c2a", C.c_void_p), ("s2a", C.c_void_p),
+                ("patch", C.c_void_p)]
 
 
 def load(path=None):
@@ -110,6 +129,11 @@ def load(path=None):
     lib.mia_profile_pairs.restype = C.c_int
     lib.mia_profile_read.argtypes = [C.c_void_p, C.POINTER(C.c_float), C.c_int, C.POINTER(C.c_int)]
     lib.mia_profile_read.restype = C.c_int
+    lib.mia_lc_workspace_size.argtypes = [C.POINTER(LcConfig), C.c_int64, C.c_int64, C.POINTER(C.c_size_t)]
+    lib.mia_lc_workspace_size.restype = C.c_int
+    lib.mia_lc_count.argtypes = [C.c_void_p, C.POINTER(LcConfig), C.POINTER(LcSample), C.POINTER(LcSample),
+                                 C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.mia_lc_count.restype = C.c_int
     _lib = lib
     return lib
 

@@ -229,3 +229,70 @@ def mu_table(mu_r_bins, num_bins_pi):
         return _wrap_index(ind, num_bins_pi)
 
     return _table(f, -1.0, 1.0, list(mu_r_bins))
+
+
+# ---- lightcone counters (measure_w_lightcone.py, measure_m_lightcone.py) ------
+#
+# Same formulas as above, but the lightcone counters differ in what happens
+# past the last bin: only the w counter with shapes clamps 'ind == n -> n-1'
+# (measure_w_lightcone.py:170-173); the others hand the index to np.add.at,
+# which raises IndexError.  Those intervals carry bin -2.
+
+def _index_or_error(ind, n, clamp):
+    ind = np.where(ind < 0, ind + n, ind)          # numpy's negative-index wrap
+    if clamp:
+        ind = np.where(ind == n, n - 1, ind)
+    return np.where(ind >= n, -2, ind)
+
+
+@_memo
+def lc_r_table(kind, r_bins, r_min, r_max, num_bins_r, clamp):
+    """Bin of q (w: r_p^2; multipoles: r^2), -1 outside [r_bins[0], r_bins[-1])
+    (measure_w_lightcone.py:161-173, measure_m_lightcone.py:167-176)."""
+    r_bins = np.asarray(r_bins, dtype=np.float64)
+    dlog = (np.log10(r_max) - np.log10(r_min)) / num_bins_r
+    c0 = np.log10(r_bins[0]) / dlog
+
+    def f(q):
+        q = np.asarray(q, dtype=np.float64)
+        r = np.sqrt(q)
+        ok = (r >= r_bins[0]) & (r < r_bins[-1])
+        with np.errstate(divide="ignore", invalid="ignore"):
+            ind = np.floor(np.log10(r) / dlog - c0)
+        ind = _index_or_error(np.where(ok, ind, 0).astype(np.int64), num_bins_r, clamp)
+        return np.where(ok, ind, -1)
+
+    top = max(r_bins[-1], r_max) ** 2 * 4.0
+    bottom = min(r_bins[0], r_min) ** 2 / 4.0
+    return _table(f, bottom, top, [float(x) ** 2 for x in r_bins])
+
+
+@_memo
+def lc_pi_table(pi_bins, num_bins_pi, clamp):
+    """Bin of Pi, -1 outside [pi_bins[0], pi_bins[-1]) (measure_w_lightcone.py:161-173)."""
+    pi_bins = np.asarray(pi_bins, dtype=np.float64)
+    step = (pi_bins[-1] - pi_bins[0]) / num_bins_pi
+    c = pi_bins[0] / step
+
+    def f(x):
+        x = np.asarray(x, dtype=np.float64)
+        ok = (x >= pi_bins[0]) & (x < pi_bins[-1])
+        ind = _index_or_error(np.where(ok, np.floor(x / step - c), 0).astype(np.int64), num_bins_pi, clamp)
+        return np.where(ok, ind, -1)
+
+    span = pi_bins[-1] - pi_bins[0]
+    return _table(f, pi_bins[0] - span, pi_bins[-1] + span, list(pi_bins))
+
+
+@_memo
+def lc_mu_table(mu_r_bins, num_bins_pi):
+    """Bin of mu_r = Pi / r over [-1, 1], no clamp (measure_m_lightcone.py:172-176)."""
+    mu_r_bins = np.asarray(mu_r_bins, dtype=np.float64)
+    step = 2.0 / num_bins_pi
+    c = mu_r_bins[0] / step
+
+    def f(x):
+        x = np.asarray(x, dtype=np.float64)
+        return _index_or_error(np.floor(x / step - c).astype(np.int64), num_bins_pi, False)
+
+    return _table(f, -1.0, 1.0, list(mu_r_bins))

@@ -19,7 +19,7 @@ CSRC = os.path.join(HERE, "csrc")
 LIB_NAME = "libmeasureia_gb300.so"
 LIB_PATH = os.path.join(HERE, LIB_NAME)
 BUILD_DIR = os.path.join(HERE, "_build")
-SOURCES = ["mia_prep.cu", "mia_pairs.cu", "mia_post.cu", "mia_capi.cu"]
+SOURCES = ["mia_prep.cu", "mia_pairs.cu", "mia_post.cu", "mia_lightcone.cu", "mia_capi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden"]
 

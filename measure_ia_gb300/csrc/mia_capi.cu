@@ -827,4 +827,36 @@ int mia_measure_static(mia_context* ctx, const mia_config* cfg, const mia_catalo
   return mia_measure(ctx, cfg, cat, base, (size_t)MIA_STATIC_SCRATCH_BYTES, res, stream);
 }
 
+int mia_lc_workspace_size(const mia_lc_config* cfg, int64_t n_pos, int64_t n_shape, size_t* bytes) {
+  LcPlan p;
+  const char* why = nullptr;
+  if (!bytes || !lc_plan(cfg, n_pos, n_shape, &p, &why)) return MIA_ERR_ARG;
+  *bytes = p.total;
+  return MIA_OK;
+}
+
+int mia_lc_count(mia_context* ctx, const mia_lc_config* cfg, const mia_lc_sample* pos, const mia_lc_sample* shp,
+                 void* workspace, size_t workspace_bytes, double* out, int64_t* counts, uint32_t* status,
+                 void* stream) {
+  if (!ctx) return MIA_ERR_ARG;
+  if (!cfg || !pos || !shp || !out || !counts || !status) return fail(ctx, MIA_ERR_ARG, "null argument");
+  LcPlan p;
+  const char* why = nullptr;
+  if (!lc_plan(cfg, pos->n, shp->n, &p, &why)) return fail(ctx, MIA_ERR_ARG, std::string("lightcone: ") + why);
+  if (pos->n > 0 && (!pos->ra || !pos->dec || !pos->chi || !pos->w || !pos->cos_dec))
+    return fail(ctx, MIA_ERR_ARG, "lightcone: position arrays");
+  if (shp->n > 0 && (!shp->ra || !shp->dec || !shp->chi || !shp->w)) return fail(ctx, MIA_ERR_ARG, "lightcone: shape arrays");
+  if (shp->n > 0 && cfg->with_shapes && (!shp->e || !shp->c2a || !shp->s2a))
+    return fail(ctx, MIA_ERR_ARG, "lightcone: shape terms (e, cos 2 phi, sin 2 phi)");
+  if (cfg->n_patch > 0 && ((pos->n > 0 && !pos->patch) || (shp->n > 0 && !shp->patch)))
+    return fail(ctx, MIA_ERR_ARG, "lightcone: patch labels");
+  if (!workspace || workspace_bytes < p.total || ((uintptr_t)workspace & 255))
+    return fail(ctx, MIA_ERR_WORKSPACE, "workspace missing, not 256-byte aligned, or smaller than the size query");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  MIA_CUDA(cudaSetDevice(ctx->device));
+  MIA_CUDA(launch_lc(cfg, p, *pos, *shp, workspace, out, counts, status, ctx->num_sms, st));
+  ctx->err.clear();
+  return MIA_OK;
+}
+
 }  // extern "C"

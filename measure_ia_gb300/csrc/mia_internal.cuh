@@ -359,6 +359,21 @@ cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, unsigned long l
 cudaError_t launch_post(const Params& P, const Work& w, const mia_layout& lay, double* out, double volume,
                         long long n_pos, long long n_shape, cudaStream_t st);
 cudaError_t launch_fixed_out(const Params& P, const Work& w, const Out& o, cudaStream_t st);
+// Lightcone pair counts (mia_lightcone.cu): workspace plan and launcher.
+struct LcPlan {
+  long long n_cells;
+  int n_tiles, Q, nb, P, warps;
+  size_t smem;
+  size_t off_scount, off_sstart, off_sfill, off_pcount, off_pstart, off_pfill, off_tiles, off_scell, off_pcell;
+  size_t off_shp, off_pos, off_A, off_B, off_cA, off_cB, off_next, total;
+};
+bool lc_plan(const mia_lc_config* cfg, long long n_pos, long long n_shape, LcPlan* plan, const char** why);
+cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& plan, const mia_lc_sample& pos,
+                      const mia_lc_sample& shp, void* workspace, double* out, int64_t* counts, uint32_t* status,
+                      int num_sms, cudaStream_t st);
+// exclusive prefix sum of n ints into out[0..n] (out[n] = total), tiles: (n / kScanTile + 1) ints
+cudaError_t exclusive_scan(const int* in, long long n, int* out, int* tiles, cudaStream_t st);
+
 cudaError_t launch_cross_cov(int n_real, int n_bins, const double* a, long long sa, const double* b, long long sb,
                              double* cov, double* std, cudaStream_t st);
 

@@ -1,0 +1,492 @@
+// Lightcone pair counts: the brute-force counters of MeasureIALightcone
+// (measure_w_lightcone.py:45-343, measure_m_lightcone.py:45-363) with the
+// per-patch re-counts of the pooled jackknife driver
+// (measure_jackknife.py:265-484) folded into one pass.
+//
+// The reference loops over positions and, for each, evaluates every shape
+// with numpy.  Here the shapes are counting-sorted into a grid of
+// (DEC band, comoving-distance slab, RA bin) cells; the positions, sorted into
+// the same grid, are taken one per warp by a persistent kernel, and each warp
+// reads only the cells its position's separation window can reach.  The
+// window is a superset: every candidate is decided by the reference's own
+// FP64 operation sequence (division-free FP64 bound first, then the exact
+// arithmetic with _rn intrinsics), so the bins are the reference's bit for bit.
+//
+// Jackknife: the realisation without patch i holds the pairs with neither
+// member in i.  With A[i] = sums over pairs whose position is in i and B[i] =
+// sums over pairs whose shape is in i but whose position is not, realisation
+// i = total - A[i] - B[i].  A is accumulated per warp in shared memory (the
+// positions are grid-sorted, so a warp's patch changes rarely); B, the pairs
+// that straddle two patches, goes to global atomics.
+#include <cstdio>
+
+#include "mia_internal.cuh"
+
+namespace mia {
+
+namespace {
+
+constexpr int kLcMaxWarps = 8;
+constexpr int kLcChunk = 4;            // positions per warp grab
+constexpr double kDegToRad = 3.141592653589793 / 180.0;
+
+struct LcGrid {
+  double ra0, inv_ra, dec0, inv_dec, chi0, inv_chi;
+  int n_ra, n_dec, n_chi;
+};
+
+__device__ __forceinline__ int cell_1d(double x, double x0, double inv, int n) {
+  const double t = (x - x0) * inv;     // monotone in x: window bounds and objects agree
+  if (!(t >= 0.0)) return 0;
+  if (t >= (double)n) return n - 1;
+  return (int)t;
+}
+
+__device__ __forceinline__ int cell_of(const LcGrid& g, double ra, double dec, double chi) {
+  const int a = cell_1d(ra, g.ra0, g.inv_ra, g.n_ra);
+  const int d = cell_1d(dec, g.dec0, g.inv_dec, g.n_dec);
+  const int c = cell_1d(chi, g.chi0, g.inv_chi, g.n_chi);
+  return (d * g.n_chi + c) * g.n_ra + a;
+}
+
+__global__ void k_lc_cells(const double* __restrict__ ra, const double* __restrict__ dec,
+                           const double* __restrict__ chi, long long n, LcGrid g, int* __restrict__ cell,
+                           int* __restrict__ count) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int c = cell_of(g, ra[i], dec[i], chi[i]);
+    cell[i] = c;
+    atomicAdd(&count[c], 1);
+  }
+}
+
+struct LcSorted {   // one sample in cell order
+  double *ra, *dec, *chi, *w, *aux0, *aux1, *aux2;   // aux: positions cos_dec; shapes e, c2a, s2a
+  int* patch;
+};
+
+__global__ void k_lc_scatter(mia_lc_sample in, long long n, const int* __restrict__ cell, int* __restrict__ fill,
+                             LcSorted out, int is_pos, int with_shapes) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const int d = atomicAdd(&fill[cell[i]], 1);
+    out.ra[d] = in.ra[i];
+    out.dec[d] = in.dec[i];
+    out.chi[d] = in.chi[i];
+    out.w[d] = in.w[i];
+    out.patch[d] = in.patch ? in.patch[i] : 0;
+    if (is_pos) {
+      out.aux0[d] = in.cos_dec[i];
+    } else if (with_shapes) {
+      out.aux0[d] = in.e[i];
+      out.aux1[d] = in.c2a[i];
+      out.aux2[d] = in.s2a[i];
+    }
+  }
+}
+
+struct LcParams {
+  int n_r, n_p, nb, n_patch, Q;
+  int n_qbreak, n_pbreak;
+  double h_extra, rp_cut, r_lim, pi_lo, pi_hi;
+  double q_hi;                 // r_lim^2 with a relative margin (division-free bound)
+  LcGrid g;
+  long long n_pos;
+};
+
+struct LcAcc {
+  double* A;                   // [max(1, n_patch)][Q][nb]
+  double* B;                   // [n_patch][Q][nb]
+  unsigned long long* cA;      // [max(1, n_patch)][nb]
+  unsigned long long* cB;      // [n_patch][nb]
+  unsigned* next;              // work counter
+  unsigned* status;
+};
+
+struct LcTables {              // bin tables, passed by value (2.3 KB of launch parameters)
+  double qbr[MIA_MAX_BREAKS], pbr[MIA_MAX_BREAKS];
+  int qbn[MIA_MAX_BREAKS + 1], pbn[MIA_MAX_BREAKS + 1];
+};
+
+// searchsorted(breaks, x, side='right') -> bins[]
+__device__ __forceinline__ int lookup(const double* br, const int* bins, int n, double x) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (br[mid] <= x) lo = mid + 1; else hi = mid;
+  }
+  return bins[lo];
+}
+
+template <int KIND, int SHAPES, int JK>
+__global__ void __launch_bounds__(kLcMaxWarps * 32)
+k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorted shp, const int* __restrict__ start,
+           const LcAcc acc) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nb = P.nb;
+  constexpr int Q = SHAPES ? 3 : 1;
+  // tables, then per-warp histograms (Q doubles and one count per bin)
+  double* s_qbr = reinterpret_cast<double*>(smem_raw);
+  double* s_pbr = s_qbr + MIA_MAX_BREAKS;
+  int* s_qbn = reinterpret_cast<int*>(s_pbr + MIA_MAX_BREAKS);
+  int* s_pbn = s_qbn + (MIA_MAX_BREAKS + 1);
+  // histograms start 16-byte aligned after the tables (kLcFixedSmem bytes in all)
+  double* hist_base = reinterpret_cast<double*>(smem_raw + ((2 * MIA_MAX_BREAKS * 8 + 2 * (MIA_MAX_BREAKS + 1) * 4 + 15) & ~15));
+  double* h = hist_base + (size_t)warp * ((size_t)Q * nb + (nb + 1) / 2);
+  unsigned* hc = reinterpret_cast<unsigned*>(h + (size_t)Q * nb);
+  for (int i = threadIdx.x; i < MIA_MAX_BREAKS; i += blockDim.x) {
+    s_qbr[i] = T.qbr[i];
+    s_pbr[i] = T.pbr[i];
+  }
+  for (int i = threadIdx.x; i <= MIA_MAX_BREAKS; i += blockDim.x) {
+    s_qbn[i] = T.qbn[i];
+    s_pbn[i] = T.pbn[i];
+  }
+  for (int i = lane; i < Q * nb; i += 32) h[i] = 0.0;
+  for (int i = lane; i < nb; i += 32) hc[i] = 0u;
+  __syncthreads();
+
+  int cur = -1;  // patch whose sums the warp's histogram holds
+  auto flush = [&](int p) {
+    __syncwarp();
+    if (p >= 0) {
+      double* dst = acc.A + (size_t)p * Q * nb;
+      unsigned long long* cdst = acc.cA + (size_t)p * nb;
+      for (int i = lane; i < Q * nb; i += 32) {
+        const double v = h[i];
+        if (v != 0.0) atomicAdd(&dst[i], v);
+        h[i] = 0.0;
+      }
+      for (int i = lane; i < nb; i += 32) {
+        const unsigned c = hc[i];
+        if (c) atomicAdd(&cdst[i], (unsigned long long)c);
+        hc[i] = 0u;
+      }
+    }
+    __syncwarp();
+  };
+
+  const LcGrid& g = P.g;
+  const double hx = KIND == MIA_KIND_W ? P.h_extra : 1.0;
+  for (;;) {
+    unsigned base = 0;
+    if (lane == 0) base = atomicAdd(acc.next, (unsigned)kLcChunk);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if ((long long)base >= P.n_pos) break;
+    const long long stop = min((long long)base + kLcChunk, P.n_pos);
+    for (long long ip = base; ip < stop; ++ip) {
+      const double ra_n = pos.ra[ip], dec_n = pos.dec[ip], chi_n = pos.chi[ip], w_n = pos.w[ip];
+      const double cos_n = pos.aux0[ip];
+      const int p_n = JK ? pos.patch[ip] : 0;
+      if (JK && (p_n < 0 || p_n >= P.n_patch)) {   // a position must belong to a patch
+        if (lane == 0) atomicOr(acc.status, MIA_LC_BAD_PATCH);
+        continue;
+      }
+      if (p_n != cur) {
+        flush(cur);
+        cur = p_n;
+      }
+      // separation window (a superset; the pair tests below decide)
+      const double den = fabs(hx * chi_n);
+      const double span_dec = den > 1e-300 ? P.r_lim / den / kDegToRad * (1.0 + 1e-6) + 1e-9 : 1e300;
+      const double den_ra = den * fabs(cos_n);
+      const double span_ra = den_ra > 1e-300 ? P.r_lim / den_ra / kDegToRad * (1.0 + 1e-6) + 1e-9 : 1e300;
+      const double m = 1e-9 * (fabs(chi_n) + P.r_lim + fabs(P.pi_lo) + fabs(P.pi_hi)) + 1e-9;
+      double chi_lo, chi_hi;
+      if (KIND == MIA_KIND_W) {
+        chi_lo = chi_n + P.pi_lo - m;
+        chi_hi = chi_n + P.pi_hi + m;
+      } else {
+        chi_lo = chi_n - P.r_lim - m;
+        chi_hi = chi_n + P.r_lim + m;
+      }
+      const int d0 = cell_1d(dec_n - span_dec, g.dec0, g.inv_dec, g.n_dec);
+      const int d1 = cell_1d(dec_n + span_dec, g.dec0, g.inv_dec, g.n_dec);
+      const int a0 = cell_1d(ra_n - span_ra, g.ra0, g.inv_ra, g.n_ra);
+      const int a1 = cell_1d(ra_n + span_ra, g.ra0, g.inv_ra, g.n_ra);
+      const int c0 = cell_1d(chi_lo, g.chi0, g.inv_chi, g.n_chi);
+      const int c1 = cell_1d(chi_hi, g.chi0, g.inv_chi, g.n_chi);
+      const double kx = kDegToRad * chi_n * cos_n * hx, ky = kDegToRad * chi_n * hx;
+      for (int d = d0; d <= d1; ++d) {
+        for (int c = c0; c <= c1; ++c) {
+          const int row = (d * g.n_chi + c) * g.n_ra;
+          const int j0 = start[row + a0], j1 = start[row + a1 + 1];
+          for (int j = j0 + lane; j < j1; j += 32) {
+            const double ra_s = shp.ra[j], dec_s = shp.dec[j], chi_s = shp.chi[j];
+            const double los = __dsub_rn(chi_s, chi_n);
+            // division-free bound (relative error ~1e-15, margin 1e-9 in q_hi)
+            const double ax = (ra_s - ra_n) * kx, ay = (dec_s - dec_n) * ky;
+            double qa = ax * ax + ay * ay;
+            if (KIND == MIA_KIND_MULTIPOLES) qa = qa / (hx * hx) + los * los;
+            if (qa > P.q_hi) continue;
+            // the reference's arithmetic
+            const double dra = __dmul_rn(__ddiv_rn(__dsub_rn(ra_s, ra_n), 180.0), 3.141592653589793);
+            const double ddec = __dmul_rn(__ddiv_rn(__dsub_rn(dec_s, dec_n), 180.0), 3.141592653589793);
+            const double dx = __dmul_rn(__dmul_rn(dra, chi_n), cos_n);
+            const double dy = __dmul_rn(ddec, chi_n);
+            const double dxh = P.h_extra != 1.0 ? __dmul_rn(dx, P.h_extra) : dx;
+            const double dyh = P.h_extra != 1.0 ? __dmul_rn(dy, P.h_extra) : dy;
+            const double qp = __dadd_rn(__dmul_rn(dxh, dxh), __dmul_rn(dyh, dyh));
+            int ib, jb;
+            if (KIND == MIA_KIND_W) {
+              ib = lookup(s_qbr, s_qbn, P.n_qbreak, qp);
+              if (ib == -1) continue;
+              jb = lookup(s_pbr, s_pbn, P.n_pbreak, los);
+              if (jb == -1) continue;
+            } else {
+              if (!(__dsqrt_rn(qp) > P.rp_cut)) continue;
+              const double q = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(los, los));
+              ib = lookup(s_qbr, s_qbn, P.n_qbreak, q);
+              if (ib == -1) continue;
+              const double mu = __ddiv_rn(los, __dsqrt_rn(q));
+              jb = lookup(s_pbr, s_pbn, P.n_pbreak, mu);
+              if (jb == -1) continue;
+            }
+            if (ib < 0 || jb < 0) {   // np.add.at would raise IndexError here
+              atomicOr(acc.status, MIA_LC_INDEX_ERROR);
+              continue;
+            }
+            const int bin = ib * P.n_p + jb;
+            const double ww = __dmul_rn(w_n, shp.w[j]);
+            double ep = 0.0, ex = 0.0;
+            if (SHAPES) {
+              const double rp = __dsqrt_rn(qp);
+              if (rp > 0.0) {
+                const double ux = dxh / rp, uy = dyh / rp;
+                const double c2s = ux * ux - uy * uy, s2s = 2.0 * ux * uy;
+                const double e = shp.aux0[j], c2a = shp.aux1[j], s2a = shp.aux2[j];
+                ep = -e * (c2a * c2s + s2a * s2s);
+                ex = -e * (s2a * c2s - c2a * s2s);
+              }
+            }
+            atomicAdd(&h[bin], ww);
+            if (SHAPES) {
+              atomicAdd(&h[nb + bin], ww * ep);
+              atomicAdd(&h[2 * nb + bin], ww * ex);
+            }
+            atomicAdd(&hc[bin], 1u);
+            if (JK) {
+              const int p_s = shp.patch[j];
+              if (p_s >= P.n_patch) atomicOr(acc.status, MIA_LC_BAD_PATCH);
+              if (p_s >= 0 && p_s < P.n_patch && p_s != p_n) {
+                double* dst = acc.B + (size_t)p_s * Q * nb;
+                atomicAdd(&dst[bin], ww);
+                if (SHAPES) {
+                  atomicAdd(&dst[nb + bin], ww * ep);
+                  atomicAdd(&dst[2 * nb + bin], ww * ex);
+                }
+                atomicAdd(&acc.cB[(size_t)p_s * nb + bin], 1ull);
+              }
+            }
+          }
+        }
+      }
+    }
+  }
+  flush(cur);
+}
+
+// totals and realisations: out[q][0][b] = sum_i A[i][q][b]; out[q][1+i][b] =
+// total - A[i] - B[i]; the same for the integer counts.
+__global__ void k_lc_finish(const double* __restrict__ A, const double* __restrict__ B,
+                            const unsigned long long* __restrict__ cA, const unsigned long long* __restrict__ cB,
+                            int n_patch, int Q, int nb, double* out, long long* counts) {
+  const int P = n_patch > 0 ? n_patch : 1;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n_real = 1 + n_patch;
+  if (t < Q * nb) {
+    const int q = t / nb, b = t - q * nb;
+    double tot = 0.0;
+    for (int i = 0; i < P; ++i) tot += A[((size_t)i * Q + q) * nb + b];
+    double* o = out + (size_t)q * n_real * nb;
+    o[b] = tot;
+    for (int i = 0; i < n_patch; ++i)
+      o[(size_t)(1 + i) * nb + b] = (tot - A[((size_t)i * Q + q) * nb + b]) - B[((size_t)i * Q + q) * nb + b];
+  } else if (t < Q * nb + nb) {
+    const int b = t - Q * nb;
+    unsigned long long tot = 0;
+    for (int i = 0; i < P; ++i) tot += cA[(size_t)i * nb + b];
+    counts[b] = (long long)tot;
+    for (int i = 0; i < n_patch; ++i)
+      counts[(size_t)(1 + i) * nb + b] = (long long)(tot - cA[(size_t)i * nb + b] - cB[(size_t)i * nb + b]);
+  }
+}
+
+size_t al(size_t x) { return (x + 255) & ~size_t(255); }
+
+LcSorted carve(unsigned char* base, long long n, bool is_pos) {
+  LcSorted s;
+  const size_t nn = (size_t)n + 8;
+  double* d = reinterpret_cast<double*>(base);
+  s.ra = d;
+  s.dec = d + nn;
+  s.chi = d + 2 * nn;
+  s.w = d + 3 * nn;
+  s.aux0 = d + 4 * nn;
+  if (is_pos) {
+    s.aux1 = s.aux2 = nullptr;
+    s.patch = reinterpret_cast<int*>(d + 5 * nn);
+  } else {
+    s.aux1 = d + 5 * nn;
+    s.aux2 = d + 6 * nn;
+    s.patch = reinterpret_cast<int*>(d + 7 * nn);
+  }
+  return s;
+}
+
+size_t lc_per_warp(int Q, int nb) { return (size_t)Q * nb * 8 + (size_t)(nb + 1) / 2 * 8; }
+constexpr size_t kLcFixedSmem = 2 * MIA_MAX_BREAKS * 8 + 2 * (MIA_MAX_BREAKS + 1) * 4 + 32;
+constexpr size_t kLcSmemBudget = 200 * 1024;
+
+template <int KIND, int SHAPES, int JK>
+cudaError_t launch_lc_pairs(const LcParams& P, const LcTables& T, const LcSorted& pos, const LcSorted& shp,
+                            const int* start, const LcAcc& acc, int warps, size_t smem, int num_sms,
+                            cudaStream_t st) {
+  auto kern = k_lc_pairs<KIND, SHAPES, JK>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const long long want = (P.n_pos + kLcChunk - 1) / kLcChunk;
+  long long blocks = std::min<long long>((long long)num_sms * per_sm, (want + warps - 1) / warps);
+  if (blocks < 1) blocks = 1;
+  kern<<<(int)blocks, warps * 32, smem, st>>>(P, T, pos, shp, start, acc);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+bool lc_plan(const mia_lc_config* c, long long n_pos, long long n_shape, LcPlan* p, const char** why) {
+  memset(p, 0, sizeof(*p));
+  if (!c) { *why = "null config"; return false; }
+  if (c->kind != MIA_KIND_W && c->kind != MIA_KIND_MULTIPOLES) { *why = "kind"; return false; }
+  if (c->n_r < 1 || c->n_p < 1 || c->n_r > MIA_MAX_BINS_R || c->n_p > MIA_MAX_BINS_P) { *why = "bin counts"; return false; }
+  if (c->n_patch < 0 || c->n_patch > 100000) { *why = "n_patch"; return false; }
+  if (c->n_qbreak < 0 || c->n_qbreak > MIA_MAX_BREAKS || c->n_pbreak < 0 || c->n_pbreak > MIA_MAX_BREAKS ||
+      !c->q_break || !c->q_bin || !c->p_break || !c->p_bin) { *why = "bin tables"; return false; }
+  if (c->n_ra < 1 || c->n_dec < 1 || c->n_chi < 1 || !(c->ra_cell > 0) || !(c->dec_cell > 0) || !(c->chi_cell > 0) ||
+      !std::isfinite(c->ra0) || !std::isfinite(c->dec0) || !std::isfinite(c->chi0)) {
+    *why = "cell grid"; return false;
+  }
+  if (!(c->r_lim > 0) || !std::isfinite(c->r_lim) || !(c->h_extra > 0) || !std::isfinite(c->h_extra)) {
+    *why = "r_lim / h_extra"; return false;
+  }
+  if (n_pos < 0 || n_shape < 0 || n_pos > (1ll << 31) - 64 || n_shape > (1ll << 31) - 64) { *why = "sample sizes"; return false; }
+  p->n_cells = (long long)c->n_ra * c->n_dec * c->n_chi;
+  if (p->n_cells > (1ll << 27)) { *why = "too many cells"; return false; }
+  p->Q = c->with_shapes ? 3 : 1;
+  p->nb = c->n_r * c->n_p;
+  p->P = c->n_patch > 0 ? c->n_patch : 1;
+  if (kLcFixedSmem + lc_per_warp(p->Q, p->nb) > kLcSmemBudget) { *why = "too many bins for the lightcone counter"; return false; }
+  p->warps = (int)std::min<size_t>(kLcMaxWarps, (kLcSmemBudget - kLcFixedSmem) / lc_per_warp(p->Q, p->nb));
+  p->smem = kLcFixedSmem + (size_t)p->warps * lc_per_warp(p->Q, p->nb);
+  p->n_tiles = (int)((p->n_cells + kScanTile - 1) / kScanTile) + 1;
+  size_t o = 0;
+  auto take = [&](size_t bytes) { size_t at = o; o += al(bytes); return at; };
+  p->off_scount = take((size_t)(p->n_cells + 1) * 4);
+  p->off_sstart = take((size_t)(p->n_cells + 2) * 4);
+  p->off_sfill = take((size_t)(p->n_cells + 1) * 4);
+  p->off_pcount = take((size_t)(p->n_cells + 1) * 4);
+  p->off_pstart = take((size_t)(p->n_cells + 2) * 4);
+  p->off_pfill = take((size_t)(p->n_cells + 1) * 4);
+  p->off_tiles = take((size_t)p->n_tiles * 4);
+  p->off_scell = take((size_t)n_shape * 4 + 4);
+  p->off_pcell = take((size_t)n_pos * 4 + 4);
+  p->off_shp = take(((size_t)n_shape + 8) * 8 * 8);
+  p->off_pos = take(((size_t)n_pos + 8) * 6 * 8);
+  p->off_A = take((size_t)p->P * p->Q * p->nb * 8);
+  p->off_B = take((size_t)c->n_patch * p->Q * p->nb * 8 + 8);
+  p->off_cA = take((size_t)p->P * p->nb * 8);
+  p->off_cB = take((size_t)c->n_patch * p->nb * 8 + 8);
+  p->off_next = take(256);
+  p->total = o;
+  return true;
+}
+
+cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sample& pos,
+                      const mia_lc_sample& shp, void* workspace, double* out, int64_t* counts, uint32_t* status,
+                      int num_sms, cudaStream_t st) {
+  unsigned char* ws = static_cast<unsigned char*>(workspace);
+  int* scount = reinterpret_cast<int*>(ws + p.off_scount);
+  int* sstart = reinterpret_cast<int*>(ws + p.off_sstart);
+  int* sfill = reinterpret_cast<int*>(ws + p.off_sfill);
+  int* pcount = reinterpret_cast<int*>(ws + p.off_pcount);
+  int* pstart = reinterpret_cast<int*>(ws + p.off_pstart);
+  int* pfill = reinterpret_cast<int*>(ws + p.off_pfill);
+  int* tiles = reinterpret_cast<int*>(ws + p.off_tiles);
+  int* scell = reinterpret_cast<int*>(ws + p.off_scell);
+  int* pcell = reinterpret_cast<int*>(ws + p.off_pcell);
+  const LcSorted S = carve(ws + p.off_shp, shp.n, false);
+  const LcSorted Ps = carve(ws + p.off_pos, pos.n, true);
+  LcAcc acc;
+  acc.A = reinterpret_cast<double*>(ws + p.off_A);
+  acc.B = reinterpret_cast<double*>(ws + p.off_B);
+  acc.cA = reinterpret_cast<unsigned long long*>(ws + p.off_cA);
+  acc.cB = reinterpret_cast<unsigned long long*>(ws + p.off_cB);
+  acc.next = reinterpret_cast<unsigned*>(ws + p.off_next);
+  acc.status = status;
+
+  LcGrid g;
+  g.ra0 = cfg->ra0; g.inv_ra = 1.0 / cfg->ra_cell; g.n_ra = cfg->n_ra;
+  g.dec0 = cfg->dec0; g.inv_dec = 1.0 / cfg->dec_cell; g.n_dec = cfg->n_dec;
+  g.chi0 = cfg->chi0; g.inv_chi = 1.0 / cfg->chi_cell; g.n_chi = cfg->n_chi;
+
+  cudaError_t e;
+  const size_t cells_b = (size_t)(p.n_cells + 1) * 4;
+  if ((e = cudaMemsetAsync(scount, 0, cells_b, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(pcount, 0, cells_b, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(ws + p.off_A, 0, p.total - p.off_A, st)) != cudaSuccess) return e;
+  if ((e = cudaMemsetAsync(status, 0, sizeof(uint32_t), st)) != cudaSuccess) return e;
+  auto grid_for = [&](long long n) {
+    const long long b = (n + 255) / 256;
+    return (int)std::max(1ll, std::min(b, (long long)num_sms * 8));
+  };
+  if (shp.n > 0) k_lc_cells<<<grid_for(shp.n), 256, 0, st>>>(shp.ra, shp.dec, shp.chi, shp.n, g, scell, scount);
+  if (pos.n > 0) k_lc_cells<<<grid_for(pos.n), 256, 0, st>>>(pos.ra, pos.dec, pos.chi, pos.n, g, pcell, pcount);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = exclusive_scan(scount, p.n_cells, sstart, tiles, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(sfill, sstart, (size_t)p.n_cells * 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  if ((e = exclusive_scan(pcount, p.n_cells, pstart, tiles, st)) != cudaSuccess) return e;
+  if ((e = cudaMemcpyAsync(pfill, pstart, (size_t)p.n_cells * 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
+  if (shp.n > 0) k_lc_scatter<<<grid_for(shp.n), 256, 0, st>>>(shp, shp.n, scell, sfill, S, 0, cfg->with_shapes);
+  if (pos.n > 0) k_lc_scatter<<<grid_for(pos.n), 256, 0, st>>>(pos, pos.n, pcell, pfill, Ps, 1, 0);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+
+  LcParams P;
+  P.n_r = cfg->n_r; P.n_p = cfg->n_p; P.nb = p.nb; P.n_patch = cfg->n_patch; P.Q = p.Q;
+  P.n_qbreak = cfg->n_qbreak; P.n_pbreak = cfg->n_pbreak;
+  P.h_extra = cfg->h_extra; P.rp_cut = cfg->rp_cut; P.r_lim = cfg->r_lim;
+  P.pi_lo = cfg->pi_lo; P.pi_hi = cfg->pi_hi;
+  P.q_hi = cfg->r_lim * cfg->r_lim * (1.0 + 1e-9);
+  P.g = g;
+  P.n_pos = pos.n;
+  LcTables T;
+  for (int i = 0; i < MIA_MAX_BREAKS; ++i) {
+    T.qbr[i] = i < cfg->n_qbreak ? cfg->q_break[i] : 0.0;
+    T.pbr[i] = i < cfg->n_pbreak ? cfg->p_break[i] : 0.0;
+  }
+  for (int i = 0; i <= MIA_MAX_BREAKS; ++i) {
+    T.qbn[i] = i <= cfg->n_qbreak ? cfg->q_bin[i] : -1;
+    T.pbn[i] = i <= cfg->n_pbreak ? cfg->p_bin[i] : -1;
+  }
+  if (pos.n > 0 && shp.n > 0) {
+    const bool jk = cfg->n_patch > 0;
+    const int w = p.warps;
+#define MIA_LC_CASE(K, S_, J)                                                                      \
+  if (cfg->kind == K && (cfg->with_shapes != 0) == (S_ != 0) && jk == (J != 0))                   \
+    e = launch_lc_pairs<K, S_, J>(P, T, Ps, S, sstart, acc, w, p.smem, num_sms, st);
+    e = cudaErrorInvalidValue;
+    MIA_LC_CASE(MIA_KIND_W, 0, 0) MIA_LC_CASE(MIA_KIND_W, 0, 1) MIA_LC_CASE(MIA_KIND_W, 1, 0)
+    MIA_LC_CASE(MIA_KIND_W, 1, 1) MIA_LC_CASE(MIA_KIND_MULTIPOLES, 0, 0) MIA_LC_CASE(MIA_KIND_MULTIPOLES, 0, 1)
+    MIA_LC_CASE(MIA_KIND_MULTIPOLES, 1, 0) MIA_LC_CASE(MIA_KIND_MULTIPOLES, 1, 1)
+#undef MIA_LC_CASE
+    if (e != cudaSuccess) return e;
+  }
+  const int n_thr = (p.Q + 1) * p.nb;
+  k_lc_finish<<<(n_thr + 255) / 256, 256, 0, st>>>(acc.A, acc.B, acc.cA, acc.cB, cfg->n_patch, p.Q, p.nb, out,
+                                                    reinterpret_cast<long long*>(counts));
+  return cudaGetLastError();
+}
+
+}  // namespace mia

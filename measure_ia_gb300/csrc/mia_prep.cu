@@ -463,4 +463,8 @@ cudaError_t launch_prep(const Plan& plan, const Params& P, const mia_catalog& ca
   return cudaGetLastError();
 }
 
+cudaError_t exclusive_scan(const int* in, long long n, int* out, int* tiles, cudaStream_t st) {
+  return scan(in, n, out, tiles, nullptr, st);
+}
+
 }  // namespace mia

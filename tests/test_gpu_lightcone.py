@@ -1,0 +1,196 @@
+"""Lightcone path on the GPU (MeasureIALightcone through mia_lc_count).
+
+* Every dataset of the seven reference runs in ``tests/golden/lc_*.npz``:
+  the same dataset names, values within 1e-10 relative (array scale as the
+  floor), non-finite entries at the same places.
+* Each counter alone against the oracle on randomised catalogues: integer
+  pair counts per bin bit-exact for the full sample and for every patch
+  realisation (the reference re-counts each patch; here one pass), sums
+  within 1e-10.
+* The reference's failures: IndexError past the last bin of an unclamped
+  counter, KeyError for gg jackknife covariances.
+"""
+
+import numpy as np
+import pytest
+
+from golden_io import lc_case_names, load_lc_case
+from oracle import lightcone_oracle as LO
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+def _close(got, ref, what, rtol=RTOL):
+    got = np.asarray(got, dtype=np.float64)
+    ref = np.asarray(ref, dtype=np.float64)
+    assert got.shape == ref.shape, (what, got.shape, ref.shape)
+    fin = np.isfinite(ref)
+    np.testing.assert_array_equal(np.isfinite(got), fin, err_msg=f"{what}: non-finite pattern")
+    g, r = got[fin], ref[fin]
+    if r.size:
+        lim = rtol * np.abs(r) + rtol * np.max(np.abs(r))
+        err = np.abs(g - r)
+        assert np.all(err <= lim), f"{what}: max err {err.max():.3e} (scale {np.max(np.abs(r)):.3e})"
+
+
+def _run_product(meta, data, rnd, jk, cosmo, out):
+    from measure_ia_gb300 import MeasureIALightcone
+    call = dict(meta["call"])
+    call.pop("cosmology", None)
+    call.pop("measure_cov", None)
+    lc = MeasureIALightcone({k: np.array(v) for k, v in data.items()}, {k: np.array(v) for k, v in rnd.items()},
+                            out, num_nodes=2, **meta["binning"])
+    jkp = {k: np.array(v) for k, v in jk.items()} if meta["measure_cov"] else None
+    if meta["kind"] == "w":
+        lc.measure_xi_w(meta["estimator"], "lc", meta["corr_type"], jk_patches=jkp, measure_cov=meta["measure_cov"],
+                        cosmology=cosmo, **call)
+    else:
+        lc.measure_xi_multipoles(meta["estimator"], "lc", meta["corr_type"], jk_patches=jkp,
+                                 calc_errors=meta["measure_cov"], cosmology=cosmo, **call)
+    return lc
+
+
+@pytest.mark.parametrize("name", lc_case_names())
+def test_matches_reference_runs(name, tmp_path):
+    from measure_ia_gb300 import open_output, read_output
+    meta, data, rnd, jk, outs, cosmo = load_lc_case(name)
+    out = str(tmp_path / "lc.hdf5")
+    _run_product(meta, data, rnd, jk, cosmo, out)
+    store = open_output(out)
+    assert set(store.keys()) == set(outs), sorted(set(store.keys()) ^ set(outs))[:10]
+    for path, ref in outs.items():
+        _close(store.read(path), ref, path)
+    assert set(read_output(out)) == set(outs)
+
+
+def test_gg_covariance_fails_like_the_reference(tmp_path):
+    from measure_ia_gb300 import open_output
+    meta, data, rnd, jk, outs, cosmo = load_lc_case("w_clusters_gg")
+    meta = dict(meta, measure_cov=True)
+    jk = {"position": np.arange(len(data["RA"])) % 3, "shape": np.arange(len(data["RA_shape_sample"])) % 3,
+          "randoms": np.arange(len(rnd["RA"])) % 3}
+    out = str(tmp_path / "gg.hdf5")
+    with pytest.raises(KeyError):
+        _run_product(meta, data, rnd, jk, cosmo, out)
+    # the full-sample products and the realisation counts were written first
+    keys = set(open_output(out).keys())
+    assert "w/xi_gg/lc" in keys and "w/xi_gg/lc_jk3/lc_0_DD" in keys and "w/xi_gg/lc_jk3/lc_2_RR" in keys
+
+
+# ---- single counters against the oracle --------------------------------------
+
+def _catalogue(seed, n_p, n_s, ra, dec, z):
+    rng = np.random.default_rng(seed)
+    par = max(3, n_p // 25)
+    cen = np.c_[rng.uniform(*ra, par), rng.uniform(*dec, par), rng.uniform(*z, par)]
+    pick = rng.integers(0, par, n_p)
+    spread = 0.02 * (ra[1] - ra[0])
+    sel = {"RA": cen[pick, 0] + rng.normal(0, spread, n_p), "DEC": np.clip(cen[pick, 1] + rng.normal(0, spread, n_p),
+                                                                            -89.99, 89.99),
+           "Redshift": np.abs(cen[pick, 2] + rng.normal(0, 0.002, n_p)), "weight": np.exp(rng.normal(0, 0.3, n_p))}
+    k = rng.choice(n_p, n_s, replace=False)
+    sel.update({"RA_shape_sample": sel["RA"][k] + rng.normal(0, 1e-3, n_s), "DEC_shape_sample": sel["DEC"][k],
+                "Redshift_shape_sample": sel["Redshift"][k] + rng.normal(0, 1e-3, n_s),
+                "weight_shape_sample": np.exp(rng.normal(0, 0.3, n_s)),
+                "e1": rng.uniform(-0.5, 0.5, n_s), "e2": rng.uniform(-0.5, 0.5, n_s)})
+    return sel
+
+
+SWEEP = [
+    # kind, shapes, over_h, rp_cut, n_patch, RA range, DEC range, z range, r range, n_r, n_p, pi_max
+    ("w", True, False, None, 4, (10, 40), (-10, 10), (0.1, 0.3), (0.3, 25.0), 6, 5, 30.0),
+    ("w", False, True, None, 5, (350, 360), (60, 80), (0.05, 0.2), (0.2, 15.0), 5, 8, 20.0),
+    ("w", True, True, None, 3, (0, 15), (-85, -70), (0.3, 0.5), (0.5, 40.0), 8, 6, 40.0),
+    ("m", True, False, None, 4, (100, 130), (20, 40), (0.1, 0.25), (0.3, 25.0), 6, 10, 30.0),
+    ("m", False, False, 1.5, 6, (200, 230), (-30, 0), (0.2, 0.4), (0.5, 30.0), 7, 8, 30.0),
+    ("m", True, True, 0.5, 0, (40, 60), (0, 20), (0.05, 0.15), (0.2, 12.0), 4, 12, 12.0),
+    ("w", False, False, None, 0, (0.5, 3.0), (88.0, 89.9), (0.1, 0.2), (0.1, 10.0), 5, 4, 10.0),
+]
+
+
+def _prep(sel, chi, with_shapes):
+    dec = sel["DEC"]
+    pos = {"ra": sel["RA"], "dec": dec, "chi": chi(sel["Redshift"]), "w": sel["weight"],
+           "cos_dec": np.cos(dec / 180 * np.pi)}
+    shp = {"ra": sel["RA_shape_sample"], "dec": sel["DEC_shape_sample"], "chi": chi(sel["Redshift_shape_sample"]),
+           "w": sel["weight_shape_sample"]}
+    if with_shapes:
+        e1, e2 = sel["e1"], sel["e2"]
+        theta = 1. / 2 * np.arctan2(e2, e1)
+        semi = np.array([np.cos(theta), np.sin(theta)])
+        axis = semi / np.sqrt(np.sum(semi ** 2, axis=0))
+        phi = np.arctan2(axis[1], axis[0])
+        shp.update(e=np.sqrt(e1 ** 2 + e2 ** 2), c2a=np.cos(2 * phi), s2a=np.sin(2 * phi))
+    return pos, shp
+
+
+def _subset(sel, mp, ms):
+    pk = ("RA", "DEC", "Redshift", "weight")
+    return {k: (v[mp] if k in pk else v[ms]) for k, v in sel.items()}
+
+
+@pytest.mark.parametrize("case", range(len(SWEEP)))
+def test_counter_against_oracle(case):
+    from measure_ia_gb300.cosmology import FlatLCDM
+    from measure_ia_gb300.lightcone import LightconeCounter
+    kind, shapes, over_h, rp_cut, n_patch, ra, dec, z, rr, n_r, n_p, pi_max = SWEEP[case]
+    sel = _catalogue(500 + case, 700, 500, ra, dec, z)
+    cosmo = FlatLCDM()
+    h = cosmo["h"]
+    b = LO.LcBinning(rr[0], rr[1], n_r, n_p, pi_max)
+    chi_raw = lambda a: cosmo.comoving_radial_distance(a)
+    chi_h = lambda zz: chi_raw(1 / (1 + zz)) * (h if over_h else 1.0)
+    rng = np.random.default_rng(900 + case)
+    pp = rng.integers(0, max(1, n_patch), len(sel["RA"]))
+    sp = rng.integers(0, max(1, n_patch), len(sel["RA_shape_sample"]))
+    pos, shp = _prep(sel, chi_h, shapes)
+    if n_patch:
+        pos["patch"], shp["patch"] = pp, sp.astype(np.int32)
+    counter = LightconeCounter(kind, shapes, b.r_bins, rr[0], rr[1], b.pi_bins if kind == "w" else b.mu_r_bins,
+                               h_extra=h if over_h else 1.0, rp_cut=0.0 if rp_cut is None else rp_cut)
+    sums, counts = counter.count(pos, shp, n_patch)
+    unit = lambda s: dict(s, weight=np.ones(len(s["RA"])), weight_shape_sample=np.ones(len(s["RA_shape_sample"])))
+    reals = [(np.ones(len(pp), bool), np.ones(len(sp), bool))] + [(pp != i, sp != i) for i in range(n_patch)]
+    assert counts[0].sum() > 0
+    for k, (mp, ms) in enumerate(reals):
+        s = _subset(sel, mp, ms)
+        _, _, cnt = LO.pair_counts(kind, False, b, unit(s), chi_raw, h, over_h, rp_cut)
+        got = counts[k].astype(np.float64)
+        got[got == 0] = 1
+        np.testing.assert_array_equal(got, cnt, err_msg=f"counts of realisation {k}")
+        SP, SX, DD = LO.pair_counts(kind, shapes, b, s, chi_raw, h, over_h, rp_cut)
+        dd = sums[0, k].copy()
+        dd[(dd == 0) | (counts[k] == 0)] = 1
+        _close(dd, DD, f"DD {k}")
+        if shapes:
+            _close(sums[1, k], SP, f"S+D {k}")
+            _close(sums[2, k], SX, f"SxD {k}")
+
+
+def test_index_past_last_bin_raises():
+    """mu = 1 exactly (a shape straight behind a position) indexes bin n in
+    the multipole counter, which has no clamp: IndexError, as in the reference
+    (reachable with rp_cut < 0, so that r_p = 0 passes the cut)."""
+    from measure_ia_gb300.cosmology import FlatLCDM
+    from measure_ia_gb300.lightcone import LightconeCounter
+    sel = {"RA": np.array([20.0, 21.0]), "DEC": np.array([5.0, 5.5]), "Redshift": np.array([0.2, 0.2]),
+           "weight": np.ones(2), "RA_shape_sample": np.array([20.0]), "DEC_shape_sample": np.array([5.0]),
+           "Redshift_shape_sample": np.array([0.2005]), "weight_shape_sample": np.ones(1)}
+    cosmo = FlatLCDM()
+    b = LO.LcBinning(0.1, 20.0, 5, 4, 20.0)
+    chi = lambda a: cosmo.comoving_radial_distance(a)
+    with pytest.raises(IndexError):
+        LO.pair_counts("m", False, b, sel, chi, 0.7, False, -1.0)
+    pos, shp = _prep(sel, lambda zz: chi(1 / (1 + zz)), False)
+    counter = LightconeCounter("m", False, b.r_bins, 0.1, 20.0, b.mu_r_bins, rp_cut=-1.0)
+    with pytest.raises(IndexError):
+        counter.count(pos, shp)
+    # with rp_cut = 0 the pair is cut and both count the same
+    counter = LightconeCounter("m", False, b.r_bins, 0.1, 20.0, b.mu_r_bins, rp_cut=0.0)
+    _, counts = counter.count(pos, shp)
+    _, _, dd = LO.pair_counts("m", False, b, sel, chi, 0.7, False, 0.0)
+    got = counts[0].astype(np.float64)
+    got[got == 0] = 1
+    np.testing.assert_array_equal(got, dd)

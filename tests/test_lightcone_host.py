@@ -1,0 +1,98 @@
+"""Host side of the lightcone path (no GPU): distances, bin tables, patch
+assignment and the reference's argument errors."""
+
+import numpy as np
+import pytest
+
+
+def test_flat_lcdm_distance():
+    from scipy.integrate import quad
+    from measure_ia_gb300.cosmology import FlatLCDM, comoving_radial_distance, default_cosmology
+    c = FlatLCDM(Omega_c=0.25, Omega_b=0.05, h=0.68)
+    z = np.array([0.0, 0.01, 0.3, 1.0, 2.5, 8.0])
+    want = np.array([quad(lambda x: 1.0 / float(c.E(x)), 0.0, zz, epsabs=0, epsrel=1e-13)[0] for zz in z])
+    want *= 299792.458 / 68.0
+    got = comoving_radial_distance(c, 1 / (1 + z))
+    np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-9)
+    assert default_cosmology()["h"] == 0.7
+    # matter + radiation + Lambda = 1 (flat)
+    assert abs(c.Omega_m + c.Omega_r + c.Omega_l - 1.0) < 1e-15
+
+
+@pytest.mark.parametrize("clamp", [True, False])
+def test_lightcone_tables_follow_the_reference_formula(clamp):
+    from measure_ia_gb300 import binning as B
+    rng = np.random.default_rng(3)
+    r_min, r_max, n = 0.3, 25.0, 6
+    rb = np.logspace(np.log10(r_min), np.log10(r_max), n + 1)
+    tab = B.lc_r_table("w", rb, r_min, r_max, n, clamp)
+    r = np.concatenate([rng.uniform(0.1, 30.0, 20000), rb, np.nextafter(rb, 0), np.nextafter(rb, 99)])
+    q = r * r
+    sep = np.sqrt(q)
+    dlog = (np.log10(r_max) - np.log10(r_min)) / n
+    ok = (sep >= rb[0]) & (sep < rb[-1])
+    ind = np.floor(np.log10(sep) / dlog - np.log10(rb[0]) / dlog).astype(int)
+    if clamp:
+        ind[ind == n] = n - 1
+    want = np.where(ok, np.where(ind >= n, -2, ind), -1)
+    np.testing.assert_array_equal(tab.lookup(q), want)
+    pb = np.linspace(-30.0, 30.0, 6)
+    pt = B.lc_pi_table(pb, 5, clamp)
+    x = np.concatenate([rng.uniform(-40, 40, 20000), pb, np.nextafter(pb, -99), np.nextafter(pb, 99)])
+    step = (pb[-1] - pb[0]) / 5
+    okp = (x >= pb[0]) & (x < pb[-1])
+    indp = np.floor(x / step - pb[0] / step).astype(int)
+    if clamp:
+        indp[indp == 5] = 4
+    np.testing.assert_array_equal(pt.lookup(x), np.where(okp, np.where(indp >= 5, -2, indp), -1))
+
+
+def test_mu_table_has_no_clamp():
+    from measure_ia_gb300 import binning as B
+    mb = np.linspace(-1, 1, 9)
+    t = B.lc_mu_table(mb, 8)
+    assert t.lookup(np.array([1.0]))[0] == -2          # np.add.at would raise
+    assert t.lookup(np.array([-1.0]))[0] == 0
+    # just below 1 the reference's floor(mu / dmu - mu_0 / dmu) still rounds to n
+    x = np.array([np.nextafter(1.0, 0), 0.9999, 0.99, 0.75, np.nextafter(0.75, 0)])
+    ind = np.floor(x / 0.25 - (-1.0) / 0.25).astype(int)
+    np.testing.assert_array_equal(t.lookup(x), np.where(ind >= 8, -2, ind))
+    assert ind[0] == 8 and ind[1] == 7
+
+
+def test_sky_kmeans_patches():
+    from measure_ia_gb300.lightcone import assign_jackknife_patches
+    rng = np.random.default_rng(0)
+    rnd = {"RA": rng.uniform(10, 50, 3000), "DEC": rng.uniform(-10, 10, 3000)}
+    rnd["RA_shape_sample"], rnd["DEC_shape_sample"] = rnd["RA"][:1000], rnd["DEC"][:1000]
+    data = {"RA": rng.uniform(10, 50, 500), "DEC": rng.uniform(-10, 10, 500)}
+    data["RA_shape_sample"], data["DEC_shape_sample"] = data["RA"][:200], data["DEC"][:200]
+    a = assign_jackknife_patches(data, rnd, 6)
+    b = assign_jackknife_patches(data, rnd, 6)
+    assert set(a) == {"randoms_position", "randoms_shape", "position", "shape"}
+    for k in a:
+        np.testing.assert_array_equal(a[k], b[k])             # seeded: reproducible
+    assert set(np.unique(a["randoms_position"])) == set(range(6))
+    np.testing.assert_array_equal(a["randoms_shape"], a["randoms_position"][:1000])
+
+
+def test_reference_argument_errors():
+    from measure_ia_gb300 import MeasureIALightcone
+    data = {"RA": np.ones(3), "DEC": np.ones(3), "Redshift": np.ones(3), "RA_shape_sample": np.ones(2),
+            "DEC_shape_sample": np.ones(2), "Redshift_shape_sample": np.ones(2), "e1": np.zeros(2), "e2": np.zeros(2)}
+    with pytest.raises(ValueError):
+        MeasureIALightcone(dict(data), None, None, pi_max=None)
+    lc = MeasureIALightcone(dict(data), None, None, pi_max=10.0)
+    assert np.array_equal(lc.data["weight"], np.ones(3))       # default weights, as the reference
+    with pytest.raises(KeyError, match="add randoms"):
+        lc.measure_xi_w("clusters", "d", "both")
+    with pytest.raises(KeyError, match="No randoms given"):
+        lc.measure_xi_w("galaxies", "d", "both")
+    with pytest.raises(KeyError, match="Unknown input for IA_estimator"):
+        lc.measure_xi_w("stars", "d", "both")
+    lc = MeasureIALightcone(dict(data), {"RA": np.ones(4), "DEC": np.ones(4), "Redshift": np.ones(4)}, None,
+                            pi_max=10.0)
+    with pytest.raises(ValueError, match="provide either jk_patches or num_jk"):
+        lc.measure_xi_w("clusters", "d", "both", measure_cov=True)
+    with pytest.raises(KeyError, match="Unknown value for corr_type"):
+        lc.measure_xi_multipoles("clusters", "d", "g-", calc_errors=False)
