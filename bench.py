@@ -470,6 +470,195 @@ def run_large(args, local):
                        "n_positions": int(len(data["Position"])), "n_shapes": int(len(data["Position_shape_sample"]))}}
 
 
+# ---------------------------------------------------------------------------
+# lightcone workload (MeasureIALightcone.measure_xi_w, clusters estimator)
+# ---------------------------------------------------------------------------
+
+LC_DESC = ("lightcone survey 40 x 25 deg (1000 deg^2), 0.1 < z < 0.5: 200k clustered galaxies (100k shapes), "
+           "1M randoms; w_gg + w_g+ (clusters estimator: S+D, S+R, RD, RR counters), 10 log r_p bins 0.1-60 Mpc, "
+           "20 Pi bins |Pi| < 60 Mpc, 50 jackknife patches (10 x 5 RA/DEC grid)")
+# FP64 operations per binned pair in the reference's per-pair numpy sequence
+# (a division, square root, log10 or trig call counted as one): with shapes
+# (S+D, S+R) 36, counts only (RD, RR) 26.
+LC_OPS = {True: 36, False: 26}
+
+
+def lightcone_catalogue(seed=77, n_par=10000, n_rand=1_000_000, n_shape=100_000):
+    rng = np.random.default_rng(seed)
+    cen = np.c_[rng.uniform(0, 40, n_par), rng.uniform(-12.5, 12.5, n_par), rng.uniform(0.1, 0.5, n_par)]
+    kids = rng.poisson(20, n_par)
+    par = np.repeat(np.arange(n_par), kids)
+    n = len(par)
+    data = {"RA": np.clip(cen[par, 0] + rng.normal(0, 0.05, n), 0, 40),
+            "DEC": np.clip(cen[par, 1] + rng.normal(0, 0.05, n), -12.5, 12.5),
+            "Redshift": np.clip(cen[par, 2] + rng.normal(0, 0.0005, n), 0.1, 0.5)}
+    k = np.sort(rng.choice(n, min(n_shape, n), replace=False))
+    eps, ang = rng.uniform(0, 0.6, len(k)), rng.uniform(0, np.pi, len(k))
+    data.update(RA_shape_sample=data["RA"][k], DEC_shape_sample=data["DEC"][k], Redshift_shape_sample=data["Redshift"][k],
+                e1=eps * np.cos(2 * ang), e2=eps * np.sin(2 * ang))
+    rnd = {"RA": rng.uniform(0, 40, n_rand), "DEC": rng.uniform(-12.5, 12.5, n_rand), "Redshift": rng.uniform(0.1, 0.5, n_rand)}
+    grid = lambda ra, dec: (np.minimum(9, (ra / 4.0).astype(int)) * 5 + np.minimum(4, ((dec + 12.5) / 5.0).astype(int)))
+    jk = {"position": grid(data["RA"], data["DEC"]), "shape": grid(data["RA_shape_sample"], data["DEC_shape_sample"]),
+          "randoms": grid(rnd["RA"], rnd["DEC"])}
+    return data, rnd, jk
+
+
+def _lc_counters(data, rnd, jk):
+    """The four counters of measure_xi_w('clusters', corr_type='both') with
+    their host inputs, as MeasureIALightcone prepares them."""
+    from measure_ia_gb300 import MeasureIALightcone
+    from measure_ia_gb300.cosmology import default_cosmology
+    from measure_ia_gb300.lightcone import _Run
+    lc = MeasureIALightcone(dict(data), dict(rnd), None, separation_limits=[0.1, 60.0], num_bins_r=10,
+                            num_bins_pi=20, pi_max=60.0)
+    r = dict(lc.randoms_data)
+    r.update(RA_shape_sample=r["RA"], DEC_shape_sample=r["DEC"], Redshift_shape_sample=r["Redshift"],
+             weight=np.ones(len(r["RA"])))
+    r["weight_shape_sample"] = r["weight"]
+    cosmo = default_cosmology()
+    run = _Run(lc, "w", "clusters", "lc", "both", lc.data, r, lambda z: cosmo.comoving_radial_distance(1 / (1 + z)),
+               0.7, False, None, None, None)
+    out = []
+    for name, pf, sf, shapes, pp, sp in (("S+D", "D", "D", True, "position", "shape"),
+                                         ("S+R", "R", "D", True, "randoms", "shape"),
+                                         ("RD", "D", "R", False, "position", "randoms"),
+                                         ("RR", "R", "R", False, "randoms", "randoms")):
+        sel = run._select(run._combo(pf, sf, shapes), None, shapes)
+        lo, hi = int(min(jk[pp])), int(max(jk[pp]))
+        pos, shp = run._samples(sel, shapes, np.asarray(jk[pp]) - lo, run._shape_labels(jk[sp], lo, hi))
+        out.append((name, shapes, run._counter(shapes), pos, shp, hi - lo + 1))
+    return lc, out
+
+
+def measured_dgemm_tflops(device):
+    import torch
+    a = torch.randn(4096, 4096, dtype=torch.float64, device=device)
+    b = torch.randn(4096, 4096, dtype=torch.float64, device=device)
+    for _ in range(2):
+        torch.matmul(a, b)
+    torch.cuda.synchronize(device)
+    best = 1e9
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize(device)
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return 2 * 4096 ** 3 / best / 1e12
+
+
+def lightcone_cpu(data, rnd, n_sample, processes=None):
+    """The oracle's restatement of the reference's brute-force RR counter
+    (measure_w_lightcone.py:216-343, a numpy loop over positions) on the
+    first n_sample random positions against all random shapes: (binned
+    pairs, seconds)."""
+    from measure_ia_gb300.cosmology import default_cosmology
+    from oracle import lightcone_oracle as LO
+    cosmo = default_cosmology()
+    b = LO.LcBinning(0.1, 60.0, 10, 20, 60.0)
+    sel = {"RA": rnd["RA"][:n_sample], "DEC": rnd["DEC"][:n_sample], "Redshift": rnd["Redshift"][:n_sample],
+           "weight": np.ones(n_sample), "RA_shape_sample": rnd["RA"], "DEC_shape_sample": rnd["DEC"],
+           "Redshift_shape_sample": rnd["Redshift"], "weight_shape_sample": np.ones(len(rnd["RA"]))}
+    t0 = time.perf_counter()
+    _, _, dd = LO.pair_counts("w", False, b, sel, lambda a: cosmo.comoving_radial_distance(a), 0.7, False,
+                              empty_to_one=False)
+    secs = time.perf_counter() - t0
+    return float(dd.sum()), secs   # unit weights: DD = pair counts
+
+
+def run_lightcone(args, local):
+    import torch
+    data, rnd, jk = lightcone_catalogue()
+    cores = 1
+    cpu = None
+    if not args.no_cpu:
+        pairs, secs = lightcone_cpu(data, rnd, args.lc_cpu_sample)
+        cpu = {"value": pairs / secs, "unit": "binned pairs/s", "cores": cores, "kind": "port",
+               "sample": f"RR counter: first {args.lc_cpu_sample} random positions x all 1M random shapes, "
+                         f"{secs:.1f} s (the reference's per-position numpy loop, one process)"}
+    lc, counters = _lc_counters(data, rnd, jk)
+    jobs = [(name, shapes, c, c.prepare(pos, shp, npatch)) for name, shapes, c, pos, shp, npatch in counters]
+    stream = torch.cuda.current_stream(local)
+    for _ in range(max(3, args.warmup)):
+        for _, _, c, j in jobs:
+            c.run(j, stream.cuda_stream)
+    torch.cuda.synchronize(local)
+    binned = {}
+    for name, shapes, c, j in jobs:
+        sums, counts = c.fetch(j)
+        binned[name] = (shapes, int(counts[0].sum()))
+    per, per_counter = [], {name: [] for name, *_ in jobs}
+    with ClockSampler(local) as clk:
+        torch.cuda.synchronize(local)
+        for _ in range(args.steps):
+            evs = []
+            t0 = torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            for name, _, c, j in jobs:
+                c.run(j, stream.cuda_stream)
+                e = torch.cuda.Event(enable_timing=True)
+                e.record(stream)
+                evs.append((name, e))
+            torch.cuda.synchronize(local)
+            prev = t0
+            for name, e in evs:
+                per_counter[name].append(prev.elapsed_time(e))
+                prev = e
+            per.append(t0.elapsed_time(evs[-1][1]))
+    ms = float(np.mean(per))
+    total_binned = sum(v[1] for v in binned.values())
+    ops = sum(LC_OPS[s] * n for s, n in binned.values())
+    peak = measured_dgemm_tflops(local)
+    achieved = ops / (ms / 1e3) / 1e12
+    # end to end through the public API: host arrays in, HDF5-layout products out (in memory)
+    from measure_ia_gb300 import MeasureIALightcone
+    e2e = []
+    for _ in range(max(1, min(2, args.steps))):
+        lc2 = MeasureIALightcone(dict(data), dict(rnd), None, separation_limits=[0.1, 60.0], num_bins_r=10,
+                                 num_bins_pi=20, pi_max=60.0, num_nodes=2)
+        torch.cuda.synchronize(local)
+        t = time.perf_counter()
+        lc2.measure_xi_w("clusters", "lc", "both", jk_patches={k: np.array(v) for k, v in jk.items()})
+        torch.cuda.synchronize(local)
+        e2e.append(time.perf_counter() - t)
+    h2d = sum(j.h2d for *_, j in jobs)
+    d2h = sum(j.out.numel() * 8 + j.cnt.numel() * 8 + 4 for *_, j in jobs)
+    return {"metric": "binned pairs/s, lightcone w_gg+w_g+ (MeasureIALightcone.measure_xi_w, clusters, 50 patches)",
+            "value": total_binned / (ms / 1e3), "unit": "binned pairs/s", "ms_per_step": ms, "step_ms": per,
+            "counter_ms": {k: float(np.mean(v)) for k, v in per_counter.items()},
+            "binned_pairs_per_step": {k: v[1] for k, v in binned.items()}, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "config": {"workload": LC_DESC, "n_positions": len(data["RA"]),
+                                        "n_shapes": len(data["RA_shape_sample"]), "n_randoms": len(rnd["RA"]),
+                                        "l2": "inputs larger than L2 (RR: 1M x 1M sorted samples, 8 x 8 MB arrays)"},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                         "traffic": None, "kernel": "k_lc_pairs (+ cell-list build), all four counters",
+                         "note": "achieved = FP64 ops per binned pair of the reference's numpy sequence (36 with "
+                                 "shapes, 26 counts only) x binned pairs / device time of the four counters; "
+                                 "peak = DGEMM measured here (torch.matmul float64 4096^3, best of 5): no FP64 "
+                                 "figure in MEASURED_PEAKS.json"},
+            "cpu_baseline": cpu,
+            "e2e": {"value": total_binned / float(np.mean(e2e)), "unit": "binned pairs/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "seconds": e2e},
+            "gpu_launches": 4 * 13 * args.steps,
+            "clocks": clk.summary()}
+
+
+def lightcone_reference_line(args):
+    data, rnd, jk = lightcone_catalogue()
+    res = [lightcone_cpu(data, rnd, args.lc_cpu_sample) for _ in range(args.steps)]
+    pairs, secs = sum(r[0] for r in res), sum(r[1] for r in res)
+    v = pairs / secs
+    return {"metric": "binned pairs/s, lightcone w_gg+w_g+ (MeasureIALightcone.measure_xi_w, clusters, 50 patches)",
+            "value": v, "unit": "binned pairs/s", "n_gpus": 0, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic", "impl": "reference", "config": {"workload": LC_DESC},
+            "cpu_baseline": {"value": v, "unit": "binned pairs/s", "cores": 1, "kind": "port",
+                             "sample": f"RR counter: first {args.lc_cpu_sample} random positions x all 1M random "
+                                       "shapes per step"},
+            "e2e": {"value": v, "unit": "binned pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -484,7 +673,9 @@ def main():
     ap.add_argument("--knobs", default="", help="CELL,REFINE,SPU[,CELL_LOS,REFINE_LOS] launch knobs instead of tuning (profiling runs)")
     ap.add_argument("--no-multipoles", action="store_true", help="skip the multipole rate and accuracy report")
     ap.add_argument("--fp64", action="store_true", help="batch48 / large: also time the plain FP64 form")
-    ap.add_argument("--workload", default="config2", choices=["config2", "batch48", "large", "config0", "config1"],
+    ap.add_argument("--lc-cpu-sample", type=int, default=60, help="lightcone: random positions in the CPU sample")
+    ap.add_argument("--workload", default="config2",
+                    choices=["config2", "batch48", "large", "config0", "config1", "lightcone"],
                     help="config2 = the headline line; batch48 and large print their own lines")
     ap.add_argument("--centres", type=int, default=80000, help="Neyman-Scott parents (profiling runs)")
     ap.add_argument("--shapes", type=int, default=1_000_000, help="shape-sample size (profiling runs)")
@@ -492,11 +683,16 @@ def main():
     rank, ws, local = world()
     if args.impl == "reference" and rank != 0:
         return  # the CPU reference arm runs on rank 0 only
+    if args.impl == "reference" and args.workload == "lightcone":
+        print(json.dumps(lightcone_reference_line(args)))
+        return
     if args.workload != "config2":
         import torch
         torch.cuda.set_device(local)
         if args.workload == "batch48":
             line = run_batch48(args, local)
+        elif args.workload == "lightcone":
+            line = run_lightcone(args, local)
         elif args.workload == "large":
             line = run_large(args, local)
         else:

@@ -94,11 +94,10 @@ class LightconeCounter:
         cfg.ra_cell, cfg.dec_cell, cfg.chi_cell = (float(x) for x in cell)
         cfg.n_ra, cfg.n_dec, cfg.n_chi = (int(x) for x in n)
 
-    def count(self, pos, shp, n_patch=0):
-        """pos: ra, dec, chi, w, cos_dec (and patch); shp: ra, dec, chi, w
-        (and e, c2a, s2a with shapes; patch).  Host float64 arrays.  Returns
-        (sums (Q, 1 + n_patch, n_r, n_p), counts (1 + n_patch, n_r, n_p))
-        with Q = 3 (DD, S+D, SxD) or 1 (DD)."""
+    def prepare(self, pos, shp, n_patch=0):
+        """Upload one pair of samples and size the launch: pos holds ra, dec,
+        chi, w, cos_dec (and patch); shp holds ra, dec, chi, w (and e, c2a,
+        s2a with shapes; patch).  Host float64 arrays."""
         import torch
         dev = torch.device("cuda", self.device)
         cfg = L.LcConfig()
@@ -113,6 +112,10 @@ class LightconeCounter:
         cfg.h_extra, cfg.rp_cut, cfg.r_lim = self.h_extra, self.rp_cut, self.r_lim
         cfg.pi_lo, cfg.pi_hi = self.pi_lo, self.pi_hi
         n_pos, n_shp = len(pos["ra"]), len(shp["ra"])
+        for k in ("ra", "dec", "chi", "w"):
+            for smp in (pos, shp):
+                if not np.all(np.isfinite(smp[k])):
+                    raise ValueError(f"lightcone {k} values must be finite")
         if n_shp:
             self._grid(cfg, pos, shp)
         else:
@@ -126,10 +129,6 @@ class LightconeCounter:
             keep.append(t)
             return t.data_ptr()
 
-        for k in ("ra", "dec", "chi", "w"):
-            for s in (pos, shp):
-                if not np.all(np.isfinite(s[k])):
-                    raise ValueError(f"lightcone {k} values must be finite")
         sp = L.LcSample()
         sp.n = n_pos
         if n_pos:
@@ -155,26 +154,50 @@ class LightconeCounter:
         ws = torch.empty(nbytes.value + 256, dtype=torch.uint8, device=dev)
         base = ws.data_ptr()
         base += (-base) % 256
-        out = torch.empty(Q * (1 + n_patch) * nb, dtype=torch.float64, device=dev)
-        cnt = torch.empty((1 + n_patch) * nb, dtype=torch.int64, device=dev)
-        status = torch.zeros(1, dtype=torch.int32, device=dev)
+        job = _LcJob(cfg=cfg, pos=sp, shp=ss, keep=keep + [ws], ws=base, ws_bytes=nbytes.value, n_patch=int(n_patch),
+                     Q=Q, h2d=sum(t.numel() * t.element_size() for t in keep))
+        job.out = torch.empty(Q * (1 + n_patch) * nb, dtype=torch.float64, device=dev)
+        job.cnt = torch.empty((1 + n_patch) * nb, dtype=torch.int64, device=dev)
+        job.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        return job
+
+    def run(self, job, stream=None):
+        """Enqueue the count on ``stream`` (default: torch's current stream)."""
+        import torch
         from .engine import context
+        lib = L.load()
         ctx = context(self.device)
-        stream = torch.cuda.current_stream(dev).cuda_stream
-        rc = lib.mia_lc_count(ctx, C.byref(cfg), C.byref(sp), C.byref(ss), C.c_void_p(base), nbytes.value,
-                              C.c_void_p(out.data_ptr()), C.c_void_p(cnt.data_ptr()), C.c_void_p(status.data_ptr()),
-                              C.c_void_p(stream))
+        if stream is None:
+            stream = torch.cuda.current_stream(torch.device("cuda", self.device)).cuda_stream
+        rc = lib.mia_lc_count(ctx, C.byref(job.cfg), C.byref(job.pos), C.byref(job.shp), C.c_void_p(job.ws),
+                              job.ws_bytes, C.c_void_p(job.out.data_ptr()), C.c_void_p(job.cnt.data_ptr()),
+                              C.c_void_p(job.status.data_ptr()), C.c_void_p(stream))
         if rc != L.MIA_OK:
             raise L.MiaError(rc, lib.mia_last_error(ctx).decode())
-        sums = out.cpu().numpy().reshape(Q, 1 + n_patch, self.n_r, self.n_p)
-        counts = cnt.cpu().numpy().reshape(1 + n_patch, self.n_r, self.n_p)
-        flags = int(status.cpu().item())
+
+    def fetch(self, job):
+        """(sums (Q, 1 + n_patch, n_r, n_p), counts (1 + n_patch, n_r, n_p))
+        with Q = 3 (DD, S+D, SxD) or 1 (DD); raises what the reference raises."""
+        sums = job.out.cpu().numpy().reshape(job.Q, 1 + job.n_patch, self.n_r, self.n_p)
+        counts = job.cnt.cpu().numpy().reshape(1 + job.n_patch, self.n_r, self.n_p)
+        flags = int(job.status.cpu().item())
         if flags & L.MIA_LC_BAD_PATCH:
-            raise ValueError(f"jackknife patch labels must lie in 0..{n_patch - 1} (positions) or be -1 (shapes)")
+            raise ValueError(f"jackknife patch labels must lie in 0..{job.n_patch - 1} (positions) or be -1 (shapes)")
         if flags & L.MIA_LC_INDEX_ERROR:
             n = self.n_r
             raise IndexError(f"index {n} is out of bounds for axis 0 with size {n}")
         return sums, counts
+
+    def count(self, pos, shp, n_patch=0):
+        """prepare + run + fetch."""
+        job = self.prepare(pos, shp, n_patch)
+        self.run(job)
+        return self.fetch(job)
+
+
+class _LcJob:
+    def __init__(self, **kw):
+        self.__dict__.update(kw)
 
 
 # ----------------------------------------------------------------------------

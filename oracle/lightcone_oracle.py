@@ -98,11 +98,11 @@ def _axis_terms(sel):
     return e, phi_axis
 
 
-def pair_counts(kind, with_shapes, b: LcBinning, sel, chi, h, over_h=False, rp_cut=None):
+def pair_counts(kind, with_shapes, b: LcBinning, sel, chi, h, over_h=False, rp_cut=None, empty_to_one=True):
     """(S+D, SxD, DD) of one brute-force counter, DD with empty bins set to 1
-    as the reference leaves them; S+D and SxD are None when ``with_shapes``
-    is False.  An index past the last bin raises IndexError, as np.add.at
-    does in the reference."""
+    as the reference leaves them (``empty_to_one=False`` keeps the raw sums);
+    S+D and SxD are None when ``with_shapes`` is False.  An index past the
+    last bin raises IndexError, as np.add.at does in the reference."""
     RA, DEC = sel["RA"], sel["DEC"]
     RA_s, DEC_s = sel["RA_shape_sample"], sel["DEC_shape_sample"]
     weight, weight_shape = sel["weight"], sel["weight_shape_sample"]
@@ -161,7 +161,8 @@ def pair_counts(kind, with_shapes, b: LcBinning, sel, chi, h, over_h=False, rp_c
         if with_shapes:
             np.add.at(SP, (ind_r, ind_p), ww * e_plus[mask])
             np.add.at(SX, (ind_r, ind_p), ww * e_cross[mask])
-    DD[np.where(DD == 0)] = 1
+    if empty_to_one:
+        DD[np.where(DD == 0)] = 1
     return SP, SX, DD
 
 
