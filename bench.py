@@ -569,7 +569,8 @@ def lightcone_cpu(data, rnd, n_sample, processes=None):
 
 def run_lightcone(args, local):
     import torch
-    data, rnd, jk = lightcone_catalogue()
+    data, rnd, jk = lightcone_catalogue(n_par=args.lc_parents, n_rand=args.lc_randoms,
+                                        n_shape=min(100_000, args.lc_parents * 10))
     cores = 1
     cpu = None
     if not args.no_cpu:
@@ -645,7 +646,8 @@ def run_lightcone(args, local):
 
 
 def lightcone_reference_line(args):
-    data, rnd, jk = lightcone_catalogue()
+    data, rnd, jk = lightcone_catalogue(n_par=args.lc_parents, n_rand=args.lc_randoms,
+                                        n_shape=min(100_000, args.lc_parents * 10))
     res = [lightcone_cpu(data, rnd, args.lc_cpu_sample) for _ in range(args.steps)]
     pairs, secs = sum(r[0] for r in res), sum(r[1] for r in res)
     v = pairs / secs
@@ -674,6 +676,8 @@ def main():
     ap.add_argument("--no-multipoles", action="store_true", help="skip the multipole rate and accuracy report")
     ap.add_argument("--fp64", action="store_true", help="batch48 / large: also time the plain FP64 form")
     ap.add_argument("--lc-cpu-sample", type=int, default=60, help="lightcone: random positions in the CPU sample")
+    ap.add_argument("--lc-randoms", type=int, default=1_000_000, help="lightcone: randoms (profiling runs)")
+    ap.add_argument("--lc-parents", type=int, default=10000, help="lightcone: clustered parents (profiling runs)")
     ap.add_argument("--workload", default="config2",
                     choices=["config2", "batch48", "large", "config0", "config1", "lightcone"],
                     help="config2 = the headline line; batch48 and large print their own lines")

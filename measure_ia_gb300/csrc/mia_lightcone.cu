@@ -60,21 +60,35 @@ __global__ void k_lc_cells(const double* __restrict__ ra, const double* __restri
 }
 
 struct LcSorted {   // one sample in cell order
-  double *ra, *dec, *chi, *w, *aux0, *aux1, *aux2;   // aux: positions cos_dec; shapes e, c2a, s2a
+  double *ra, *dec, *chi, *w, *aux0, *aux1, *aux2;   // positions: cos_dec, cx, cy; shapes: e, c2a, s2a
   int* patch;
+  float4* hl;          // (ra_hi, ra_lo, dec_hi, dec_lo): x = hi + lo to ~2^-48 relative
+  float2* chl;         // (chi_hi, chi_lo)
 };
+
+__device__ __forceinline__ float2 split(double x) {
+  const float hi = __double2float_rn(x);
+  return make_float2(hi, __double2float_rn(x - (double)hi));
+}
 
 __global__ void k_lc_scatter(mia_lc_sample in, long long n, const int* __restrict__ cell, int* __restrict__ fill,
                              LcSorted out, int is_pos, int with_shapes) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const int d = atomicAdd(&fill[cell[i]], 1);
-    out.ra[d] = in.ra[i];
-    out.dec[d] = in.dec[i];
-    out.chi[d] = in.chi[i];
+    const double ra = in.ra[i], dec = in.dec[i], chi = in.chi[i];
+    out.ra[d] = ra;
+    out.dec[d] = dec;
+    out.chi[d] = chi;
     out.w[d] = in.w[i];
     out.patch[d] = in.patch ? in.patch[i] : 0;
+    const float2 a = split(ra), b = split(dec);
+    out.hl[d] = make_float4(a.x, a.y, b.x, b.y);
+    out.chl[d] = split(chi);
     if (is_pos) {
-      out.aux0[d] = in.cos_dec[i];
+      const double c = in.cos_dec[i];
+      out.aux0[d] = c;
+      out.aux1[d] = kDegToRad * chi * c;   // dx ~ (ra_s - ra_p) * cx, few ulp from the reference's dx
+      out.aux2[d] = kDegToRad * chi;       // dy ~ (dec_s - dec_p) * cy
     } else if (with_shapes) {
       out.aux0[d] = in.e[i];
       out.aux1[d] = in.c2a[i];
@@ -86,8 +100,9 @@ __global__ void k_lc_scatter(mia_lc_sample in, long long n, const int* __restric
 struct LcParams {
   int n_r, n_p, nb, n_patch, Q;
   int n_qbreak, n_pbreak;
-  double h_extra, rp_cut, r_lim, pi_lo, pi_hi;
-  double q_hi;                 // r_lim^2 with a relative margin (division-free bound)
+  double h_extra, h2, rp_cut, r_lim, pi_lo, pi_hi;
+  float qf_hi;                 // FP32 prefilter bound on q (r_lim^2 (1 + 1e-4))
+  float los_lo, los_hi;        // w: FP32 prefilter bounds on Pi
   LcGrid g;
   long long n_pos;
 };
@@ -116,21 +131,39 @@ __device__ __forceinline__ int lookup(const double* br, const int* bins, int n, 
   return bins[lo];
 }
 
+// lookup of an approximate x: `near` is set when a breakpoint lies within tol
+// of x, where the approximation could fall in the wrong interval
+__device__ __forceinline__ int lookup_guarded(const double* br, const int* bins, int n, double x, double tol,
+                                              bool& near) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (br[mid] <= x) lo = mid + 1; else hi = mid;
+  }
+  if (lo > 0 && x - br[lo - 1] <= tol) near = true;
+  if (lo < n && br[lo] - x <= tol) near = true;
+  return bins[lo];
+}
+
+constexpr double kGuard = 1e-12;   // relative; the approximate q, mu are within ~1e-15 of the reference's
+constexpr int kQueue = 64;         // per-warp queue of prefilter survivors
+
 template <int KIND, int SHAPES, int JK>
 __global__ void __launch_bounds__(kLcMaxWarps * 32)
 k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorted shp, const int* __restrict__ start,
            const LcAcc acc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
   const int nb = P.nb;
   constexpr int Q = SHAPES ? 3 : 1;
-  // tables, then per-warp histograms (Q doubles and one count per bin)
+  // tables, per-warp queues, then per-warp histograms (Q doubles and one count per bin)
   double* s_qbr = reinterpret_cast<double*>(smem_raw);
   double* s_pbr = s_qbr + MIA_MAX_BREAKS;
   int* s_qbn = reinterpret_cast<int*>(s_pbr + MIA_MAX_BREAKS);
   int* s_pbn = s_qbn + (MIA_MAX_BREAKS + 1);
-  // histograms start 16-byte aligned after the tables (kLcFixedSmem bytes in all)
-  double* hist_base = reinterpret_cast<double*>(smem_raw + ((2 * MIA_MAX_BREAKS * 8 + 2 * (MIA_MAX_BREAKS + 1) * 4 + 15) & ~15));
+  int2* queues = reinterpret_cast<int2*>(smem_raw + ((2 * MIA_MAX_BREAKS * 8 + 2 * (MIA_MAX_BREAKS + 1) * 4 + 15) & ~15));
+  int2* queue = queues + warp * kQueue;
+  double* hist_base = reinterpret_cast<double*>(queues + n_warps * kQueue);
   double* h = hist_base + (size_t)warp * ((size_t)Q * nb + (nb + 1) / 2);
   unsigned* hc = reinterpret_cast<unsigned*>(h + (size_t)Q * nb);
   for (int i = threadIdx.x; i < MIA_MAX_BREAKS; i += blockDim.x) {
@@ -146,7 +179,9 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
   __syncthreads();
 
   int cur = -1;  // patch whose sums the warp's histogram holds
-  auto flush = [&](int p) {
+  int cnt = 0;   // entries in the warp's queue
+
+  auto flush_hist = [&](int p) {
     __syncwarp();
     if (p >= 0) {
       double* dst = acc.A + (size_t)p * Q * nb;
@@ -165,6 +200,122 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     __syncwarp();
   };
 
+  // One prefilter survivor per lane (valid lanes only): decide its bins with
+  // the division-free FP64 form, re-run the reference's exact sequence when a
+  // decision lies within the guard band, and accumulate.
+  auto process = [&](bool valid, int2 e) {
+    if (!valid) return;
+    const int j = e.x, ip = e.y;
+    const double ra_n = pos.ra[ip], dec_n = pos.dec[ip], chi_n = pos.chi[ip];
+    const double ra_s = shp.ra[j], dec_s = shp.dec[j], chi_s = shp.chi[j];
+    const double los = __dsub_rn(chi_s, chi_n);
+    const double dra = __dsub_rn(ra_s, ra_n), ddec = __dsub_rn(dec_s, dec_n);
+    const double dx = dra * pos.aux1[ip], dy = ddec * pos.aux2[ip];
+    const double qn = dx * dx + dy * dy;        // unscaled projected separation^2
+    bool near = false;
+    int ib = -1, jb = -1;
+    double ux = dx, uy = dy, qd = qn;           // the direction for e+ / ex (scale free)
+    if (KIND == MIA_KIND_W) {
+      jb = lookup(s_pbr, s_pbn, P.n_pbreak, los);
+      if (jb == -1) return;
+      const double qp = qn * P.h2;
+      ib = lookup_guarded(s_qbr, s_qbn, P.n_qbreak, qp, kGuard * qp, near);
+      if (!near && ib == -1) return;
+    } else {
+      const double qp = qn * P.h2;
+      bool cut_ok;
+      if (P.rp_cut < 0.0) {
+        cut_ok = true;
+      } else if (P.rp_cut == 0.0) {
+        if (qn < 1e-200) near = true;           // r_p > 0: decided exactly below underflow scales
+        cut_ok = qn > 0.0;
+      } else {
+        const double rc2 = P.rp_cut * P.rp_cut;
+        if (fabs(qp - rc2) <= kGuard * rc2) near = true;
+        cut_ok = qp > rc2;
+      }
+      if (!near && !cut_ok) return;
+      const double q = qn + los * los;
+      ib = lookup_guarded(s_qbr, s_qbn, P.n_qbreak, q, kGuard * q, near);
+      if (!near && ib == -1) return;
+      if (!near) {
+        const double mu = los * rsqrt(q);
+        jb = lookup_guarded(s_pbr, s_pbn, P.n_pbreak, mu, kGuard, near);
+      }
+    }
+    if (near) {
+      // the reference's sequence (measure_w_lightcone.py:137-172, measure_m_lightcone.py:140-176)
+      const double dra_e = __dmul_rn(__ddiv_rn(dra, 180.0), 3.141592653589793);
+      const double ddec_e = __dmul_rn(__ddiv_rn(ddec, 180.0), 3.141592653589793);
+      const double dx_e = __dmul_rn(__dmul_rn(dra_e, chi_n), pos.aux0[ip]);
+      const double dy_e = __dmul_rn(ddec_e, chi_n);
+      const double dxh = P.h_extra != 1.0 ? __dmul_rn(dx_e, P.h_extra) : dx_e;
+      const double dyh = P.h_extra != 1.0 ? __dmul_rn(dy_e, P.h_extra) : dy_e;
+      const double qp = __dadd_rn(__dmul_rn(dxh, dxh), __dmul_rn(dyh, dyh));
+      ux = dxh;
+      uy = dyh;
+      qd = qp;
+      if (KIND == MIA_KIND_W) {
+        ib = lookup(s_qbr, s_qbn, P.n_qbreak, qp);
+        if (ib == -1) return;
+      } else {
+        if (!(__dsqrt_rn(qp) > P.rp_cut)) return;
+        const double q = __dadd_rn(__dadd_rn(__dmul_rn(dx_e, dx_e), __dmul_rn(dy_e, dy_e)), __dmul_rn(los, los));
+        ib = lookup(s_qbr, s_qbn, P.n_qbreak, q);
+        if (ib == -1) return;
+        jb = lookup(s_pbr, s_pbn, P.n_pbreak, __ddiv_rn(los, __dsqrt_rn(q)));
+        if (jb == -1) return;
+      }
+    }
+    if (ib < 0 || jb < 0) {   // np.add.at would raise IndexError here
+      atomicOr(acc.status, MIA_LC_INDEX_ERROR);
+      return;
+    }
+    const int bin = ib * P.n_p + jb;
+    const double ww = __dmul_rn(pos.w[ip], shp.w[j]);
+    double ep = 0.0, ex = 0.0;
+    if (SHAPES && qd > 0.0) {
+      double r;
+      if (qd > 1e-30 && qd < 1e30) {          // reciprocal: FP32 seed, two Newton steps
+        r = (double)__frcp_rn((float)qd);
+        r = r * (2.0 - qd * r);
+        r = r * (2.0 - qd * r);
+      } else {
+        r = 1.0 / qd;
+      }
+      const double c2s = (ux * ux - uy * uy) * r, s2s = 2.0 * ux * uy * r;
+      const double ee = shp.aux0[j], c2a = shp.aux1[j], s2a = shp.aux2[j];
+      ep = -ee * (c2a * c2s + s2a * s2s);
+      ex = -ee * (s2a * c2s - c2a * s2s);
+    }
+    atomicAdd(&h[bin], ww);
+    if (SHAPES) {
+      atomicAdd(&h[nb + bin], ww * ep);
+      atomicAdd(&h[2 * nb + bin], ww * ex);
+    }
+    atomicAdd(&hc[bin], 1u);
+    if (JK) {
+      const int p_s = shp.patch[j];
+      if (p_s >= P.n_patch) atomicOr(acc.status, MIA_LC_BAD_PATCH);
+      if (p_s >= 0 && p_s < P.n_patch && p_s != cur) {
+        double* dst = acc.B + (size_t)p_s * Q * nb;
+        atomicAdd(&dst[bin], ww);
+        if (SHAPES) {
+          atomicAdd(&dst[nb + bin], ww * ep);
+          atomicAdd(&dst[2 * nb + bin], ww * ex);
+        }
+        atomicAdd(&acc.cB[(size_t)p_s * nb + bin], 1ull);
+      }
+    }
+  };
+
+  auto drain = [&]() {   // process what is queued (fewer than 32 entries)
+    __syncwarp();
+    process(lane < cnt, queue[lane]);
+    cnt = 0;
+    __syncwarp();
+  };
+
   const LcGrid& g = P.g;
   const double hx = KIND == MIA_KIND_W ? P.h_extra : 1.0;
   for (;;) {
@@ -174,7 +325,7 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     if ((long long)base >= P.n_pos) break;
     const long long stop = min((long long)base + kLcChunk, P.n_pos);
     for (long long ip = base; ip < stop; ++ip) {
-      const double ra_n = pos.ra[ip], dec_n = pos.dec[ip], chi_n = pos.chi[ip], w_n = pos.w[ip];
+      const double ra_n = pos.ra[ip], dec_n = pos.dec[ip], chi_n = pos.chi[ip];
       const double cos_n = pos.aux0[ip];
       const int p_n = JK ? pos.patch[ip] : 0;
       if (JK && (p_n < 0 || p_n >= P.n_patch)) {   // a position must belong to a patch
@@ -182,10 +333,11 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
         continue;
       }
       if (p_n != cur) {
-        flush(cur);
+        drain();
+        flush_hist(cur);
         cur = p_n;
       }
-      // separation window (a superset; the pair tests below decide)
+      // separation window (a superset; the pair tests decide)
       const double den = fabs(hx * chi_n);
       const double span_dec = den > 1e-300 ? P.r_lim / den / kDegToRad * (1.0 + 1e-6) + 1e-9 : 1e300;
       const double den_ra = den * fabs(cos_n);
@@ -205,76 +357,43 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
       const int a1 = cell_1d(ra_n + span_ra, g.ra0, g.inv_ra, g.n_ra);
       const int c0 = cell_1d(chi_lo, g.chi0, g.inv_chi, g.n_chi);
       const int c1 = cell_1d(chi_hi, g.chi0, g.inv_chi, g.n_chi);
-      const double kx = kDegToRad * chi_n * cos_n * hx, ky = kDegToRad * chi_n * hx;
+      // FP32 prefilter: relative error of the separation terms below 1e-6,
+      // so the 1e-4 margins only ever let extra pairs through
+      const float4 nhl = pos.hl[ip];
+      const float2 nch = pos.chl[ip];
+      const float kx = (float)(kDegToRad * chi_n * cos_n * hx), ky = (float)(kDegToRad * chi_n * hx);
       for (int d = d0; d <= d1; ++d) {
         for (int c = c0; c <= c1; ++c) {
           const int row = (d * g.n_chi + c) * g.n_ra;
           const int j0 = start[row + a0], j1 = start[row + a1 + 1];
-          for (int j = j0 + lane; j < j1; j += 32) {
-            const double ra_s = shp.ra[j], dec_s = shp.dec[j], chi_s = shp.chi[j];
-            const double los = __dsub_rn(chi_s, chi_n);
-            // division-free bound (relative error ~1e-15, margin 1e-9 in q_hi)
-            const double ax = (ra_s - ra_n) * kx, ay = (dec_s - dec_n) * ky;
-            double qa = ax * ax + ay * ay;
-            if (KIND == MIA_KIND_MULTIPOLES) qa = qa / (hx * hx) + los * los;
-            if (qa > P.q_hi) continue;
-            // the reference's arithmetic
-            const double dra = __dmul_rn(__ddiv_rn(__dsub_rn(ra_s, ra_n), 180.0), 3.141592653589793);
-            const double ddec = __dmul_rn(__ddiv_rn(__dsub_rn(dec_s, dec_n), 180.0), 3.141592653589793);
-            const double dx = __dmul_rn(__dmul_rn(dra, chi_n), cos_n);
-            const double dy = __dmul_rn(ddec, chi_n);
-            const double dxh = P.h_extra != 1.0 ? __dmul_rn(dx, P.h_extra) : dx;
-            const double dyh = P.h_extra != 1.0 ? __dmul_rn(dy, P.h_extra) : dy;
-            const double qp = __dadd_rn(__dmul_rn(dxh, dxh), __dmul_rn(dyh, dyh));
-            int ib, jb;
-            if (KIND == MIA_KIND_W) {
-              ib = lookup(s_qbr, s_qbn, P.n_qbreak, qp);
-              if (ib == -1) continue;
-              jb = lookup(s_pbr, s_pbn, P.n_pbreak, los);
-              if (jb == -1) continue;
-            } else {
-              if (!(__dsqrt_rn(qp) > P.rp_cut)) continue;
-              const double q = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(los, los));
-              ib = lookup(s_qbr, s_qbn, P.n_qbreak, q);
-              if (ib == -1) continue;
-              const double mu = __ddiv_rn(los, __dsqrt_rn(q));
-              jb = lookup(s_pbr, s_pbn, P.n_pbreak, mu);
-              if (jb == -1) continue;
-            }
-            if (ib < 0 || jb < 0) {   // np.add.at would raise IndexError here
-              atomicOr(acc.status, MIA_LC_INDEX_ERROR);
-              continue;
-            }
-            const int bin = ib * P.n_p + jb;
-            const double ww = __dmul_rn(w_n, shp.w[j]);
-            double ep = 0.0, ex = 0.0;
-            if (SHAPES) {
-              const double rp = __dsqrt_rn(qp);
-              if (rp > 0.0) {
-                const double ux = dxh / rp, uy = dyh / rp;
-                const double c2s = ux * ux - uy * uy, s2s = 2.0 * ux * uy;
-                const double e = shp.aux0[j], c2a = shp.aux1[j], s2a = shp.aux2[j];
-                ep = -e * (c2a * c2s + s2a * s2s);
-                ex = -e * (s2a * c2s - c2a * s2s);
+          for (int jj = j0; jj < j1; jj += 32) {
+            const int j = jj + lane;
+            bool pass = false;
+            if (j < j1) {
+              const float4 s4 = shp.hl[j];
+              const float2 sc = shp.chl[j];
+              const float ax = ((s4.x - nhl.x) + (s4.y - nhl.y)) * kx;
+              const float ay = ((s4.z - nhl.z) + (s4.w - nhl.w)) * ky;
+              const float lf = (sc.x - nch.x) + (sc.y - nch.y);
+              if (KIND == MIA_KIND_W) {
+                pass = ax * ax + ay * ay <= P.qf_hi && lf >= P.los_lo && lf <= P.los_hi;
+              } else {
+                pass = ax * ax + ay * ay + lf * lf <= P.qf_hi;
               }
             }
-            atomicAdd(&h[bin], ww);
-            if (SHAPES) {
-              atomicAdd(&h[nb + bin], ww * ep);
-              atomicAdd(&h[2 * nb + bin], ww * ex);
-            }
-            atomicAdd(&hc[bin], 1u);
-            if (JK) {
-              const int p_s = shp.patch[j];
-              if (p_s >= P.n_patch) atomicOr(acc.status, MIA_LC_BAD_PATCH);
-              if (p_s >= 0 && p_s < P.n_patch && p_s != p_n) {
-                double* dst = acc.B + (size_t)p_s * Q * nb;
-                atomicAdd(&dst[bin], ww);
-                if (SHAPES) {
-                  atomicAdd(&dst[nb + bin], ww * ep);
-                  atomicAdd(&dst[2 * nb + bin], ww * ex);
-                }
-                atomicAdd(&acc.cB[(size_t)p_s * nb + bin], 1ull);
+            const unsigned bal = __ballot_sync(0xffffffffu, pass);
+            if (bal) {
+              if (pass) queue[cnt + __popc(bal & ((1u << lane) - 1u))] = make_int2(j, (int)ip);
+              cnt += __popc(bal);
+              if (cnt >= 32) {
+                __syncwarp();
+                const int2 mine = queue[lane];
+                __syncwarp();
+                const int rest = cnt - 32;
+                if (lane < rest) queue[lane] = queue[32 + lane];
+                cnt = rest;
+                __syncwarp();
+                process(true, mine);
               }
             }
           }
@@ -282,7 +401,8 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
       }
     }
   }
-  flush(cur);
+  drain();
+  flush_hist(cur);
 }
 
 // totals and realisations: out[q][0][b] = sum_i A[i][q][b]; out[q][1+i][b] =
@@ -313,7 +433,11 @@ __global__ void k_lc_finish(const double* __restrict__ A, const double* __restri
 
 size_t al(size_t x) { return (x + 255) & ~size_t(255); }
 
-LcSorted carve(unsigned char* base, long long n, bool is_pos) {
+// a sample in cell order: 7 double arrays, the patch labels, the FP32 hi/lo
+// copies; 11 (n + 8) doubles in all, every array 16-byte aligned
+constexpr size_t kSortedDoubles = 11;
+
+LcSorted carve(unsigned char* base, long long n) {
   LcSorted s;
   const size_t nn = (size_t)n + 8;
   double* d = reinterpret_cast<double*>(base);
@@ -322,18 +446,15 @@ LcSorted carve(unsigned char* base, long long n, bool is_pos) {
   s.chi = d + 2 * nn;
   s.w = d + 3 * nn;
   s.aux0 = d + 4 * nn;
-  if (is_pos) {
-    s.aux1 = s.aux2 = nullptr;
-    s.patch = reinterpret_cast<int*>(d + 5 * nn);
-  } else {
-    s.aux1 = d + 5 * nn;
-    s.aux2 = d + 6 * nn;
-    s.patch = reinterpret_cast<int*>(d + 7 * nn);
-  }
+  s.aux1 = d + 5 * nn;
+  s.aux2 = d + 6 * nn;
+  s.patch = reinterpret_cast<int*>(d + 7 * nn);
+  s.hl = reinterpret_cast<float4*>(d + 8 * nn);
+  s.chl = reinterpret_cast<float2*>(d + 10 * nn);
   return s;
 }
 
-size_t lc_per_warp(int Q, int nb) { return (size_t)Q * nb * 8 + (size_t)(nb + 1) / 2 * 8; }
+size_t lc_per_warp(int Q, int nb) { return (size_t)kQueue * 8 + (size_t)Q * nb * 8 + (size_t)(nb + 1) / 2 * 8; }
 constexpr size_t kLcFixedSmem = 2 * MIA_MAX_BREAKS * 8 + 2 * (MIA_MAX_BREAKS + 1) * 4 + 32;
 constexpr size_t kLcSmemBudget = 200 * 1024;
 
@@ -393,8 +514,8 @@ bool lc_plan(const mia_lc_config* c, long long n_pos, long long n_shape, LcPlan*
   p->off_tiles = take((size_t)p->n_tiles * 4);
   p->off_scell = take((size_t)n_shape * 4 + 4);
   p->off_pcell = take((size_t)n_pos * 4 + 4);
-  p->off_shp = take(((size_t)n_shape + 8) * 8 * 8);
-  p->off_pos = take(((size_t)n_pos + 8) * 6 * 8);
+  p->off_shp = take(((size_t)n_shape + 8) * kSortedDoubles * 8);
+  p->off_pos = take(((size_t)n_pos + 8) * kSortedDoubles * 8);
   p->off_A = take((size_t)p->P * p->Q * p->nb * 8);
   p->off_B = take((size_t)c->n_patch * p->Q * p->nb * 8 + 8);
   p->off_cA = take((size_t)p->P * p->nb * 8);
@@ -417,8 +538,8 @@ cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sa
   int* tiles = reinterpret_cast<int*>(ws + p.off_tiles);
   int* scell = reinterpret_cast<int*>(ws + p.off_scell);
   int* pcell = reinterpret_cast<int*>(ws + p.off_pcell);
-  const LcSorted S = carve(ws + p.off_shp, shp.n, false);
-  const LcSorted Ps = carve(ws + p.off_pos, pos.n, true);
+  const LcSorted S = carve(ws + p.off_shp, shp.n);
+  const LcSorted Ps = carve(ws + p.off_pos, pos.n);
   LcAcc acc;
   acc.A = reinterpret_cast<double*>(ws + p.off_A);
   acc.B = reinterpret_cast<double*>(ws + p.off_B);
@@ -456,9 +577,14 @@ cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sa
   LcParams P;
   P.n_r = cfg->n_r; P.n_p = cfg->n_p; P.nb = p.nb; P.n_patch = cfg->n_patch; P.Q = p.Q;
   P.n_qbreak = cfg->n_qbreak; P.n_pbreak = cfg->n_pbreak;
-  P.h_extra = cfg->h_extra; P.rp_cut = cfg->rp_cut; P.r_lim = cfg->r_lim;
+  P.h_extra = cfg->h_extra; P.h2 = cfg->h_extra * cfg->h_extra; P.rp_cut = cfg->rp_cut; P.r_lim = cfg->r_lim;
   P.pi_lo = cfg->pi_lo; P.pi_hi = cfg->pi_hi;
-  P.q_hi = cfg->r_lim * cfg->r_lim * (1.0 + 1e-9);
+  P.qf_hi = (float)(cfg->r_lim * cfg->r_lim * (1.0 + 1e-4));
+  {
+    const double mpi = 1e-4 * (fabs(cfg->pi_lo) + fabs(cfg->pi_hi)) + 1e-6;
+    P.los_lo = (float)(cfg->pi_lo - mpi);
+    P.los_hi = (float)(cfg->pi_hi + mpi);
+  }
   P.g = g;
   P.n_pos = pos.n;
   LcTables T;
