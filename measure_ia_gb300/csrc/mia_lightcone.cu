@@ -116,6 +116,9 @@ struct LcAcc {
   unsigned* status;
 };
 
+// shared-memory bytes of the tables: double and FP32 breaks, bins; 16-byte rounded
+constexpr size_t kLcTableBytes = (2 * MIA_MAX_BREAKS * 8 + 2 * MIA_MAX_BREAKS * 4 + 2 * (MIA_MAX_BREAKS + 1) * 4 + 15) & ~size_t(15);
+
 struct LcTables {              // bin tables, passed by value (2.3 KB of launch parameters)
   double qbr[MIA_MAX_BREAKS], pbr[MIA_MAX_BREAKS];
   int qbn[MIA_MAX_BREAKS + 1], pbn[MIA_MAX_BREAKS + 1];
@@ -131,10 +134,9 @@ __device__ __forceinline__ int lookup(const double* br, const int* bins, int n, 
   return bins[lo];
 }
 
-// lookup of an approximate x: `near` is set when a breakpoint lies within tol
-// of x, where the approximation could fall in the wrong interval
-__device__ __forceinline__ int lookup_guarded(const double* br, const int* bins, int n, double x, double tol,
-                                              bool& near) {
+// lookup of an approximate x in FP32: `near` is set when a breakpoint
+// (rounded to FP32) lies within tol of x, where x could be on the wrong side
+__device__ __forceinline__ int lookup_f(const float* br, const int* bins, int n, float x, float tol, bool& near) {
   int lo = 0, hi = n;
   while (lo < hi) {
     const int mid = (lo + hi) >> 1;
@@ -145,8 +147,12 @@ __device__ __forceinline__ int lookup_guarded(const double* br, const int* bins,
   return bins[lo];
 }
 
-constexpr double kGuard = 1e-12;   // relative; the approximate q, mu are within ~1e-15 of the reference's
-constexpr int kQueue = 64;         // per-warp queue of prefilter survivors
+// FP32 decisions: the separation terms from the hi/lo coordinates are within
+// ~1e-6 relative of the reference's (plus an absolute term from the 2^-48
+// hi/lo representation, bounded per position); pairs within kRelGuard of a
+// breakpoint (or of the r_p cut) take the reference's exact FP64 sequence.
+constexpr float kRelGuard = 4e-6f;
+constexpr int kQueue = 64;         // per-warp queue of survivors (int4 entries)
 
 template <int KIND, int SHAPES, int JK>
 __global__ void __launch_bounds__(kLcMaxWarps * 32)
@@ -156,19 +162,23 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
   const int nb = P.nb;
   constexpr int Q = SHAPES ? 3 : 1;
-  // tables, per-warp queues, then per-warp histograms (Q doubles and one count per bin)
+  // tables (double and FP32 breaks), per-warp queues, then per-warp histograms
   double* s_qbr = reinterpret_cast<double*>(smem_raw);
   double* s_pbr = s_qbr + MIA_MAX_BREAKS;
-  int* s_qbn = reinterpret_cast<int*>(s_pbr + MIA_MAX_BREAKS);
+  float* s_qbf = reinterpret_cast<float*>(s_pbr + MIA_MAX_BREAKS);
+  float* s_pbf = s_qbf + MIA_MAX_BREAKS;
+  int* s_qbn = reinterpret_cast<int*>(s_pbf + MIA_MAX_BREAKS);
   int* s_pbn = s_qbn + (MIA_MAX_BREAKS + 1);
-  int2* queues = reinterpret_cast<int2*>(smem_raw + ((2 * MIA_MAX_BREAKS * 8 + 2 * (MIA_MAX_BREAKS + 1) * 4 + 15) & ~15));
-  int2* queue = queues + warp * kQueue;
+  int4* queues = reinterpret_cast<int4*>(smem_raw + kLcTableBytes);
+  int4* queue = queues + warp * kQueue;
   double* hist_base = reinterpret_cast<double*>(queues + n_warps * kQueue);
   double* h = hist_base + (size_t)warp * ((size_t)Q * nb + (nb + 1) / 2);
   unsigned* hc = reinterpret_cast<unsigned*>(h + (size_t)Q * nb);
   for (int i = threadIdx.x; i < MIA_MAX_BREAKS; i += blockDim.x) {
     s_qbr[i] = T.qbr[i];
     s_pbr[i] = T.pbr[i];
+    s_qbf[i] = __double2float_rn(T.qbr[i]);
+    s_pbf[i] = __double2float_rn(T.pbr[i]);
   }
   for (int i = threadIdx.x; i <= MIA_MAX_BREAKS; i += blockDim.x) {
     s_qbn[i] = T.qbn[i];
@@ -200,94 +210,7 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     __syncwarp();
   };
 
-  // One prefilter survivor per lane (valid lanes only): decide its bins with
-  // the division-free FP64 form, re-run the reference's exact sequence when a
-  // decision lies within the guard band, and accumulate.
-  auto process = [&](bool valid, int2 e) {
-    if (!valid) return;
-    const int j = e.x, ip = e.y;
-    const double ra_n = pos.ra[ip], dec_n = pos.dec[ip], chi_n = pos.chi[ip];
-    const double ra_s = shp.ra[j], dec_s = shp.dec[j], chi_s = shp.chi[j];
-    const double los = __dsub_rn(chi_s, chi_n);
-    const double dra = __dsub_rn(ra_s, ra_n), ddec = __dsub_rn(dec_s, dec_n);
-    const double dx = dra * pos.aux1[ip], dy = ddec * pos.aux2[ip];
-    const double qn = dx * dx + dy * dy;        // unscaled projected separation^2
-    bool near = false;
-    int ib = -1, jb = -1;
-    double ux = dx, uy = dy, qd = qn;           // the direction for e+ / ex (scale free)
-    if (KIND == MIA_KIND_W) {
-      jb = lookup(s_pbr, s_pbn, P.n_pbreak, los);
-      if (jb == -1) return;
-      const double qp = qn * P.h2;
-      ib = lookup_guarded(s_qbr, s_qbn, P.n_qbreak, qp, kGuard * qp, near);
-      if (!near && ib == -1) return;
-    } else {
-      const double qp = qn * P.h2;
-      bool cut_ok;
-      if (P.rp_cut < 0.0) {
-        cut_ok = true;
-      } else if (P.rp_cut == 0.0) {
-        if (qn < 1e-200) near = true;           // r_p > 0: decided exactly below underflow scales
-        cut_ok = qn > 0.0;
-      } else {
-        const double rc2 = P.rp_cut * P.rp_cut;
-        if (fabs(qp - rc2) <= kGuard * rc2) near = true;
-        cut_ok = qp > rc2;
-      }
-      if (!near && !cut_ok) return;
-      const double q = qn + los * los;
-      ib = lookup_guarded(s_qbr, s_qbn, P.n_qbreak, q, kGuard * q, near);
-      if (!near && ib == -1) return;
-      if (!near) {
-        const double mu = los * rsqrt(q);
-        jb = lookup_guarded(s_pbr, s_pbn, P.n_pbreak, mu, kGuard, near);
-      }
-    }
-    if (near) {
-      // the reference's sequence (measure_w_lightcone.py:137-172, measure_m_lightcone.py:140-176)
-      const double dra_e = __dmul_rn(__ddiv_rn(dra, 180.0), 3.141592653589793);
-      const double ddec_e = __dmul_rn(__ddiv_rn(ddec, 180.0), 3.141592653589793);
-      const double dx_e = __dmul_rn(__dmul_rn(dra_e, chi_n), pos.aux0[ip]);
-      const double dy_e = __dmul_rn(ddec_e, chi_n);
-      const double dxh = P.h_extra != 1.0 ? __dmul_rn(dx_e, P.h_extra) : dx_e;
-      const double dyh = P.h_extra != 1.0 ? __dmul_rn(dy_e, P.h_extra) : dy_e;
-      const double qp = __dadd_rn(__dmul_rn(dxh, dxh), __dmul_rn(dyh, dyh));
-      ux = dxh;
-      uy = dyh;
-      qd = qp;
-      if (KIND == MIA_KIND_W) {
-        ib = lookup(s_qbr, s_qbn, P.n_qbreak, qp);
-        if (ib == -1) return;
-      } else {
-        if (!(__dsqrt_rn(qp) > P.rp_cut)) return;
-        const double q = __dadd_rn(__dadd_rn(__dmul_rn(dx_e, dx_e), __dmul_rn(dy_e, dy_e)), __dmul_rn(los, los));
-        ib = lookup(s_qbr, s_qbn, P.n_qbreak, q);
-        if (ib == -1) return;
-        jb = lookup(s_pbr, s_pbn, P.n_pbreak, __ddiv_rn(los, __dsqrt_rn(q)));
-        if (jb == -1) return;
-      }
-    }
-    if (ib < 0 || jb < 0) {   // np.add.at would raise IndexError here
-      atomicOr(acc.status, MIA_LC_INDEX_ERROR);
-      return;
-    }
-    const int bin = ib * P.n_p + jb;
-    const double ww = __dmul_rn(pos.w[ip], shp.w[j]);
-    double ep = 0.0, ex = 0.0;
-    if (SHAPES && qd > 0.0) {
-      double r;
-      if (qd > 1e-30 && qd < 1e30) {          // reciprocal: FP32 seed, two Newton steps
-        r = (double)__frcp_rn((float)qd);
-        r = r * (2.0 - qd * r);
-        r = r * (2.0 - qd * r);
-      } else {
-        r = 1.0 / qd;
-      }
-      const double c2s = (ux * ux - uy * uy) * r, s2s = 2.0 * ux * uy * r;
-      const double ee = shp.aux0[j], c2a = shp.aux1[j], s2a = shp.aux2[j];
-      ep = -ee * (c2a * c2s + s2a * s2s);
-      ex = -ee * (s2a * c2s - c2a * s2s);
-    }
+  auto accumulate = [&](int j, int bin, double ww, double ep, double ex) {
     atomicAdd(&h[bin], ww);
     if (SHAPES) {
       atomicAdd(&h[nb + bin], ww * ep);
@@ -309,6 +232,77 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     }
   };
 
+  // e+ / ex from a separation direction (ux, uy) with qd = ux^2 + uy^2
+  auto shape_terms = [&](int j, double ux, double uy, double qd, double& ep, double& ex) {
+    ep = ex = 0.0;
+    if (!(qd > 0.0)) return;                   // r_p = 0: the reference's NaN terms are set to 0
+    double r;
+    if (qd > 1e-30 && qd < 1e30) {             // reciprocal: FP32 seed, two Newton steps
+      r = (double)__frcp_rn((float)qd);
+      r = r * (2.0 - qd * r);
+      r = r * (2.0 - qd * r);
+    } else {
+      r = 1.0 / qd;
+    }
+    const double c2s = (ux * ux - uy * uy) * r, s2s = 2.0 * ux * uy * r;
+    const double ee = shp.aux0[j], c2a = shp.aux1[j], s2a = shp.aux2[j];
+    ep = -ee * (c2a * c2s + s2a * s2s);
+    ex = -ee * (s2a * c2s - c2a * s2s);
+  };
+
+  // One queued survivor per valid lane: e.z >= 0 is its bin (decided in
+  // FP32); e.z < 0 means a decision fell in the guard band: the reference's
+  // exact sequence decides (measure_w_lightcone.py:137-172,
+  // measure_m_lightcone.py:140-176).
+  auto process = [&](bool valid, int4 e) {
+    if (!valid) return;
+    const int j = e.x, ip = e.y;
+    const double ra_n = pos.ra[ip], dec_n = pos.dec[ip], chi_n = pos.chi[ip];
+    const double ra_s = shp.ra[j], dec_s = shp.dec[j], chi_s = shp.chi[j];
+    const double dra = __dsub_rn(ra_s, ra_n), ddec = __dsub_rn(dec_s, dec_n);
+    int bin = e.z;
+    double ux, uy, qd;
+    if (bin >= 0) {
+      ux = dra * pos.aux1[ip];
+      uy = ddec * pos.aux2[ip];
+      qd = ux * ux + uy * uy;
+    } else {
+      const double los = __dsub_rn(chi_s, chi_n);
+      const double dra_e = __dmul_rn(__ddiv_rn(dra, 180.0), 3.141592653589793);
+      const double ddec_e = __dmul_rn(__ddiv_rn(ddec, 180.0), 3.141592653589793);
+      const double dx_e = __dmul_rn(__dmul_rn(dra_e, chi_n), pos.aux0[ip]);
+      const double dy_e = __dmul_rn(ddec_e, chi_n);
+      const double dxh = P.h_extra != 1.0 ? __dmul_rn(dx_e, P.h_extra) : dx_e;
+      const double dyh = P.h_extra != 1.0 ? __dmul_rn(dy_e, P.h_extra) : dy_e;
+      const double qp = __dadd_rn(__dmul_rn(dxh, dxh), __dmul_rn(dyh, dyh));
+      ux = dxh;
+      uy = dyh;
+      qd = qp;
+      int ib, jb;
+      if (KIND == MIA_KIND_W) {
+        ib = lookup(s_qbr, s_qbn, P.n_qbreak, qp);
+        if (ib == -1) return;
+        jb = lookup(s_pbr, s_pbn, P.n_pbreak, los);
+        if (jb == -1) return;
+      } else {
+        if (!(__dsqrt_rn(qp) > P.rp_cut)) return;
+        const double q = __dadd_rn(__dadd_rn(__dmul_rn(dx_e, dx_e), __dmul_rn(dy_e, dy_e)), __dmul_rn(los, los));
+        ib = lookup(s_qbr, s_qbn, P.n_qbreak, q);
+        if (ib == -1) return;
+        jb = lookup(s_pbr, s_pbn, P.n_pbreak, __ddiv_rn(los, __dsqrt_rn(q)));
+        if (jb == -1) return;
+      }
+      if (ib < 0 || jb < 0) {   // np.add.at would raise IndexError here
+        atomicOr(acc.status, MIA_LC_INDEX_ERROR);
+        return;
+      }
+      bin = ib * P.n_p + jb;
+    }
+    double ep = 0.0, ex = 0.0;
+    if (SHAPES) shape_terms(j, ux, uy, qd, ep, ex);
+    accumulate(j, bin, __dmul_rn(pos.w[ip], shp.w[j]), ep, ex);
+  };
+
   auto drain = [&]() {   // process what is queued (fewer than 32 entries)
     __syncwarp();
     process(lane < cnt, queue[lane]);
@@ -318,6 +312,7 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
 
   const LcGrid& g = P.g;
   const double hx = KIND == MIA_KIND_W ? P.h_extra : 1.0;
+  const float h2f = (float)P.h2, rc2f = (float)(P.rp_cut * P.rp_cut);
   for (;;) {
     unsigned base = 0;
     if (lane == 0) base = atomicAdd(acc.next, (unsigned)kLcChunk);
@@ -337,6 +332,7 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
         flush_hist(cur);
         cur = p_n;
       }
+      const double w_n = pos.w[ip];
       // separation window (a superset; the pair tests decide)
       const double den = fabs(hx * chi_n);
       const double span_dec = den > 1e-300 ? P.r_lim / den / kDegToRad * (1.0 + 1e-6) + 1e-9 : 1e300;
@@ -357,37 +353,86 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
       const int a1 = cell_1d(ra_n + span_ra, g.ra0, g.inv_ra, g.n_ra);
       const int c0 = cell_1d(chi_lo, g.chi0, g.inv_chi, g.n_chi);
       const int c1 = cell_1d(chi_hi, g.chi0, g.inv_chi, g.n_chi);
-      // FP32 prefilter: relative error of the separation terms below 1e-6,
-      // so the 1e-4 margins only ever let extra pairs through
       const float4 nhl = pos.hl[ip];
       const float2 nch = pos.chl[ip];
-      const float kx = (float)(kDegToRad * chi_n * cos_n * hx), ky = (float)(kDegToRad * chi_n * hx);
+      const double kxd = kDegToRad * chi_n * cos_n * hx, kyd = kDegToRad * chi_n * hx;
+      const float kx = (float)kxd, ky = (float)kyd;
+      // Absolute errors from the hi/lo representation (each coordinate to
+      // 2^-48 of itself; a difference of two to 2^-47 of the larger, which the
+      // window bounds): ep on the projected terms ax, ay, gl on lf.  Relative
+      // errors of the FP32 arithmetic stay below 1.2e-6 of q (kRelGuard = 4e-6).
+      const double ep = 1.1 * 7.2e-15 * ((fabs(ra_n) + fmin(span_ra, 1e30)) * fabs(kxd) +
+                                         (fabs(dec_n) + fmin(span_dec, 1e30)) * fabs(kyd));
+      const double gld = 1.1 * 7.2e-15 * (2.0 * fabs(chi_n) + P.r_lim + fabs(P.pi_lo) + fabs(P.pi_hi));
+      const float gl = (float)gld;
+      // on q (w: r_p^2; multipoles: r^2, which adds the lf term) with sqrt(q) <= 1.0001 r_lim
+      const float gq = (float)(2.1 * P.r_lim * (ep + (KIND == MIA_KIND_W ? 0.0 : gld)) + ep * ep + gld * gld);
+      const float gqp = (float)(P.h2 * (2.1 * P.r_lim * ep + ep * ep));   // on r_p^2 (multipoles' cut)
+      const float gmu = (float)(2.0 * (gld + ep));                          // times 1/r, on mu
       for (int d = d0; d <= d1; ++d) {
         for (int c = c0; c <= c1; ++c) {
           const int row = (d * g.n_chi + c) * g.n_ra;
           const int j0 = start[row + a0], j1 = start[row + a1 + 1];
           for (int jj = j0; jj < j1; jj += 32) {
             const int j = jj + lane;
-            bool pass = false;
+            bool take = false;   // binned (bin decided) or in the guard band
+            bool near = false;
+            int bin = -1;
             if (j < j1) {
               const float4 s4 = shp.hl[j];
               const float2 sc = shp.chl[j];
               const float ax = ((s4.x - nhl.x) + (s4.y - nhl.y)) * kx;
               const float ay = ((s4.z - nhl.z) + (s4.w - nhl.w)) * ky;
               const float lf = (sc.x - nch.x) + (sc.y - nch.y);
+              const float qn = ax * ax + ay * ay;
+              int ib = -1, jb = -1;
               if (KIND == MIA_KIND_W) {
-                pass = ax * ax + ay * ay <= P.qf_hi && lf >= P.los_lo && lf <= P.los_hi;
+                if (qn <= P.qf_hi && lf >= P.los_lo && lf <= P.los_hi) {
+                  jb = lookup_f(s_pbf, s_pbn, P.n_pbreak, lf, kRelGuard * fabsf(lf) + gl, near);
+                  if (near || jb != -1) {
+                    ib = lookup_f(s_qbf, s_qbn, P.n_qbreak, qn, kRelGuard * qn + gq, near);
+                    take = near || ib != -1;
+                  }
+                }
               } else {
-                pass = ax * ax + ay * ay + lf * lf <= P.qf_hi;
+                const float q = qn + lf * lf;
+                if (q <= P.qf_hi) {
+                  bool cut_ok = true;
+                  if (P.rp_cut >= 0.0) {
+                    const float qp = qn * h2f;
+                    if (fabsf(qp - rc2f) <= kRelGuard * fmaxf(qp, rc2f) + gqp) near = true;
+                    cut_ok = qp > rc2f;
+                  }
+                  if (near || cut_ok) {
+                    ib = lookup_f(s_qbf, s_qbn, P.n_qbreak, q, kRelGuard * q + gq, near);
+                    if (near || ib != -1) {
+                      const float rq = rsqrtf(q);
+                      jb = lookup_f(s_pbf, s_pbn, P.n_pbreak, lf * rq, kRelGuard + gmu * rq, near);
+                      take = true;
+                    }
+                  }
+                }
+              }
+              if (take && !near) {
+                if (ib < 0 || jb < 0) {   // np.add.at would raise IndexError here
+                  atomicOr(acc.status, MIA_LC_INDEX_ERROR);
+                  take = false;
+                } else {
+                  bin = ib * P.n_p + jb;
+                }
+              }
+              if (!SHAPES && take && !near) {   // counts only: w_p w_s is all there is to add
+                accumulate(j, bin, __dmul_rn(w_n, shp.w[j]), 0.0, 0.0);
+                take = false;
               }
             }
-            const unsigned bal = __ballot_sync(0xffffffffu, pass);
+            const unsigned bal = __ballot_sync(0xffffffffu, take);
             if (bal) {
-              if (pass) queue[cnt + __popc(bal & ((1u << lane) - 1u))] = make_int2(j, (int)ip);
+              if (take) queue[cnt + __popc(bal & ((1u << lane) - 1u))] = make_int4(j, (int)ip, near ? -1 : bin, 0);
               cnt += __popc(bal);
               if (cnt >= 32) {
                 __syncwarp();
-                const int2 mine = queue[lane];
+                const int4 mine = queue[lane];
                 __syncwarp();
                 const int rest = cnt - 32;
                 if (lane < rest) queue[lane] = queue[32 + lane];
@@ -454,8 +499,8 @@ LcSorted carve(unsigned char* base, long long n) {
   return s;
 }
 
-size_t lc_per_warp(int Q, int nb) { return (size_t)kQueue * 8 + (size_t)Q * nb * 8 + (size_t)(nb + 1) / 2 * 8; }
-constexpr size_t kLcFixedSmem = 2 * MIA_MAX_BREAKS * 8 + 2 * (MIA_MAX_BREAKS + 1) * 4 + 32;
+size_t lc_per_warp(int Q, int nb) { return (size_t)kQueue * 16 + (size_t)Q * nb * 8 + (size_t)(nb + 1) / 2 * 8; }
+constexpr size_t kLcFixedSmem = kLcTableBytes + 16;
 constexpr size_t kLcSmemBudget = 200 * 1024;
 
 template <int KIND, int SHAPES, int JK>
