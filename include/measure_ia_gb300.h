@@ -291,6 +291,8 @@ typedef struct {
   /* cell grid over the shapes (host-chosen; objects outside go to the edge cells) */
   double ra0, ra_cell, dec0, dec_cell, chi0, chi_cell;
   int n_ra, n_dec, n_chi;
+  int unit_weights;         /* 1: every weight of both samples is exactly 1.0, so DD is the
+                               pair count (the reference's sum of ones) and is not summed */
 } mia_lc_config;
 
 typedef struct {            /* device arrays of n entries */

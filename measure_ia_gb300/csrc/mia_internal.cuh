@@ -365,7 +365,7 @@ struct LcPlan {
   int n_tiles, Q, nb, P, warps;
   size_t smem;
   size_t off_scount, off_sstart, off_sfill, off_pcount, off_pstart, off_pfill, off_tiles, off_scell, off_pcell;
-  size_t off_shp, off_pos, off_A, off_B, off_cA, off_cB, off_next, total;
+  size_t off_shp, off_pos, off_A, off_B, off_cA, off_cB, off_win, off_next, total;
 };
 bool lc_plan(const mia_lc_config* cfg, long long n_pos, long long n_shape, LcPlan* plan, const char** why);
 cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& plan, const mia_lc_sample& pos,

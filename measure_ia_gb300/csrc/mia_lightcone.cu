@@ -103,9 +103,68 @@ struct LcParams {
   double h_extra, h2, rp_cut, r_lim, pi_lo, pi_hi;
   float qf_hi;                 // FP32 prefilter bound on q (r_lim^2 (1 + 1e-4))
   float los_lo, los_hi;        // w: FP32 prefilter bounds on Pi
+  float qa, qb, pa, pb;        // first guesses of the table interval: log2(q) * qa + qb, x * pa + pb
+  int unit;                    // unit weights: DD is the pair count, not summed
   LcGrid g;
   long long n_pos;
 };
+
+// Per-position window and FP32 constants, computed once per position
+// (k_lc_windows) instead of once per warp in the pair kernel.
+struct LcWin {
+  int d0, d1, a0, a1, c0, c1;
+  float kx, ky;                // Mpc per degree of RA / DEC difference (times h_extra for w)
+  float gq, gqp, gmu, gl;      // absolute error bounds (see k_lc_windows)
+};
+
+// Per sorted position: the cell ranges its separation window reaches (a
+// superset; the pair tests decide) and the FP32 constants of the prefilter.
+// Error bounds: each hi/lo coordinate is within 2^-48 of itself, so a
+// difference of two is within 2^-47 of the larger, which the window bounds;
+// ep bounds that error on the projected terms ax, ay (Mpc), gl on the
+// line-of-sight difference lf.  The FP32 arithmetic itself stays within
+// 1.2e-6 relative of q (the guard, kRelGuard, is 4e-6).
+template <int KIND>
+__global__ void k_lc_windows(const LcParams P, const LcSorted pos, LcWin* __restrict__ win) {
+  const LcGrid& g = P.g;
+  const double hx = KIND == MIA_KIND_W ? P.h_extra : 1.0;
+  for (long long ip = blockIdx.x * (long long)blockDim.x + threadIdx.x; ip < P.n_pos;
+       ip += (long long)gridDim.x * blockDim.x) {
+    const double ra_n = pos.ra[ip], dec_n = pos.dec[ip], chi_n = pos.chi[ip], cos_n = pos.aux0[ip];
+    const double den = fabs(hx * chi_n);
+    const double span_dec = den > 1e-300 ? P.r_lim / den / kDegToRad * (1.0 + 1e-6) + 1e-9 : 1e300;
+    const double den_ra = den * fabs(cos_n);
+    const double span_ra = den_ra > 1e-300 ? P.r_lim / den_ra / kDegToRad * (1.0 + 1e-6) + 1e-9 : 1e300;
+    const double m = 1e-9 * (fabs(chi_n) + P.r_lim + fabs(P.pi_lo) + fabs(P.pi_hi)) + 1e-9;
+    double chi_lo, chi_hi;
+    if (KIND == MIA_KIND_W) {
+      chi_lo = chi_n + P.pi_lo - m;
+      chi_hi = chi_n + P.pi_hi + m;
+    } else {
+      chi_lo = chi_n - P.r_lim - m;
+      chi_hi = chi_n + P.r_lim + m;
+    }
+    LcWin w;
+    w.d0 = cell_1d(dec_n - span_dec, g.dec0, g.inv_dec, g.n_dec);
+    w.d1 = cell_1d(dec_n + span_dec, g.dec0, g.inv_dec, g.n_dec);
+    w.a0 = cell_1d(ra_n - span_ra, g.ra0, g.inv_ra, g.n_ra);
+    w.a1 = cell_1d(ra_n + span_ra, g.ra0, g.inv_ra, g.n_ra);
+    w.c0 = cell_1d(chi_lo, g.chi0, g.inv_chi, g.n_chi);
+    w.c1 = cell_1d(chi_hi, g.chi0, g.inv_chi, g.n_chi);
+    const double kxd = kDegToRad * chi_n * cos_n * hx, kyd = kDegToRad * chi_n * hx;
+    w.kx = (float)kxd;
+    w.ky = (float)kyd;
+    const double ep = 1.1 * 7.2e-15 * ((fabs(ra_n) + fmin(span_ra, 1e30)) * fabs(kxd) +
+                                       (fabs(dec_n) + fmin(span_dec, 1e30)) * fabs(kyd));
+    const double gld = 1.1 * 7.2e-15 * (2.0 * fabs(chi_n) + P.r_lim + fabs(P.pi_lo) + fabs(P.pi_hi));
+    w.gl = (float)gld;
+    // on q (w: r_p^2; multipoles: r^2, which adds the lf term) with sqrt(q) <= 1.0001 r_lim
+    w.gq = (float)(2.1 * P.r_lim * (ep + (KIND == MIA_KIND_W ? 0.0 : gld)) + ep * ep + gld * gld);
+    w.gqp = (float)(P.h2 * (2.1 * P.r_lim * ep + ep * ep));   // on r_p^2 (the multipoles' cut)
+    w.gmu = (float)(2.0 * (gld + ep));                          // times 1/r, on mu
+    win[ip] = w;
+  }
+}
 
 struct LcAcc {
   double* A;                   // [max(1, n_patch)][Q][nb]
@@ -134,17 +193,18 @@ __device__ __forceinline__ int lookup(const double* br, const int* bins, int n, 
   return bins[lo];
 }
 
-// lookup of an approximate x in FP32: `near` is set when a breakpoint
-// (rounded to FP32) lies within tol of x, where x could be on the wrong side
-__device__ __forceinline__ int lookup_f(const float* br, const int* bins, int n, float x, float tol, bool& near) {
-  int lo = 0, hi = n;
-  while (lo < hi) {
-    const int mid = (lo + hi) >> 1;
-    if (br[mid] <= x) lo = mid + 1; else hi = mid;
-  }
-  if (lo > 0 && x - br[lo - 1] <= tol) near = true;
-  if (lo < n && br[lo] - x <= tol) near = true;
-  return bins[lo];
+// Interval of an approximate x in FP32 among the (FP32-rounded) breaks: from
+// a first guess t0, walk to t = #{breaks <= x}, the binary search's answer.
+// `near` is set when a break lies within tol of x, where x could be on the
+// wrong side of it.
+__device__ __forceinline__ int lookup_f(const float* br, const int* bins, int n, float x, float t0, float tol,
+                                        bool& near) {
+  int t = (int)fminf(fmaxf(t0, 0.0f), (float)n);
+  while (t < n && br[t] <= x) ++t;
+  while (t > 0 && br[t - 1] > x) --t;
+  if (t > 0 && x - br[t - 1] <= tol) near = true;
+  if (t < n && br[t] - x <= tol) near = true;
+  return bins[t];
 }
 
 // FP32 decisions: the separation terms from the hi/lo coordinates are within
@@ -157,7 +217,7 @@ constexpr int kQueue = 64;         // per-warp queue of survivors (int4 entries)
 template <int KIND, int SHAPES, int JK>
 __global__ void __launch_bounds__(kLcMaxWarps * 32)
 k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorted shp, const int* __restrict__ start,
-           const LcAcc acc) {
+           const LcWin* __restrict__ win, const LcAcc acc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
   const int nb = P.nb;
@@ -211,7 +271,7 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
   };
 
   auto accumulate = [&](int j, int bin, double ww, double ep, double ex) {
-    atomicAdd(&h[bin], ww);
+    if (!P.unit) atomicAdd(&h[bin], ww);
     if (SHAPES) {
       atomicAdd(&h[nb + bin], ww * ep);
       atomicAdd(&h[2 * nb + bin], ww * ex);
@@ -222,7 +282,7 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
       if (p_s >= P.n_patch) atomicOr(acc.status, MIA_LC_BAD_PATCH);
       if (p_s >= 0 && p_s < P.n_patch && p_s != cur) {
         double* dst = acc.B + (size_t)p_s * Q * nb;
-        atomicAdd(&dst[bin], ww);
+        if (!P.unit) atomicAdd(&dst[bin], ww);
         if (SHAPES) {
           atomicAdd(&dst[nb + bin], ww * ep);
           atomicAdd(&dst[2 * nb + bin], ww * ex);
@@ -310,8 +370,6 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     __syncwarp();
   };
 
-  const LcGrid& g = P.g;
-  const double hx = KIND == MIA_KIND_W ? P.h_extra : 1.0;
   const float h2f = (float)P.h2, rc2f = (float)(P.rp_cut * P.rp_cut);
   for (;;) {
     unsigned base = 0;
@@ -320,8 +378,6 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     if ((long long)base >= P.n_pos) break;
     const long long stop = min((long long)base + kLcChunk, P.n_pos);
     for (long long ip = base; ip < stop; ++ip) {
-      const double ra_n = pos.ra[ip], dec_n = pos.dec[ip], chi_n = pos.chi[ip];
-      const double cos_n = pos.aux0[ip];
       const int p_n = JK ? pos.patch[ip] : 0;
       if (JK && (p_n < 0 || p_n >= P.n_patch)) {   // a position must belong to a patch
         if (lane == 0) atomicOr(acc.status, MIA_LC_BAD_PATCH);
@@ -333,45 +389,14 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
         cur = p_n;
       }
       const double w_n = pos.w[ip];
-      // separation window (a superset; the pair tests decide)
-      const double den = fabs(hx * chi_n);
-      const double span_dec = den > 1e-300 ? P.r_lim / den / kDegToRad * (1.0 + 1e-6) + 1e-9 : 1e300;
-      const double den_ra = den * fabs(cos_n);
-      const double span_ra = den_ra > 1e-300 ? P.r_lim / den_ra / kDegToRad * (1.0 + 1e-6) + 1e-9 : 1e300;
-      const double m = 1e-9 * (fabs(chi_n) + P.r_lim + fabs(P.pi_lo) + fabs(P.pi_hi)) + 1e-9;
-      double chi_lo, chi_hi;
-      if (KIND == MIA_KIND_W) {
-        chi_lo = chi_n + P.pi_lo - m;
-        chi_hi = chi_n + P.pi_hi + m;
-      } else {
-        chi_lo = chi_n - P.r_lim - m;
-        chi_hi = chi_n + P.r_lim + m;
-      }
-      const int d0 = cell_1d(dec_n - span_dec, g.dec0, g.inv_dec, g.n_dec);
-      const int d1 = cell_1d(dec_n + span_dec, g.dec0, g.inv_dec, g.n_dec);
-      const int a0 = cell_1d(ra_n - span_ra, g.ra0, g.inv_ra, g.n_ra);
-      const int a1 = cell_1d(ra_n + span_ra, g.ra0, g.inv_ra, g.n_ra);
-      const int c0 = cell_1d(chi_lo, g.chi0, g.inv_chi, g.n_chi);
-      const int c1 = cell_1d(chi_hi, g.chi0, g.inv_chi, g.n_chi);
+      const LcWin wn = win[ip];
+      const int d0 = wn.d0, d1 = wn.d1, a0 = wn.a0, a1 = wn.a1, c0 = wn.c0, c1 = wn.c1;
+      const float kx = wn.kx, ky = wn.ky, gq = wn.gq, gqp = wn.gqp, gmu = wn.gmu, gl = wn.gl;
       const float4 nhl = pos.hl[ip];
       const float2 nch = pos.chl[ip];
-      const double kxd = kDegToRad * chi_n * cos_n * hx, kyd = kDegToRad * chi_n * hx;
-      const float kx = (float)kxd, ky = (float)kyd;
-      // Absolute errors from the hi/lo representation (each coordinate to
-      // 2^-48 of itself; a difference of two to 2^-47 of the larger, which the
-      // window bounds): ep on the projected terms ax, ay, gl on lf.  Relative
-      // errors of the FP32 arithmetic stay below 1.2e-6 of q (kRelGuard = 4e-6).
-      const double ep = 1.1 * 7.2e-15 * ((fabs(ra_n) + fmin(span_ra, 1e30)) * fabs(kxd) +
-                                         (fabs(dec_n) + fmin(span_dec, 1e30)) * fabs(kyd));
-      const double gld = 1.1 * 7.2e-15 * (2.0 * fabs(chi_n) + P.r_lim + fabs(P.pi_lo) + fabs(P.pi_hi));
-      const float gl = (float)gld;
-      // on q (w: r_p^2; multipoles: r^2, which adds the lf term) with sqrt(q) <= 1.0001 r_lim
-      const float gq = (float)(2.1 * P.r_lim * (ep + (KIND == MIA_KIND_W ? 0.0 : gld)) + ep * ep + gld * gld);
-      const float gqp = (float)(P.h2 * (2.1 * P.r_lim * ep + ep * ep));   // on r_p^2 (multipoles' cut)
-      const float gmu = (float)(2.0 * (gld + ep));                          // times 1/r, on mu
       for (int d = d0; d <= d1; ++d) {
         for (int c = c0; c <= c1; ++c) {
-          const int row = (d * g.n_chi + c) * g.n_ra;
+          const int row = (d * P.g.n_chi + c) * P.g.n_ra;
           const int j0 = start[row + a0], j1 = start[row + a1 + 1];
           for (int jj = j0; jj < j1; jj += 32) {
             const int j = jj + lane;
@@ -388,9 +413,9 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
               int ib = -1, jb = -1;
               if (KIND == MIA_KIND_W) {
                 if (qn <= P.qf_hi && lf >= P.los_lo && lf <= P.los_hi) {
-                  jb = lookup_f(s_pbf, s_pbn, P.n_pbreak, lf, kRelGuard * fabsf(lf) + gl, near);
+                  jb = lookup_f(s_pbf, s_pbn, P.n_pbreak, lf, lf * P.pa + P.pb, kRelGuard * fabsf(lf) + gl, near);
                   if (near || jb != -1) {
-                    ib = lookup_f(s_qbf, s_qbn, P.n_qbreak, qn, kRelGuard * qn + gq, near);
+                    ib = lookup_f(s_qbf, s_qbn, P.n_qbreak, qn, __log2f(qn) * P.qa + P.qb, kRelGuard * qn + gq, near);
                     take = near || ib != -1;
                   }
                 }
@@ -404,10 +429,11 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
                     cut_ok = qp > rc2f;
                   }
                   if (near || cut_ok) {
-                    ib = lookup_f(s_qbf, s_qbn, P.n_qbreak, q, kRelGuard * q + gq, near);
+                    ib = lookup_f(s_qbf, s_qbn, P.n_qbreak, q, __log2f(q) * P.qa + P.qb, kRelGuard * q + gq, near);
                     if (near || ib != -1) {
                       const float rq = rsqrtf(q);
-                      jb = lookup_f(s_pbf, s_pbn, P.n_pbreak, lf * rq, kRelGuard + gmu * rq, near);
+                      const float mu = lf * rq;
+                      jb = lookup_f(s_pbf, s_pbn, P.n_pbreak, mu, mu * P.pa + P.pb, kRelGuard + gmu * rq, near);
                       take = true;
                     }
                   }
@@ -422,7 +448,7 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
                 }
               }
               if (!SHAPES && take && !near) {   // counts only: w_p w_s is all there is to add
-                accumulate(j, bin, __dmul_rn(w_n, shp.w[j]), 0.0, 0.0);
+                accumulate(j, bin, P.unit ? 1.0 : __dmul_rn(w_n, shp.w[j]), 0.0, 0.0);
                 take = false;
               }
             }
@@ -454,11 +480,18 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
 // total - A[i] - B[i]; the same for the integer counts.
 __global__ void k_lc_finish(const double* __restrict__ A, const double* __restrict__ B,
                             const unsigned long long* __restrict__ cA, const unsigned long long* __restrict__ cB,
-                            int n_patch, int Q, int nb, double* out, long long* counts) {
+                            int n_patch, int Q, int nb, int unit, double* out, long long* counts) {
   const int P = n_patch > 0 ? n_patch : 1;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int n_real = 1 + n_patch;
-  if (t < Q * nb) {
+  if (unit && t < nb) {   // unit weights: DD is the pair count (exact in FP64 below 2^53)
+    const int b = t;
+    unsigned long long tot = 0;
+    for (int i = 0; i < P; ++i) tot += cA[(size_t)i * nb + b];
+    out[b] = (double)tot;
+    for (int i = 0; i < n_patch; ++i)
+      out[(size_t)(1 + i) * nb + b] = (double)(tot - cA[(size_t)i * nb + b] - cB[(size_t)i * nb + b]);
+  } else if (t < Q * nb) {
     const int q = t / nb, b = t - q * nb;
     double tot = 0.0;
     for (int i = 0; i < P; ++i) tot += A[((size_t)i * Q + q) * nb + b];
@@ -505,7 +538,7 @@ constexpr size_t kLcSmemBudget = 200 * 1024;
 
 template <int KIND, int SHAPES, int JK>
 cudaError_t launch_lc_pairs(const LcParams& P, const LcTables& T, const LcSorted& pos, const LcSorted& shp,
-                            const int* start, const LcAcc& acc, int warps, size_t smem, int num_sms,
+                            const int* start, const LcWin* win, const LcAcc& acc, int warps, size_t smem, int num_sms,
                             cudaStream_t st) {
   auto kern = k_lc_pairs<KIND, SHAPES, JK>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -517,7 +550,7 @@ cudaError_t launch_lc_pairs(const LcParams& P, const LcTables& T, const LcSorted
   const long long want = (P.n_pos + kLcChunk - 1) / kLcChunk;
   long long blocks = std::min<long long>((long long)num_sms * per_sm, (want + warps - 1) / warps);
   if (blocks < 1) blocks = 1;
-  kern<<<(int)blocks, warps * 32, smem, st>>>(P, T, pos, shp, start, acc);
+  kern<<<(int)blocks, warps * 32, smem, st>>>(P, T, pos, shp, start, win, acc);
   return cudaGetLastError();
 }
 
@@ -565,6 +598,7 @@ bool lc_plan(const mia_lc_config* c, long long n_pos, long long n_shape, LcPlan*
   p->off_B = take((size_t)c->n_patch * p->Q * p->nb * 8 + 8);
   p->off_cA = take((size_t)p->P * p->nb * 8);
   p->off_cB = take((size_t)c->n_patch * p->nb * 8 + 8);
+  p->off_win = take(((size_t)n_pos + 1) * sizeof(LcWin));
   p->off_next = take(256);
   p->total = o;
   return true;
@@ -632,6 +666,29 @@ cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sa
   }
   P.g = g;
   P.n_pos = pos.n;
+  P.unit = cfg->unit_weights ? 1 : 0;
+  // first guesses of the table intervals: breaks 0 and n-1 map to 1 and n
+  auto affine = [](const double* br, int n, bool logq, float* a, float* b) {
+    *a = 0.0f;
+    *b = 0.0f;
+    if (n < 2) return;
+    const double x0 = logq ? log2(br[0] > 0 ? br[0] : 1e-300) : br[0];
+    const double x1 = logq ? log2(br[n - 1] > 0 ? br[n - 1] : 1e-300) : br[n - 1];
+    if (!(x1 > x0) || !std::isfinite(x0) || !std::isfinite(x1)) return;
+    const double sl = (n - 1) / (x1 - x0);
+    *a = (float)sl;
+    *b = (float)(1.0 - sl * x0);
+  };
+  affine(cfg->q_break, cfg->n_qbreak, true, &P.qa, &P.qb);
+  affine(cfg->p_break, cfg->n_pbreak, false, &P.pa, &P.pb);
+  LcWin* win = reinterpret_cast<LcWin*>(ws + p.off_win);
+  if (pos.n > 0) {
+    if (cfg->kind == MIA_KIND_W)
+      k_lc_windows<MIA_KIND_W><<<grid_for(pos.n), 256, 0, st>>>(P, Ps, win);
+    else
+      k_lc_windows<MIA_KIND_MULTIPOLES><<<grid_for(pos.n), 256, 0, st>>>(P, Ps, win);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  }
   LcTables T;
   for (int i = 0; i < MIA_MAX_BREAKS; ++i) {
     T.qbr[i] = i < cfg->n_qbreak ? cfg->q_break[i] : 0.0;
@@ -646,7 +703,7 @@ cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sa
     const int w = p.warps;
 #define MIA_LC_CASE(K, S_, J)                                                                      \
   if (cfg->kind == K && (cfg->with_shapes != 0) == (S_ != 0) && jk == (J != 0))                   \
-    e = launch_lc_pairs<K, S_, J>(P, T, Ps, S, sstart, acc, w, p.smem, num_sms, st);
+    e = launch_lc_pairs<K, S_, J>(P, T, Ps, S, sstart, win, acc, w, p.smem, num_sms, st);
     e = cudaErrorInvalidValue;
     MIA_LC_CASE(MIA_KIND_W, 0, 0) MIA_LC_CASE(MIA_KIND_W, 0, 1) MIA_LC_CASE(MIA_KIND_W, 1, 0)
     MIA_LC_CASE(MIA_KIND_W, 1, 1) MIA_LC_CASE(MIA_KIND_MULTIPOLES, 0, 0) MIA_LC_CASE(MIA_KIND_MULTIPOLES, 0, 1)
@@ -655,7 +712,8 @@ cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sa
     if (e != cudaSuccess) return e;
   }
   const int n_thr = (p.Q + 1) * p.nb;
-  k_lc_finish<<<(n_thr + 255) / 256, 256, 0, st>>>(acc.A, acc.B, acc.cA, acc.cB, cfg->n_patch, p.Q, p.nb, out,
+  k_lc_finish<<<(n_thr + 255) / 256, 256, 0, st>>>(acc.A, acc.B, acc.cA, acc.cB, cfg->n_patch, p.Q, p.nb,
+                                                    cfg->unit_weights ? 1 : 0, out,
                                                     reinterpret_cast<long long*>(counts));
   return cudaGetLastError();
 }

@@ -116,6 +116,7 @@ class LightconeCounter:
             for smp in (pos, shp):
                 if not np.all(np.isfinite(smp[k])):
                     raise ValueError(f"lightcone {k} values must be finite")
+        cfg.unit_weights = int(bool(np.all(np.asarray(pos["w"]) == 1.0) and np.all(np.asarray(shp["w"]) == 1.0)))
         if n_shp:
             self._grid(cfg, pos, shp)
         else:
