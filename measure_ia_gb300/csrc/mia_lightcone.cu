@@ -27,7 +27,7 @@ namespace mia {
 namespace {
 
 constexpr int kLcMaxWarps = 8;
-constexpr int kLcMaxSlots = 8;         // cross-patch histograms per warp (at most)
+constexpr int kLcChunk = 4;            // positions per warp grab
 constexpr double kDegToRad = 3.141592653589793 / 180.0;
 
 struct LcGrid {
@@ -105,8 +105,6 @@ struct LcParams {
   float los_lo, los_hi;        // w: FP32 prefilter bounds on Pi
   float qa, qb, pa, pb;        // first guesses of the table interval: log2(q) * qa + qb, x * pa + pb
   int unit;                    // unit weights: DD is the pair count, not summed
-  int slots;                   // per-warp shared histograms for cross-patch pairs (by shape patch)
-  int chunk;                   // consecutive positions per warp grab
   LcGrid g;
   long long n_pos;
 };
@@ -233,13 +231,9 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
   int* s_pbn = s_qbn + (MIA_MAX_BREAKS + 1);
   int4* queues = reinterpret_cast<int4*>(smem_raw + kLcTableBytes);
   int4* queue = queues + warp * kQueue;
-  int* keys_base = reinterpret_cast<int*>(queues + n_warps * kQueue);
-  int* keys = keys_base + warp * kLcMaxSlots;          // shape patch of each B slot, -1 = free
-  double* hist_base = reinterpret_cast<double*>(keys_base + n_warps * kLcMaxSlots);
-  const size_t hw = (size_t)Q * nb + (nb + 1) / 2;     // doubles per histogram (sums, then counts)
-  double* h = hist_base + (size_t)warp * hw * (1 + P.slots);
+  double* hist_base = reinterpret_cast<double*>(queues + n_warps * kQueue);
+  double* h = hist_base + (size_t)warp * ((size_t)Q * nb + (nb + 1) / 2);
   unsigned* hc = reinterpret_cast<unsigned*>(h + (size_t)Q * nb);
-  double* bslot = h + hw;                              // P.slots histograms after the warp's own
   for (int i = threadIdx.x; i < MIA_MAX_BREAKS; i += blockDim.x) {
     s_qbr[i] = T.qbr[i];
     s_pbr[i] = T.pbr[i];
@@ -250,8 +244,8 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     s_qbn[i] = T.qbn[i];
     s_pbn[i] = T.pbn[i];
   }
-  for (size_t i = lane; i < hw * (1 + P.slots); i += 32) h[i] = 0.0;
-  if (lane < kLcMaxSlots) keys[lane] = -1;
+  for (int i = lane; i < Q * nb; i += 32) h[i] = 0.0;
+  for (int i = lane; i < nb; i += 32) hc[i] = 0u;
   __syncthreads();
 
   int cur = -1;  // patch whose sums the warp's histogram holds
@@ -273,27 +267,6 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
         hc[i] = 0u;
       }
     }
-    // cross-patch slots: to their patches' B sums, and free
-    for (int k = 0; k < P.slots; ++k) {
-      const int key = keys[k];
-      if (key < 0) continue;
-      double* sl = bslot + (size_t)k * hw;
-      unsigned* sc = reinterpret_cast<unsigned*>(sl + (size_t)Q * nb);
-      double* dst = acc.B + (size_t)key * Q * nb;
-      unsigned long long* cdst = acc.cB + (size_t)key * nb;
-      for (int i = lane; i < Q * nb; i += 32) {
-        const double v = sl[i];
-        if (v != 0.0) atomicAdd(&dst[i], v);
-        sl[i] = 0.0;
-      }
-      for (int i = lane; i < nb; i += 32) {
-        const unsigned c = sc[i];
-        if (c) atomicAdd(&cdst[i], (unsigned long long)c);
-        sc[i] = 0u;
-      }
-      __syncwarp();
-      if (lane == 0) keys[k] = -1;
-    }
     __syncwarp();
   };
 
@@ -308,33 +281,13 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
       const int p_s = shp.patch[j];
       if (p_s >= P.n_patch) atomicOr(acc.status, MIA_LC_BAD_PATCH);
       if (p_s >= 0 && p_s < P.n_patch && p_s != cur) {
-        int k = -1;
-        if (P.slots > 0) {   // the warp's slot for this patch (direct mapped), claimed if free
-          const int s = p_s % P.slots;
-          int key = keys[s];
-          if (key < 0) {
-            const int old = atomicCAS(&keys[s], -1, p_s);
-            key = old < 0 ? p_s : old;
-          }
-          if (key == p_s) k = s;
+        double* dst = acc.B + (size_t)p_s * Q * nb;
+        if (!P.unit) atomicAdd(&dst[bin], ww);
+        if (SHAPES) {
+          atomicAdd(&dst[nb + bin], ww * ep);
+          atomicAdd(&dst[2 * nb + bin], ww * ex);
         }
-        if (k >= 0) {
-          double* sl = bslot + (size_t)k * hw;
-          if (!P.unit) atomicAdd(&sl[bin], ww);
-          if (SHAPES) {
-            atomicAdd(&sl[nb + bin], ww * ep);
-            atomicAdd(&sl[2 * nb + bin], ww * ex);
-          }
-          atomicAdd(reinterpret_cast<unsigned*>(sl + (size_t)Q * nb) + bin, 1u);
-        } else {
-          double* dst = acc.B + (size_t)p_s * Q * nb;
-          if (!P.unit) atomicAdd(&dst[bin], ww);
-          if (SHAPES) {
-            atomicAdd(&dst[nb + bin], ww * ep);
-            atomicAdd(&dst[2 * nb + bin], ww * ex);
-          }
-          atomicAdd(&acc.cB[(size_t)p_s * nb + bin], 1ull);
-        }
+        atomicAdd(&acc.cB[(size_t)p_s * nb + bin], 1ull);
       }
     }
   };
@@ -420,10 +373,10 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
   const float h2f = (float)P.h2, rc2f = (float)(P.rp_cut * P.rp_cut);
   for (;;) {
     unsigned base = 0;
-    if (lane == 0) base = atomicAdd(acc.next, (unsigned)P.chunk);
+    if (lane == 0) base = atomicAdd(acc.next, (unsigned)kLcChunk);
     base = __shfl_sync(0xffffffffu, base, 0);
     if ((long long)base >= P.n_pos) break;
-    const long long stop = min((long long)base + P.chunk, P.n_pos);
+    const long long stop = min((long long)base + kLcChunk, P.n_pos);
     for (long long ip = base; ip < stop; ++ip) {
       const int p_n = JK ? pos.patch[ip] : 0;
       if (JK && (p_n < 0 || p_n >= P.n_patch)) {   // a position must belong to a patch
@@ -579,10 +532,7 @@ LcSorted carve(unsigned char* base, long long n) {
   return s;
 }
 
-size_t lc_hist_bytes(int Q, int nb) { return (size_t)Q * nb * 8 + (size_t)(nb + 1) / 2 * 8; }
-size_t lc_per_warp(int Q, int nb, int slots) {
-  return (size_t)kQueue * 16 + kLcMaxSlots * 4 + (size_t)(1 + slots) * lc_hist_bytes(Q, nb);
-}
+size_t lc_per_warp(int Q, int nb) { return (size_t)kQueue * 16 + (size_t)Q * nb * 8 + (size_t)(nb + 1) / 2 * 8; }
 constexpr size_t kLcFixedSmem = kLcTableBytes + 16;
 constexpr size_t kLcSmemBudget = 200 * 1024;
 
@@ -597,7 +547,7 @@ cudaError_t launch_lc_pairs(const LcParams& P, const LcTables& T, const LcSorted
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, warps * 32, smem);
   if (e != cudaSuccess) return e;
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  const long long want = (P.n_pos + P.chunk - 1) / P.chunk;
+  const long long want = (P.n_pos + kLcChunk - 1) / kLcChunk;
   long long blocks = std::min<long long>((long long)num_sms * per_sm, (want + warps - 1) / warps);
   if (blocks < 1) blocks = 1;
   kern<<<(int)blocks, warps * 32, smem, st>>>(P, T, pos, shp, start, win, acc);
@@ -627,14 +577,9 @@ bool lc_plan(const mia_lc_config* c, long long n_pos, long long n_shape, LcPlan*
   p->Q = c->with_shapes ? 3 : 1;
   p->nb = c->n_r * c->n_p;
   p->P = c->n_patch > 0 ? c->n_patch : 1;
-  if (kLcFixedSmem + lc_per_warp(p->Q, p->nb, 0) > kLcSmemBudget) { *why = "too many bins for the lightcone counter"; return false; }
-  // cross-patch slots (jackknife only) while 8 warps still fit, in at most 100 KB (two blocks per SM)
-  p->slots = 0;
-  if (c->n_patch > 0)
-    for (int k = kLcMaxSlots; k >= 1; --k)
-      if (kLcFixedSmem + kLcMaxWarps * lc_per_warp(p->Q, p->nb, k) <= 100 * 1024) { p->slots = k; break; }
-  p->warps = (int)std::min<size_t>(kLcMaxWarps, (kLcSmemBudget - kLcFixedSmem) / lc_per_warp(p->Q, p->nb, p->slots));
-  p->smem = kLcFixedSmem + (size_t)p->warps * lc_per_warp(p->Q, p->nb, p->slots);
+  if (kLcFixedSmem + lc_per_warp(p->Q, p->nb) > kLcSmemBudget) { *why = "too many bins for the lightcone counter"; return false; }
+  p->warps = (int)std::min<size_t>(kLcMaxWarps, (kLcSmemBudget - kLcFixedSmem) / lc_per_warp(p->Q, p->nb));
+  p->smem = kLcFixedSmem + (size_t)p->warps * lc_per_warp(p->Q, p->nb);
   p->n_tiles = (int)((p->n_cells + kScanTile - 1) / kScanTile) + 1;
   size_t o = 0;
   auto take = [&](size_t bytes) { size_t at = o; o += al(bytes); return at; };
@@ -722,10 +667,6 @@ cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sa
   P.g = g;
   P.n_pos = pos.n;
   P.unit = cfg->unit_weights ? 1 : 0;
-  P.slots = p.slots;
-  // long runs of neighbouring positions per warp (fewer histogram flushes), but
-  // at least ~8 runs per warp of a full grid for the load balance
-  P.chunk = (int)std::max(4ll, std::min(32ll, (long long)pos.n / ((long long)num_sms * 32 * 8)));
   // first guesses of the table intervals: breaks 0 and n-1 map to 1 and n
   auto affine = [](const double* br, int n, bool logq, float* a, float* b) {
     *a = 0.0f;
