@@ -503,9 +503,10 @@ def lightcone_catalogue(seed=77, n_par=10000, n_rand=1_000_000, n_shape=100_000)
     return data, rnd, jk
 
 
-def _lc_counters(data, rnd, jk):
-    """The four counters of measure_xi_w('clusters', corr_type='both') with
-    their host inputs, as MeasureIALightcone prepares them."""
+def _lc_counters(data, rnd, jk, kind="w"):
+    """The four counters of measure_xi_w (kind 'w') or measure_xi_multipoles
+    (kind 'm') with 'clusters' and corr_type 'both', with their host inputs,
+    as MeasureIALightcone prepares them."""
     from measure_ia_gb300 import MeasureIALightcone
     from measure_ia_gb300.cosmology import default_cosmology
     from measure_ia_gb300.lightcone import _Run
@@ -516,7 +517,7 @@ def _lc_counters(data, rnd, jk):
              weight=np.ones(len(r["RA"])))
     r["weight_shape_sample"] = r["weight"]
     cosmo = default_cosmology()
-    run = _Run(lc, "w", "clusters", "lc", "both", lc.data, r, lambda z: cosmo.comoving_radial_distance(1 / (1 + z)),
+    run = _Run(lc, kind, "clusters", "lc", "both", lc.data, r, lambda z: cosmo.comoving_radial_distance(1 / (1 + z)),
                0.7, False, None, None, None)
     out = []
     for name, pf, sf, shapes, pp, sp in (("S+D", "D", "D", True, "position", "shape"),
@@ -524,7 +525,7 @@ def _lc_counters(data, rnd, jk):
                                          ("RD", "D", "R", False, "position", "randoms"),
                                          ("RR", "R", "R", False, "randoms", "randoms")):
         sel = run._select(run._combo(pf, sf, shapes), None, shapes)
-        lo, hi = int(min(jk[pp])), int(max(jk[pp]))
+        lo, hi = int(np.min(jk[pp])), int(np.max(jk[pp]))
         pos, shp = run._samples(sel, shapes, np.asarray(jk[pp]) - lo, run._shape_labels(jk[sp], lo, hi))
         out.append((name, shapes, run._counter(shapes), pos, shp, hi - lo + 1))
     return lc, out
@@ -609,6 +610,24 @@ def run_lightcone(args, local):
             per.append(t0.elapsed_time(evs[-1][1]))
     ms = float(np.mean(per))
     total_binned = sum(v[1] for v in binned.values())
+    # the multipole counters (r, mu_r bins: 10 log r bins 0.1-60, 20 mu_r bins), same catalogue
+    _, mcounters = _lc_counters(data, rnd, jk, kind="m")
+    mjobs = [(name, c, c.prepare(pos, shp, npatch)) for name, shapes, c, pos, shp, npatch in mcounters]
+    for _ in range(max(3, args.warmup)):
+        for _, c, j in mjobs:
+            c.run(j, stream.cuda_stream)
+    torch.cuda.synchronize(local)
+    mbinned = sum(int(c.fetch(j)[1][0].sum()) for _, c, j in mjobs)
+    mper = []
+    for _ in range(args.steps):
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _, c, j in mjobs:
+            c.run(j, stream.cuda_stream)
+        t1.record(stream)
+        torch.cuda.synchronize(local)
+        mper.append(t0.elapsed_time(t1))
+    del mjobs
     ops = sum(LC_OPS[s] * n for s, n in binned.values())
     peak = measured_dgemm_tflops(local)
     achieved = ops / (ms / 1e3) / 1e12
@@ -641,7 +660,10 @@ def run_lightcone(args, local):
             "cpu_baseline": cpu,
             "e2e": {"value": total_binned / float(np.mean(e2e)), "unit": "binned pairs/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "seconds": e2e},
-            "gpu_launches": 4 * 13 * args.steps,
+            "multipoles": {"value": mbinned / (float(np.mean(mper)) / 1e3), "unit": "binned pairs/s",
+                           "ms_per_step": float(np.mean(mper)), "binned_pairs_per_step": mbinned,
+                           "note": "the four counters of measure_xi_multipoles('clusters', 'both'), same catalogue"},
+            "gpu_launches": 4 * 14 * args.steps,
             "clocks": clk.summary()}
 
 

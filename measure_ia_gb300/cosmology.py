@@ -13,9 +13,13 @@ with those two capabilities works here:
 :class:`FlatLCDM` is a flat universe of matter, a cosmological constant,
 photons at T_CMB = 2.7255 K and three massless neutrino species
 (N_eff = 3.044), the ingredients of pyccl's default background.  Its
-distance is the integral of c / H(z) by 48-point Gauss-Legendre quadrature,
-accurate to ~1e-13 relative for z < 20.  It is not pyccl's spline
-integration, so distances agree with pyccl's only to that method's accuracy.
+distance is the integral of c / H(z): tabulated at the nodes z_k = k / 2048
+(48-point Gauss-Legendre quadrature per interval, summed outward from
+z = 0) and interpolated with cubic Hermite polynomials that use the exact
+derivative c / H(z) at the nodes, accurate to ~1e-12 relative.  A redshift
+gets the same distance whatever else is in the array (the table's nodes do
+not depend on the range asked for).  It is not pyccl's spline integration,
+so distances agree with pyccl's only to that method's accuracy.
 """
 
 from __future__ import annotations
@@ -47,15 +51,50 @@ class FlatLCDM:
         zp = 1.0 + np.asarray(z, dtype=np.float64)
         return np.sqrt(self.Omega_m * zp ** 3 + self.Omega_r * zp ** 4 + self.Omega_l)
 
+    DZ = 1.0 / 2048.0
+
+    def _integral(self, z0, z1):
+        """int_z0^z1 dz / E(z) for arrays of interval ends (48-point Gauss-Legendre)."""
+        half = (z1 - z0) / 2.0
+        mid = (z1 + z0) / 2.0
+        zz = mid[:, None] + half[:, None] * _GL_X[None, :]
+        return half * (_GL_W[None, :] / self.E(zz)).sum(axis=1)
+
+    def _table(self, k_lo, k_hi):
+        """Distances (units of c/H0) at the nodes k_lo..k_hi (k_lo <= 0 <= k_hi)."""
+        t = getattr(self, "_tab", None)
+        if t is not None and t[0] <= k_lo and t[1] >= k_hi:
+            return t
+        k_lo = min(k_lo, t[0] if t else 0, 0)
+        k_hi = max(k_hi, t[1] if t else 0, 0)
+        up = np.arange(0, k_hi + 1, dtype=np.float64) * self.DZ
+        down = np.arange(0, k_lo - 1, -1, dtype=np.float64) * self.DZ
+        cu = np.concatenate([[0.0], np.cumsum(self._integral(up[:-1], up[1:]))])
+        cd = np.concatenate([[0.0], np.cumsum(self._integral(down[:-1], down[1:]))])
+        vals = np.concatenate([cd[::-1][:-1], cu])          # nodes k_lo .. k_hi
+        self._tab = (k_lo, k_hi, vals)
+        return self._tab
+
     def comoving_radial_distance(self, a):
         """Comoving distance in Mpc to scale factor(s) ``a``."""
         a = np.asarray(a, dtype=np.float64)
-        z = 1.0 / a - 1.0
-        flat = z.reshape(-1)
-        half = flat[:, None] / 2.0
-        zz = half * (_GL_X[None, :] + 1.0)
-        chi = (half[:, 0] * (_GL_W[None, :] / self.E(zz)).sum(axis=1)) * (C_KM_S / (100.0 * self.h))
-        return chi.reshape(z.shape)
+        z = (1.0 / a - 1.0).reshape(-1)
+        if z.size == 0:
+            return np.zeros(a.shape)
+        if not np.all(np.isfinite(z)):
+            raise ValueError("redshifts must be finite")
+        k = np.floor(z / self.DZ)
+        k_lo, k_hi, vals = self._table(int(k.min()) - 1, int(k.max()) + 2)
+        i = (k - k_lo).astype(np.int64)
+        z0 = k * self.DZ
+        t = (z - z0) / self.DZ
+        f0, f1 = vals[i], vals[i + 1]
+        d0 = self.DZ / self.E(z0)
+        d1 = self.DZ / self.E(z0 + self.DZ)
+        t2 = t * t
+        t3 = t2 * t
+        chi = (2 * t3 - 3 * t2 + 1) * f0 + (t3 - 2 * t2 + t) * d0 + (-2 * t3 + 3 * t2) * f1 + (t3 - t2) * d1
+        return (chi * (C_KM_S / (100.0 * self.h))).reshape(a.shape)
 
 
 def comoving_radial_distance(cosmology, a):

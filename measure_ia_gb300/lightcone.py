@@ -470,7 +470,7 @@ class _Run:
         real = None
         if patches is not None and self.masks is None:
             pp, sp = patches
-            lo, hi = int(min(pp)), int(max(pp))
+            lo, hi = int(np.min(pp)), int(np.max(pp))
             pos, shp = self._samples(sel, with_shapes, np.asarray(pp) - lo, self._shape_labels(sp, lo, hi))
             sums, cnt = counter.count(pos, shp, hi - lo + 1)
             real = (lo, hi, sums, cnt)
@@ -481,7 +481,7 @@ class _Run:
         if patches is None:
             return
         pp, sp = patches
-        lo, hi = int(min(pp)), int(max(pp))
+        lo, hi = int(np.min(pp)), int(np.max(pp))
         if real is None:   # masks: realisations select with the 'Redshift' masks (measure_jackknife.py:346-356)
             mp = np.asarray(self.masks["Redshift"], dtype=bool)
             ms = np.asarray(self.masks["Redshift_shape_sample"], dtype=bool)
@@ -527,9 +527,16 @@ class _Run:
         mp = np.ones(len(pp), dtype=bool) if self.masks is None else np.asarray(self.masks["Redshift"], dtype=bool)
         ms = np.ones(len(sp), dtype=bool) if self.masks is None else \
             np.asarray(self.masks["Redshift_shape_sample"], dtype=bool)
+        # objects outside patch i: the (masked) total less those in i
+        def outside(lab, m):
+            lab = np.asarray(lab).astype(np.int64)[m] - lo
+            inside = np.bincount(lab[(lab >= 0) & (lab <= hi - lo)], minlength=hi - lo + 1)
+            return int(np.count_nonzero(m)) - inside
+
+        out_s, out_p = outside(sp, ms), outside(pp, mp)
         for k, i in enumerate(range(lo, hi + 1)):
-            self.nsj.setdefault(f"{i}", {})[names[0]] = int(np.sum((np.asarray(sp) != i) & ms))
-            self.nsj[f"{i}"][names[1]] = int(np.sum((np.asarray(pp) != i) & mp))
+            self.nsj.setdefault(f"{i}", {})[names[0]] = int(out_s[k])
+            self.nsj[f"{i}"][names[1]] = int(out_p[k])
             dd = self._dd(sums[0, 1 + k], cnt[1 + k])
             if with_shapes:
                 for sub, tag, v in (("xi_g_plus", "SplusD", sums[1, 1 + k]), ("xi_gg", "DD", dd)):
@@ -632,7 +639,7 @@ class _Run:
         self.integrate(d)
         if jk is None:
             return
-        lo, hi = int(min(jk["shape"])), int(max(jk["shape"]))
+        lo, hi = int(np.min(jk["shape"])), int(np.max(jk["shape"]))
         n_p = hi - lo + 1
         grp, grp_r = f"{d}_jk{n_p}", f"{dr}_jk{n_p}"
         for i in range(lo, hi + 1):
