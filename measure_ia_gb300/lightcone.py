@@ -467,6 +467,9 @@ class _Run:
         combo = self._combo(pos_from, shape_from, with_shapes)
         counter = self._counter(with_shapes)
         sel = self._select(combo, self.masks, with_shapes)
+        # the reference hands the masks to the S+D and S+R realisations only
+        # (measure_IA.py:562-590); the count realisations use every object
+        rmasks = self.masks if with_shapes else None
         real = None
         if patches is not None and self.masks is None:
             pp, sp = patches
@@ -482,18 +485,23 @@ class _Run:
             return
         pp, sp = patches
         lo, hi = int(np.min(pp)), int(np.max(pp))
-        if real is None:   # masks: realisations select with the 'Redshift' masks (measure_jackknife.py:346-356)
-            mp = np.asarray(self.masks["Redshift"], dtype=bool)
-            ms = np.asarray(self.masks["Redshift_shape_sample"], dtype=bool)
-            mt = {k: mp for k in _POS_KEYS}
-            mt.update({k: ms for k in _SHAPE_KEYS})
-            mt["e1"] = mt["e2"] = ms
-            rsel = self._select(combo, mt, with_shapes)
+        if real is None:   # masks: the realisations select with the 'Redshift' masks (measure_jackknife.py:346-356)
+            if rmasks is None:
+                mp = np.ones(len(pp), dtype=bool)
+                ms = np.ones(len(sp), dtype=bool)
+                rsel = self._select(combo, None, with_shapes)
+            else:
+                mp = np.asarray(rmasks["Redshift"], dtype=bool)
+                ms = np.asarray(rmasks["Redshift_shape_sample"], dtype=bool)
+                mt = {k: mp for k in _POS_KEYS}
+                mt.update({k: ms for k in _SHAPE_KEYS})
+                mt["e1"] = mt["e2"] = ms
+                rsel = self._select(combo, mt, with_shapes)
             pos, shp = self._samples(rsel, with_shapes, (np.asarray(pp) - lo)[mp],
                                      self._shape_labels(sp, lo, hi)[ms])
             sums, cnt = counter.count(pos, shp, hi - lo + 1)
             real = (lo, hi, sums, cnt)
-        self._write_realisations(real, with_shapes, real_name, real_suffix, names, patches)
+        self._write_realisations(real, with_shapes, real_name, real_suffix, names, patches, rmasks)
 
     @staticmethod
     def _shape_labels(sp, lo, hi):
@@ -517,16 +525,15 @@ class _Run:
             self.put(f"{top}/xi_gg/{name}{rs}", self.rc)
             self.put(f"{top}/xi_gg/{name}{ps}", self.pc)
 
-    def _write_realisations(self, real, with_shapes, name, suffix, names, patches):
+    def _write_realisations(self, real, with_shapes, name, suffix, names, patches, masks):
         """measure_jackknife.py:340-470 (pooled driver): datasets of each
         realisation, and the per-realisation sample sizes."""
         lo, hi, sums, cnt = real
         top, rs, ps = self.top, self.rs, self.ps
         grp = f"{name}_jk{hi - lo + 1}"
         pp, sp = patches
-        mp = np.ones(len(pp), dtype=bool) if self.masks is None else np.asarray(self.masks["Redshift"], dtype=bool)
-        ms = np.ones(len(sp), dtype=bool) if self.masks is None else \
-            np.asarray(self.masks["Redshift_shape_sample"], dtype=bool)
+        mp = np.ones(len(pp), dtype=bool) if masks is None else np.asarray(masks["Redshift"], dtype=bool)
+        ms = np.ones(len(sp), dtype=bool) if masks is None else np.asarray(masks["Redshift_shape_sample"], dtype=bool)
         # objects outside patch i: the (masked) total less those in i
         def outside(lab, m):
             lab = np.asarray(lab).astype(np.int64)[m] - lo

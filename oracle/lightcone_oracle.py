@@ -364,7 +364,9 @@ def measure(kind, IA_estimator, dataset_name, corr_type, data, randoms, b: LcBin
         for i in range(lo, hi + 1):
             mp = patches_pos != i
             msh = patches_shape != i
-            if masks is not None:
+            # only the S+D and S+R realisations get the masks (measure_IA.py:562-590 pass
+            # masks=masks; the count realisations at :610-680 do not)
+            if masks is not None and not count_pairs:
                 mp = mp * masks["Redshift"]
                 msh = msh * masks["Redshift_shape_sample"]
             nsj.setdefault(f"{i}", {})[names[0]] = sum(msh)

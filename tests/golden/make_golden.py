@@ -409,7 +409,22 @@ LC_CASES = {
                             dict(separation_limits=[0.4, 20.0], num_bins_r=5, num_bins_pi=6, pi_max=20.0)),
     "m_galaxies_gplus": ("m", "galaxies", "g+", dict(seed=37, n_pos=400, n_shape=250, n_rand=700), {},
                          dict(separation_limits=[0.3, 18.0], num_bins_r=6, num_bins_pi=10, pi_max=20.0)),
+    # masks: the reference applies the data's masks to the randoms' arrays too, so
+    # randoms and data have the same lengths here (shape sample = position sample)
+    "w_clusters_both_masks": ("w", "clusters", "both", dict(seed=38, n_pos=500, n_shape=500, n_rand=500,
+                                                            weights=True), dict(masks=True),
+                              dict(separation_limits=[0.3, 25.0], num_bins_r=6, num_bins_pi=5, pi_max=30.0)),
 }
+
+
+def lightcone_masks(data, seed=99):
+    rng = np.random.default_rng(seed)
+    mp = rng.uniform(size=len(data["RA"])) < 0.75
+    ms = rng.uniform(size=len(data["RA_shape_sample"])) < 0.75
+    m = {k: mp for k in ("Redshift", "RA", "DEC", "weight")}
+    m.update({k: ms for k in ("Redshift_shape_sample", "RA_shape_sample", "DEC_shape_sample", "e1", "e2",
+                              "weight_shape_sample")})
+    return m
 
 
 def run_lightcone(name):
@@ -429,6 +444,8 @@ def run_lightcone(name):
     cosmo_kw = call.pop("cosmology", None)
     cosmology = _ccl_cosmology(**cosmo_kw) if cosmo_kw else None
     measure_cov = call.pop("measure_cov", True)
+    if call.pop("masks", False):
+        call["masks"] = lightcone_masks(data)
     lc = MeasureIALightcone({k: np.array(v) for k, v in data.items()}, {k: np.array(v) for k, v in rnd.items()},
                             outfile, num_nodes=2, **bkw)
     jk = {k: np.array(v) for k, v in patches.items()} if measure_cov else None

@@ -96,3 +96,14 @@ def load_lc_case(name):
     ckw = meta["call"].get("cosmology")
     h = ckw["h"] if ckw else 0.7
     return meta, data, rnd, jk, outs, TableCosmology(z["chi/a"], z["chi/chi"], h)
+
+
+def lc_masks(data, seed=99):
+    """The masks make_golden.py used for a lightcone case with call['masks']."""
+    rng = np.random.default_rng(seed)
+    mp = rng.uniform(size=len(data["RA"])) < 0.75
+    ms = rng.uniform(size=len(data["RA_shape_sample"])) < 0.75
+    m = {k: mp for k in ("Redshift", "RA", "DEC", "weight")}
+    m.update({k: ms for k in ("Redshift_shape_sample", "RA_shape_sample", "DEC_shape_sample", "e1", "e2",
+                              "weight_shape_sample")})
+    return m

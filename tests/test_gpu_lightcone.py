@@ -1,6 +1,6 @@
 """Lightcone path on the GPU (MeasureIALightcone through mia_lc_count).
 
-* Every dataset of the seven reference runs in ``tests/golden/lc_*.npz``:
+* Every dataset of the reference runs in ``tests/golden/lc_*.npz``:
   the same dataset names, values within 1e-10 relative (array scale as the
   floor), non-finite entries at the same places.
 * Each counter alone against the oracle on randomised catalogues: integer
@@ -14,7 +14,7 @@
 import numpy as np
 import pytest
 
-from golden_io import lc_case_names, load_lc_case
+from golden_io import lc_case_names, lc_masks, load_lc_case
 from oracle import lightcone_oracle as LO
 
 pytestmark = pytest.mark.gpu
@@ -40,6 +40,8 @@ def _run_product(meta, data, rnd, jk, cosmo, out):
     call = dict(meta["call"])
     call.pop("cosmology", None)
     call.pop("measure_cov", None)
+    if call.pop("masks", False):
+        call["masks"] = lc_masks(data)
     lc = MeasureIALightcone({k: np.array(v) for k, v in data.items()}, {k: np.array(v) for k, v in rnd.items()},
                             out, num_nodes=2, **meta["binning"])
     jkp = {k: np.array(v) for k, v in jk.items()} if meta["measure_cov"] else None

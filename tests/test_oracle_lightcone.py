@@ -6,7 +6,7 @@ sums differs), and the reference's failure on gg jackknife covariances."""
 import numpy as np
 import pytest
 
-from golden_io import assert_close, lc_case_names, load_lc_case
+from golden_io import assert_close, lc_case_names, lc_masks, load_lc_case
 from oracle import lightcone_oracle as LO
 
 
@@ -17,11 +17,12 @@ def run_oracle(meta, data, rnd, jk, cosmo):
     return LO.measure(meta["kind"], meta["estimator"], "lc", meta["corr_type"], dict(data), dict(rnd), b,
                       cosmo.comoving_radial_distance, cosmo["h"],
                       jk_patches={k: v for k, v in jk.items()} if meta["measure_cov"] else None,
-                      measure_cov=meta["measure_cov"], over_h=call.get("over_h", False), rp_cut=call.get("rp_cut"))
+                      measure_cov=meta["measure_cov"], over_h=call.get("over_h", False), rp_cut=call.get("rp_cut"),
+                      masks=lc_masks(data) if call.get("masks") else None)
 
 
 def test_fixtures_present():
-    assert len(lc_case_names()) >= 7
+    assert len(lc_case_names()) >= 8
 
 
 @pytest.mark.parametrize("name", lc_case_names())
