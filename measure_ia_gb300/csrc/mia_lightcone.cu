@@ -90,9 +90,12 @@ __global__ void k_lc_scatter(mia_lc_sample in, long long n, const int* __restric
       out.aux1[d] = kDegToRad * chi * c;   // dx ~ (ra_s - ra_p) * cx, few ulp from the reference's dx
       out.aux2[d] = kDegToRad * chi;       // dy ~ (dec_s - dec_p) * cy
     } else if (with_shapes) {
+      // w_s |e| cos 2phi_a and w_s |e| sin 2phi_a: a pair's S+D and SxD terms are
+      // then -w_p (wa cos 2phi_s + wb sin 2phi_s) and -w_p (wb cos 2phi_s - wa sin 2phi_s)
+      const double we = in.w[i] * in.e[i];
       out.aux0[d] = in.e[i];
-      out.aux1[d] = in.c2a[i];
-      out.aux2[d] = in.s2a[i];
+      out.aux1[d] = we * in.c2a[i];
+      out.aux2[d] = we * in.s2a[i];
     }
   }
 }
@@ -270,11 +273,11 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     __syncwarp();
   };
 
-  auto accumulate = [&](int j, int bin, double ww, double ep, double ex) {
+  auto accumulate = [&](int j, int bin, double ww, double sp, double sx) {
     if (!P.unit) atomicAdd(&h[bin], ww);
     if (SHAPES) {
-      atomicAdd(&h[nb + bin], ww * ep);
-      atomicAdd(&h[2 * nb + bin], ww * ex);
+      atomicAdd(&h[nb + bin], sp);
+      atomicAdd(&h[2 * nb + bin], sx);
     }
     atomicAdd(&hc[bin], 1u);
     if (JK) {
@@ -284,30 +287,36 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
         double* dst = acc.B + (size_t)p_s * Q * nb;
         if (!P.unit) atomicAdd(&dst[bin], ww);
         if (SHAPES) {
-          atomicAdd(&dst[nb + bin], ww * ep);
-          atomicAdd(&dst[2 * nb + bin], ww * ex);
+          atomicAdd(&dst[nb + bin], sp);
+          atomicAdd(&dst[2 * nb + bin], sx);
         }
         atomicAdd(&acc.cB[(size_t)p_s * nb + bin], 1ull);
       }
     }
   };
 
-  // e+ / ex from a separation direction (ux, uy) with qd = ux^2 + uy^2
-  auto shape_terms = [&](int j, double ux, double uy, double qd, double& ep, double& ex) {
-    ep = ex = 0.0;
+  // S+D and SxD terms of a pair from its separation (ux, uy) (any common scale):
+  // e+ = -e cos 2(phi_a - phi_s), ex = -e sin 2(phi_a - phi_s) with cos 2phi_s =
+  // (ux^2 - uy^2) / q, sin 2phi_s = 2 ux uy / q, q = ux^2 + uy^2; the shape's
+  // w_s e cos 2phi_a, w_s e sin 2phi_a come precomputed (k_lc_scatter).  1/q is an
+  // FP32 seed and one Newton step (relative error ~1e-14 of the term).
+  auto shape_terms = [&](int j, double w_n, double ux, double uy, double& sp, double& sx) {
+    sp = sx = 0.0;
+    const double ux2 = ux * ux;
+    const double qd = fma(uy, uy, ux2);
     if (!(qd > 0.0)) return;                   // r_p = 0: the reference's NaN terms are set to 0
     double r;
-    if (qd > 1e-30 && qd < 1e30) {             // reciprocal: FP32 seed, two Newton steps
+    if (qd > 1e-30 && qd < 1e30) {
       r = (double)__frcp_rn((float)qd);
-      r = r * (2.0 - qd * r);
-      r = r * (2.0 - qd * r);
+      r = r * fma(-qd, r, 2.0);
     } else {
       r = 1.0 / qd;
     }
-    const double c2s = (ux * ux - uy * uy) * r, s2s = 2.0 * ux * uy * r;
-    const double ee = shp.aux0[j], c2a = shp.aux1[j], s2a = shp.aux2[j];
-    ep = -ee * (c2a * c2s + s2a * s2s);
-    ex = -ee * (s2a * c2s - c2a * s2s);
+    const double A = fma(-uy, uy, ux2), B = (ux + ux) * uy;
+    const double k = -w_n * r;
+    const double wa = shp.aux1[j], wb = shp.aux2[j];
+    sp = k * fma(wa, A, wb * B);
+    sx = k * fma(wb, A, -(wa * B));
   };
 
   // One queued survivor per valid lane: e.z >= 0 is its bin (decided in
@@ -321,11 +330,10 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     const double ra_s = shp.ra[j], dec_s = shp.dec[j], chi_s = shp.chi[j];
     const double dra = __dsub_rn(ra_s, ra_n), ddec = __dsub_rn(dec_s, dec_n);
     int bin = e.z;
-    double ux, uy, qd;
+    double ux, uy;
     if (bin >= 0) {
       ux = dra * pos.aux1[ip];
       uy = ddec * pos.aux2[ip];
-      qd = ux * ux + uy * uy;
     } else {
       const double los = __dsub_rn(chi_s, chi_n);
       const double dra_e = __dmul_rn(__ddiv_rn(dra, 180.0), 3.141592653589793);
@@ -337,7 +345,6 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
       const double qp = __dadd_rn(__dmul_rn(dxh, dxh), __dmul_rn(dyh, dyh));
       ux = dxh;
       uy = dyh;
-      qd = qp;
       int ib, jb;
       if (KIND == MIA_KIND_W) {
         ib = lookup(s_qbr, s_qbn, P.n_qbreak, qp);
@@ -358,9 +365,10 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
       }
       bin = ib * P.n_p + jb;
     }
-    double ep = 0.0, ex = 0.0;
-    if (SHAPES) shape_terms(j, ux, uy, qd, ep, ex);
-    accumulate(j, bin, __dmul_rn(pos.w[ip], shp.w[j]), ep, ex);
+    const double w_n = pos.w[ip];
+    double sp = 0.0, sx = 0.0;
+    if (SHAPES) shape_terms(j, w_n, ux, uy, sp, sx);
+    accumulate(j, bin, P.unit ? 1.0 : __dmul_rn(w_n, shp.w[j]), sp, sx);
   };
 
   auto drain = [&]() {   // process what is queued (fewer than 32 entries)

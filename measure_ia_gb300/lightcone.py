@@ -50,7 +50,8 @@ class LightconeCounter:
     """One of the reference's four lightcone pair counters, with patch
     realisations, through ``mia_lc_count``."""
 
-    def __init__(self, kind, with_shapes, r_bins, r_min, r_max, p_bins, h_extra=1.0, rp_cut=0.0, device=0):
+    def __init__(self, kind, with_shapes, r_bins, r_min, r_max, p_bins, h_extra=1.0, rp_cut=0.0, device=0,
+                 cell_div=(8.0, 3.0, 3.0)):
         if kind not in ("w", "m"):
             raise ValueError(kind)
         self.kind, self.with_shapes, self.device = kind, bool(with_shapes), device
@@ -71,10 +72,14 @@ class LightconeCounter:
         self.pi_lo, self.pi_hi = (float(p_bins[0]), float(p_bins[-1])) if kind == "w" else (0.0, 0.0)
         self.h_extra = float(h_extra)
         self.rp_cut = float(rp_cut)
+        # launch geometry (results do not depend on it): cells per separation
+        # window half-width along RA, DEC and the comoving distance
+        self.cell_div = tuple(float(x) for x in cell_div)
 
     def _grid(self, cfg, pos, shp):
-        """Cells of about half a separation window (RA: a quarter) at the
-        median position distance, at most ~2^22 cells."""
+        """Cells of 1/cell_div of the separation window's half-width (RA,
+        DEC) and of the line-of-sight window (distance) at the median position
+        distance, at most ~2^22 cells."""
         ra, dec, chi = shp["ra"], shp["dec"], shp["chi"]
         lo = np.array([ra.min(), dec.min(), chi.min()])
         hi = np.array([ra.max(), dec.max(), chi.max()])
@@ -83,7 +88,8 @@ class LightconeCounter:
         cos_med = float(np.median(np.abs(pos["cos_dec"]))) if len(pos["cos_dec"]) else 1.0
         span = self.r_lim / max(hx * chi_med, 1e-12) / (np.pi / 180.0)
         chi_span = (self.pi_hi - self.pi_lo) if self.kind == "w" else 2.0 * self.r_lim
-        want = np.array([span / max(cos_med, 1e-3) / 4.0, span / 2.0, chi_span / 2.0])
+        dv = self.cell_div
+        want = np.array([span / max(cos_med, 1e-3) / dv[0], span / dv[1], chi_span / dv[2]])
         ext = np.maximum(hi - lo, 1e-9)
         want = np.maximum(want, ext / 4096.0)
         n = np.maximum(1, np.ceil(ext / want)).astype(np.int64)
