@@ -196,3 +196,21 @@ def test_index_past_last_bin_raises():
     got = counts[0].astype(np.float64)
     got[got == 0] = 1
     np.testing.assert_array_equal(got, dd)
+
+
+def test_empty_samples():
+    """No positions, no shapes, or no pair in range: zero counts, DD read as 1
+    where empty (the reference's DD == 0 -> 1), no error."""
+    from measure_ia_gb300.lightcone import LightconeCounter
+    b = LO.LcBinning(0.5, 10.0, 4, 4, 10.0)
+    one = {"ra": np.array([10.0]), "dec": np.array([0.0]), "chi": np.array([500.0]), "w": np.ones(1),
+           "cos_dec": np.ones(1)}
+    far = {"ra": np.array([50.0]), "dec": np.array([40.0]), "chi": np.array([900.0]), "w": np.ones(1),
+           "e": np.full(1, 0.3), "c2a": np.ones(1), "s2a": np.zeros(1)}
+    empty_p = {k: v[:0] for k, v in one.items()}
+    empty_s = {k: v[:0] for k, v in far.items()}
+    for shapes in (False, True):
+        c = LightconeCounter("w", shapes, b.r_bins, 0.5, 10.0, b.pi_bins)
+        for pos, shp in ((empty_p, far), (one, empty_s), (one, far), (empty_p, empty_s)):
+            sums, counts = c.count(pos, shp, 0)
+            assert counts.sum() == 0 and np.all(sums == 0.0)
