@@ -8,6 +8,7 @@ the C ABI of ``include/measure_ia_gb300.h``.
 from .lightcone import MeasureIALightcone
 from .measure_ia import MeasureIABox
 from .output import open_output, read_output
+from .read_data import ReadData
 from .sim_info import SimInfo
 
-__all__ = ["MeasureIABox", "MeasureIALightcone", "SimInfo", "open_output", "read_output"]
+__all__ = ["MeasureIABox", "MeasureIALightcone", "ReadData", "SimInfo", "open_output", "read_output"]

@@ -15,15 +15,21 @@ heap's trailing free block, B-tree nodes allocated for 2K children, the
 datatype and fill messages marked constant) are kept so that the files look
 like h5py's.
 
-The reader covers the same layout plus what h5py writes into it:
-continuation messages, B-trees of several levels, compact storage and
-version-2 dataspaces.  Anything else raises ``NotImplementedError``.
+The reader covers the same layout plus what h5py and the HDF5 library write
+into it: continuation messages, B-trees of several levels, compact storage,
+version-2 dataspaces, and chunked storage (version-1 chunk B-tree) with the
+deflate, shuffle and fletcher32 filters.  Anything else raises
+``NotImplementedError``.  The writer can store a dataset chunked and
+deflate-compressed (``chunks=``); no HDF5 library exists on the hosts this was
+built on, so chunked files have only been read back by this module.
 """
 
 from __future__ import annotations
 
+import mmap
 import os
 import struct
+import zlib
 
 import numpy as np
 
@@ -37,7 +43,9 @@ FREE_NULL = 1                    # end of a local heap's free list
 SUPERBLOCK_BYTES = 96
 
 _MSG_DATASPACE, _MSG_DATATYPE, _MSG_FILL, _MSG_LAYOUT = 0x0001, 0x0003, 0x0005, 0x0008
-_MSG_CONTINUATION, _MSG_SYMBOL_TABLE = 0x0010, 0x0011
+_MSG_FILTERS, _MSG_CONTINUATION, _MSG_SYMBOL_TABLE = 0x000B, 0x0010, 0x0011
+CHUNK_K = 32                     # indexed-storage K of superblock version 0: 2K chunks per B-tree node
+FILTER_DEFLATE, FILTER_SHUFFLE, FILTER_FLETCHER32 = 1, 2, 3
 
 
 def _pad8(n):
@@ -102,11 +110,80 @@ def _entry(name_off, header, scratch=None) -> bytes:
     return struct.pack("<QQIIQQ", name_off, header, 1, 0, *scratch)
 
 
-def _write_dataset(img: _Image, value: np.ndarray) -> int:
+def _write_chunked(img: _Image, v: np.ndarray, dt: np.dtype, chunk_rows: int, level: int) -> int:
+    """A dataset split into chunks of ``chunk_rows`` rows, each shuffled and
+    deflated, indexed by a version-1 chunk B-tree (leaves of up to 2K chunks)."""
+    if v.ndim == 0:
+        raise ValueError("a scalar cannot be chunked")
+    a = np.ascontiguousarray(v, dtype=dt)
+    rows = max(1, int(chunk_rows))
+    cdims = [rows] + list(a.shape[1:])
+    esize = dt.itemsize
+    rank = a.ndim
+    chunks = []
+    for r0 in range(0, max(a.shape[0], 1), rows):
+        block = np.zeros(cdims, dtype=dt)
+        part = a[r0:r0 + rows]
+        block[:len(part)] = part
+        raw = block.tobytes()
+        shuffled = np.frombuffer(raw, np.uint8).reshape(-1, esize).T.tobytes()
+        data = zlib.compress(shuffled, level)
+        at = img.alloc(len(data))
+        img.put(at, data)
+        chunks.append((r0, at, len(data)))
+    nodes = []
+    per = 2 * CHUNK_K
+    key_bytes = 8 + 8 * (rank + 1)
+
+    def key(size, r0):
+        return struct.pack("<II", size, 0) + struct.pack("<Q", r0) + b"\0" * (8 * rank)
+
+    groups = [chunks[i:i + per] for i in range(0, len(chunks), per)] or [[]]
+    node_bytes = 24 + (2 * per + 1) * key_bytes
+    addrs = [img.alloc(node_bytes) for _ in groups]
+    for j, g in enumerate(groups):
+        left = addrs[j - 1] if j > 0 else UNDEF
+        right = addrs[j + 1] if j + 1 < len(groups) else UNDEF
+        body = b""
+        for r0, at, size in g:
+            body += key(size, r0) + struct.pack("<Q", at)
+        end = (g[-1][0] + rows) if g else 0
+        body += key(0, end)
+        img.put(addrs[j], b"TREE" + struct.pack("<BBHQQ", 1, 0, len(g), left, right) + body)
+        nodes.append((addrs[j], g[0][0] if g else 0))
+    if len(nodes) > 1:
+        top = img.alloc(node_bytes)
+        body = b""
+        for at, r0 in nodes:
+            body += key(0, r0) + struct.pack("<Q", at)
+        body += key(0, (chunks[-1][0] + rows))
+        img.put(top, b"TREE" + struct.pack("<BBHQQ", 1, 1, len(nodes), UNDEF, UNDEF) + body)
+        root = top
+    else:
+        root = nodes[0][0]
+    filt = struct.pack("<BB6x", 1, 2)
+    filt += struct.pack("<HHHH", FILTER_SHUFFLE, 0, 1, 1) + struct.pack("<I", esize) + b"\0" * 4
+    filt += struct.pack("<HHHH", FILTER_DEFLATE, 0, 1, 1) + struct.pack("<I", level) + b"\0" * 4
+    layout = struct.pack("<BBBQ", 3, 2, rank + 1, root) + b"".join(struct.pack("<I", d) for d in cdims + [esize])
+    hdr = _object_header([
+        _message(_MSG_DATASPACE, _dataspace(v.shape)),
+        _message(_MSG_DATATYPE, _datatype(np.dtype(dt)), flags=1),
+        _message(_MSG_FILL, bytes([2, 2, 2, 1]) + struct.pack("<I", 0), flags=1),
+        _message(_MSG_FILTERS, filt),
+        _message(_MSG_LAYOUT, layout)])
+    addr = img.alloc(len(hdr))
+    img.put(addr, hdr)
+    return addr
+
+
+def _write_dataset(img: _Image, value: np.ndarray, chunks=None) -> int:
     v = np.asarray(value)
     if v.dtype.kind == "b":
         raise TypeError("boolean datasets are not supported by the HDF5 writer")
     dt = v.dtype.newbyteorder("<") if v.dtype.byteorder != "|" else v.dtype
+    _datatype(np.dtype(dt))
+    if chunks:
+        return _write_chunked(img, v, np.dtype(dt), chunks, 4)
     raw = np.ascontiguousarray(v, dtype=dt).tobytes()
 
     def header(data_at):
@@ -124,7 +201,7 @@ def _write_dataset(img: _Image, value: np.ndarray) -> int:
     return addr
 
 
-def _write_group(img: _Image, children: dict) -> tuple[int, int, int]:
+def _write_group(img: _Image, children: dict, chunks=None) -> tuple[int, int, int]:
     """Writes a group and (recursively) its members; returns the addresses
     of its object header, B-tree root and local heap."""
     names = sorted(children, key=lambda s: s.encode())
@@ -133,10 +210,10 @@ def _write_group(img: _Image, children: dict) -> tuple[int, int, int]:
     for n in names:
         c = children[n]
         if isinstance(c, dict):
-            h, bt, hp = _write_group(img, c)
+            h, bt, hp = _write_group(img, c, chunks)
             entries[n] = (h, (bt, hp))
         else:
-            entries[n] = (_write_dataset(img, c), None)
+            entries[n] = (_write_dataset(img, c, chunks), None)
     # local heap: "" at offset 0, the names, then one free block
     heap_data = bytearray(b"\0" * 8)
     offs = {}
@@ -206,11 +283,13 @@ def _tree(datasets: dict) -> dict:
     return root
 
 
-def write_file(path, datasets: dict) -> None:
+def write_file(path, datasets: dict, chunks=None) -> None:
     """Writes ``{'group/sub/name': array}`` as a new HDF5 file at ``path``
-    (replacing it atomically: the file appears complete or not at all)."""
+    (replacing it atomically: the file appears complete or not at all).
+    ``chunks=n`` stores every non-scalar dataset in chunks of n rows,
+    shuffled and deflate-compressed."""
     img = _Image()
-    h, bt, hp = _write_group(img, _tree(datasets))
+    h, bt, hp = _write_group(img, _tree(datasets), chunks)
     sb = SIGNATURE + bytes([0, 0, 0, 0, 0, 8, 8, 0]) + struct.pack("<HHI", LEAF_K, NODE_K, 0)
     sb += struct.pack("<QQQQ", 0, UNDEF, len(img.b), UNDEF) + _entry(0, h, (bt, hp))
     img.put(0, sb)
@@ -262,7 +341,7 @@ class _Reader:
             raise ValueError("bad local heap")
         seg, = self.u("Q", heap + 24)
         s = seg + off
-        return self.b[s:self.b.index(b"\0", s)].decode()
+        return bytes(self.b[s:self.b.find(b"\0", s)]).decode()
 
     def members(self, btree, heap):
         out, stack = {}, [btree]
@@ -305,6 +384,8 @@ class _Reader:
         if self.b[lay] != 3:
             raise NotImplementedError(f"layout message version {self.b[lay]}")
         n = int(np.prod(shape)) if rank else 1
+        if self.b[lay + 1] == 2:
+            return self._chunked(t, lay, shape, dt)
         if self.b[lay + 1] == 1:
             addr, _ = self.u("QQ", lay + 2)
             raw = b"" if addr == UNDEF else self.b[addr:addr + n * size]
@@ -314,8 +395,171 @@ class _Reader:
             nbytes, = self.u("H", lay + 2)
             raw = self.b[lay + 4:lay + 4 + nbytes]
         else:
-            raise NotImplementedError("chunked storage")
+            raise NotImplementedError(f"layout class {self.b[lay + 1]}")
         return np.frombuffer(raw, dtype=dt, count=n).reshape(shape).astype(dt.newbyteorder("="))
+
+    def _filters(self, t):
+        """[(filter id, client data)] of the filter pipeline message, in order."""
+        if _MSG_FILTERS not in t:
+            return []
+        _, p, _ = t[_MSG_FILTERS]
+        ver, nf = self.b[p], self.b[p + 1]
+        q = p + (8 if ver == 1 else 2)
+        out = []
+        for _ in range(nf):
+            fid, = self.u("H", q)
+            q += 2
+            nlen = 0
+            if ver == 1 or fid >= 256:
+                nlen, = self.u("H", q)
+                q += 2
+            _flags, ncd = self.u("HH", q)
+            q += 4
+            if ver == 1:
+                q += (nlen + 7) & ~7
+            else:
+                q += nlen
+            cd = list(self.u(f"{ncd}I", q)) if ncd else []
+            q += 4 * ncd
+            if ver == 1 and ncd % 2:
+                q += 4
+            out.append((fid, cd))
+        return out
+
+    def _chunked(self, t, lay, shape, dt):
+        dims = self.b[lay + 2]
+        btree, = self.u("Q", lay + 3)
+        cd = [self.u("I", lay + 11 + 4 * i)[0] for i in range(dims)]
+        cdims, esize = cd[:-1], cd[-1]
+        rank = len(shape)
+        filters = self._filters(t)
+        out = np.zeros(shape, dtype=dt.newbyteorder("="))
+        if btree == UNDEF:
+            return out
+        key_bytes = 8 + 8 * dims
+        stack = [btree]
+        while stack:
+            node = stack.pop()
+            if self.b[node:node + 4] != b"TREE" or self.b[node + 4] != 1:
+                raise ValueError("bad chunk B-tree node")
+            level, used = self.b[node + 5], self.u("H", node + 6)[0]
+            p = node + 24
+            for _ in range(used):
+                size, mask = self.u("II", p)
+                offs = self.u(f"{rank}Q", p + 8)
+                child, = self.u("Q", p + key_bytes)
+                p += key_bytes + 8
+                if level > 0:
+                    stack.append(child)
+                    continue
+                raw = self.b[child:child + size]
+                for k in range(len(filters) - 1, -1, -1):
+                    fid, cdv = filters[k]
+                    if mask & (1 << k):
+                        continue
+                    if fid == FILTER_DEFLATE:
+                        raw = zlib.decompress(raw)
+                    elif fid == FILTER_SHUFFLE:
+                        es = cdv[0] if cdv else esize
+                        a = np.frombuffer(raw, np.uint8)
+                        m = len(a) // es
+                        raw = a[:m * es].reshape(es, m).T.tobytes() + a[m * es:].tobytes()
+                    elif fid == FILTER_FLETCHER32:
+                        raw = raw[:-4]
+                    else:
+                        raise NotImplementedError(f"HDF5 filter {fid}")
+                block = np.frombuffer(raw, dtype=dt, count=int(np.prod(cdims))).reshape(cdims)
+                sl_out = tuple(slice(o, min(o + c, s)) for o, c, s in zip(offs, cdims, shape))
+                sl_in = tuple(slice(0, x.stop - x.start) for x in sl_out)
+                out[sl_out] = block[sl_in]
+        return out
+
+
+class File:
+    """Read access to one HDF5 file by dataset path, the file memory-mapped
+    (a dataset's bytes are read when it is asked for)."""
+
+    def __init__(self, path):
+        self._f = open(path, "rb")
+        try:
+            self._m = mmap.mmap(self._f.fileno(), 0, access=mmap.ACCESS_READ)
+            self.r = _Reader(self._m)
+        except Exception:
+            self.close()
+            raise
+
+    def close(self):
+        for x in ("_m", "_f"):
+            obj = getattr(self, x, None)
+            if obj is not None:
+                obj.close()
+                setattr(self, x, None)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _find(self, path):
+        addr = self.r.root
+        for part in [p for p in str(path).split("/") if p]:
+            msgs = self.r.messages(addr)
+            st = [m for m in msgs if m[0] == _MSG_SYMBOL_TABLE]
+            if not st:
+                raise KeyError(f"'{path}': '{part}' is inside a dataset")
+            members = self.r.members(*self.r.u("QQ", st[0][1]))
+            if part not in members:
+                raise KeyError(f"Unable to open object '{part}' (no such member in '{path}')")
+            addr = members[part]
+        return addr
+
+    def keys(self, group=""):
+        msgs = self.r.messages(self._find(group))
+        st = [m for m in msgs if m[0] == _MSG_SYMBOL_TABLE]
+        if not st:
+            raise KeyError(f"'{group}' is not a group")
+        return sorted(self.r.members(*self.r.u("QQ", st[0][1])))
+
+    def __contains__(self, path):
+        try:
+            self._find(path)
+            return True
+        except KeyError:
+            return False
+
+    def read(self, path):
+        msgs = self.r.messages(self._find(path))
+        if not any(m[0] == _MSG_LAYOUT for m in msgs):
+            raise KeyError(f"'{path}' is not a dataset")
+        return self.r.dataset(msgs)
+
+    def contiguous_extent(self, path):
+        """(file offset, bytes, dtype, shape) of a contiguous dataset, else None."""
+        msgs = self.r.messages(self._find(path))
+        t = {m[0]: m for m in msgs}
+        if _MSG_LAYOUT not in t or _MSG_FILTERS in t:
+            return None
+        _, lay, _ = t[_MSG_LAYOUT]
+        if self.r.b[lay] != 3 or self.r.b[lay + 1] != 1:
+            return None
+        addr, nbytes = self.r.u("QQ", lay + 2)
+        if addr == UNDEF:
+            return None
+        _, d, _ = t[_MSG_DATASPACE]
+        ver, rank = self.r.b[d], self.r.b[d + 1]
+        dims_at = d + (8 if ver == 1 else 4)
+        shape = tuple(self.r.u("Q", dims_at + 8 * i)[0] for i in range(rank))
+        _, a, _ = t[_MSG_DATATYPE]
+        cls, bits, size = self.r.b[a] & 0x0F, self.r.b[a + 1], self.r.u("I", a + 4)[0]
+        order = ">" if bits & 1 else "<"
+        if cls == 1:
+            dt = np.dtype(f"{order}f{size}")
+        elif cls == 0:
+            dt = np.dtype(f"{order}{'i' if bits & 0x08 else 'u'}{size}")
+        else:
+            return None
+        return addr, nbytes, dt, shape
 
 
 def read_file(path) -> dict:
