@@ -78,13 +78,38 @@ class _Reader:
             r1 = max(r0, r1)
             row_bytes = nbytes // rows if rows else 0
             host = torch.empty((r1 - r0) * row_bytes, dtype=torch.uint8, pin_memory=True)
-            with open(self.path, "rb") as fh:
-                fh.seek(off + r0 * row_bytes)
-                fh.readinto(memoryview(host.numpy()))
+            _pread_into(self.path, off + r0 * row_bytes, memoryview(host.numpy()))
             arr = host.numpy().view(dt.newbyteorder("=")).reshape((r1 - r0,) + tuple(shape[1:]))
             return torch.from_numpy(arr).to(device, non_blocking=True)
         a = np.ascontiguousarray(self.read(path, cut))
         return torch.from_numpy(a).pin_memory().to(device, non_blocking=True)
+
+
+_PREAD_PART = 8 << 20
+
+
+def _pread_into(path, offset, mv):
+    """Fill ``mv`` from ``path`` at ``offset``; large ranges are read in
+    parallel slices of 8 MB (the reads release the GIL)."""
+    n = len(mv)
+    fd = os.open(path, os.O_RDONLY)
+    try:
+        def part(a, b):
+            while a < b:
+                got = os.preadv(fd, [mv[a:b]], offset + a)
+                if got <= 0:
+                    raise OSError(f"short read of {path} at {offset + a}")
+                a += got
+
+        if n <= 2 * _PREAD_PART:
+            part(0, n)
+            return
+        import concurrent.futures as cf
+        cuts = list(range(0, n, _PREAD_PART)) + [n]
+        with cf.ThreadPoolExecutor(max_workers=min(8, len(cuts) - 1)) as ex:
+            list(ex.map(lambda ab: part(*ab), zip(cuts[:-1], cuts[1:])))
+    finally:
+        os.close(fd)
 
 
 def _concat(parts, stack):
