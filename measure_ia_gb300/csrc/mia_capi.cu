@@ -33,6 +33,11 @@ namespace {
 
 size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// Bytes of a dataset's fixed-point sums: (2 (1+J) + 2) nb sums of acc_words words.
+size_t acc_bytes(const Plan& p) {
+  return sizeof(long long) * (size_t)p.acc_words * (size_t)p.nb * (2 * ((size_t)p.J + 1) + 2);
+}
+
 }  // namespace
 
 bool make_plan(const mia_config* cfg, long long n_pos, long long n_shape, Plan* pl, const char** why) {
@@ -179,8 +184,10 @@ bool make_plan(const mia_config* cfg, long long n_pos, long long n_shape, Plan* 
   take(p.off_wu, sizeof(WorkUnit) * (size_t)p.n_wu_max);
   take(p.off_reg, (size_t)(p.J + 1) * 48 + 64);
   take(p.off_edges, sizeof(int2) * (size_t)p.edge_capacity);
-  // mixed form: 64-bit fixed-point sums (w and S+D per region, SxD and var)
-  take(p.off_acc, mixed ? sizeof(long long) * (size_t)p.nb * (2 * ((size_t)p.J + 1) + 2) : 0);
+  // fixed-point sums (w and S+D per region, SxD and var): one 64-bit word per
+  // sum in the mixed form, two (128-bit) in the FP64 form
+  p.acc_words = mixed ? 1 : 2;
+  take(p.off_acc, acc_bytes(p));
   p.total = o;
   return true;
 }
@@ -218,10 +225,11 @@ void bind_work(const Plan& p, void* base, Work* w) {
   w->reg.r1 = reinterpret_cast<long long*>(reg + 32 * J1);
   w->reg.r2 = reinterpret_cast<long long*>(reg + 40 * J1);
   long long* acc = reinterpret_cast<long long*>(b + p.off_acc);
+  const size_t aw = (size_t)p.acc_words;
   w->acc_dd = acc;
-  w->acc_sp = acc + J1 * p.nb;
-  w->acc_sx = acc + 2 * J1 * p.nb;
-  w->acc_vr = acc + (2 * J1 + 1) * p.nb;
+  w->acc_sp = acc + aw * J1 * p.nb;
+  w->acc_sx = acc + aw * 2 * J1 * p.nb;
+  w->acc_vr = acc + aw * (2 * J1 + 1) * p.nb;
 }
 
 // Bind the per-galaxy arrays once the sample sizes are known.
@@ -707,9 +715,7 @@ int mia_batch_enqueue(mia_context* ctx, const mia_config* cfg, int n, const mia_
     MIA_CUDA(cudaMemsetAsync(&d.w.status->bad_index, 0xFF, sizeof(unsigned long long), st));
     MIA_CUDA(cudaMemsetAsync(base + pl.off_pcount, 0, pl.off_tiles - pl.off_pcount, st));
     MIA_CUDA(cudaMemsetAsync(base + pl.off_reg, 0, (size_t)(pl.J + 1) * 48 + 64, st));
-    if (P.precision == MIA_MIXED)
-      MIA_CUDA(cudaMemsetAsync(base + pl.off_acc, 0,
-                               sizeof(long long) * (size_t)pl.nb * (2 * ((size_t)pl.J + 1) + 2), st));
+    MIA_CUDA(cudaMemsetAsync(base + pl.off_acc, 0, acc_bytes(pl), st));
     MIA_CUDA(cudaMemsetAsync(results[i].out, 0, sizeof(double) * (size_t)lay.total, st));
     MIA_CUDA(cudaMemsetAsync(results[i].npairs, 0, sizeof(unsigned long long) * J1 * nb, st));
     MIA_CUDA(launch_prep(pl, P, cats[i], d.w, st));
@@ -725,10 +731,8 @@ int mia_batch_enqueue(mia_context* ctx, const mia_config* cfg, int n, const mia_
   for (int i = 0; i < n; ++i) {
     Dataset d;
     make_dataset(bp.plans[i], b + bp.off[i], cats[i], results[i], lay, &d);
-    if (P.precision == MIA_MIXED) {
-      MIA_CUDA(launch_edge_retest(P, d.w, d.o, st, ctx->num_sms));
-      MIA_CUDA(launch_fixed_out(P, d.w, d.o, st));  // exact fixed-point sums -> the output doubles
-    }
+    if (P.precision == MIA_MIXED) MIA_CUDA(launch_edge_retest(P, d.w, d.o, st, ctx->num_sms));
+    MIA_CUDA(launch_fixed_out(P, d.w, d.o, st));  // exact fixed-point sums -> the output doubles
     MIA_CUDA(launch_post(P, d.w, lay, results[i].out, cfg->volume, cats[i].n_pos, cats[i].n_shape, st));
   }
   ctx->err.clear();

@@ -96,6 +96,7 @@ struct Plan {
   size_t off_reg;
   size_t off_edges;
   size_t off_acc;
+  int acc_words;        // 64-bit words per fixed-point sum: 1 (mixed form) or 2 (FP64 form)
   size_t total;
 };
 
@@ -128,6 +129,79 @@ __device__ inline double region_scale(unsigned long long maxws_bits, long long n
   return ldexp(1.0, e);
 }
 
+// ---- exact 128-bit fixed-point sums (FP64 form) ------------------------------
+//
+// A term v enters a sum as the integer nearest v * 2^E (ties away from zero),
+// a two's-complement 128-bit value in two 64-bit words (lo, hi).  E is chosen
+// per dataset so that the largest possible term is at most 2^88: a term keeps
+// every bit down to 2^-88 of the largest one, and a sum has room for 2^38
+// terms of the largest size.  Adding the words is exact and commutative, so a
+// sum does not depend on the order in which the pairs arrive; it is rounded
+// to a double once, at the end.  Infinities and NaNs cannot be represented and
+// are left to the caller (they go to the output doubles directly, so that a
+// bin holding one reads inf or NaN as a plain sum would).
+struct Fix128 {
+  unsigned long long lo, hi;
+};
+
+// E with m * 2^E <= 2^88 (m > 0 finite), limited so that 2^-E is a normal double.
+__device__ inline int fix128_exponent(double m) {
+  if (!(m > 0.0) || !(m < 1e300)) m = 1.0;
+  const int e = ilogb(309485009821345068724781056.0 / m);  // 2^88
+  return e > 1000 ? 1000 : (e < -1000 ? -1000 : e);
+}
+
+// v * 2^E to the nearest integer, from v's bit fields (integer arithmetic
+// only); false when v is not finite or |v| 2^E reaches 2^126.
+__device__ __forceinline__ bool to_fix128(double v, int E, Fix128& f) {
+  const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+  const int be = (int)((bits >> 52) & 0x7ff);
+  unsigned long long mant = bits & 0xFFFFFFFFFFFFFull;
+  f.lo = 0;
+  f.hi = 0;
+  if (be == 0x7ff) return false;
+  if (be) mant |= 1ull << 52;
+  const int sh = (be ? be : 1) - 1075 + E;  // |v| 2^E = mant 2^sh
+  if (sh >= 0) {
+    if (sh > 126 - 53) return false;
+    if (sh >= 64) {
+      f.hi = mant << (sh - 64);
+    } else {
+      f.lo = mant << sh;
+      f.hi = sh ? mant >> (64 - sh) : 0ull;
+    }
+  } else if (sh > -64) {
+    const int s = -sh;
+    f.lo = (mant + (1ull << (s - 1))) >> s;   // mant < 2^53: no overflow
+  }
+  if (bits >> 63) {
+    f.lo = ~f.lo + 1ull;
+    f.hi = ~f.hi + (f.lo == 0ull ? 1ull : 0ull);
+  }
+  return true;
+}
+
+// a[0..1] += f with 64-bit atomics: the carry out of the low word is read
+// from the value the low-word add returned, so concurrent adds never lose one.
+__device__ __forceinline__ void add_fix128(unsigned long long* a, const Fix128& f) {
+  const unsigned long long old = atomicAdd(a, f.lo);
+  const unsigned long long c = f.hi + (old + f.lo < old ? 1ull : 0ull);
+  if (c) atomicAdd(a + 1, c);
+}
+
+// The sum (lo, hi) times inv (= 2^-E) as a double: the magnitude's two words
+// are converted and added in round-to-nearest (deterministic; within 2 ulp).
+__device__ __forceinline__ double fix128_value(unsigned long long lo, unsigned long long hi, double inv) {
+  const bool neg = (long long)hi < 0;
+  if (neg) {
+    lo = ~lo + 1ull;
+    hi = ~hi + (lo == 0ull ? 1ull : 0ull);
+  }
+  double m = __dadd_rn(__dmul_rn(__ull2double_rn(hi), 18446744073709551616.0), __ull2double_rn(lo));
+  m = __dmul_rn(m, inv);
+  return neg ? -m : m;
+}
+
 // Fixed-point scales of one dataset (powers of two), from its largest weight
 // product m = max|w_p| * max(|w_s|, |w_s e|) and responsivity R:
 //   S+D, SxD : |term| * 2^S <= 2^30 -- signed terms, typically a few per cent
@@ -146,6 +220,8 @@ struct Scales {
   float sc_dd, sc_sp, c_vr;
   double inv_dd, inv_sp, inv_vr;
   double sd_dd, sd_sp, sd_vr;   // the scales as doubles (edge re-test)
+  int e128, e128v;              // FP64 form: 128-bit fixed-point exponents (w, S+D, SxD; variance)
+  double inv128, inv128v;       // 2^-e128, 2^-e128v
 };
 
 __device__ inline Scales dataset_scales(const Status* st, double twoR) {
@@ -169,6 +245,10 @@ __device__ inline Scales dataset_scales(const Status* st, double twoR) {
   sc.inv_dd = ldexp(1.0, -Sdd);
   sc.inv_sp = ldexp(1.0, -Ssp);
   sc.inv_vr = ldexp(1.0, -Svr);
+  sc.e128 = fix128_exponent(m);
+  sc.e128v = fix128_exponent(mv);
+  sc.inv128 = ldexp(1.0, -sc.e128);
+  sc.inv128v = ldexp(1.0, -sc.e128v);
   return sc;
 }
 
@@ -222,9 +302,10 @@ struct Work {
   WorkUnit* wu;
   RegionStats reg;
   int2* edges;
-  // mixed form: exact 64-bit fixed-point sums of every pair's terms, in the
-  // dataset's scales (dataset_scales): w and S+D for all pairs and each
-  // jackknife region ((1+J) * nb), SxD and the variance terms (nb)
+  // exact fixed-point sums of every pair's terms, in the dataset's scales
+  // (dataset_scales): w and S+D for all pairs and each jackknife region
+  // ((1+J) * nb), SxD and the variance terms (nb).  Mixed form: one 64-bit
+  // word per sum; FP64 form: two (Fix128 lo, hi) per sum
   long long *acc_dd, *acc_sp, *acc_sx, *acc_vr;
   long long edge_capacity;
 };

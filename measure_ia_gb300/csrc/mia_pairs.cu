@@ -39,10 +39,10 @@ __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(
 //   mixed: cnt, dd lo, sp lo, sx lo (+ var lo) replicated; the high words of
 //          the 64-bit sums (dd, sp, sx (+ var)) once per (slot, bin): only
 //          carries reach them, so they need no copies
-//   fp64 : cnt (u32) + dd, sp, sx (+ var) doubles, hw = knb
+//   fp64 : cnt (u32) + dd, sp, sx (+ var) 128-bit sums (Fix128), hw = knb
 __host__ __device__ inline size_t hist_u32_words(int hw, int knb, int mixed, int var) {
   if (mixed) return (size_t)hw * (4 + var) + (size_t)knb * (3 + var);
-  return (size_t)hw * (1 + 6 + 2 * var) + 4;
+  return (size_t)hw * (1 + 4 * (3 + var)) + 4;
 }
 
 struct TablesSmem {
@@ -65,7 +65,7 @@ __host__ __device__ inline SmemLayout smem_layout(int J, int spu, int hw, int kn
   L.slot_region = o;
   o = align16(o + sizeof(int) * kMaxSlots);
   L.shapes = o;
-  o = align16(o + (size_t)spu * (mixed ? 48 : 56));
+  o = align16(o + (size_t)spu * (mixed ? 48 : 60));
   L.seg_begin = o;
   o = align16(o + sizeof(int) * kSegsPerPass);
   L.seg_pref = o;
@@ -119,25 +119,38 @@ __device__ __forceinline__ void acc_global_fixed(const Work& w, const Out& o, in
   }
 }
 
+// One term of the FP64 form into a dataset sum: its 128-bit fixed-point value
+// into acc[2 i], or, when the term is not finite, the term itself into the
+// output double out[i] (which the sums are added to at the end).
+__device__ __forceinline__ void add_term(long long* acc, double* out, size_t i, double v, int E) {
+  Fix128 f;
+  if (to_fix128(v, E, f))
+    add_fix128(reinterpret_cast<unsigned long long*>(acc) + 2 * i, f);
+  else
+    atomicAdd(&out[i], v);
+}
+
 // Direct global accumulation in the plain FP64 form (pairs whose position
-// region has no slot).
-__device__ __forceinline__ void acc_global(const Out& o, int nb, int J, int a, int b, int bin, double dd, double sp,
-                                           double sx, double var, int want_var) {
+// region has no slot, or with a term that is not finite): count plus exact
+// 128-bit sums, for all pairs, region a and region b != a.
+__device__ __forceinline__ void acc_global(const Work& w, const Out& o, const Scales& sc, int nb, int J, int a, int b,
+                                           int bin, double dd, double sp, double sx, double var, int want_var) {
+  const int E = sc.e128;
   atomicAdd(&o.npairs[bin], 1ULL);
-  atomicAdd(&o.dd[bin], dd);
-  atomicAdd(&o.splus[bin], sp);
-  atomicAdd(&o.scross[bin], sx);
-  if (want_var) atomicAdd(&o.variance[bin], var);
+  add_term(w.acc_dd, o.dd, bin, dd, E);
+  add_term(w.acc_sp, o.splus, bin, sp, E);
+  add_term(w.acc_sx, o.scross, bin, sx, E);
+  if (want_var) add_term(w.acc_vr, o.variance, bin, var, sc.e128v);
   if (J > 0) {
     size_t ia = (size_t)(1 + a) * nb + bin;
     atomicAdd(&o.npairs[ia], 1ULL);
-    atomicAdd(&o.dd[ia], dd);
-    atomicAdd(&o.splus[ia], sp);
+    add_term(w.acc_dd, o.dd, ia, dd, E);
+    add_term(w.acc_sp, o.splus, ia, sp, E);
     if (b != a) {
       size_t ib = (size_t)(1 + b) * nb + bin;
       atomicAdd(&o.npairs[ib], 1ULL);
-      atomicAdd(&o.dd[ib], dd);
-      atomicAdd(&o.splus[ib], sp);
+      add_term(w.acc_dd, o.dd, ib, dd, E);
+      add_term(w.acc_sp, o.splus, ib, sp, E);
     }
   }
 }
@@ -402,7 +415,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
   unsigned* h_cnt = hist;
   unsigned *dd_lo = nullptr, *sp_lo = nullptr, *sx_lo = nullptr, *vr_lo = nullptr;
   int *dd_hi = nullptr, *sp_hi = nullptr, *sx_hi = nullptr, *vr_hi = nullptr;
-  double *dd_d = nullptr, *sp_d = nullptr, *sx_d = nullptr, *vr_d = nullptr;
+  unsigned long long *dd_q = nullptr, *sp_q = nullptr, *sx_q = nullptr, *vr_q = nullptr;  // Fix128 pairs
   if (MIXED) {
     dd_lo = hist + KB;
     sp_lo = hist + 2 * KB;
@@ -415,16 +428,16 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
     sx_hi = hi + 2 * knb;
     if (VAR) vr_hi = hi + 3 * knb;
   } else {
-    // doubles start at an 8-byte boundary after the counts
+    // 128-bit sums (two 64-bit words each) start at a 16-byte boundary after the counts
     size_t off = align16(sizeof(unsigned) * (size_t)KB);
-    double* base = reinterpret_cast<double*>(reinterpret_cast<unsigned char*>(hist) + off);
-    dd_d = base;
-    sp_d = base + KB;
-    sx_d = base + 2 * KB;
-    if (VAR) vr_d = base + 3 * KB;
+    unsigned long long* base = reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(hist) + off);
+    dd_q = base;
+    sp_q = base + 2 * KB;
+    sx_q = base + 4 * KB;
+    if (VAR) vr_q = base + 6 * KB;
   }
   const int hist_u32 = MIXED ? (int)hist_u32_words(KB, K * nb, 1, VAR)
-                             : (int)(align16(sizeof(unsigned) * (size_t)KB) / 4) + KB * 2 * (3 + VAR);
+                             : (int)(align16(sizeof(unsigned) * (size_t)KB) / 4) + KB * 4 * (3 + VAR);
 
   // rows of position cells: fine-grid extents along d1 and d2 around a shape cell
   const int N1 = P.full[1] ? P.nf[1] : P.m[1] + 2 * P.Rf[1];
@@ -573,17 +586,33 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
         Z[rank] = z;
       }
     } else {
+      // FP64 form: the unit's shapes in line-of-sight order too (the sums are
+      // order-free), with their line-of-sight coordinates in FP32 for the window
       double* D = reinterpret_cast<double*>(smem + SL.shapes);
       const int M = P.shapes_per_unit;
-      for (int i = tid; i < S; i += blockDim.x) {
-        int g = u.begin + i;
-        D[i] = w.sx[g];
-        D[M + i] = w.sy[g];
-        D[2 * M + i] = w.sz[g];
-        D[3 * M + i] = w.sax[g];
-        D[4 * M + i] = w.say[g];
-        D[5 * M + i] = w.se[g];
-        D[6 * M + i] = w.sws[g];
+      float* Z = reinterpret_cast<float*>(D + 7 * M);
+      float* zs = reinterpret_cast<float*>(seg_begin);  // free until the segments are built
+      const int g = u.begin + tid;
+      float z = 0.f;
+      if (tid < S) {
+        z = (float)w.sz[g];
+        zs[tid] = z;
+      }
+      __syncthreads();
+      if (tid < S) {
+        int rank = 0;
+        for (int j = 0; j < S; ++j) {
+          const float zj = zs[j];
+          rank += (zj < z || (zj == z && j < tid)) ? 1 : 0;
+        }
+        D[rank] = w.sx[g];
+        D[M + rank] = w.sy[g];
+        D[2 * M + rank] = w.sz[g];
+        D[3 * M + rank] = w.sax[g];
+        D[4 * M + rank] = w.say[g];
+        D[5 * M + rank] = w.se[g];
+        D[6 * M + rank] = w.sws[g];
+        Z[rank] = z;
       }
     }
     __syncthreads();
@@ -761,14 +790,49 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
         int seg = 0;
         const double* D = reinterpret_cast<const double*>(smem + SL.shapes);
         const int M = P.shapes_per_unit;
-        for (int t = tid; t < total; t += blockDim.x) {
-          while (t >= seg_pref[seg + 1]) ++seg;
-          const int pidx = seg_begin[seg] + (t - seg_pref[seg]);
-          const int plab = w.plab_s[pidx];
+        const float* Z = reinterpret_cast<const float*>(D + 7 * M);
+        // warp-uniform iterations, so that a warp's lanes can agree on one shape range
+        for (int tb = 0; tb < total; tb += blockDim.x) {
+          const int t = tb + tid;
+          int pidx = 0, code = 13;
+          if (t < total) {
+            while (t >= seg_pref[seg + 1]) ++seg;
+            pidx = seg_begin[seg] + (t - seg_pref[seg]);
+            code = seg_shift[seg];
+          }
+          const int plab = t < total ? w.plab_s[pidx] : 0;
           const int slot = slot_of[plab];
           const int base = slot * nb;
           const double qx = w.px[pidx], qy = w.py[pidx], qz = w.pz[pidx], pw = w.pw[pidx];
-          for (int i = 0; i < S; ++i) {
+          // the shapes that can bin with this position: the same conservative
+          // FP32 window over the line-of-sight order as the mixed form (the
+          // position's image next to the cell: code from the row's shift).
+          // Every decision below stays the exact FP64 one.
+          int i_lo = S, i_hi = 0;
+          if (t < total) {
+            if (FULL && P.full[2]) {
+              i_lo = 0;
+              i_hi = S;
+            } else {
+              float win = P.zwin;
+              if (!FULL) {
+                const float px = (float)(qx + (code % 3 - 1) * P.L), py = (float)(qy + ((code / 3) % 3 - 1) * P.L);
+                const float gx = fmaxf(0.0f, fmaxf(s_box[0] - px, px - s_box[1]));
+                const float gy = fmaxf(0.0f, fmaxf(s_box[2] - py, py - s_box[3]));
+                const float g2 = fmaf(gx, gx, gy * gy);
+                if (g2 > P.q_cut) {
+                  win = -1.0f;
+                } else if (KIND == MIA_KIND_MULTIPOLES) {
+                  win = fminf(win, sqrtf(fmaxf(P.q_cut - g2, 0.0f) + 1e-4f * P.q_cut) + P.zwin - P.range_los32);
+                }
+              }
+              if (win >= 0.0f) z_window(Z, S, (float)(qz + (code / 9 - 1) * P.L), win, i_lo, i_hi);
+            }
+          }
+          const int wlo = __reduce_min_sync(0xffffffffu, i_lo);
+          const int whi = __reduce_max_sync(0xffffffffu, i_hi);
+          if (t >= total) continue;
+          for (int i = wlo; i < whi; ++i) {
             PairResult r = pair_exact(P, *w.tables, D[i], D[M + i], D[2 * M + i], D[3 * M + i], D[4 * M + i],
                                       D[5 * M + i], qx, qy, qz);
             if (r.bin < 0) continue;
@@ -777,16 +841,22 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
             const double sx = __dmul_rn(ww, r.ex);
             double tv = 0.0;
             if (VAR) tv = __ddiv_rn(sp, twoR);
-            if (slot >= 0) {
+            const double vr = __dmul_rn(tv, tv);
+            Fix128 fd, fp, fx, fv;
+            bool ok = to_fix128(ww, sc.e128, fd);
+            ok &= to_fix128(sp, sc.e128, fp);
+            ok &= to_fix128(sx, sc.e128, fx);
+            if (VAR) ok &= to_fix128(vr, sc.e128v, fv);
+            if (slot >= 0 && ok) {
               const int hi = base + r.bin;
               atomicAdd(&h_cnt[hi], 1u);
-              atomicAdd(&dd_d[hi], ww);
-              atomicAdd(&sp_d[hi], sp);
-              atomicAdd(&sx_d[hi], sx);
-              if (VAR) atomicAdd(&vr_d[hi], __dmul_rn(tv, tv));
+              add_fix128(dd_q + 2 * hi, fd);
+              add_fix128(sp_q + 2 * hi, fp);
+              add_fix128(sx_q + 2 * hi, fx);
+              if (VAR) add_fix128(vr_q + 2 * hi, fv);
             } else {
-              acc_global(o, nb, P.J, u.label, plab, r.bin, ww, sp, sx, __dmul_rn(tv, tv), VAR);
-              atomicOr(&w.status->flags, kStatusNoSlot);
+              acc_global(w, o, sc, nb, P.J, u.label, plab, r.bin, ww, sp, sx, vr, VAR);
+              if (slot < 0) atomicOr(&w.status->flags, kStatusNoSlot);
               ++my_binned;
             }
           }
@@ -838,22 +908,27 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
           }
         }
       } else {
-        const double dd = dd_d[idx], sp = sp_d[idx], sx = sx_d[idx], vr = VAR ? vr_d[idx] : 0.0;
-        atomicAdd(&o.npairs[bin], (unsigned long long)cnt);
-        atomicAdd(&o.dd[bin], dd);
-        atomicAdd(&o.splus[bin], sp);
-        atomicAdd(&o.scross[bin], sx);
-        if (VAR) atomicAdd(&o.variance[bin], vr);
+        // the unit's exact 128-bit partials into the dataset's sums
+        typedef unsigned long long u64;
+        const Fix128 vd{dd_q[2 * idx], dd_q[2 * idx + 1]}, vp{sp_q[2 * idx], sp_q[2 * idx + 1]},
+            vx{sx_q[2 * idx], sx_q[2 * idx + 1]};
+        u64* const add = reinterpret_cast<u64*>(w.acc_dd);
+        u64* const asp = reinterpret_cast<u64*>(w.acc_sp);
+        atomicAdd(&o.npairs[bin], (u64)cnt);
+        add_fix128(add + 2 * bin, vd);
+        add_fix128(asp + 2 * bin, vp);
+        add_fix128(reinterpret_cast<u64*>(w.acc_sx) + 2 * bin, vx);
+        if (VAR) add_fix128(reinterpret_cast<u64*>(w.acc_vr) + 2 * bin, Fix128{vr_q[2 * idx], vr_q[2 * idx + 1]});
         if (P.J > 0) {
-          size_t ia = (size_t)(1 + a) * nb + bin;
-          atomicAdd(&o.npairs[ia], (unsigned long long)cnt);
-          atomicAdd(&o.dd[ia], dd);
-          atomicAdd(&o.splus[ia], sp);
+          const size_t ia = (size_t)(1 + a) * nb + bin;
+          atomicAdd(&o.npairs[ia], (u64)cnt);
+          add_fix128(add + 2 * ia, vd);
+          add_fix128(asp + 2 * ia, vp);
           if (b != a) {
-            size_t ibb = (size_t)(1 + b) * nb + bin;
-            atomicAdd(&o.npairs[ibb], (unsigned long long)cnt);
-            atomicAdd(&o.dd[ibb], dd);
-            atomicAdd(&o.splus[ibb], sp);
+            const size_t ibb = (size_t)(1 + b) * nb + bin;
+            atomicAdd(&o.npairs[ibb], (u64)cnt);
+            add_fix128(add + 2 * ibb, vd);
+            add_fix128(asp + 2 * ibb, vp);
           }
         }
       }
@@ -893,17 +968,33 @@ __global__ void k_edge_retest(Params P, Work w, Out o) {
   if ((threadIdx.x & 31) == 0 && binned) atomicAdd(&w.status->binned, binned);
 }
 
-// Mixed form: the dataset's exact fixed-point sums into the output doubles
-// (w and S+D per region, SxD and the variance terms), before post-processing.
+// The dataset's exact fixed-point sums into the output doubles (w and S+D per
+// region, SxD and the variance terms), before post-processing.  Mixed form:
+// 64-bit sums.  FP64 form: 128-bit sums, added to what the output doubles
+// already hold (the terms that were not finite, else zero).
 __global__ void k_fixed_out(Params P, Work w, Out o) {
   const Scales sc = dataset_scales(w.status, dataset_twoR(w.reg, P.J));
   const int n1 = (1 + P.J) * P.nb;
+  typedef unsigned long long u64;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n1; i += gridDim.x * blockDim.x) {
-    o.dd[i] = (double)w.acc_dd[i] * sc.inv_dd;
-    o.splus[i] = (double)w.acc_sp[i] * sc.inv_sp;
-    if (i < P.nb) {
-      o.scross[i] = (double)w.acc_sx[i] * sc.inv_sp;
-      if (P.want_variance) o.variance[i] = (double)w.acc_vr[i] * sc.inv_vr;
+    if (P.precision == MIA_MIXED) {
+      o.dd[i] = (double)w.acc_dd[i] * sc.inv_dd;
+      o.splus[i] = (double)w.acc_sp[i] * sc.inv_sp;
+      if (i < P.nb) {
+        o.scross[i] = (double)w.acc_sx[i] * sc.inv_sp;
+        if (P.want_variance) o.variance[i] = (double)w.acc_vr[i] * sc.inv_vr;
+      }
+    } else {
+      auto val = [&](const long long* a, double inv) {
+        const u64* q = reinterpret_cast<const u64*>(a) + 2 * (size_t)i;
+        return fix128_value(q[0], q[1], inv);
+      };
+      o.dd[i] = __dadd_rn(val(w.acc_dd, sc.inv128), o.dd[i]);
+      o.splus[i] = __dadd_rn(val(w.acc_sp, sc.inv128), o.splus[i]);
+      if (i < P.nb) {
+        o.scross[i] = __dadd_rn(val(w.acc_sx, sc.inv128), o.scross[i]);
+        if (P.want_variance) o.variance[i] = __dadd_rn(val(w.acc_vr, sc.inv128v), o.variance[i]);
+      }
     }
   }
 }
