@@ -531,6 +531,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
                 slot_region[ns++] = reg;
               }
             }
+        // positions on a sub-box face carry region 0 wherever they are
         if (slot_of[0] < 0 && ns < K) {
           slot_of[0] = ns;
           slot_region[ns++] = 0;

@@ -184,3 +184,43 @@ def test_multipoles_rp_cut(i, precision):
     rtol = FP64_RTOL if precision == "fp64" else MIXED_RTOL
     _close(m["DD"], c.DD, rtol, "DD")
     _close(m["splusd"], c.SplusD, rtol, "S+D")
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("kind", ["w", "m"])
+def test_positions_on_subbox_faces(kind, precision, tmp_path):
+    """Galaxies exactly on jackknife sub-box faces carry region 0 wherever
+    they are (measure_IA_base.py:428-451); a quarter of the positions and of
+    the shapes sit on a face here.  Counts per region bit-exact, values as in
+    the sweep."""
+    from measure_ia_gb300 import MeasureIABox, open_output
+    rng = np.random.default_rng(4242)
+    L, n_sub = 120.0, 2
+    faces = np.array([0.0, L / n_sub])
+    pos = rng.uniform(0.0, L, (5000, 3))
+    on = rng.uniform(size=len(pos)) < 0.25
+    pos[on, rng.integers(0, 3, on.sum())] = faces[rng.integers(0, 2, on.sum())]
+    pick = np.sort(rng.choice(len(pos), 2000, replace=False))
+    spos = pos[pick].copy()
+    on_s = rng.uniform(size=len(spos)) < 0.25
+    spos[on_s, rng.integers(0, 3, on_s.sum())] = faces[rng.integers(0, 2, on_s.sum())]
+    ang = rng.uniform(0.0, np.pi, len(spos))
+    data = {"Position": pos, "Position_shape_sample": spos, "Axis_Direction": np.c_[np.cos(ang), np.sin(ang)],
+            "q": rng.uniform(0.2, 1.0, len(spos)), "weight": np.exp(rng.normal(0.0, 0.3, len(pos))),
+            "weight_shape_sample": np.exp(rng.normal(0.0, 0.3, len(spos))), "LOS": 2}
+    r_min, r_max, n_r, n_p, pi_max = 0.2, 15.0, 8, 6, 15.0
+    b = O.Binning(boxsize=L, r_min=r_min, r_max=r_max, num_bins_r=n_r, num_bins_pi=n_p, pi_max=pi_max)
+    ref = dict(O.measure(kind, b, _copy(data), "f", "both", n_sub ** 3, None, "distortion", "tree"))
+    c = ref.pop("__counts__")
+    out = str(tmp_path / "faces.hdf5")
+    box = MeasureIABox(_copy(data), out, None, None, [r_min, r_max], n_r, n_p, pi_max, boxsize=L,
+                       precision=precision)
+    fn = box.measure_xi_w if kind == "w" else box.measure_xi_multipoles
+    fn("f", "both", n_sub ** 3, temp_file_path=str(tmp_path), ellipticity="distortion")
+    m = box.last_measurement
+    np.testing.assert_array_equal(m.npairs[0], c.npairs)
+    np.testing.assert_array_equal(m.npairs[1:], c.npairs_jk)
+    store = open_output(out)
+    rtol = FP64_RTOL if precision == "fp64" else MIXED_RTOL
+    for path, v in ref.items():
+        _close(store.read(path), v, rtol, path)
