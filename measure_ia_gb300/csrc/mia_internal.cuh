@@ -443,10 +443,10 @@ cudaError_t launch_fixed_out(const Params& P, const Work& w, const Out& o, cudaS
 // Lightcone pair counts (mia_lightcone.cu): workspace plan and launcher.
 struct LcPlan {
   long long n_cells;
-  int n_tiles, Q, nb, P, warps;
+  int n_tiles, Q, hq, nb, P, warps;
   size_t smem;
   size_t off_scount, off_sstart, off_sfill, off_pcount, off_pstart, off_pfill, off_tiles, off_scell, off_pcell;
-  size_t off_shp, off_pos, off_A, off_B, off_cA, off_cB, off_win, off_next, total;
+  size_t off_shp, off_pos, off_A, off_B, off_cA, off_cB, off_A128, off_B128, off_wmax, off_win, off_next, total;
 };
 bool lc_plan(const mia_lc_config* cfg, long long n_pos, long long n_shape, LcPlan* plan, const char** why);
 cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& plan, const mia_lc_sample& pos,

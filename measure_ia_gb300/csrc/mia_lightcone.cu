@@ -18,6 +18,12 @@
 // i = total - A[i] - B[i].  A is accumulated per warp in shared memory (the
 // positions are grid-sorted, so a warp's patch changes rarely); B, the pairs
 // that straddle two patches, goes to global atomics.
+//
+// Every sum is an exact fixed-point integer (scale 2^E with the largest
+// possible term at 2^46, so a term keeps every bit down to 2^-46 of the
+// largest one): a warp's partials are 64-bit and flushed before 2^16 terms
+// can reach one, the totals 128-bit (Fix128).  The sums do not depend on the
+// order in which warps meet the pairs, and total - A[i] - B[i] is exact.
 #include <cstdio>
 
 #include "mia_internal.cuh"
@@ -71,9 +77,16 @@ __device__ __forceinline__ float2 split(double x) {
   return make_float2(hi, __double2float_rn(x - (double)hi));
 }
 
+// (also the sample's largest |w| -- for shapes max(|w|, |w e|) -- as a bit
+// pattern into wmax: non-negative doubles order as their integer patterns)
 __global__ void k_lc_scatter(mia_lc_sample in, long long n, const int* __restrict__ cell, int* __restrict__ fill,
-                             LcSorted out, int is_pos, int with_shapes) {
+                             LcSorted out, int is_pos, int with_shapes, unsigned long long* __restrict__ wmax) {
+  unsigned long long mx = 0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double wa = fabs(in.w[i]);
+    const double mw = (!is_pos && with_shapes) ? fmax(wa, fabs(in.w[i] * in.e[i])) : wa;
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(mw);
+    mx = bits > mx ? bits : mx;
     const int d = atomicAdd(&fill[cell[i]], 1);
     const double ra = in.ra[i], dec = in.dec[i], chi = in.chi[i];
     out.ra[d] = ra;
@@ -98,6 +111,11 @@ __global__ void k_lc_scatter(mia_lc_sample in, long long n, const int* __restric
       out.aux2[d] = we * in.s2a[i];
     }
   }
+  for (int of = 16; of > 0; of >>= 1) {
+    const unsigned long long o = __shfl_down_sync(0xffffffffu, mx, of);
+    mx = o > mx ? o : mx;
+  }
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(wmax, mx);
 }
 
 struct LcParams {
@@ -108,6 +126,7 @@ struct LcParams {
   float los_lo, los_hi;        // w: FP32 prefilter bounds on Pi
   float qa, qb, pa, pb;        // first guesses of the table interval: log2(q) * qa + qb, x * pa + pb
   int unit;                    // unit weights: DD is the pair count, not summed
+  int hq;                      // value arrays in a warp's histogram: Q, or 0 (unit-weight counts)
   LcGrid g;
   long long n_pos;
 };
@@ -170,13 +189,27 @@ __global__ void k_lc_windows(const LcParams P, const LcSorted pos, LcWin* __rest
 }
 
 struct LcAcc {
-  double* A;                   // [max(1, n_patch)][Q][nb]
-  double* B;                   // [n_patch][Q][nb]
+  unsigned long long* A128;    // [max(1, n_patch)][Q][nb] Fix128 (lo, hi)
+  unsigned long long* B128;    // [n_patch][Q][nb] Fix128
+  double* A;                   // [max(1, n_patch)][Q][nb]: terms that are not finite (else 0)
+  double* B;                   // [n_patch][Q][nb]: the same
+  const unsigned long long* wmax;   // largest |w| of the positions, max(|w|, |w e|) of the shapes
   unsigned long long* cA;      // [max(1, n_patch)][nb]
   unsigned long long* cB;      // [n_patch][nb]
   unsigned* next;              // work counter
   unsigned* status;
 };
+
+// Fixed-point exponent of a counter: E with m 2^E <= 2^46 for the largest
+// possible term m (weight products; the shape terms are bounded by
+// |w_p| |w_s e|), so that 2^16 terms fit a signed 64-bit partial.
+__device__ inline int lc_exponent(const unsigned long long* wmax) {
+  double m = __longlong_as_double((long long)wmax[0]) * __longlong_as_double((long long)wmax[1]);
+  if (!(m > 0.0) || !(m < 1e300)) m = 1.0;
+  const int e = ilogb(70368744177664.0 / m);  // 2^46
+  return e > 1000 ? 1000 : (e < -1000 ? -1000 : e);
+}
+constexpr int kLcFlushSteps = 2000;   // half-steps (<= 32 terms each) between partial flushes
 
 // shared-memory bytes of the tables: double and FP32 breaks, bins; 16-byte rounded
 constexpr size_t kLcTableBytes = (2 * MIA_MAX_BREAKS * 8 + 2 * MIA_MAX_BREAKS * 4 + 2 * (MIA_MAX_BREAKS + 1) * 4 + 15) & ~size_t(15);
@@ -217,8 +250,9 @@ __device__ __forceinline__ int lookup_f(const float* br, const int* bins, int n,
 constexpr float kRelGuard = 4e-6f;
 constexpr int kQueue = 64;         // per-warp queue of survivors (int4 entries)
 
-template <int KIND, int SHAPES, int JK>
-__global__ void __launch_bounds__(kLcMaxWarps * 32)
+// UNIT: every weight is 1 (DD is the pair count; no weight products summed)
+template <int KIND, int SHAPES, int JK, int UNIT>
+__global__ void __launch_bounds__(kLcMaxWarps * 32, 4)
 k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorted shp, const int* __restrict__ start,
            const LcWin* __restrict__ win, const LcAcc acc) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -234,9 +268,13 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
   int* s_pbn = s_qbn + (MIA_MAX_BREAKS + 1);
   int4* queues = reinterpret_cast<int4*>(smem_raw + kLcTableBytes);
   int4* queue = queues + warp * kQueue;
-  double* hist_base = reinterpret_cast<double*>(queues + n_warps * kQueue);
-  double* h = hist_base + (size_t)warp * ((size_t)Q * nb + (nb + 1) / 2);
-  unsigned* hc = reinterpret_cast<unsigned*>(h + (size_t)Q * nb);
+  // per warp: hq * nb signed 64-bit partial sums, then nb u32 counts
+  unsigned long long* hist_base = reinterpret_cast<unsigned long long*>(queues + n_warps * kQueue);
+  const int hw = P.hq * nb;
+  unsigned long long* h = hist_base + (size_t)warp * ((size_t)hw + (nb + 1) / 2);
+  unsigned* hc = reinterpret_cast<unsigned*>(h + hw);
+  const int E = lc_exponent(acc.wmax);
+  int steps = 0;   // half-steps (<= 32 terms each) since the last flush (warp-uniform)
   for (int i = threadIdx.x; i < MIA_MAX_BREAKS; i += blockDim.x) {
     s_qbr[i] = T.qbr[i];
     s_pbr[i] = T.pbr[i];
@@ -247,7 +285,7 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     s_qbn[i] = T.qbn[i];
     s_pbn[i] = T.pbn[i];
   }
-  for (int i = lane; i < Q * nb; i += 32) h[i] = 0.0;
+  for (int i = lane; i < hw; i += 32) h[i] = 0ull;
   for (int i = lane; i < nb; i += 32) hc[i] = 0u;
   __syncthreads();
 
@@ -257,12 +295,12 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
   auto flush_hist = [&](int p) {
     __syncwarp();
     if (p >= 0) {
-      double* dst = acc.A + (size_t)p * Q * nb;
+      unsigned long long* dst = acc.A128 + (size_t)p * Q * nb * 2;
       unsigned long long* cdst = acc.cA + (size_t)p * nb;
-      for (int i = lane; i < Q * nb; i += 32) {
-        const double v = h[i];
-        if (v != 0.0) atomicAdd(&dst[i], v);
-        h[i] = 0.0;
+      for (int i = lane; i < hw; i += 32) {
+        const unsigned long long v = h[i];   // two's complement: sign-extend to 128 bits
+        if (v) add_fix128(dst + 2 * i, Fix128{v, (unsigned long long)((long long)v >> 63)});
+        h[i] = 0ull;
       }
       for (int i = lane; i < nb; i += 32) {
         const unsigned c = hc[i];
@@ -273,22 +311,31 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     __syncwarp();
   };
 
+  // a pair's terms into the warp's histogram (A, patch cur) and, when the
+  // shape lies in another patch, into B; a term that is not finite goes to
+  // the double arrays instead (a bin holding one reads inf or NaN)
   auto accumulate = [&](int j, int bin, double ww, double sp, double sx) {
-    if (!P.unit) atomicAdd(&h[bin], ww);
-    if (SHAPES) {
-      atomicAdd(&h[nb + bin], sp);
-      atomicAdd(&h[2 * nb + bin], sx);
+    Fix128 f[3];
+    bool ok[3] = {true, true, true};
+    const double v[3] = {ww, sp, sx};
+    const int q0 = UNIT ? 1 : 0, q1 = SHAPES ? 3 : 1;
+    for (int q = q0; q < q1; ++q) {
+      // a finite term within the partials' range (|t| 2^E < 2^47; the bound
+      // on the terms makes it at most 2^46)
+      ok[q] = to_fix128(v[q], E, f[q]) && f[q].hi == (unsigned long long)((long long)f[q].lo >> 63) &&
+              (f[q].lo + (1ull << 47)) < (1ull << 48);
+      if (ok[q]) atomicAdd(h + q * nb + bin, f[q].lo);
+      else atomicAdd(&acc.A[((size_t)cur * Q + q) * nb + bin], v[q]);
     }
     atomicAdd(&hc[bin], 1u);
     if (JK) {
       const int p_s = shp.patch[j];
       if (p_s >= P.n_patch) atomicOr(acc.status, MIA_LC_BAD_PATCH);
       if (p_s >= 0 && p_s < P.n_patch && p_s != cur) {
-        double* dst = acc.B + (size_t)p_s * Q * nb;
-        if (!P.unit) atomicAdd(&dst[bin], ww);
-        if (SHAPES) {
-          atomicAdd(&dst[nb + bin], sp);
-          atomicAdd(&dst[2 * nb + bin], sx);
+        const size_t base = (size_t)p_s * Q * nb + bin;
+        for (int q = q0; q < q1; ++q) {
+          if (ok[q]) add_fix128(acc.B128 + 2 * (base + (size_t)q * nb), f[q]);
+          else atomicAdd(&acc.B[base + (size_t)q * nb], v[q]);
         }
         atomicAdd(&acc.cB[(size_t)p_s * nb + bin], 1ull);
       }
@@ -368,7 +415,7 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     const double w_n = pos.w[ip];
     double sp = 0.0, sx = 0.0;
     if (SHAPES) shape_terms(j, w_n, ux, uy, sp, sx);
-    accumulate(j, bin, P.unit ? 1.0 : __dmul_rn(w_n, shp.w[j]), sp, sx);
+    accumulate(j, bin, UNIT ? 1.0 : __dmul_rn(w_n, shp.w[j]), sp, sx);
   };
 
   auto drain = [&]() {   // process what is queued (fewer than 32 entries)
@@ -456,7 +503,7 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
                 }
               }
               if (!SHAPES && take && !near) {   // counts only: w_p w_s is all there is to add
-                accumulate(j, bin, P.unit ? 1.0 : __dmul_rn(w_n, shp.w[j]), 0.0, 0.0);
+                accumulate(j, bin, UNIT ? 1.0 : __dmul_rn(w_n, shp.w[j]), 0.0, 0.0);
                 take = false;
               }
             }
@@ -475,6 +522,13 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
                 process(true, mine);
               }
             }
+            // a step adds at most 64 terms to the partials (32 decided here,
+            // 32 from the queue); 1000 steps stay below 2^16 terms of < 2^47
+            steps += 2;
+            if (steps >= kLcFlushSteps) {
+              flush_hist(cur);
+              steps = 0;
+            }
           }
         }
       }
@@ -485,10 +539,24 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
 }
 
 // totals and realisations: out[q][0][b] = sum_i A[i][q][b]; out[q][1+i][b] =
-// total - A[i] - B[i]; the same for the integer counts.
-__global__ void k_lc_finish(const double* __restrict__ A, const double* __restrict__ B,
+// total - A[i] - B[i], in exact 128-bit integers, rounded once (plus the same
+// combination of the terms that were not finite); the integer counts likewise.
+__device__ __forceinline__ void add128(unsigned long long& lo, unsigned long long& hi, const unsigned long long* v) {
+  const unsigned long long l = lo + v[0];
+  hi = hi + v[1] + (l < lo ? 1ull : 0ull);
+  lo = l;
+}
+__device__ __forceinline__ void sub128(unsigned long long& lo, unsigned long long& hi, const unsigned long long* v) {
+  const unsigned long long l = lo - v[0];
+  hi = hi - v[1] - (lo < v[0] ? 1ull : 0ull);
+  lo = l;
+}
+
+__global__ void k_lc_finish(const unsigned long long* __restrict__ A128, const unsigned long long* __restrict__ B128,
+                            const double* __restrict__ A, const double* __restrict__ B,
                             const unsigned long long* __restrict__ cA, const unsigned long long* __restrict__ cB,
-                            int n_patch, int Q, int nb, int unit, double* out, long long* counts) {
+                            const unsigned long long* __restrict__ wmax, int n_patch, int Q, int nb, int unit,
+                            double* out, long long* counts) {
   const int P = n_patch > 0 ? n_patch : 1;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int n_real = 1 + n_patch;
@@ -501,12 +569,23 @@ __global__ void k_lc_finish(const double* __restrict__ A, const double* __restri
       out[(size_t)(1 + i) * nb + b] = (double)(tot - cA[(size_t)i * nb + b] - cB[(size_t)i * nb + b]);
   } else if (t < Q * nb) {
     const int q = t / nb, b = t - q * nb;
-    double tot = 0.0;
-    for (int i = 0; i < P; ++i) tot += A[((size_t)i * Q + q) * nb + b];
+    const double inv = ldexp(1.0, -lc_exponent(wmax));
+    unsigned long long tl = 0, th = 0;
+    double pt = 0.0;
+    for (int i = 0; i < P; ++i) {
+      const size_t k = ((size_t)i * Q + q) * nb + b;
+      add128(tl, th, A128 + 2 * k);
+      pt += A[k];
+    }
     double* o = out + (size_t)q * n_real * nb;
-    o[b] = tot;
-    for (int i = 0; i < n_patch; ++i)
-      o[(size_t)(1 + i) * nb + b] = (tot - A[((size_t)i * Q + q) * nb + b]) - B[((size_t)i * Q + q) * nb + b];
+    o[b] = fix128_value(tl, th, inv) + pt;
+    for (int i = 0; i < n_patch; ++i) {
+      const size_t k = ((size_t)i * Q + q) * nb + b;
+      unsigned long long rl = tl, rh = th;
+      sub128(rl, rh, A128 + 2 * k);
+      sub128(rl, rh, B128 + 2 * k);
+      o[(size_t)(1 + i) * nb + b] = fix128_value(rl, rh, inv) + ((pt - A[k]) - B[k]);
+    }
   } else if (t < Q * nb + nb) {
     const int b = t - Q * nb;
     unsigned long long tot = 0;
@@ -540,15 +619,16 @@ LcSorted carve(unsigned char* base, long long n) {
   return s;
 }
 
-size_t lc_per_warp(int Q, int nb) { return (size_t)kQueue * 16 + (size_t)Q * nb * 8 + (size_t)(nb + 1) / 2 * 8; }
+// per warp: the survivor queue, hq * nb 64-bit partial sums, nb u32 counts
+size_t lc_per_warp(int hq, int nb) { return (size_t)kQueue * 16 + (size_t)hq * nb * 8 + (size_t)(nb + 1) / 2 * 8; }
 constexpr size_t kLcFixedSmem = kLcTableBytes + 16;
 constexpr size_t kLcSmemBudget = 200 * 1024;
 
-template <int KIND, int SHAPES, int JK>
+template <int KIND, int SHAPES, int JK, int UNIT>
 cudaError_t launch_lc_pairs(const LcParams& P, const LcTables& T, const LcSorted& pos, const LcSorted& shp,
                             const int* start, const LcWin* win, const LcAcc& acc, int warps, size_t smem, int num_sms,
                             cudaStream_t st) {
-  auto kern = k_lc_pairs<KIND, SHAPES, JK>;
+  auto kern = k_lc_pairs<KIND, SHAPES, JK, UNIT>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
@@ -583,11 +663,12 @@ bool lc_plan(const mia_lc_config* c, long long n_pos, long long n_shape, LcPlan*
   p->n_cells = (long long)c->n_ra * c->n_dec * c->n_chi;
   if (p->n_cells > (1ll << 27)) { *why = "too many cells"; return false; }
   p->Q = c->with_shapes ? 3 : 1;
+  p->hq = (!c->with_shapes && c->unit_weights) ? 0 : p->Q;
   p->nb = c->n_r * c->n_p;
   p->P = c->n_patch > 0 ? c->n_patch : 1;
-  if (kLcFixedSmem + lc_per_warp(p->Q, p->nb) > kLcSmemBudget) { *why = "too many bins for the lightcone counter"; return false; }
-  p->warps = (int)std::min<size_t>(kLcMaxWarps, (kLcSmemBudget - kLcFixedSmem) / lc_per_warp(p->Q, p->nb));
-  p->smem = kLcFixedSmem + (size_t)p->warps * lc_per_warp(p->Q, p->nb);
+  if (kLcFixedSmem + lc_per_warp(p->hq, p->nb) > kLcSmemBudget) { *why = "too many bins for the lightcone counter"; return false; }
+  p->warps = (int)std::min<size_t>(kLcMaxWarps, (kLcSmemBudget - kLcFixedSmem) / lc_per_warp(p->hq, p->nb));
+  p->smem = kLcFixedSmem + (size_t)p->warps * lc_per_warp(p->hq, p->nb);
   p->n_tiles = (int)((p->n_cells + kScanTile - 1) / kScanTile) + 1;
   size_t o = 0;
   auto take = [&](size_t bytes) { size_t at = o; o += al(bytes); return at; };
@@ -606,6 +687,9 @@ bool lc_plan(const mia_lc_config* c, long long n_pos, long long n_shape, LcPlan*
   p->off_B = take((size_t)c->n_patch * p->Q * p->nb * 8 + 8);
   p->off_cA = take((size_t)p->P * p->nb * 8);
   p->off_cB = take((size_t)c->n_patch * p->nb * 8 + 8);
+  p->off_A128 = take((size_t)p->P * p->Q * p->nb * 16);
+  p->off_B128 = take((size_t)c->n_patch * p->Q * p->nb * 16 + 16);
+  p->off_wmax = take(16);
   p->off_win = take(((size_t)n_pos + 1) * sizeof(LcWin));
   p->off_next = take(256);
   p->total = o;
@@ -628,6 +712,10 @@ cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sa
   const LcSorted S = carve(ws + p.off_shp, shp.n);
   const LcSorted Ps = carve(ws + p.off_pos, pos.n);
   LcAcc acc;
+  acc.A128 = reinterpret_cast<unsigned long long*>(ws + p.off_A128);
+  acc.B128 = reinterpret_cast<unsigned long long*>(ws + p.off_B128);
+  unsigned long long* wmax = reinterpret_cast<unsigned long long*>(ws + p.off_wmax);
+  acc.wmax = wmax;
   acc.A = reinterpret_cast<double*>(ws + p.off_A);
   acc.B = reinterpret_cast<double*>(ws + p.off_B);
   acc.cA = reinterpret_cast<unsigned long long*>(ws + p.off_cA);
@@ -657,8 +745,8 @@ cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sa
   if ((e = cudaMemcpyAsync(sfill, sstart, (size_t)p.n_cells * 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
   if ((e = exclusive_scan(pcount, p.n_cells, pstart, tiles, st)) != cudaSuccess) return e;
   if ((e = cudaMemcpyAsync(pfill, pstart, (size_t)p.n_cells * 4, cudaMemcpyDeviceToDevice, st)) != cudaSuccess) return e;
-  if (shp.n > 0) k_lc_scatter<<<grid_for(shp.n), 256, 0, st>>>(shp, shp.n, scell, sfill, S, 0, cfg->with_shapes);
-  if (pos.n > 0) k_lc_scatter<<<grid_for(pos.n), 256, 0, st>>>(pos, pos.n, pcell, pfill, Ps, 1, 0);
+  if (shp.n > 0) k_lc_scatter<<<grid_for(shp.n), 256, 0, st>>>(shp, shp.n, scell, sfill, S, 0, cfg->with_shapes, wmax + 1);
+  if (pos.n > 0) k_lc_scatter<<<grid_for(pos.n), 256, 0, st>>>(pos, pos.n, pcell, pfill, Ps, 1, 0, wmax);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
 
   LcParams P;
@@ -675,6 +763,7 @@ cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sa
   P.g = g;
   P.n_pos = pos.n;
   P.unit = cfg->unit_weights ? 1 : 0;
+  P.hq = p.hq;
   // first guesses of the table intervals: breaks 0 and n-1 map to 1 and n
   auto affine = [](const double* br, int n, bool logq, float* a, float* b) {
     *a = 0.0f;
@@ -709,19 +798,22 @@ cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sa
   if (pos.n > 0 && shp.n > 0) {
     const bool jk = cfg->n_patch > 0;
     const int w = p.warps;
-#define MIA_LC_CASE(K, S_, J)                                                                      \
-  if (cfg->kind == K && (cfg->with_shapes != 0) == (S_ != 0) && jk == (J != 0))                   \
-    e = launch_lc_pairs<K, S_, J>(P, T, Ps, S, sstart, win, acc, w, p.smem, num_sms, st);
+#define MIA_LC_CASE(K, S_, J, U)                                                                   \
+  if (cfg->kind == K && (cfg->with_shapes != 0) == (S_ != 0) && jk == (J != 0) && unit == (U != 0))  \
+    e = launch_lc_pairs<K, S_, J, U>(P, T, Ps, S, sstart, win, acc, w, p.smem, num_sms, st);
+#define MIA_LC_CASES(K, S_, J) MIA_LC_CASE(K, S_, J, 0) MIA_LC_CASE(K, S_, J, 1)
+    const bool unit = cfg->unit_weights != 0;
     e = cudaErrorInvalidValue;
-    MIA_LC_CASE(MIA_KIND_W, 0, 0) MIA_LC_CASE(MIA_KIND_W, 0, 1) MIA_LC_CASE(MIA_KIND_W, 1, 0)
-    MIA_LC_CASE(MIA_KIND_W, 1, 1) MIA_LC_CASE(MIA_KIND_MULTIPOLES, 0, 0) MIA_LC_CASE(MIA_KIND_MULTIPOLES, 0, 1)
-    MIA_LC_CASE(MIA_KIND_MULTIPOLES, 1, 0) MIA_LC_CASE(MIA_KIND_MULTIPOLES, 1, 1)
+    MIA_LC_CASES(MIA_KIND_W, 0, 0) MIA_LC_CASES(MIA_KIND_W, 0, 1) MIA_LC_CASES(MIA_KIND_W, 1, 0)
+    MIA_LC_CASES(MIA_KIND_W, 1, 1) MIA_LC_CASES(MIA_KIND_MULTIPOLES, 0, 0) MIA_LC_CASES(MIA_KIND_MULTIPOLES, 0, 1)
+    MIA_LC_CASES(MIA_KIND_MULTIPOLES, 1, 0) MIA_LC_CASES(MIA_KIND_MULTIPOLES, 1, 1)
+#undef MIA_LC_CASES
 #undef MIA_LC_CASE
     if (e != cudaSuccess) return e;
   }
   const int n_thr = (p.Q + 1) * p.nb;
-  k_lc_finish<<<(n_thr + 255) / 256, 256, 0, st>>>(acc.A, acc.B, acc.cA, acc.cB, cfg->n_patch, p.Q, p.nb,
-                                                    cfg->unit_weights ? 1 : 0, out,
+  k_lc_finish<<<(n_thr + 255) / 256, 256, 0, st>>>(acc.A128, acc.B128, acc.A, acc.B, acc.cA, acc.cB, wmax,
+                                                    cfg->n_patch, p.Q, p.nb, cfg->unit_weights ? 1 : 0, out,
                                                     reinterpret_cast<long long*>(counts));
   return cudaGetLastError();
 }

@@ -214,3 +214,30 @@ def test_empty_samples():
         for pos, shp in ((empty_p, far), (one, empty_s), (one, far), (empty_p, empty_s)):
             sums, counts = c.count(pos, shp, 0)
             assert counts.sum() == 0 and np.all(sums == 0.0)
+
+
+@pytest.mark.parametrize("kind", ["w", "m"])
+def test_counter_sums_are_order_free(kind):
+    """The counter's sums are exact integers: a second run gives the same
+    bits, and halving every weight gives exactly a quarter of DD, S+D, SxD
+    in the total and in every realisation."""
+    from measure_ia_gb300.cosmology import FlatLCDM
+    from measure_ia_gb300.lightcone import LightconeCounter
+    sel = _catalogue(77, 3000, 2000, (10, 40), (-10, 10), (0.1, 0.3))
+    cosmo = FlatLCDM()
+    b = LO.LcBinning(0.3, 25.0, 6, 5, 30.0)
+    chi = lambda zz: cosmo.comoving_radial_distance(1 / (1 + zz))
+    rng = np.random.default_rng(7)
+    pos, shp = _prep(sel, chi, True)
+    pos["patch"] = rng.integers(0, 5, len(sel["RA"]))
+    shp["patch"] = rng.integers(0, 5, len(sel["RA_shape_sample"])).astype(np.int32)
+    counter = LightconeCounter(kind, True, b.r_bins, 0.3, 25.0, b.pi_bins if kind == "w" else b.mu_r_bins)
+    s1, c1 = counter.count(pos, shp, 5)
+    s2, c2 = counter.count(pos, shp, 5)
+    np.testing.assert_array_equal(s1, s2)
+    np.testing.assert_array_equal(c1, c2)
+    half = lambda d: dict(d, w=0.5 * d["w"])
+    s3, c3 = counter.count(half(pos), half(shp), 5)
+    np.testing.assert_array_equal(c3, c1)
+    np.testing.assert_array_equal(s1, 4 * s3)
+    assert c1[0].sum() > 0 and np.abs(s1[1, 0]).max() > 0
