@@ -137,6 +137,9 @@ struct LcWin {
   int d0, d1, a0, a1, c0, c1;
   float kx, ky;                // Mpc per degree of RA / DEC difference (times h_extra for w)
   float gq, gqp, gmu, gl;      // absolute error bounds (see k_lc_windows)
+  // the position and the window's half-widths in RA / DEC cell units, for
+  // trimming each DEC row's RA range to the window's ellipse (sra < 0: no trim)
+  float tra, tdec, sra, sdec;
 };
 
 // Per sorted position: the cell ranges its separation window reaches (a
@@ -184,6 +187,12 @@ __global__ void k_lc_windows(const LcParams P, const LcSorted pos, LcWin* __rest
     w.gq = (float)(2.1 * P.r_lim * (ep + (KIND == MIA_KIND_W ? 0.0 : gld)) + ep * ep + gld * gld);
     w.gqp = (float)(P.h2 * (2.1 * P.r_lim * ep + ep * ep));   // on r_p^2 (the multipoles' cut)
     w.gmu = (float)(2.0 * (gld + ep));                          // times 1/r, on mu
+    w.tra = (float)((ra_n - g.ra0) * g.inv_ra);
+    w.tdec = (float)((dec_n - g.dec0) * g.inv_dec);
+    const double sra = span_ra * g.inv_ra, sdec = span_dec * g.inv_dec;
+    const bool trim = sra < 1e6 && sdec < 1e6 && sdec > 1e-6 && fabs((double)w.tra) < 1e6 && fabs((double)w.tdec) < 1e6;
+    w.sra = trim ? (float)sra : -1.0f;
+    w.sdec = trim ? (float)sdec : 1.0f;
     win[ip] = w;
   }
 }
@@ -450,9 +459,27 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
       const float4 nhl = pos.hl[ip];
       const float2 nch = pos.chl[ip];
       for (int d = d0; d <= d1; ++d) {
+        // a shape in DEC band d is at least `gap` cells from the position in
+        // DEC, so within r_lim it is at most sra sqrt(1 - (gap / sdec)^2)
+        // cells away in RA (the window's ellipse); FP32 with margins of
+        // 2e-3 cells and 1e-5 relative keeps the range a superset
+        int ra0 = a0, ra1 = a1;
+        if (wn.sra >= 0.0f) {
+          float gap = 0.0f;
+          if (d > 0) gap = fmaxf(gap, (float)d - wn.tdec);
+          if (d < P.g.n_dec - 1) gap = fmaxf(gap, wn.tdec - (float)(d + 1));
+          const float rr = fmaxf(gap - 2e-3f, 0.0f) / wn.sdec;
+          if (rr >= 1.0f) continue;
+          const float wc = wn.sra * sqrtf(1.0f - rr * rr) * (1.0f + 1e-5f) + 2e-3f;
+          // clamped as cell_1d clamps: the end cells also hold what lies beyond
+          const int nr = P.g.n_ra - 1;
+          ra0 = max(a0, min(nr, max(0, (int)floorf(wn.tra - wc))));
+          ra1 = min(a1, min(nr, max(0, (int)floorf(wn.tra + wc))));
+          if (ra0 > ra1) continue;
+        }
         for (int c = c0; c <= c1; ++c) {
           const int row = (d * P.g.n_chi + c) * P.g.n_ra;
-          const int j0 = start[row + a0], j1 = start[row + a1 + 1];
+          const int j0 = start[row + ra0], j1 = start[row + ra1 + 1];
           for (int jj = j0; jj < j1; jj += 32) {
             const int j = jj + lane;
             bool take = false;   // binned (bin decided) or in the guard band
