@@ -293,6 +293,10 @@ typedef struct {
   int n_ra, n_dec, n_chi;
   int unit_weights;         /* 1: every weight of both samples is exactly 1.0, so DD is the
                                pair count (the reference's sum of ones) and is not summed */
+  int wide_sums;            /* sums are exact fixed-point integers; 0: a term keeps every bit
+                               down to 2^-46 of the largest possible term (64-bit warp
+                               partials), 1: down to 2^-88 (128-bit partials, more shared
+                               memory); for weights spanning more than ~2^12 */
 } mia_lc_config;
 
 typedef struct {            /* device arrays of n entries */

@@ -71,7 +71,8 @@ class LcConfig(C.Structure):
                 ("h_extra", C.c_double), ("rp_cut", C.c_double), ("r_lim", C.c_double), ("pi_lo", C.c_double),
                 ("pi_hi", C.c_double), ("ra0", C.c_double), ("ra_cell", C.c_double), ("dec0", C.c_double),
                 ("dec_cell", C.c_double), ("chi0", C.c_double), ("chi_cell", C.c_double), ("n_ra", C.c_int),
-                ("n_dec", C.c_int), ("n_chi", C.c_int), ("unit_weights", C.c_int)]
+                ("n_dec", C.c_int), ("n_chi", C.c_int), ("unit_weights", C.c_int),
+                ("wide_sums", C.c_int)]
 
 
 class LcSample(C.Structure):

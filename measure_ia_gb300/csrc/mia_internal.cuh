@@ -443,7 +443,7 @@ cudaError_t launch_fixed_out(const Params& P, const Work& w, const Out& o, cudaS
 // Lightcone pair counts (mia_lightcone.cu): workspace plan and launcher.
 struct LcPlan {
   long long n_cells;
-  int n_tiles, Q, hq, nb, P, warps;
+  int n_tiles, Q, hq, nb, P, warps, wide;
   size_t smem;
   size_t off_scount, off_sstart, off_sfill, off_pcount, off_pstart, off_pfill, off_tiles, off_scell, off_pcell;
   size_t off_shp, off_pos, off_A, off_B, off_cA, off_cB, off_A128, off_B128, off_wmax, off_win, off_next, total;

@@ -209,12 +209,14 @@ struct LcAcc {
   unsigned* status;
 };
 
-// Fixed-point exponent of a counter: E with m 2^E <= 2^46 for the largest
-// possible term m (weight products; the shape terms are bounded by
-// |w_p| |w_s e|), so that 2^16 terms fit a signed 64-bit partial.
-__device__ inline int lc_exponent(const unsigned long long* wmax) {
+// Fixed-point exponent of a counter from the largest possible term m (weight
+// products; the shape terms are bounded by |w_p| |w_s e|): 64-bit warp
+// partials, m 2^E <= 2^46, so that 2^16 terms fit one; wide (128-bit)
+// partials, m 2^E <= 2^88 (fix128_exponent).
+__device__ inline int lc_exponent(const unsigned long long* wmax, int wide) {
   double m = __longlong_as_double((long long)wmax[0]) * __longlong_as_double((long long)wmax[1]);
   if (!(m > 0.0) || !(m < 1e300)) m = 1.0;
+  if (wide) return fix128_exponent(m);
   const int e = ilogb(70368744177664.0 / m);  // 2^46
   return e > 1000 ? 1000 : (e < -1000 ? -1000 : e);
 }
@@ -259,8 +261,9 @@ __device__ __forceinline__ int lookup_f(const float* br, const int* bins, int n,
 constexpr float kRelGuard = 4e-6f;
 constexpr int kQueue = 64;         // per-warp queue of survivors (int4 entries)
 
-// UNIT: every weight is 1 (DD is the pair count; no weight products summed)
-template <int KIND, int SHAPES, int JK, int UNIT>
+// UNIT: every weight is 1 (DD is the pair count; no weight products summed).
+// WIDE: 128-bit warp partials (two words per sum) instead of 64-bit ones.
+template <int KIND, int SHAPES, int JK, int UNIT, int WIDE>
 __global__ void __launch_bounds__(kLcMaxWarps * 32, 4)
 k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorted shp, const int* __restrict__ start,
            const LcWin* __restrict__ win, const LcAcc acc) {
@@ -279,10 +282,11 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
   int4* queue = queues + warp * kQueue;
   // per warp: hq * nb signed 64-bit partial sums, then nb u32 counts
   unsigned long long* hist_base = reinterpret_cast<unsigned long long*>(queues + n_warps * kQueue);
-  const int hw = P.hq * nb;
+  constexpr int PW = WIDE ? 2 : 1;   // 64-bit words per partial sum
+  const int hw = PW * P.hq * nb;
   unsigned long long* h = hist_base + (size_t)warp * ((size_t)hw + (nb + 1) / 2);
   unsigned* hc = reinterpret_cast<unsigned*>(h + hw);
-  const int E = lc_exponent(acc.wmax);
+  const int E = lc_exponent(acc.wmax, WIDE);
   int steps = 0;   // half-steps (<= 32 terms each) since the last flush (warp-uniform)
   for (int i = threadIdx.x; i < MIA_MAX_BREAKS; i += blockDim.x) {
     s_qbr[i] = T.qbr[i];
@@ -306,10 +310,17 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     if (p >= 0) {
       unsigned long long* dst = acc.A128 + (size_t)p * Q * nb * 2;
       unsigned long long* cdst = acc.cA + (size_t)p * nb;
-      for (int i = lane; i < hw; i += 32) {
-        const unsigned long long v = h[i];   // two's complement: sign-extend to 128 bits
-        if (v) add_fix128(dst + 2 * i, Fix128{v, (unsigned long long)((long long)v >> 63)});
-        h[i] = 0ull;
+      for (int i = lane; i < P.hq * nb; i += 32) {
+        Fix128 v;
+        if (WIDE) {
+          v = Fix128{h[2 * i], h[2 * i + 1]};
+          h[2 * i] = 0ull;
+          h[2 * i + 1] = 0ull;
+        } else {
+          v = Fix128{h[i], (unsigned long long)((long long)h[i] >> 63)};   // sign-extended
+          h[i] = 0ull;
+        }
+        if (v.lo | v.hi) add_fix128(dst + 2 * i, v);
       }
       for (int i = lane; i < nb; i += 32) {
         const unsigned c = hc[i];
@@ -329,12 +340,18 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
     const double v[3] = {ww, sp, sx};
     const int q0 = UNIT ? 1 : 0, q1 = SHAPES ? 3 : 1;
     for (int q = q0; q < q1; ++q) {
-      // a finite term within the partials' range (|t| 2^E < 2^47; the bound
-      // on the terms makes it at most 2^46)
-      ok[q] = to_fix128(v[q], E, f[q]) && f[q].hi == (unsigned long long)((long long)f[q].lo >> 63) &&
-              (f[q].lo + (1ull << 47)) < (1ull << 48);
-      if (ok[q]) atomicAdd(h + q * nb + bin, f[q].lo);
-      else atomicAdd(&acc.A[((size_t)cur * Q + q) * nb + bin], v[q]);
+      // a finite term within the partials' range (64-bit: |t| 2^E < 2^47,
+      // which the bound on the terms keeps at most 2^46)
+      ok[q] = to_fix128(v[q], E, f[q]);
+      if (!WIDE)
+        ok[q] = ok[q] && f[q].hi == (unsigned long long)((long long)f[q].lo >> 63) &&
+                (f[q].lo + (1ull << 47)) < (1ull << 48);
+      if (ok[q]) {
+        if (WIDE) add_fix128(h + 2 * (q * nb + bin), f[q]);
+        else atomicAdd(h + q * nb + bin, f[q].lo);
+      } else {
+        atomicAdd(&acc.A[((size_t)cur * Q + q) * nb + bin], v[q]);
+      }
     }
     atomicAdd(&hc[bin], 1u);
     if (JK) {
@@ -582,8 +599,8 @@ __device__ __forceinline__ void sub128(unsigned long long& lo, unsigned long lon
 __global__ void k_lc_finish(const unsigned long long* __restrict__ A128, const unsigned long long* __restrict__ B128,
                             const double* __restrict__ A, const double* __restrict__ B,
                             const unsigned long long* __restrict__ cA, const unsigned long long* __restrict__ cB,
-                            const unsigned long long* __restrict__ wmax, int n_patch, int Q, int nb, int unit,
-                            double* out, long long* counts) {
+                            const unsigned long long* __restrict__ wmax, int wide, int n_patch, int Q, int nb,
+                            int unit, double* out, long long* counts) {
   const int P = n_patch > 0 ? n_patch : 1;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int n_real = 1 + n_patch;
@@ -596,7 +613,7 @@ __global__ void k_lc_finish(const unsigned long long* __restrict__ A128, const u
       out[(size_t)(1 + i) * nb + b] = (double)(tot - cA[(size_t)i * nb + b] - cB[(size_t)i * nb + b]);
   } else if (t < Q * nb) {
     const int q = t / nb, b = t - q * nb;
-    const double inv = ldexp(1.0, -lc_exponent(wmax));
+    const double inv = ldexp(1.0, -lc_exponent(wmax, wide));
     unsigned long long tl = 0, th = 0;
     double pt = 0.0;
     for (int i = 0; i < P; ++i) {
@@ -647,15 +664,17 @@ LcSorted carve(unsigned char* base, long long n) {
 }
 
 // per warp: the survivor queue, hq * nb 64-bit partial sums, nb u32 counts
-size_t lc_per_warp(int hq, int nb) { return (size_t)kQueue * 16 + (size_t)hq * nb * 8 + (size_t)(nb + 1) / 2 * 8; }
+size_t lc_per_warp(int hq, int nb, int wide) {
+  return (size_t)kQueue * 16 + (size_t)hq * nb * (wide ? 16 : 8) + (size_t)(nb + 1) / 2 * 8;
+}
 constexpr size_t kLcFixedSmem = kLcTableBytes + 16;
 constexpr size_t kLcSmemBudget = 200 * 1024;
 
-template <int KIND, int SHAPES, int JK, int UNIT>
+template <int KIND, int SHAPES, int JK, int UNIT, int WIDE>
 cudaError_t launch_lc_pairs(const LcParams& P, const LcTables& T, const LcSorted& pos, const LcSorted& shp,
                             const int* start, const LcWin* win, const LcAcc& acc, int warps, size_t smem, int num_sms,
                             cudaStream_t st) {
-  auto kern = k_lc_pairs<KIND, SHAPES, JK, UNIT>;
+  auto kern = k_lc_pairs<KIND, SHAPES, JK, UNIT, WIDE>;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
@@ -691,11 +710,13 @@ bool lc_plan(const mia_lc_config* c, long long n_pos, long long n_shape, LcPlan*
   if (p->n_cells > (1ll << 27)) { *why = "too many cells"; return false; }
   p->Q = c->with_shapes ? 3 : 1;
   p->hq = (!c->with_shapes && c->unit_weights) ? 0 : p->Q;
+  p->wide = (c->wide_sums && !c->unit_weights) ? 1 : 0;
   p->nb = c->n_r * c->n_p;
   p->P = c->n_patch > 0 ? c->n_patch : 1;
-  if (kLcFixedSmem + lc_per_warp(p->hq, p->nb) > kLcSmemBudget) { *why = "too many bins for the lightcone counter"; return false; }
-  p->warps = (int)std::min<size_t>(kLcMaxWarps, (kLcSmemBudget - kLcFixedSmem) / lc_per_warp(p->hq, p->nb));
-  p->smem = kLcFixedSmem + (size_t)p->warps * lc_per_warp(p->hq, p->nb);
+  const size_t per_warp = lc_per_warp(p->hq, p->nb, p->wide);
+  if (kLcFixedSmem + per_warp > kLcSmemBudget) { *why = "too many bins for the lightcone counter"; return false; }
+  p->warps = (int)std::min<size_t>(kLcMaxWarps, (kLcSmemBudget - kLcFixedSmem) / per_warp);
+  p->smem = kLcFixedSmem + (size_t)p->warps * per_warp;
   p->n_tiles = (int)((p->n_cells + kScanTile - 1) / kScanTile) + 1;
   size_t o = 0;
   auto take = [&](size_t bytes) { size_t at = o; o += al(bytes); return at; };
@@ -825,10 +846,11 @@ cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sa
   if (pos.n > 0 && shp.n > 0) {
     const bool jk = cfg->n_patch > 0;
     const int w = p.warps;
-#define MIA_LC_CASE(K, S_, J, U)                                                                   \
-  if (cfg->kind == K && (cfg->with_shapes != 0) == (S_ != 0) && jk == (J != 0) && unit == (U != 0))  \
-    e = launch_lc_pairs<K, S_, J, U>(P, T, Ps, S, sstart, win, acc, w, p.smem, num_sms, st);
-#define MIA_LC_CASES(K, S_, J) MIA_LC_CASE(K, S_, J, 0) MIA_LC_CASE(K, S_, J, 1)
+#define MIA_LC_CASE(K, S_, J, U, W)                                                                 \
+  if (cfg->kind == K && (cfg->with_shapes != 0) == (S_ != 0) && jk == (J != 0) && unit == (U != 0) && \
+      (p.wide != 0) == (W != 0))                                                                     \
+    e = launch_lc_pairs<K, S_, J, U, W>(P, T, Ps, S, sstart, win, acc, w, p.smem, num_sms, st);
+#define MIA_LC_CASES(K, S_, J) MIA_LC_CASE(K, S_, J, 0, 0) MIA_LC_CASE(K, S_, J, 0, 1) MIA_LC_CASE(K, S_, J, 1, 0)
     const bool unit = cfg->unit_weights != 0;
     e = cudaErrorInvalidValue;
     MIA_LC_CASES(MIA_KIND_W, 0, 0) MIA_LC_CASES(MIA_KIND_W, 0, 1) MIA_LC_CASES(MIA_KIND_W, 1, 0)
@@ -839,7 +861,7 @@ cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sa
     if (e != cudaSuccess) return e;
   }
   const int n_thr = (p.Q + 1) * p.nb;
-  k_lc_finish<<<(n_thr + 255) / 256, 256, 0, st>>>(acc.A128, acc.B128, acc.A, acc.B, acc.cA, acc.cB, wmax,
+  k_lc_finish<<<(n_thr + 255) / 256, 256, 0, st>>>(acc.A128, acc.B128, acc.A, acc.B, acc.cA, acc.cB, wmax, p.wide,
                                                     cfg->n_patch, p.Q, p.nb, cfg->unit_weights ? 1 : 0, out,
                                                     reinterpret_cast<long long*>(counts));
   return cudaGetLastError();

@@ -100,6 +100,23 @@ class LightconeCounter:
         cfg.ra_cell, cfg.dec_cell, cfg.chi_cell = (float(x) for x in cell)
         cfg.n_ra, cfg.n_dec, cfg.n_chi = (int(x) for x in n)
 
+    def _wide_sums(self, pos, shp):
+        """128-bit warp partials when the smallest weight product is below
+        2^-12 of the largest possible term: the 64-bit partials keep every
+        bit of a term down to 2^-46 of that term only, too coarse for a bin
+        that holds nothing but small-weight pairs."""
+        wp, ws = np.abs(np.asarray(pos["w"], float)), np.abs(np.asarray(shp["w"], float))
+        if not len(wp) or not len(ws):
+            return False
+        top = ws.max()
+        if self.with_shapes and "e" in shp:
+            top = max(top, float(np.max(np.abs(ws * np.asarray(shp["e"], float)))))
+        big = wp.max() * top
+        nzp, nzs = wp[wp > 0], ws[ws > 0]
+        if not len(nzp) or not len(nzs) or not (big > 0):
+            return False
+        return bool(nzp.min() * nzs.min() < big * 2.0 ** -12)
+
     def prepare(self, pos, shp, n_patch=0):
         """Upload one pair of samples and size the launch: pos holds ra, dec,
         chi, w, cos_dec (and patch); shp holds ra, dec, chi, w (and e, c2a,
@@ -123,6 +140,7 @@ class LightconeCounter:
                 if not np.all(np.isfinite(smp[k])):
                     raise ValueError(f"lightcone {k} values must be finite")
         cfg.unit_weights = int(bool(np.all(np.asarray(pos["w"]) == 1.0) and np.all(np.asarray(shp["w"]) == 1.0)))
+        cfg.wide_sums = int(self._wide_sums(pos, shp))
         if n_shp:
             self._grid(cfg, pos, shp)
         else:

@@ -241,3 +241,37 @@ def test_counter_sums_are_order_free(kind):
     np.testing.assert_array_equal(c3, c1)
     np.testing.assert_array_equal(s1, 4 * s3)
     assert c1[0].sum() > 0 and np.abs(s1[1, 0]).max() > 0
+
+
+@pytest.mark.parametrize("kind", ["w", "m"])
+def test_counter_wide_weight_range(kind):
+    """Weights spanning ~10^8: the counter keeps its sums in 128-bit warp
+    partials (the 64-bit ones hold a term only to 2^-46 of the largest), and
+    every DD bin, however small its pairs' weights, is within 1e-10 of the
+    oracle's relative to itself."""
+    from measure_ia_gb300.cosmology import FlatLCDM
+    from measure_ia_gb300.lightcone import LightconeCounter
+    sel = _catalogue(91, 1500, 900, (10, 40), (-10, 10), (0.1, 0.3))
+    rng = np.random.default_rng(8)
+    sel["weight"] = np.exp(rng.normal(0.0, 3.0, len(sel["RA"])))
+    sel["weight_shape_sample"] = np.exp(rng.normal(0.0, 3.0, len(sel["RA_shape_sample"])))
+    cosmo = FlatLCDM()
+    h = cosmo["h"]
+    b = LO.LcBinning(0.3, 25.0, 6, 5, 30.0)
+    chi_raw = lambda a: cosmo.comoving_radial_distance(a)
+    chi = lambda zz: chi_raw(1 / (1 + zz))
+    pos, shp = _prep(sel, chi, True)
+    pp = rng.integers(0, 4, len(sel["RA"]))
+    sp = rng.integers(0, 4, len(sel["RA_shape_sample"]))
+    pos["patch"], shp["patch"] = pp, sp.astype(np.int32)
+    counter = LightconeCounter(kind, True, b.r_bins, 0.3, 25.0, b.pi_bins if kind == "w" else b.mu_r_bins)
+    assert counter._wide_sums(pos, shp)
+    sums, counts = counter.count(pos, shp, 4)
+    reals = [(np.ones(len(pp), bool), np.ones(len(sp), bool))] + [(pp != i, sp != i) for i in range(4)]
+    for k, (mp, ms) in enumerate(reals):
+        SP, SX, DD = LO.pair_counts(kind, True, b, _subset(sel, mp, ms), chi_raw, h, False, None)
+        dd = sums[0, k].copy()
+        dd[(dd == 0) | (counts[k] == 0)] = 1
+        np.testing.assert_allclose(dd, DD, rtol=1e-10, atol=0, err_msg=f"DD {k}")
+        _close(sums[1, k], SP, f"S+D {k}")
+        _close(sums[2, k], SX, f"SxD {k}")
