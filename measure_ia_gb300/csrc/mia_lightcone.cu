@@ -475,104 +475,134 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
       const float kx = wn.kx, ky = wn.ky, gq = wn.gq, gqp = wn.gqp, gmu = wn.gmu, gl = wn.gl;
       const float4 nhl = pos.hl[ip];
       const float2 nch = pos.chl[ip];
-      for (int d = d0; d <= d1; ++d) {
-        // a shape in DEC band d is at least `gap` cells from the position in
-        // DEC, so within r_lim it is at most sra sqrt(1 - (gap / sdec)^2)
-        // cells away in RA (the window's ellipse); FP32 with margins of
-        // 2e-3 cells and 1e-5 relative keeps the range a superset
-        int ra0 = a0, ra1 = a1;
-        if (wn.sra >= 0.0f) {
-          float gap = 0.0f;
-          if (d > 0) gap = fmaxf(gap, (float)d - wn.tdec);
-          if (d < P.g.n_dec - 1) gap = fmaxf(gap, wn.tdec - (float)(d + 1));
-          const float rr = fmaxf(gap - 2e-3f, 0.0f) / wn.sdec;
-          if (rr >= 1.0f) continue;
-          const float wc = wn.sra * sqrtf(1.0f - rr * rr) * (1.0f + 1e-5f) + 2e-3f;
-          // clamped as cell_1d clamps: the end cells also hold what lies beyond
-          const int nr = P.g.n_ra - 1;
-          ra0 = max(a0, min(nr, max(0, (int)floorf(wn.tra - wc))));
-          ra1 = min(a1, min(nr, max(0, (int)floorf(wn.tra + wc))));
-          if (ra0 > ra1) continue;
+      // the window's rows, (DEC band, distance slab) pairs with their RA
+      // ranges, are read 32 at a time: lane k sets up row sb + k (its shape
+      // range in cell order), a warp scan gives the rows' offsets, and the
+      // warp then walks the concatenated candidates 32 at a time, so no lane
+      // idles at the end of a row
+      const int nc = c1 - c0 + 1, nseg = (d1 - d0 + 1) * nc;
+      for (int sb = 0; sb < nseg; sb += 32) {
+        int sj0 = 0, slen = 0;
+        if (sb + lane < nseg) {
+          const int s = sb + lane, d = d0 + s / nc, c = c0 + s % nc;
+          // a shape in DEC band d is at least `gap` cells from the position in
+          // DEC, so within r_lim it is at most sra sqrt(1 - (gap / sdec)^2)
+          // cells away in RA (the window's ellipse); FP32 with margins of
+          // 2e-3 cells and 1e-5 relative keeps the range a superset
+          int ra0 = a0, ra1 = a1;
+          bool keep = true;
+          if (wn.sra >= 0.0f) {
+            float gap = 0.0f;
+            if (d > 0) gap = fmaxf(gap, (float)d - wn.tdec);
+            if (d < P.g.n_dec - 1) gap = fmaxf(gap, wn.tdec - (float)(d + 1));
+            const float rr = fmaxf(gap - 2e-3f, 0.0f) / wn.sdec;
+            keep = rr < 1.0f;
+            const float wc = wn.sra * sqrtf(fmaxf(1.0f - rr * rr, 0.0f)) * (1.0f + 1e-5f) + 2e-3f;
+            // clamped as cell_1d clamps: the end cells also hold what lies beyond
+            const int nr = P.g.n_ra - 1;
+            ra0 = max(a0, min(nr, max(0, (int)floorf(wn.tra - wc))));
+            ra1 = min(a1, min(nr, max(0, (int)floorf(wn.tra + wc))));
+            keep = keep && ra0 <= ra1;
+          }
+          if (keep) {
+            const int row = (d * P.g.n_chi + c) * P.g.n_ra;
+            sj0 = start[row + ra0];
+            slen = start[row + ra1 + 1] - sj0;
+          }
         }
-        for (int c = c0; c <= c1; ++c) {
-          const int row = (d * P.g.n_chi + c) * P.g.n_ra;
-          const int j0 = start[row + ra0], j1 = start[row + ra1 + 1];
-          for (int jj = j0; jj < j1; jj += 32) {
-            const int j = jj + lane;
-            bool take = false;   // binned (bin decided) or in the guard band
-            bool near = false;
-            int bin = -1;
-            if (j < j1) {
-              const float4 s4 = shp.hl[j];
-              const float2 sc = shp.chl[j];
-              const float ax = ((s4.x - nhl.x) + (s4.y - nhl.y)) * kx;
-              const float ay = ((s4.z - nhl.z) + (s4.w - nhl.w)) * ky;
-              const float lf = (sc.x - nch.x) + (sc.y - nch.y);
-              const float qn = ax * ax + ay * ay;
-              int ib = -1, jb = -1;
-              if (KIND == MIA_KIND_W) {
-                if (qn <= P.qf_hi && lf >= P.los_lo && lf <= P.los_hi) {
-                  jb = lookup_f(s_pbf, s_pbn, P.n_pbreak, lf, lf * P.pa + P.pb, kRelGuard * fabsf(lf) + gl, near);
-                  if (near || jb != -1) {
-                    ib = lookup_f(s_qbf, s_qbn, P.n_qbreak, qn, __log2f(qn) * P.qa + P.qb, kRelGuard * qn + gq, near);
-                    take = near || ib != -1;
-                  }
+        int incl = slen;   // inclusive prefix of the row lengths over the lanes
+        for (int of = 1; of < 32; of <<= 1) {
+          const int y = __shfl_up_sync(0xffffffffu, incl, of);
+          if (lane >= of) incl += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        int seg = 0;       // this lane's row (lane index of its setup), non-decreasing
+        for (int vb = 0; vb < total; vb += 32) {
+          const int v = vb + lane;
+          // move each lane to the row holding candidate v (warp-uniform loop:
+          // every lane takes part in the shuffles)
+          for (;;) {
+            const int end = __shfl_sync(0xffffffffu, incl, seg);
+            const bool adv = v < total && v >= end;
+            if (!__any_sync(0xffffffffu, adv)) break;
+            if (adv) ++seg;
+          }
+          const int base_j = __shfl_sync(0xffffffffu, sj0, seg);
+          const int before = __shfl_sync(0xffffffffu, incl - slen, seg);
+          const int j = base_j + (v - before);
+          bool take = false;   // binned (bin decided) or in the guard band
+          bool near = false;
+          int bin = -1;
+          if (v < total) {
+            const float4 s4 = shp.hl[j];
+            const float2 sc = shp.chl[j];
+            const float ax = ((s4.x - nhl.x) + (s4.y - nhl.y)) * kx;
+            const float ay = ((s4.z - nhl.z) + (s4.w - nhl.w)) * ky;
+            const float lf = (sc.x - nch.x) + (sc.y - nch.y);
+            const float qn = ax * ax + ay * ay;
+            int ib = -1, jb = -1;
+            if (KIND == MIA_KIND_W) {
+              if (qn <= P.qf_hi && lf >= P.los_lo && lf <= P.los_hi) {
+                jb = lookup_f(s_pbf, s_pbn, P.n_pbreak, lf, lf * P.pa + P.pb, kRelGuard * fabsf(lf) + gl, near);
+                if (near || jb != -1) {
+                  ib = lookup_f(s_qbf, s_qbn, P.n_qbreak, qn, __log2f(qn) * P.qa + P.qb, kRelGuard * qn + gq, near);
+                  take = near || ib != -1;
                 }
-              } else {
-                const float q = qn + lf * lf;
-                if (q <= P.qf_hi) {
-                  bool cut_ok = true;
-                  if (P.rp_cut >= 0.0) {
-                    const float qp = qn * h2f;
-                    if (fabsf(qp - rc2f) <= kRelGuard * fmaxf(qp, rc2f) + gqp) near = true;
-                    cut_ok = qp > rc2f;
-                  }
-                  if (near || cut_ok) {
-                    ib = lookup_f(s_qbf, s_qbn, P.n_qbreak, q, __log2f(q) * P.qa + P.qb, kRelGuard * q + gq, near);
-                    if (near || ib != -1) {
-                      const float rq = rsqrtf(q);
-                      const float mu = lf * rq;
-                      jb = lookup_f(s_pbf, s_pbn, P.n_pbreak, mu, mu * P.pa + P.pb, kRelGuard + gmu * rq, near);
-                      take = true;
-                    }
+              }
+            } else {
+              const float q = qn + lf * lf;
+              if (q <= P.qf_hi) {
+                bool cut_ok = true;
+                if (P.rp_cut >= 0.0) {
+                  const float qp = qn * h2f;
+                  if (fabsf(qp - rc2f) <= kRelGuard * fmaxf(qp, rc2f) + gqp) near = true;
+                  cut_ok = qp > rc2f;
+                }
+                if (near || cut_ok) {
+                  ib = lookup_f(s_qbf, s_qbn, P.n_qbreak, q, __log2f(q) * P.qa + P.qb, kRelGuard * q + gq, near);
+                  if (near || ib != -1) {
+                    const float rq = rsqrtf(q);
+                    const float mu = lf * rq;
+                    jb = lookup_f(s_pbf, s_pbn, P.n_pbreak, mu, mu * P.pa + P.pb, kRelGuard + gmu * rq, near);
+                    take = true;
                   }
                 }
               }
-              if (take && !near) {
-                if (ib < 0 || jb < 0) {   // np.add.at would raise IndexError here
-                  atomicOr(acc.status, MIA_LC_INDEX_ERROR);
-                  take = false;
-                } else {
-                  bin = ib * P.n_p + jb;
-                }
-              }
-              if (!SHAPES && take && !near) {   // counts only: w_p w_s is all there is to add
-                accumulate(j, bin, UNIT ? 1.0 : __dmul_rn(w_n, shp.w[j]), 0.0, 0.0);
+            }
+            if (take && !near) {
+              if (ib < 0 || jb < 0) {   // np.add.at would raise IndexError here
+                atomicOr(acc.status, MIA_LC_INDEX_ERROR);
                 take = false;
+              } else {
+                bin = ib * P.n_p + jb;
               }
             }
-            const unsigned bal = __ballot_sync(0xffffffffu, take);
-            if (bal) {
-              if (take) queue[cnt + __popc(bal & ((1u << lane) - 1u))] = make_int4(j, (int)ip, near ? -1 : bin, 0);
-              cnt += __popc(bal);
-              if (cnt >= 32) {
-                __syncwarp();
-                const int4 mine = queue[lane];
-                __syncwarp();
-                const int rest = cnt - 32;
-                if (lane < rest) queue[lane] = queue[32 + lane];
-                cnt = rest;
-                __syncwarp();
-                process(true, mine);
-              }
+            if (!SHAPES && take && !near) {   // counts only: w_p w_s is all there is to add
+              accumulate(j, bin, UNIT ? 1.0 : __dmul_rn(w_n, shp.w[j]), 0.0, 0.0);
+              take = false;
             }
-            // a step adds at most 64 terms to the partials (32 decided here,
-            // 32 from the queue); 1000 steps stay below 2^16 terms of < 2^47
-            steps += 2;
-            if (steps >= kLcFlushSteps) {
-              flush_hist(cur);
-              steps = 0;
+          }
+          const unsigned bal = __ballot_sync(0xffffffffu, take);
+          if (bal) {
+            if (take) queue[cnt + __popc(bal & ((1u << lane) - 1u))] = make_int4(j, (int)ip, near ? -1 : bin, 0);
+            cnt += __popc(bal);
+            if (cnt >= 32) {
+              __syncwarp();
+              const int4 mine = queue[lane];
+              __syncwarp();
+              const int rest = cnt - 32;
+              if (lane < rest) queue[lane] = queue[32 + lane];
+              cnt = rest;
+              __syncwarp();
+              process(true, mine);
             }
+          }
+          // a step adds at most 64 terms to the partials (32 decided here,
+          // 32 from the queue); 1000 steps stay below 2^16 terms of < 2^47
+          steps += 2;
+          if (steps >= kLcFlushSteps) {
+            flush_hist(cur);
+            steps = 0;
           }
         }
       }
