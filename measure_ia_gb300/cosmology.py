@@ -61,7 +61,8 @@ class FlatLCDM:
         return half * (_GL_W[None, :] / self.E(zz)).sum(axis=1)
 
     def _table(self, k_lo, k_hi):
-        """Distances (units of c/H0) at the nodes k_lo..k_hi (k_lo <= 0 <= k_hi)."""
+        """Distances (units of c/H0) at the nodes k_lo..k_hi (k_lo <= 0 <= k_hi),
+        and the Hermite derivatives DZ / E(z_k) there."""
         t = getattr(self, "_tab", None)
         if t is not None and t[0] <= k_lo and t[1] >= k_hi:
             return t
@@ -72,7 +73,10 @@ class FlatLCDM:
         cu = np.concatenate([[0.0], np.cumsum(self._integral(up[:-1], up[1:]))])
         cd = np.concatenate([[0.0], np.cumsum(self._integral(down[:-1], down[1:]))])
         vals = np.concatenate([cd[::-1][:-1], cu])          # nodes k_lo .. k_hi
-        self._tab = (k_lo, k_hi, vals)
+        # z_k = k * DZ exactly as the query side forms it, so the derivatives
+        # are the same doubles as E evaluated per query
+        nodes = np.arange(k_lo, k_hi + 1, dtype=np.float64) * self.DZ
+        self._tab = (k_lo, k_hi, vals, self.DZ / self.E(nodes))
         return self._tab
 
     def comoving_radial_distance(self, a):
@@ -84,13 +88,12 @@ class FlatLCDM:
         if not np.all(np.isfinite(z)):
             raise ValueError("redshifts must be finite")
         k = np.floor(z / self.DZ)
-        k_lo, k_hi, vals = self._table(int(k.min()) - 1, int(k.max()) + 2)
+        k_lo, k_hi, vals, dvals = self._table(int(k.min()) - 1, int(k.max()) + 2)
         i = (k - k_lo).astype(np.int64)
         z0 = k * self.DZ
         t = (z - z0) / self.DZ
         f0, f1 = vals[i], vals[i + 1]
-        d0 = self.DZ / self.E(z0)
-        d1 = self.DZ / self.E(z0 + self.DZ)
+        d0, d1 = dvals[i], dvals[i + 1]
         t2 = t * t
         t3 = t2 * t
         chi = (2 * t3 - 3 * t2 + 1) * f0 + (t3 - 2 * t2 + t) * d0 + (-2 * t3 + 3 * t2) * f1 + (t3 - t2) * d1

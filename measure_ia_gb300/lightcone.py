@@ -46,6 +46,17 @@ def _centres(edges):
 # one counter on the GPU
 # ----------------------------------------------------------------------------
 
+def _median_abs(a):
+    """Median of |a| (1 for an empty array), over an evenly strided subsample
+    of ~32k values for large arrays: it only sizes the cell grid."""
+    a = np.asarray(a, dtype=np.float64)
+    if not len(a):
+        return 1.0
+    if len(a) > (1 << 16):
+        a = a[:: len(a) >> 15]
+    return float(np.median(np.abs(a)))
+
+
 class LightconeCounter:
     """One of the reference's four lightcone pair counters, with patch
     realisations, through ``mia_lc_count``."""
@@ -84,8 +95,8 @@ class LightconeCounter:
         lo = np.array([ra.min(), dec.min(), chi.min()])
         hi = np.array([ra.max(), dec.max(), chi.max()])
         hx = self.h_extra if self.kind == "w" else 1.0
-        chi_med = float(np.median(np.abs(pos["chi"]))) if len(pos["chi"]) else 1.0
-        cos_med = float(np.median(np.abs(pos["cos_dec"]))) if len(pos["cos_dec"]) else 1.0
+        chi_med = _median_abs(pos["chi"])
+        cos_med = _median_abs(pos["cos_dec"])
         span = self.r_lim / max(hx * chi_med, 1e-12) / (np.pi / 180.0)
         chi_span = (self.pi_hi - self.pi_lo) if self.kind == "w" else 2.0 * self.r_lim
         dv = self.cell_div
@@ -406,9 +417,26 @@ class _Run:
         self.pc = _centres(owner.pi_bins if kind == "w" else owner.mu_r_bins)
         self.out = {}
         self.nsj = {}
+        self._gs = set()          # every group that holds a stored dataset (path prefixes)
+        self._chi_memo = []       # (redshift array, distances): unmasked samples recur across counters
 
     def put(self, path, v):
-        self.out[norm_path(self.o.snap_group, path)] = np.asarray(v)
+        p = norm_path(self.o.snap_group, path)
+        self.out[p] = np.asarray(v)
+        parts = p.split("/")
+        for k in range(1, len(parts)):
+            self._gs.add("/".join(parts[:k]))
+
+    def _chi(self, z):
+        """Distances of a redshift array, reused when the same array object
+        comes back (the distance is element-wise, so a masked copy would get
+        the same values; only the identical object is reused)."""
+        for a, c in self._chi_memo:
+            if a is z:
+                return c
+        c = self.chi(np.asarray(z, dtype=np.float64))
+        self._chi_memo.append((z, c))
+        return c
 
     def get(self, path):
         return self.out[norm_path(self.o.snap_group, path)]
@@ -454,11 +482,11 @@ class _Run:
                              f"but size of corresponding boolean axis is {n_s}")
         dec = np.asarray(sel["DEC"], dtype=np.float64)
         pos = {"ra": np.asarray(sel["RA"], dtype=np.float64), "dec": dec,
-               "chi": self.chi(np.asarray(sel["Redshift"], dtype=np.float64)), "w": w[:n_p],
+               "chi": self._chi(sel["Redshift"]), "w": w[:n_p],
                "cos_dec": np.cos(dec / 180 * np.pi)}
         shp = {"ra": np.asarray(sel["RA_shape_sample"], dtype=np.float64),
                "dec": np.asarray(sel["DEC_shape_sample"], dtype=np.float64),
-               "chi": self.chi(np.asarray(sel["Redshift_shape_sample"], dtype=np.float64)), "w": ws}
+               "chi": self._chi(sel["Redshift_shape_sample"]), "w": ws}
         if with_shapes:
             e1, e2 = np.asarray(sel["e1"], dtype=np.float64), np.asarray(sel["e2"], dtype=np.float64)
             theta = 1. / 2 * np.arctan2(e2, e1)
@@ -484,26 +512,40 @@ class _Run:
         return dd
 
     # ---- one counter: full sample (+ realisations) --------------------------
-    def count(self, pos_from, shape_from, with_shapes, name, suffix, patches=None, real_name=None,
-              real_suffix=None, names=None):
-        """The full-sample counter, and, with ``patches`` = (position patches,
-        shape patches), the pooled driver's realisations of it."""
+    def launch(self, pos_from, shape_from, with_shapes, name, suffix, patches=None, real_name=None,
+               real_suffix=None, names=None):
+        """Enqueue the full-sample counter (with ``patches`` = (position
+        patches, shape patches) and no masks, the pooled driver's realisations
+        in the same pass) and return the function that fetches its result and
+        writes the products.  The host work of the next counter then overlaps
+        this one on the GPU."""
         combo = self._combo(pos_from, shape_from, with_shapes)
         counter = self._counter(with_shapes)
         sel = self._select(combo, self.masks, with_shapes)
         # the reference hands the masks to the S+D and S+R realisations only
         # (measure_IA.py:562-590); the count realisations use every object
         rmasks = self.masks if with_shapes else None
-        real = None
-        if patches is not None and self.masks is None:
+        one_pass = patches is not None and self.masks is None
+        if one_pass:
             pp, sp = patches
             lo, hi = int(np.min(pp)), int(np.max(pp))
             pos, shp = self._samples(sel, with_shapes, np.asarray(pp) - lo, self._shape_labels(sp, lo, hi))
-            sums, cnt = counter.count(pos, shp, hi - lo + 1)
-            real = (lo, hi, sums, cnt)
+            job = counter.prepare(pos, shp, hi - lo + 1)
         else:
             pos, shp = self._samples(sel, with_shapes)
-            sums, cnt = counter.count(pos, shp, 0)
+            job = counter.prepare(pos, shp, 0)
+        counter.run(job)
+        del pos, shp
+
+        def finish():
+            sums, cnt = counter.fetch(job)
+            real = (lo, hi, sums, cnt) if one_pass else None
+            self._finish(combo, counter, with_shapes, rmasks, sums, cnt, real, name, suffix, patches, real_name,
+                         real_suffix, names)
+        return finish
+
+    def _finish(self, combo, counter, with_shapes, rmasks, sums, cnt, real, name, suffix, patches, real_name,
+                real_suffix, names):
         self._write_full(sums[:, 0], cnt[0], with_shapes, name, suffix)
         if patches is None:
             return
@@ -618,12 +660,7 @@ class _Run:
                 self.put(f"{top}/xi_gg/{g}{name}", (DD - RD - SR) / RR + 1)
 
     def _groups(self):
-        gs = set()
-        for p in self.out:
-            parts = p.split("/")
-            for k in range(1, len(parts)):
-                gs.add("/".join(parts[:k]))
-        return {g[len(self.o.snap_group):] if g.startswith(self.o.snap_group) else g for g in gs}
+        return {g[len(self.o.snap_group):] if g.startswith(self.o.snap_group) else g for g in self._gs}
 
     def integrate(self, name, grp=""):
         """measure_IA_base.py:515-668 for this corr_type."""
@@ -662,10 +699,20 @@ class _Run:
         if est == "galaxies" or corr in ("gg", "both"):
             steps.append(("R", "R", False, d, "_RR", P("randoms_position", "randoms_shape"), d, "_RR",
                           ["R_S", "R_D"]))
-        # full-sample products first, as the reference writes them before any realisation
-        real_todo = []
-        for pf, sf, ws, name, suffix, patches, rname, rsuffix, names in steps:
-            self.count(pf, sf, ws, name, suffix, patches, rname, rsuffix, names)
+        # every counter is enqueued first, then finished in the reference's
+        # order; if enqueuing one fails, those before it are finished (and
+        # their products kept) before the error propagates, as in the
+        # reference's one-after-the-other flow
+        pending = []
+        try:
+            for step in steps:
+                pending.append(self.launch(*step))
+        except BaseException:
+            for fin in pending:
+                fin()
+            raise
+        for fin in pending:
+            fin()
         self.obs(d, dr, ns)
         self.integrate(d)
         if jk is None:
