@@ -61,10 +61,16 @@ class LightconeCounter:
     """One of the reference's four lightcone pair counters, with patch
     realisations, through ``mia_lc_count``."""
 
+    # cells per window half-width along RA and DEC and per distance window,
+    # from sweeps on the 1000 deg^2 / 1M-random workload
+    CELL_DIV = {"w": (8.0, 3.0, 4.0), "m": (8.0, 3.0, 6.0)}
+
     def __init__(self, kind, with_shapes, r_bins, r_min, r_max, p_bins, h_extra=1.0, rp_cut=0.0, device=0,
-                 cell_div=(8.0, 3.0, 3.0)):
+                 cell_div=None):
         if kind not in ("w", "m"):
             raise ValueError(kind)
+        if cell_div is None:
+            cell_div = self.CELL_DIV[kind]
         self.kind, self.with_shapes, self.device = kind, bool(with_shapes), device
         self.n_r, self.n_p = len(r_bins) - 1, len(p_bins) - 1
         if self.n_r > L.MAX_BINS_R or self.n_p > L.MAX_BINS_P:
