@@ -154,10 +154,21 @@ class MeasureIABox(SimInfo):
             raise ValueError("Invalid value for ellipticity. Choose 'distortion' or 'ellipticity'.")
         L_sub, layout = self._validate(corr_type, num_jk, temp_file_path)
         cat = self._select(masks)
+        for key in ("weight", "weight_shape_sample", "q"):
+            if not np.all(np.isfinite(np.asarray(cat[key], dtype=np.float64))):
+                # the reference carries these into NaN sums (a NaN q or shape
+                # weight makes its responsivity, and so every S+D bin, NaN)
+                raise ValueError(f"'{key}' values must be finite")
+        precision = self.precision
+        if precision == "mixed" and not np.all(np.isfinite(np.asarray(cat["Axis_Direction"], dtype=np.float64))):
+            # a non-finite axis gives e+ = ex = 0 in the reference (NaN -> 0,
+            # measure_w_box_jk.py:599-600); the FP64 form repeats that exactly
+            warnings.warn("mixed form: non-finite Axis_Direction, measuring in the FP64 form", RuntimeWarning)
+            precision = "fp64"
         los = self.data["LOS"]
         args = dict(boxsize=self.boxsize, r_bins=self.r_bins, r_min=self.r_min, r_max=self.r_max,
                     p_bins=self.pi_bins if kind == "w" else self.mu_r_bins, los=los, l_subboxes=L_sub,
-                    precision=self.precision, membership="brute" if layout == "brute" else "tree",
+                    precision=precision, membership="brute" if layout == "brute" else "tree",
                     ellipticity=ellipticity, want_variance=(layout == "brute" and L_sub > 0),
                     volume=self.boxsize ** 3, rp_cut=0.0 if rp_cut is None else rp_cut, device=self.device)
         counter = PairCounter(kind, **args)
@@ -171,7 +182,7 @@ class MeasureIABox(SimInfo):
         except MiaError as exc:
             # more pairs near a bin edge than the FP64 re-test queue holds:
             # the mixed form cannot finish exactly, the FP64 form always can
-            if exc.code != MIA_ERR_OVERFLOW or self.precision != "mixed":
+            if exc.code != MIA_ERR_OVERFLOW or precision != "mixed":
                 raise
             warnings.warn("mixed form: edge re-test queue overflow, measuring in the FP64 form", RuntimeWarning)
             del bufs

@@ -224,3 +224,33 @@ def test_positions_on_subbox_faces(kind, precision, tmp_path):
     rtol = FP64_RTOL if precision == "fp64" else MIXED_RTOL
     for path, v in ref.items():
         _close(store.read(path), v, rtol, path)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nan_axis_directions(precision, tmp_path):
+    """A shape with a NaN axis contributes e+ = ex = 0 (the reference's NaN -> 0,
+    measure_w_box_jk.py:599-600) and still counts in DD; the mixed form hands
+    such a catalogue to the FP64 form with a warning."""
+    from measure_ia_gb300 import MeasureIABox, open_output
+    rng = np.random.default_rng(77)
+    L, n = 100.0, 3000
+    pos = rng.uniform(0, L, (n, 3))
+    ang = rng.uniform(0, np.pi, n)
+    ax = np.c_[np.cos(ang), np.sin(ang)]
+    ax[::17] = np.nan
+    data = {"Position": pos, "Position_shape_sample": pos.copy(), "Axis_Direction": ax,
+            "q": rng.uniform(0.2, 1, n), "LOS": 2, "weight": np.exp(rng.normal(0, 0.3, n)),
+            "weight_shape_sample": np.exp(rng.normal(0, 0.3, n))}
+    b = O.Binning(boxsize=L, r_min=0.1, r_max=10.0, num_bins_r=6, num_bins_pi=4, pi_max=10.0)
+    ref = dict(O.measure("w", b, _copy(data), "a", "both", 8, None, "distortion", "tree"))
+    ref.pop("__counts__")
+    out = str(tmp_path / "nan_axis.hdf5")
+    box = MeasureIABox(_copy(data), out, None, None, [0.1, 10.0], 6, 4, 10.0, boxsize=L, precision=precision)
+    if precision == "mixed":
+        with pytest.warns(RuntimeWarning, match="Axis_Direction"):
+            box.measure_xi_w("a", "both", 8, temp_file_path=str(tmp_path))
+    else:
+        box.measure_xi_w("a", "both", 8, temp_file_path=str(tmp_path))
+    store = open_output(out)
+    for path, v in ref.items():
+        _close(store.read(path), v, FP64_RTOL, path)

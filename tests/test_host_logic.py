@@ -157,3 +157,22 @@ def test_autotune_cache_roundtrip(tmp_path, monkeypatch):
     assert set(autotune.KNOBS) <= set(autotune.load_cache()[k1])
     sides, los_sides, refines, units = autotune.candidates(20.0, 40.0)
     assert len(sides) == 6 and 40.0 in los_sides and 2 in refines and 128 in units
+
+
+@pytest.mark.parametrize("key,value", [("q", np.nan), ("weight", np.inf), ("weight_shape_sample", np.nan)])
+def test_box_rejects_non_finite_weights_and_q(key, value):
+    """A non-finite weight or q makes the reference's sums (through the
+    responsivity, every S+D bin) NaN; the box path refuses them before any
+    GPU work."""
+    from measure_ia_gb300 import MeasureIABox
+    rng = np.random.default_rng(0)
+    n = 200
+    pos = rng.uniform(0, 100.0, (n, 3))
+    ang = rng.uniform(0, np.pi, n)
+    data = {"Position": pos, "Position_shape_sample": pos.copy(), "Axis_Direction": np.c_[np.cos(ang), np.sin(ang)],
+            "q": rng.uniform(0.2, 1, n), "LOS": 2, "weight": np.ones(n), "weight_shape_sample": np.ones(n)}
+    data[key] = data[key].copy()
+    data[key][3] = value
+    box = MeasureIABox(data, None, None, None, [0.1, 10.0], 6, 4, 10.0, boxsize=100.0)
+    with pytest.raises(ValueError, match="finite"):
+        box.measure_xi_w("a", "both", 0, temp_file_path="/tmp")
