@@ -16,6 +16,12 @@
 // one per jackknife region b of the positions ("slot"), flushed at the end of
 // the unit into the global histograms of all pairs, of region a and of region
 // b != a (the attribution rule of measure_w_box_jk.py:625-644).
+//
+// Sums are exact integers in both forms, so no result depends on the order in
+// which blocks meet the pairs: the mixed form adds FP32 terms as 64-bit fixed
+// point (32-bit low words with carries), the FP64 form adds FP64 terms as
+// 128-bit fixed point (Fix128); one kernel converts each sum to a double at
+// the end.
 #include <cstdio>
 
 #include "mia_internal.cuh"
