@@ -25,6 +25,7 @@
 // can reach one, the totals 128-bit (Fix128).  The sums do not depend on the
 // order in which warps meet the pairs, and total - A[i] - B[i] is exact.
 #include <cstdio>
+#include <cstdlib>
 
 #include "mia_internal.cuh"
 
@@ -127,6 +128,7 @@ struct LcParams {
   float qa, qb, pa, pb;        // first guesses of the table interval: log2(q) * qa + qb, x * pa + pb
   int unit;                    // unit weights: DD is the pair count, not summed
   int hq;                      // value arrays in a warp's histogram: Q, or 0 (unit-weight counts)
+  int flush_steps;             // half-steps between flushes of the warp partials (2..kLcFlushSteps)
   LcGrid g;
   long long n_pos;
 };
@@ -220,7 +222,7 @@ __device__ inline int lc_exponent(const unsigned long long* wmax, int wide) {
   const int e = ilogb(70368744177664.0 / m);  // 2^46
   return e > 1000 ? 1000 : (e < -1000 ? -1000 : e);
 }
-constexpr int kLcFlushSteps = 2000;   // half-steps (<= 32 terms each) between partial flushes
+constexpr int kLcFlushSteps = 2000;   // half-steps (<= 32 terms each) between partial flushes (at most)
 
 // shared-memory bytes of the tables: double and FP32 breaks, bins; 16-byte rounded
 constexpr size_t kLcTableBytes = (2 * MIA_MAX_BREAKS * 8 + 2 * MIA_MAX_BREAKS * 4 + 2 * (MIA_MAX_BREAKS + 1) * 4 + 15) & ~size_t(15);
@@ -600,7 +602,7 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
           // a step adds at most 64 terms to the partials (32 decided here,
           // 32 from the queue); 1000 steps stay below 2^16 terms of < 2^47
           steps += 2;
-          if (steps >= kLcFlushSteps) {
+          if (steps >= P.flush_steps) {
             flush_hist(cur);
             steps = 0;
           }
@@ -842,6 +844,13 @@ cudaError_t launch_lc(const mia_lc_config* cfg, const LcPlan& p, const mia_lc_sa
   P.n_pos = pos.n;
   P.unit = cfg->unit_weights ? 1 : 0;
   P.hq = p.hq;
+  // MIA_LC_FLUSH_STEPS=<n> flushes the warp partials more often (tests of the
+  // flush path; the default is the largest interval the 64-bit partials allow)
+  P.flush_steps = kLcFlushSteps;
+  if (const char* env = std::getenv("MIA_LC_FLUSH_STEPS")) {
+    const int v = std::atoi(env);
+    if (v >= 2 && v < kLcFlushSteps) P.flush_steps = v;
+  }
   // first guesses of the table intervals: breaks 0 and n-1 map to 1 and n
   auto affine = [](const double* br, int n, bool logq, float* a, float* b) {
     *a = 0.0f;
