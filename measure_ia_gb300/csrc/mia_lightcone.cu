@@ -140,8 +140,10 @@ struct LcWin {
   float kx, ky;                // Mpc per degree of RA / DEC difference (times h_extra for w)
   float gq, gqp, gmu, gl;      // absolute error bounds (see k_lc_windows)
   // the position and the window's half-widths in RA / DEC cell units, for
-  // trimming each DEC row's RA range to the window's ellipse (sra < 0: no trim)
-  float tra, tdec, sra, sdec;
+  // trimming each DEC row's RA range to the window's ellipse (sra < 0: no trim);
+  // multipoles also in distance-slab units (schi > 0): r^2 = r_p^2 + Pi^2, so
+  // a slab's distance gap narrows the ellipse too
+  float tra, tdec, sra, sdec, tchi, schi;
 };
 
 // Per sorted position: the cell ranges its separation window reaches (a
@@ -195,6 +197,10 @@ __global__ void k_lc_windows(const LcParams P, const LcSorted pos, LcWin* __rest
     const bool trim = sra < 1e6 && sdec < 1e6 && sdec > 1e-6 && fabs((double)w.tra) < 1e6 && fabs((double)w.tdec) < 1e6;
     w.sra = trim ? (float)sra : -1.0f;
     w.sdec = trim ? (float)sdec : 1.0f;
+    w.tchi = (float)((chi_n - g.chi0) * g.inv_chi);
+    const double schi = (P.r_lim * (1.0 + 1e-6) + m) * g.inv_chi;
+    w.schi = (KIND == MIA_KIND_MULTIPOLES && trim && schi > 1e-6 && schi < 1e6 && fabs((double)w.tchi) < 1e6)
+                 ? (float)schi : -1.0f;
     win[ip] = w;
   }
 }
@@ -498,8 +504,16 @@ k_lc_pairs(const LcParams P, const LcTables T, const LcSorted pos, const LcSorte
             if (d > 0) gap = fmaxf(gap, (float)d - wn.tdec);
             if (d < P.g.n_dec - 1) gap = fmaxf(gap, wn.tdec - (float)(d + 1));
             const float rr = fmaxf(gap - 2e-3f, 0.0f) / wn.sdec;
-            keep = rr < 1.0f;
-            const float wc = wn.sra * sqrtf(fmaxf(1.0f - rr * rr, 0.0f)) * (1.0f + 1e-5f) + 2e-3f;
+            float room = 1.0f - rr * rr;
+            if (wn.schi > 0.0f) {
+              float gc = 0.0f;
+              if (c > 0) gc = fmaxf(gc, (float)c - wn.tchi);
+              if (c < P.g.n_chi - 1) gc = fmaxf(gc, wn.tchi - (float)(c + 1));
+              const float rc = fmaxf(gc - 2e-3f, 0.0f) / wn.schi;
+              room -= rc * rc;
+            }
+            keep = room > -1e-6f;
+            const float wc = wn.sra * sqrtf(fmaxf(room, 0.0f)) * (1.0f + 1e-5f) + 2e-3f;
             // clamped as cell_1d clamps: the end cells also hold what lies beyond
             const int nr = P.g.n_ra - 1;
             ra0 = max(a0, min(nr, max(0, (int)floorf(wn.tra - wc))));
