@@ -661,7 +661,7 @@ def run_lightcone(args, local):
                          "note": "achieved = FP32 lane-ops of a fixed recipe per binned pair (15 counts only, 28 "
                                  "with shapes) x binned pairs / device time of the four counters; peak = nominal "
                                  "SMs x 128 x 2070 MHz (no FP32 figure in MEASURED_PEAKS.json).  The counters are "
-                                 "issue-bound (RR ~70% issue, 13.8 warp instructions per binned pair: cell rows, "
+                                 "issue-bound (RR ~71% issue, 13.0 warp instructions per binned pair: candidate tests, "
                                  "guard-band decisions, jackknife attribution), the shape terms FP64",
                          "fp64_dgemm_tflops": dgemm},
             "cpu_baseline": cpu,
