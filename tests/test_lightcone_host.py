@@ -96,3 +96,54 @@ def test_reference_argument_errors():
         lc.measure_xi_w("clusters", "d", "both", measure_cov=True)
     with pytest.raises(KeyError, match="Unknown value for corr_type"):
         lc.measure_xi_multipoles("clusters", "d", "g-", calc_errors=False)
+
+
+def test_distance_derivatives_from_the_node_table():
+    """The Hermite derivatives c/H at the nodes come from a table built once;
+    the distances are the same doubles as with E(z) evaluated per object."""
+    from measure_ia_gb300.cosmology import FlatLCDM
+    c = FlatLCDM()
+    rng = np.random.default_rng(3)
+    z = np.concatenate([rng.uniform(0.0, 3.0, 5000), rng.uniform(-0.05, 0.01, 200), [0.0, 1 / 2048, 2.5]])
+    got = c.comoving_radial_distance(1 / (1 + z))
+    # the same interpolation with the derivatives evaluated per object
+    zz = 1 / (1 / (1 + z)) - 1
+    k = np.floor(zz / c.DZ)
+    k_lo, _, vals, _ = c._table(int(k.min()) - 1, int(k.max()) + 2)
+    i = (k - k_lo).astype(np.int64)
+    z0 = k * c.DZ
+    t = (zz - z0) / c.DZ
+    d0, d1 = c.DZ / c.E(z0), c.DZ / c.E(z0 + c.DZ)
+    t2, t3 = t * t, t * t * t
+    chi = (2 * t3 - 3 * t2 + 1) * vals[i] + (t3 - 2 * t2 + t) * d0 + (-2 * t3 + 3 * t2) * vals[i + 1] + (t3 - t2) * d1
+    np.testing.assert_array_equal(got, chi * (299792.458 / (100.0 * c.h)))
+
+
+def test_wide_sums_choice():
+    """128-bit warp partials when the smallest weight product is below 2^-12
+    of the largest possible term, 64-bit ones otherwise."""
+    from measure_ia_gb300.lightcone import LightconeCounter
+    c = LightconeCounter("w", True, np.logspace(-1, 1, 5), 0.1, 10.0, np.linspace(-10, 10, 5))
+    n = 100
+    pos = {"w": np.ones(n)}
+    shp = {"w": np.ones(n), "e": np.full(n, 0.3)}
+    assert not c._wide_sums(pos, shp)
+    shp["w"] = np.linspace(0.1, 10.0, n)                   # products from 0.1 to 10: 2^-7
+    assert not c._wide_sums(pos, shp)
+    pos["w"] = np.r_[np.ones(n - 1), 1e-3]                 # 1e-4 of the largest: below 2^-12
+    assert c._wide_sums(pos, shp)
+    pos["w"] = np.r_[np.ones(n - 1), 0.0]                  # zero weights do not count
+    assert not c._wide_sums(pos, shp)
+    shp = {"w": np.ones(n), "e": np.r_[np.full(n - 1, 0.3), 5000.0]}   # |w e| sets the largest term
+    pos["w"] = np.ones(n)
+    assert c._wide_sums(pos, shp)
+    assert not c._wide_sums({"w": np.array([])}, shp)
+
+
+def test_grid_median_subsample():
+    from measure_ia_gb300.lightcone import _median_abs
+    assert _median_abs(np.array([])) == 1.0
+    a = np.linspace(-3.0, 5.0, 1001)
+    assert _median_abs(a) == np.median(np.abs(a))
+    big = np.random.default_rng(1).uniform(100.0, 200.0, 1 << 20)
+    assert abs(_median_abs(big) - np.median(big)) < 1.0
