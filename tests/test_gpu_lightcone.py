@@ -313,3 +313,25 @@ def test_partial_flushes(kind, shapes, monkeypatch):
         if shapes:
             _close(sums[1, k], SP, f"S+D {k}")
             _close(sums[2, k], SX, f"SxD {k}")
+
+
+def test_failing_counter_keeps_earlier_products(tmp_path):
+    """The counters are enqueued ahead of their results; when a later one
+    cannot start (here RD: a randoms shape redshift is NaN), the products of
+    the counters before it are still written, as in the reference's
+    one-after-the-other flow, and nothing of RD or RR is."""
+    from measure_ia_gb300 import open_output
+    meta, data, rnd, jk, outs, cosmo = load_lc_case("w_clusters_both")
+    rnd = {k: np.array(v) for k, v in rnd.items()}
+    if "Redshift_shape_sample" not in rnd:
+        rnd.update(RA_shape_sample=rnd["RA"].copy(), DEC_shape_sample=rnd["DEC"].copy(),
+                   Redshift_shape_sample=rnd["Redshift"].copy())
+    rnd["Redshift_shape_sample"][0] = np.nan
+    meta = dict(meta, measure_cov=False)
+    out = str(tmp_path / "fail.hdf5")
+    with pytest.raises(ValueError, match="finite"):   # the package's FlatLCDM refuses a NaN redshift
+        _run_product(meta, data, rnd, jk, None, out)
+    keys = set(open_output(out).keys())
+    assert any(k.endswith("lc_SplusD") for k in keys), sorted(keys)[:10]
+    assert any("randoms" in k and k.endswith("_SplusD") for k in keys), sorted(keys)[:10]
+    assert not any(k.endswith("_RD") or k.endswith("_RR") for k in keys), sorted(keys)[:10]
