@@ -147,3 +147,69 @@ def test_grid_median_subsample():
     assert _median_abs(a) == np.median(np.abs(a))
     big = np.random.default_rng(1).uniform(100.0, 200.0, 1 << 20)
     assert abs(_median_abs(big) - np.median(big)) < 1.0
+
+
+class _FakeCounter:
+    """The GPU counter's interface with made-up results (host-side flow tests)."""
+
+    def __init__(self, n_r, n_p, with_shapes, log):
+        self.n_r, self.n_p, self.Q, self.log = n_r, n_p, 3 if with_shapes else 1, log
+
+    def prepare(self, pos, shp, n_patch=0):
+        self.log.append("prepare")
+        return n_patch
+
+    def run(self, job, stream=None):
+        self.log.append("run")
+
+    def fetch(self, job):
+        self.log.append("fetch")
+        return (np.ones((self.Q, 1 + job, self.n_r, self.n_p)), np.ones((1 + job, self.n_r, self.n_p), np.int64))
+
+
+def _lc_inputs(n=300, seed=2):
+    rng = np.random.default_rng(seed)
+    data = {"RA": rng.uniform(10, 20, n), "DEC": rng.uniform(-5, 5, n), "Redshift": rng.uniform(0.1, 0.2, n),
+            "e1": rng.uniform(-0.3, 0.3, n), "e2": rng.uniform(-0.3, 0.3, n)}
+    data.update(RA_shape_sample=data["RA"], DEC_shape_sample=data["DEC"], Redshift_shape_sample=data["Redshift"])
+    rnd = {"RA": rng.uniform(10, 20, 2 * n), "DEC": rng.uniform(-5, 5, 2 * n), "Redshift": rng.uniform(0.1, 0.2, 2 * n)}
+    rnd.update(RA_shape_sample=rnd["RA"].copy(), DEC_shape_sample=rnd["DEC"].copy(),
+               Redshift_shape_sample=rnd["Redshift"].copy())
+    return data, rnd
+
+
+def test_counters_enqueued_before_results(monkeypatch, tmp_path):
+    """All four counters are prepared and run before the first result is
+    fetched; the results are then taken in the reference's order."""
+    from measure_ia_gb300 import lightcone as LC
+    log = []
+    monkeypatch.setattr(LC._Run, "_counter", lambda self, ws: _FakeCounter(
+        len(self.o.r_bins) - 1, len(self.o.pi_bins) - 1, ws, log))
+    data, rnd = _lc_inputs()
+    lc = LC.MeasureIALightcone(data, rnd, str(tmp_path / "ok.hdf5"), separation_limits=[0.5, 10.0], num_bins_r=4,
+                               num_bins_pi=4, pi_max=20.0)
+    lc.measure_xi_w("clusters", "lc", "both", measure_cov=False)
+    assert log == ["prepare", "run"] * 4 + ["fetch"] * 4
+
+
+def test_failing_counter_keeps_earlier_products_host(monkeypatch, tmp_path):
+    """When the third counter (RD) cannot start, the first two are still
+    finished and written before the error propagates; nothing of RD or RR is
+    written (the reference runs and writes them one after the other)."""
+    from measure_ia_gb300 import lightcone as LC
+    from measure_ia_gb300.output import open_output
+    log = []
+    monkeypatch.setattr(LC._Run, "_counter", lambda self, ws: _FakeCounter(
+        len(self.o.r_bins) - 1, len(self.o.pi_bins) - 1, ws, log))
+    data, rnd = _lc_inputs()
+    rnd["Redshift_shape_sample"][0] = np.nan
+    out = str(tmp_path / "fail.hdf5")
+    lc = LC.MeasureIALightcone(data, rnd, out, separation_limits=[0.5, 10.0], num_bins_r=4, num_bins_pi=4,
+                               pi_max=20.0)
+    with pytest.raises(ValueError, match="finite"):
+        lc.measure_xi_w("clusters", "lc", "both", measure_cov=False)
+    assert log == ["prepare", "run"] * 2 + ["fetch"] * 2
+    keys = set(open_output(out).keys())
+    assert any(k.endswith("lc_SplusD") for k in keys), sorted(keys)
+    assert any("randoms" in k and k.endswith("_SplusD") for k in keys), sorted(keys)
+    assert not any(k.endswith("_RD") or k.endswith("_RR") for k in keys), sorted(keys)
