@@ -176,3 +176,40 @@ def test_box_rejects_non_finite_weights_and_q(key, value):
     box = MeasureIABox(data, None, None, None, [0.1, 10.0], 6, 4, 10.0, boxsize=100.0)
     with pytest.raises(ValueError, match="finite"):
         box.measure_xi_w("a", "both", 0, temp_file_path="/tmp")
+
+
+def test_mixed_form_hands_nan_axes_to_fp64(monkeypatch):
+    """A non-finite Axis_Direction: the mixed form's FP32 terms would not give
+    the reference's e+ = ex = 0, so the measurement runs in the FP64 form,
+    with a warning (the counter itself is replaced here: no GPU)."""
+    import warnings
+    from measure_ia_gb300 import measure_ia as M
+    seen = []
+
+    class Stop(Exception):
+        pass
+
+    class FakeCounter:
+        def __init__(self, kind, **kw):
+            seen.append(kw["precision"])
+            raise Stop()
+
+    monkeypatch.setattr(M, "PairCounter", FakeCounter)
+    rng = np.random.default_rng(0)
+    n = 100
+    pos = rng.uniform(0, 100.0, (n, 3))
+    ang = rng.uniform(0, np.pi, n)
+    ax = np.c_[np.cos(ang), np.sin(ang)]
+    data = {"Position": pos, "Position_shape_sample": pos.copy(), "Axis_Direction": ax, "q": rng.uniform(0.2, 1, n),
+            "LOS": 2, "weight": np.ones(n), "weight_shape_sample": np.ones(n)}
+    for bad, want in ((False, "mixed"), (True, "fp64")):
+        d = dict(data, Axis_Direction=ax.copy())
+        if bad:
+            d["Axis_Direction"][7] = np.nan
+        box = M.MeasureIABox(d, None, None, None, [0.1, 10.0], 6, 4, 10.0, boxsize=100.0, precision="mixed")
+        with warnings.catch_warnings(record=True) as w:
+            warnings.simplefilter("always")
+            with pytest.raises(Stop):
+                box.measure_xi_w("a", "both", 0, temp_file_path="/tmp")
+        assert seen[-1] == want
+        assert any("Axis_Direction" in str(x.message) for x in w) == bad
