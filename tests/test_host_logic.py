@@ -213,3 +213,46 @@ def test_mixed_form_hands_nan_axes_to_fp64(monkeypatch):
                 box.measure_xi_w("a", "both", 0, temp_file_path="/tmp")
         assert seen[-1] == want
         assert any("Axis_Direction" in str(x.message) for x in w) == bad
+
+
+def _header_structs():
+    """Field (name, kind) lists of the header's typedef structs, kind one of
+    pointer / int / int64 / double."""
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "measure_ia_gb300.h")
+    text = re.sub(r"/\*.*?\*/", " ", open(path).read(), flags=re.S)
+    scalar = {"int": "int", "int64_t": "int64", "double": "double"}
+    out = {}
+    for body, name in re.findall(r"typedef struct\s*\{(.*?)\}\s*(\w+)\s*;", text, flags=re.S):
+        fields = []
+        for decl in body.split(";"):
+            decl = re.sub(r"\s+", " ", decl).strip()
+            if not decl:
+                continue
+            # "<type words>[*] name, [*]name, ...": the type ends before the first declarator
+            m = re.match(r"((?:const |unsigned |long )*\w+)(\s*\*)?\s*(.*)", decl)
+            base, star, rest = m.group(1), bool(m.group(2)), m.group(3)
+            for item in rest.split(","):
+                item = item.strip()
+                ptr = star or item.startswith("*")
+                fields.append((item.lstrip("*").strip(), "pointer" if ptr else scalar[base.split()[-1]]))
+        out[name] = fields
+    return out
+
+
+def test_ctypes_structs_mirror_the_header():
+    """Every C-ABI struct the package passes by pointer has the header's
+    fields, in the header's order, with the same kinds."""
+    import ctypes as C
+    from measure_ia_gb300 import _lib as L
+    hdr = _header_structs()
+
+    def kind(t):
+        if t is C.c_void_p or (isinstance(t, type) and issubclass(t, C._Pointer)):
+            return "pointer"
+        return {C.c_int: "int", C.c_int64: "int64", C.c_double: "double"}[t]
+
+    for cname, cls in (("mia_catalog", L.Catalog), ("mia_config", L.Config), ("mia_layout", L.Layout),
+                       ("mia_result", L.Result), ("mia_lc_config", L.LcConfig), ("mia_lc_sample", L.LcSample)):
+        want = hdr[cname]
+        got = [(n, kind(t)) for n, t in cls._fields_]
+        assert got == want, (cname, [x for x in zip(got, want) if x[0] != x[1]][:3], len(got), len(want))
