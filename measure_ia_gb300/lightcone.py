@@ -34,6 +34,7 @@ import numpy as np
 
 from . import _lib as L
 from . import binning as B
+from .base import BaseHelpers, JackknifeCovariance
 from .cosmology import comoving_radial_distance, default_cosmology
 from .output import norm_path, open_output
 
@@ -299,9 +300,10 @@ _POS_KEYS = ("Redshift", "RA", "DEC", "weight")
 _SHAPE_KEYS = ("Redshift_shape_sample", "RA_shape_sample", "DEC_shape_sample", "weight_shape_sample")
 
 
-class MeasureIALightcone:
+class MeasureIALightcone(BaseHelpers, JackknifeCovariance):
     """Drop-in for the reference's ``MeasureIALightcone``: same constructor,
-    ``measure_xi_w`` and ``measure_xi_multipoles``, same datasets."""
+    ``measure_xi_w`` and ``measure_xi_multipoles``, same datasets; the
+    jackknife covariance methods and helpers of the reference's base classes."""
 
     def __init__(self, data, randoms_data, output_file_name, separation_limits=[0.1, 20.0], num_bins_r=8,
                  num_bins_pi=20, pi_max=None, num_nodes=1, device=0):

@@ -30,6 +30,7 @@ import numpy as np
 from ._lib import MIA_ERR_OVERFLOW, MiaError
 from .engine import PairCounter
 from .output import norm_path, open_output
+from .base import BaseHelpers, JackknifeCovariance
 from .sim_info import SimInfo
 
 
@@ -50,7 +51,7 @@ def _centres(edges):
     return edges[:-1] + abs((edges[1:] - edges[:-1]) / 2.0)
 
 
-class MeasureIABox(SimInfo):
+class MeasureIABox(SimInfo, BaseHelpers, JackknifeCovariance):
     """Measurements of w_gg, w_g+ and multipoles (with jackknife covariance)
     for a periodic simulation box.  ``data`` keys: 'Position' (N_p, 3),
     'Position_shape_sample' (N_s, 3), 'Axis_Direction' (N_s, 2), 'LOS',
@@ -207,79 +208,6 @@ class MeasureIABox(SimInfo):
         (measure_IA.py:165-262).  Like the reference's public method, rp_cut is
         accepted but not applied (measure_IA.py:219-258)."""
         self._run("m", dataset_name, corr_type, num_jk, temp_file_path, masks, ellipticity, None)
-
-    # ------------------------------------------------- cross-dataset covariance
-    def measure_covariance_multiple_datasets(self, corr_type, dataset_names, num_box=27, return_output=False):
-        """Jackknife covariance of one dataset with itself or of two datasets
-        (e.g. two projections) from the realisations already in the output
-        (``MeasureJackknife.measure_covariance_multiple_datasets``,
-        measure_jackknife.py:485-571): same checks, same dataset names
-        ``<d0>[_<d1>]_jackknife_cov_<n>`` and ``_jackknife_<n>`` under
-        ``<snap_group>/<corr_type>``, or (cov, std) with ``return_output``.
-        The arithmetic runs on the device (``mia_jackknife_cross_cov``)."""
-        from .engine import jackknife_cross_cov
-        valid = ["w_g_plus", "multipoles_g_plus", "w_gg", "multipoles_gg"]
-        if corr_type not in valid:
-            raise ValueError("corr_type must be 'w_g_plus', 'w_gg', 'multipoles_g_plus' or 'multipoles_gg'.")
-        store = open_output(self.output_file_name)
-        reals = []
-        for name in dataset_names:
-            grp = norm_path(self.snap_group, corr_type, f"{name}_jk{num_box}")
-            try:
-                reals.append(np.stack([np.asarray(store.read(norm_path(grp, f"{name}_{b}")), dtype=np.float64)
-                                       for b in range(num_box)]))
-            except KeyError:
-                raise KeyError(f"Unable to open object '{name}_jk{num_box}' in '{self.snap_group}/{corr_type}'")
-        if len(dataset_names) not in (1, 2):
-            raise KeyError("Too many datasets given, choose either 1 or 2")
-        cov_d, std_d = jackknife_cross_cov(reals[0], reals[1] if len(reals) == 2 else None, device=self.device)
-        cov, std = cov_d.cpu().numpy(), std_d.cpu().numpy()
-        if self.output_file_name is not None and not return_output:
-            grp = norm_path(self.snap_group, corr_type)
-            tag = "_".join(dataset_names[:2]) if len(dataset_names) == 2 else dataset_names[0]
-            store.write(grp, f"{tag}_jackknife_cov_{num_box}", cov)
-            store.write(grp, f"{tag}_jackknife_{num_box}", std)
-            store.flush()
-            return None
-        return cov, std
-
-    def create_full_cov_matrix_projections(self, corr_type, dataset_names=["LOS_x", "LOS_y", "LOS_z"], num_box=27,
-                                           return_output=False):
-        """Combined jackknife covariance of three projections and of each pair
-        (``create_full_cov_matrix_projections``, measure_jackknife.py:573-652):
-        writes the three pair covariances, then assembles the 3-projection and
-        2-projection matrices from the stored ``_jackknife_cov_<n>`` datasets.
-        Like the reference, the block it names cov_yz comes from the
-        (d0, d2) pair and cov_xz from the (d1, d2) pair."""
-        d0, d1, d2 = dataset_names[0], dataset_names[1], dataset_names[2]
-        for a, b in ((d0, d1), (d0, d2), (d1, d2)):
-            self.measure_covariance_multiple_datasets(corr_type=corr_type, dataset_names=[a, b], num_box=num_box)
-        store = open_output(self.output_file_name)
-        grp = norm_path(self.snap_group, corr_type)
-        rd = lambda name: np.asarray(store.read(norm_path(grp, name)))
-        cov_xx = rd(f"{d0}_jackknife_cov_{num_box}")
-        cov_yy = rd(f"{d1}_jackknife_cov_{num_box}")
-        cov_zz = rd(f"{d2}_jackknife_cov_{num_box}")
-        cov_xy = rd(f"{d0}_{d1}_jackknife_cov_{num_box}")
-        cov_yz = rd(f"{d0}_{d2}_jackknife_cov_{num_box}")
-        cov_xz = rd(f"{d1}_{d2}_jackknife_cov_{num_box}")
-        cov3 = np.concatenate((np.concatenate((cov_xx, cov_xy, cov_xz), axis=1),
-                               np.concatenate((cov_xy.T, cov_yy, cov_yz), axis=1),
-                               np.concatenate((cov_xz.T, cov_yz.T, cov_zz), axis=1)), axis=0)
-        cov2xy = np.concatenate((np.concatenate((cov_xx, cov_xy), axis=1),
-                                 np.concatenate((cov_xy.T, cov_yy), axis=1)), axis=0)
-        cov2xz = np.concatenate((np.concatenate((cov_xx, cov_xz), axis=1),
-                                 np.concatenate((cov_xz.T, cov_zz), axis=1)), axis=0)
-        cov2yz = np.concatenate((np.concatenate((cov_yy, cov_yz), axis=1),
-                                 np.concatenate((cov_yz.T, cov_zz), axis=1)), axis=0)
-        if return_output:
-            return cov3, cov2xy, cov2xz, cov2yz
-        store.write(grp, f"{d0}_{d1}_{d2}_combined_jackknife_cov_{num_box}", cov3)
-        store.write(grp, f"{d0}_{d1}_combined_jackknife_cov_{num_box}", cov2xy)
-        store.write(grp, f"{d0}_{d2}_combined_jackknife_cov_{num_box}", cov2xz)
-        store.write(grp, f"{d1}_{d2}_combined_jackknife_cov_{num_box}", cov2yz)
-        store.flush()
-        return None
 
     # ------------------------------------------------------------------ output
     def _write(self, kind, d, corr_type, num_jk, meas, layout):

@@ -70,6 +70,10 @@ class SimInfo:
                 "FLAMINGO_L1, FLAMINGO_L2p8, COLIBRE_L400, COLIBRE_L200].")
         self.L_0p5 = self.boxsize / 2.0
 
+    def get_specs(self):
+        """Box size and h of a named simulation (Sim_info.py:83-135)."""
+        self._specs()
+
     def get_file_info(self):
         """Group catalogue and snapshot file stems and file counts."""
         name, snap = self.simname, self.snapshot

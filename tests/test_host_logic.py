@@ -256,3 +256,49 @@ def test_ctypes_structs_mirror_the_header():
         want = hdr[cname]
         got = [(n, kind(t)) for n, t in cls._fields_]
         assert got == want, (cname, [x for x in zip(got, want) if x[0] != x[1]][:3], len(got), len(want))
+
+
+def test_reference_base_helpers():
+    """The public helpers of the reference's base classes on both drop-in
+    classes (measure_IA_base.py:186-402), against closed forms."""
+    from measure_ia_gb300 import MeasureIABox, MeasureIALightcone
+    from measure_ia_gb300.sim_info import SimInfo
+    box = MeasureIABox(None, None, None, None, boxsize=100.0)
+    lc_cls = MeasureIALightcone
+    rng = np.random.default_rng(5)
+    a, b = rng.normal(size=(7, 3)), rng.normal(size=(7, 3))
+    np.testing.assert_allclose(box.calculate_dot_product_arrays(a, b), np.einsum("ij,ij->i", a, b), rtol=1e-14)
+    e, phi = rng.uniform(0, 1, 5), rng.uniform(0, np.pi, 5)
+    ep, ex = lc_cls.get_ellipticity(e, phi)
+    np.testing.assert_allclose(ep ** 2 + ex ** 2, e ** 2, rtol=1e-12)
+    # analytic random pairs: cylinder shell over the box; 'auto' counts a pair once
+    L3, n_p, n_s = 1e6, 1000, 400
+    cross = box.get_random_pairs(2.0, 1.0, 5.0, -5.0, L3, "cross", n_p, n_s)
+    assert np.isclose(cross, n_p * n_s * np.pi * 3.0 * 10.0 / L3)
+    assert np.isclose(box.get_random_pairs(2.0, 1.0, 5.0, -5.0, L3, "auto", n_p, n_s), cross * (n_p - 1) / (2 * n_p))
+    with pytest.raises(ValueError, match="auto or cross"):
+        box.get_random_pairs(2.0, 1.0, 5.0, -5.0, L3, "nope", n_p, n_s)
+    # caps: mu = -1 is the whole sphere, mu = 1 nothing; over mu in [-1, 1] the
+    # (r, mu) count is the spherical shell's
+    assert np.isclose(box.get_volume_spherical_cap(-1.0, 3.0), 4.0 / 3.0 * np.pi * 27.0)
+    assert box.get_volume_spherical_cap(1.0, 3.0) == 0.0
+    shell = 4.0 / 3.0 * np.pi * (3.0 ** 3 - 1.0 ** 3)
+    assert np.isclose(box.get_random_pairs_r_mur(3.0, 1.0, 1.0, -1.0, L3, "cross", n_p, n_s),
+                      (n_p - 1.0) * n_s * shell / L3)
+    assert np.isclose(box.get_random_pairs_r_mur(3.0, 1.0, 1.0, -1.0, L3, "auto", n_p, n_s),
+                      (n_p - 1.0) / 2.0 * n_s * shell / L3)
+    # row-wise set differences
+    d = box.setdiff2D([[1, 2, 3], [4, 5]], [[2], [4, 5]])
+    assert [list(x) for x in d] == [[1, 3], []]
+    d = box.setdiff_omit([[1, 2, 3], [4, 5], [6]], [2, 6], [0, 2])
+    assert [list(x) for x in d] == [[1, 3], []]
+    with pytest.raises(AssertionError):
+        box.setdiff2D([[1]], [[1], [2]])
+    # SimInfo.get_specs
+    s = SimInfo("TNG100", 99)
+    s.boxsize = None
+    s.get_specs()
+    assert s.boxsize == 75.0 and s.h == 0.6774
+    for name in ("measure_covariance_multiple_datasets", "create_full_cov_matrix_projections",
+                 "assign_jackknife_patches", "get_random_pairs_r_mur"):
+        assert callable(getattr(lc_cls, name)) and callable(getattr(MeasureIABox, name))
