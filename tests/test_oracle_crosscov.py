@@ -46,3 +46,38 @@ def test_full_projection_matrices(ct):
     for m, tag in zip(full, ("cov3", "cov2xy", "cov2xz", "cov2yz")):
         np.testing.assert_array_equal(m, z[f"res/{ct}/{tag}"])
     np.testing.assert_array_equal(full[0], z[f"out/{ct}/LOS_x_LOS_y_LOS_z_combined_jackknife_cov_8"])
+
+
+@pytest.mark.parametrize("cls_name", ["MeasureIABox", "MeasureIALightcone"])
+def test_covariance_methods_on_stored_realisations(cls_name, tmp_path, monkeypatch):
+    """The two covariance methods of both drop-in classes on realisations
+    already in an output file (the reference's own, from the fixture), with
+    the device arithmetic replaced by the oracle: the file handling, names and
+    block assembly, on the CPU."""
+    import torch
+    import measure_ia_gb300 as P
+    from measure_ia_gb300 import engine, hdf5, open_output
+    z = np.load(FIX)
+    out = str(tmp_path / "stored.hdf5")
+    # the reference's stored datasets: realisations and each projection's own covariance
+    hdf5.write_file(out, {k[4:]: z[k] for k in z.files if k.startswith("out/") and "combined" not in k})
+
+    def cpu_cross_cov(a, b=None, device=0):
+        cov, std = O.jackknife_cross_cov(a, a if b is None else b)
+        return torch.from_numpy(np.asarray(cov)), torch.from_numpy(np.asarray(std))
+
+    monkeypatch.setattr(engine, "jackknife_cross_cov", cpu_cross_cov)
+    if cls_name == "MeasureIABox":
+        obj = P.MeasureIABox(None, out, None, None, boxsize=205.0)
+    else:
+        obj = P.MeasureIALightcone(None, None, out, pi_max=20.0)
+    assert obj.snap_group == ""
+    for ct in ("w_g_plus", "w_gg"):
+        c, s = obj.measure_covariance_multiple_datasets(ct, ["LOS_x", "LOS_z"], num_box=8, return_output=True)
+        np.testing.assert_array_equal(c, z[f"res/{ct}/pair_cov"])
+        full = obj.create_full_cov_matrix_projections(ct, ["LOS_x", "LOS_y", "LOS_z"], num_box=8, return_output=True)
+        for m, tag in zip(full, ("cov3", "cov2xy", "cov2xz", "cov2yz")):
+            np.testing.assert_array_equal(m, z[f"res/{ct}/{tag}"])
+        obj.create_full_cov_matrix_projections(ct, ["LOS_x", "LOS_y", "LOS_z"], num_box=8)
+    st = open_output(out)
+    assert "w_g_plus/LOS_x_LOS_y_LOS_z_combined_jackknife_cov_8" in set(st.keys())
