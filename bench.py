@@ -349,7 +349,6 @@ def run_batch48(args, local):
     # every pairwise jackknife cross-covariance of the 48 catalogues' w_g+,
     # on the device from the batch outputs, against the oracle's numpy loop
     # on the host (on rank 0's host cores, for the record)
-    from measure_ia_gb300.engine import jackknife_cross_cov
     pairs = [(i, j) for i in range(len(dcats)) for j in range(i + 1, len(dcats))]
     for i, j in pairs[:4]:
         batch.cross_covariance(i, j)
