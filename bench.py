@@ -111,25 +111,67 @@ class ClockSampler:
 # CPU reference (the oracle's restatement of the reference's tree + Pool path)
 # ---------------------------------------------------------------------------
 
+def cpu_sample_shapes(n_shape, n_sample, seed=7):
+    """The seeded sample of shape indices the CPU reference measures."""
+    rng = np.random.default_rng(seed)
+    return np.sort(rng.choice(n_shape, size=min(n_sample, n_shape), replace=False))
+
+
 def cpu_reference(data, n_sample_shapes, processes):
-    """Binned pairs/s of the reference algorithm (KD-tree pre-selection at
-    r_min and r_max, per-pair numpy binning with jackknife scatter, a process
-    pool over shape chunks of 1000) on the first ``n_sample_shapes`` shapes
-    against all positions."""
+    """The reference algorithm of measure_xi_w's multiprocessing backend
+    (measure_w_box_jk.py:648-857) on a seeded sample of ``n_sample_shapes``
+    shapes against all positions: labels and responsivity, the periodic
+    position KD-tree built once (:764), then a fork Pool over chunks of
+    shapes (:765-768) whose workers query that tree and bin the pairs with
+    the reference's numpy sequence (:543-646).  The chunk is the reference's
+    default 1000 shapes, or sample / processes when that is smaller, so that
+    every process has work.  Returns (binned pairs, seconds, tree seconds,
+    chunk)."""
     from oracle import ia_oracle as O
     b = O.Binning(boxsize=L_BOX, r_min=0.1, r_max=20.0, num_bins_r=10, num_bins_pi=8, pi_max=20.0)
-    pos, spos = data["Position"], data["Position_shape_sample"]
-    axis = data["Axis_Direction"] / np.sqrt((data["Axis_Direction"] ** 2).sum(1))[:, None]
-    e = O.ellipticity_size(data["q"])
-    ws = data["weight_shape_sample"]
+    idx = cpu_sample_shapes(len(data["Position_shape_sample"]), n_sample_shapes)
+    pos, spos = data["Position"], data["Position_shape_sample"][idx]
+    axis_raw, q, ws = data["Axis_Direction"][idx], data["q"][idx], data["weight_shape_sample"][idx]
+    chunk = max(1, min(1000, -(-len(idx) // processes)))
     t0 = time.perf_counter()
+    axis = axis_raw / np.sqrt((axis_raw ** 2).sum(1))[:, None]
+    e = O.ellipticity_size(q)
     R = O.responsivity(ws, e)
     lab_p = O.jackknife_labels(pos, b.L_0p5, 3)
     lab_s = O.jackknife_labels(spos, b.L_0p5, 3)
-    c = O.count_pairs_parallel("w", b, 2, pos, data["weight"], spos, axis, e, ws, R, lab_p, lab_s, 27,
-                               (0, n_sample_shapes), processes=processes, chunk=max(1, n_sample_shapes // (4 * processes)))
+    c, t_tree = O.count_pairs_parallel("w", b, 2, pos, data["weight"], spos, axis, e, ws, R, lab_p, lab_s, 27,
+                                       (0, len(idx)), processes=processes, chunk=chunk)
     dt = time.perf_counter() - t0
-    return int(c.npairs.sum()), dt
+    return int(c.npairs.sum()), dt, t_tree, chunk
+
+
+def cpu_model():
+    """The host CPU's model name (for the record), or the machine type."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu model")):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    import platform
+    return platform.machine()
+
+
+def cpu_line(data, pairs, secs, t_tree, chunk, n_sample, cores, steps=1):
+    """The cpu_baseline object of a CPU-reference measurement."""
+    v = pairs / secs
+    n_shape = len(data["Position_shape_sample"])
+    per_step, tree = secs / steps, t_tree / steps
+    return {"value": v, "unit": "binned pairs/s", "cores": cores, "kind": "port",
+            "sample": (f"{n_sample} seeded shapes x all {len(data['Position'])} positions per step, fork Pool of "
+                       f"{cores} processes over chunks of {chunk} shapes, one position KD-tree build per step "
+                       f"({tree:.2f} s of {per_step:.2f} s); {cpu_model()}"),
+            "extrapolated_full_step_s": tree + (per_step - tree) * n_shape / n_sample,
+            "note": ("the oracle's restatement of the reference's multiprocessing backend: scipy KD-tree "
+                     "pre-selection, per-pair numpy binning (np.bincount where the reference uses the slower "
+                     "np.add.at); extrapolated_full_step_s = one tree build plus the sample's pair time scaled "
+                     "linearly to all shapes (labelled extrapolated: not run at full size)")}
 
 
 # ---------------------------------------------------------------------------
@@ -180,15 +222,15 @@ def time_counter(pc, dcat, steps, warmup, stream, ws=1, kernel_ms=None):
     return ms, per, pc.fetch(bufs)
 
 
-def profiled_traffic():
-    """DRAM bytes (read + write) per pair-kernel launch on this workload, from
-    the committed ncu summary, or None."""
-    import re
+def profiled_traffic(kernel="k_pairs", workload="config2_w_jk27"):
+    """DRAM bytes (read + write) per launch of the pair kernel on this
+    workload from one ncu capture, as recorded in profiles/traffic.json (the
+    capture's command and summary are named there), or None."""
     try:
-        with open(os.path.join(ROOT, "profiles", "pairs_config2_w_jk27.md")) as f:
-            m = re.search(r"^dram_bytes_per_launch:\s*(\d+)", f.read(), re.M)
-        return int(m.group(1)) if m else None
-    except OSError:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            rec = json.load(f).get(f"{kernel}/{workload}")
+        return int(rec["dram_bytes_per_launch"]) if rec else None
+    except (OSError, ValueError, KeyError, TypeError):
         return None
 
 
@@ -284,7 +326,10 @@ def run_gpu(args, data, rank, ws, local):
         pinned.numpy()[...] = a
         host[k] = pinned.numpy()
     host["LOS"] = 2
-    box = MeasureIABox(dict(host), None, None, None, [0.1, 20.0], 10, 8, 20.0, boxsize=L_BOX, num_nodes=2,
+    import tempfile
+    out_dir = tempfile.mkdtemp(prefix="mia_bench_")
+    out_file = os.path.join(out_dir, "bench_output.hdf5")  # the products' HDF5 file, rewritten every step
+    box = MeasureIABox(dict(host), out_file, None, None, [0.1, 20.0], 10, 8, 20.0, boxsize=L_BOX, num_nodes=2,
                        precision="mixed", device=local, autotune=not args.no_tune)
     box.measure_xi_w("bench", "both", 27, temp_file_path="/tmp")  # warm-up (tuner cache hit)
     e2e_steps = max(1, min(args.steps, 3))
@@ -294,61 +339,103 @@ def run_gpu(args, data, rank, ws, local):
         box.measure_xi_w("bench", "both", 27, temp_file_path="/tmp")
     torch.cuda.synchronize()
     res["e2e_s"] = (time.perf_counter() - t0) / e2e_steps
+    res["e2e_file_bytes"] = os.path.getsize(out_file)
+    import shutil
+    shutil.rmtree(out_dir, ignore_errors=True)
     res["h2d"] = sum(np.asarray(data[k]).nbytes for k in keys)
     res["d2h"] = pcm.layout.total * 8 + (1 + 27) * 80 * 8
     return res
 
 
+def _time_graph(g, steps, warmup, stream):
+    """ms per replay of a CUDA graph (CUDA events on the replay stream)."""
+    import torch
+    for _ in range(warmup):
+        g.replay()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        g.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
 def run_batch48(args, local):
     """48 catalogues (12 mass bins x 4 snapshots), sizes log-uniform in
     [5e3, 2e6] galaxies, each drawn with the clustered recipe (parents = N/50,
-    shapes = N/4, independent seeds), measured in one persistent pair-kernel
-    launch replayed from a CUDA graph, against the same catalogues measured
-    one after the other."""
+    shapes = N/4, independent seeds), w_gg + w_g+ and the multipoles (20 mu_r
+    bins) of every catalogue with 27 jackknife regions: both measurements'
+    batches (one persistent pair-kernel launch each) in one CUDA graph,
+    against the same catalogues measured one after the other."""
     import torch
     from measure_ia_gb300.catalogs import neyman_scott_catalog
-    from measure_ia_gb300.engine import BatchCounter, PairCounter
+    from measure_ia_gb300.engine import BatchCounter, PairCounter, capture_batches
     rng = np.random.default_rng(48)
     sizes = np.exp(rng.uniform(np.log(5e3), np.log(2e6), 48))
     cats = [neyman_scott_catalog(max(2, int(n / 50)), L_BOX, max(100, int(n / 4)), 1000 + i, mean_children=50,
                                  sigma=1.0) for i, n in enumerate(sizes)]
-    pc = PairCounter("w", boxsize=L_BOX, r_bins=R_BINS, r_min=0.1, r_max=20.0, p_bins=PI_BINS, l_subboxes=3,
-                     precision="mixed", device=local)
-    dcats = [pc.to_device(c) for c in cats]
-    pc = _pick(pc, dcats[int(np.argmax(sizes))], args)  # launch knobs of the largest catalogue
+    common = dict(boxsize=L_BOX, r_bins=R_BINS, r_min=0.1, r_max=20.0, l_subboxes=3, precision="mixed", device=local)
+    pcs = {"w": PairCounter("w", p_bins=PI_BINS, **common),
+           "m": PairCounter("m", p_bins=np.linspace(-1.0, 1.0, 21), **common)}
+    dcats = [pcs["w"].to_device(c) for c in cats]
+    big = int(np.argmax(sizes))
+    pcs = {k: _pick(pc, dcats[big], args) for k, pc in pcs.items()}  # launch knobs of the largest catalogue
     stream = torch.cuda.current_stream(local)
-    # one after the other
-    bufs = [pc.allocate(d["Position"].shape[0], d["Position_shape_sample"].shape[0]) for d in dcats]
-    for d, b in zip(dcats, bufs):
-        pc.run(d, b, stream)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
+    out = {}
+    batches = {}
+    for kind, pc in pcs.items():
+        # one after the other
+        bufs = [pc.allocate(d["Position"].shape[0], d["Position_shape_sample"].shape[0]) for d in dcats]
         for d, b in zip(dcats, bufs):
             pc.run(d, b, stream)
-    torch.cuda.synchronize()
-    seq_ms = (time.perf_counter() - t0) * 1e3 / args.steps
-    binned = sum(pc.fetch(b).stats["binned_pairs"] for b in bufs)
-    # batched, replayed from a CUDA graph
-    batch = BatchCounter(pc, dcats)
-    batch.prepare()
-    batch.run()
-    batch.capture()
-    for _ in range(args.warmup):
-        batch.replay()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(args.steps):
-        batch.graph.replay()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    batch.status()
-    ms = e0.elapsed_time(e1) / args.steps
-    same = all(np.array_equal(batch.fetch(i).npairs, pc.fetch(b).npairs) for i, b in enumerate(bufs))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for d, b in zip(dcats, bufs):
+                pc.run(d, b, stream)
+        torch.cuda.synchronize()
+        seq_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        singles = [pc.fetch(b) for b in bufs]
+        binned = sum(m.stats["binned_pairs"] for m in singles)
+        # batched, replayed from a CUDA graph of its own
+        batch = BatchCounter(pc, dcats)
+        batch.prepare()
+        batch.run()
+        batch.capture()
+        ms = _time_graph(batch.graph, args.steps, args.warmup, stream)
+        batch.status()
+        same = all(np.array_equal(batch.fetch(i).npairs, singles[i].npairs) for i in range(len(dcats)))
+        batches[kind] = batch
+        out[kind] = {"value": binned / (ms / 1e3), "ms_per_step": ms, "one_after_the_other_ms": seq_ms,
+                     "binned_pairs_per_step": binned, "counts_equal_to_one_by_one": bool(same), "knobs": pc.knobs}
+        if args.fp64:  # the plain FP64 form, one catalogue after the other, one step
+            pc64 = PairCounter(kind, **{**common, "precision": "fp64"},
+                               p_bins=PI_BINS if kind == "w" else np.linspace(-1.0, 1.0, 21), **pc.knobs)
+            ms64, exact, errs = 0.0, True, []
+            for i, d in enumerate(dcats):
+                t, _, m64 = time_counter(pc64, d, 1, 0, stream)
+                ms64 += t
+                exact &= bool(np.array_equal(m64.npairs, batch.fetch(i).npairs))
+                errs.append(_errors(m64, batch.fetch(i), (("proj_gp", "g+"), ("proj_gg", "gg"))))
+            worst = {k: max(e[k][q] for e in errs) for k in ("g+", "gg")
+                     for q in ("max_rel_to_vector_scale",)}
+            worst_bin = {k: max(e[k]["max_rel_per_bin"] for e in errs) for k in ("g+", "gg")}
+            out[kind]["fp64_form"] = {"value": binned / (ms64 / 1e3), "ms_per_step": ms64,
+                                      "counts_bit_exact_mixed_vs_fp64": exact,
+                                      "max_rel_to_vector_scale_over_catalogues": worst,
+                                      "max_rel_per_bin_over_catalogues": worst_bin}
+    # both measurements of all 48 catalogues in one graph
+    g = capture_batches([batches["w"], batches["m"]])
+    ms_both = _time_graph(g, args.steps, args.warmup, stream)
+    for b in batches.values():
+        b.status()
+    binned_both = out["w"]["binned_pairs_per_step"] + out["m"]["binned_pairs_per_step"]
     # every pairwise jackknife cross-covariance of the 48 catalogues' w_g+,
     # on the device from the batch outputs, against the oracle's numpy loop
     # on the host (on rank 0's host cores, for the record)
+    batch = batches["w"]
     pairs = [(i, j) for i in range(len(dcats)) for j in range(i + 1, len(dcats))]
     for i, j in pairs[:4]:
         batch.cross_covariance(i, j)
@@ -374,27 +461,15 @@ def run_batch48(args, local):
     nr = len(R_BINS) - 1
     full_exact = all(np.array_equal(full[i * nr:(i + 1) * nr, j * nr:(j + 1) * nr].cpu().numpy(), h[0])
                      for (i, j), h in zip(pairs, host))
-    fp64 = None
-    if args.fp64:  # the plain FP64 form, one catalogue after the other, one step
-        pc64 = PairCounter("w", boxsize=L_BOX, r_bins=R_BINS, r_min=0.1, r_max=20.0, p_bins=PI_BINS, l_subboxes=3,
-                           precision="fp64", device=local, **pc.knobs)
-        ms64, exact, errs = 0.0, True, []
-        for i, d in enumerate(dcats):
-            t, _, m64 = time_counter(pc64, d, 1, 0, stream)
-            ms64 += t
-            exact &= bool(np.array_equal(m64.npairs, batch.fetch(i).npairs))
-            errs.append(_errors(m64, batch.fetch(i), (("proj_gp", "w_g+"), ("proj_gg", "w_gg"))))
-        worst = {k: max(e[k]["max_rel_to_vector_scale"] for e in errs) for k in ("w_g+", "w_gg")}
-        fp64 = {"value": binned / (ms64 / 1e3), "ms_per_step": ms64, "counts_bit_exact_mixed_vs_fp64": exact,
-                "max_rel_to_vector_scale_over_catalogues": worst}
-    return {"metric": "binned pairs/s, 48 uneven catalogues, w_gg+w_g+ 27JK, mixed form", "value": binned / (ms / 1e3),
-            "unit": "binned pairs/s", "ms_per_step": ms, "one_after_the_other_ms": seq_ms,
-            "binned_pairs_per_step": binned, "counts_equal_to_one_by_one": bool(same), "fp64_form": fp64,
+    return {"metric": "binned pairs/s, 48 uneven catalogues, w_gg+w_g+ and multipoles 27JK in one CUDA graph, "
+                      "mixed form",
+            "value": binned_both / (ms_both / 1e3), "unit": "binned pairs/s", "ms_per_step": ms_both,
+            "binned_pairs_per_step": binned_both, "w": out["w"], "multipoles": out["m"],
             "cross_covariances": {"pairs": len(pairs), "device_ms_pair_by_pair": xcov_ms,
                                   "device_ms_all_in_one_launch": full_ms, "host_oracle_ms": host_ms,
                                   "bit_exact_vs_oracle": bool(xcov_exact and full_exact)},
-            "knobs": pc.knobs,
-            "config": {"workload": "48 catalogues, sizes log-uniform 5e3-2e6 (config 3)",
+            "config": {"workload": "48 catalogues, sizes log-uniform 5e3-2e6 (config 3): w (10 x 8 bins) and "
+                                   "multipoles (10 x 20 mu_r bins), 27 jackknife regions, one graph",
                        "n_positions_total": int(sum(len(c["Position"]) for c in cats)),
                        "n_shapes_total": int(sum(len(c["Position_shape_sample"]) for c in cats))}}
 
@@ -757,7 +832,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-sample", type=int, default=500, help="shapes in the CPU-baseline sample")
+    ap.add_argument("--cpu-sample", type=int, default=1600, help="seeded shapes in the CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU-baseline leg (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--only-mixed", action="store_true", help="time the mixed form only (profiling runs)")
@@ -808,19 +883,19 @@ def main():
 
     if args.impl == "reference":
         results = []
-        for _ in range(args.warmup):
-            cpu_reference(data, max(100, args.cpu_sample // 4), cores)
+        for _ in range(args.warmup):  # the same per-step work on a smaller sample
+            cpu_reference(data, max(cores, args.cpu_sample // 8), cores)
         for _ in range(args.steps):
             results.append(cpu_reference(data, args.cpu_sample, cores))
         pairs = sum(r[0] for r in results)
         secs = sum(r[1] for r in results)
-        v = pairs / secs
+        cpu = cpu_line(data, pairs, secs, sum(r[2] for r in results), results[0][3], args.cpu_sample, cores,
+                       args.steps)
+        v = cpu["value"]
         line = {"metric": METRIC, "value": v, "unit": "binned pairs/s", "n_gpus": 0, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "impl": "reference",
-                "config": config,
-                "cpu_baseline": {"value": v, "unit": "binned pairs/s", "cores": cores, "kind": "port",
-                                 "sample": f"first {args.cpu_sample} shapes x all {n_pos} positions per step"},
+                "config": config, "cpu_baseline": cpu,
                 "e2e": {"value": v, "unit": "binned pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
@@ -828,9 +903,8 @@ def main():
     # CPU baseline first, before any CUDA context exists (the pool forks)
     cpu = None
     if rank == 0 and not args.no_cpu:
-        pairs, secs = cpu_reference(data, args.cpu_sample, cores)
-        cpu = {"value": pairs / secs, "unit": "binned pairs/s", "cores": cores, "kind": "port",
-               "sample": f"first {args.cpu_sample} shapes x all {n_pos} positions, {secs:.1f} s"}
+        pairs, secs, t_tree, chunk = cpu_reference(data, args.cpu_sample, cores)
+        cpu = cpu_line(data, pairs, secs, t_tree, chunk, args.cpu_sample, cores)
     if ws > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
@@ -864,10 +938,12 @@ def main():
                      "note": "achieved = 32 FP32 lane-ops per binned pair / the pair kernel's mean launch time "
                              "(CUDA events on the launching stream, timed steps); peak = nominal SMs x 128 x "
                              "2070 MHz (no FP32 figure in MEASURED_PEAKS.json); traffic = DRAM bytes per "
-                             "launch from profiles/pairs_config2_w_jk27.md (ncu)"},
+                             "launch from one ncu capture (profiles/traffic.json)"},
         "cpu_baseline": cpu,
         "e2e": {"value": r["binned"] / r["e2e_s"], "unit": "binned pairs/s", "h2d_bytes_per_step": r["h2d"],
-                "d2h_bytes_per_step": r["d2h"]},
+                "d2h_bytes_per_step": r["d2h"], "hdf5_file_bytes": r.get("e2e_file_bytes"),
+                "note": "MeasureIABox.measure_xi_w from pinned host arrays: H2D of the catalogue, the measurement, "
+                        "D2H of every product and the HDF5 output file written, every step"},
         "gpu_launches": launches_per_step * args.steps,
         "step_ms": r["per_step"],
         "launch_knobs": r["knobs"],

@@ -231,12 +231,15 @@ MIA_API int mia_profile_read(mia_context* ctx, float* ms, int n, int* n_out);
    scratch is a 64 MiB array in the library's device module, held on every
    GPU that loads the library until the process exits.  Measurements whose
    scratch need (mia_workspace_size) exceeds MIA_STATIC_SCRATCH_BYTES are
-   rejected with MIA_ERR_WORKSPACE.  The first call on a device looks up the
-   array's device address (cudaGetSymbolAddress); make that first call before
-   any stream capture.  All calls share the one array, so calls that overlap
-   on the GPU (other streams, other host threads) race; every call clears what
-   must start at zero.  Inputs and outputs are still caller-provided device
-   buffers.  No counterpart in the reference. */
+   rejected with MIA_ERR_WORKSPACE; invalid arguments get mia_measure's
+   errors and messages.  Each call looks up the array's device address
+   (cudaGetSymbolAddress) with the context's device current; a device's
+   first call also loads the library's module there, so make that first call
+   before any stream capture (after a cudaDeviceReset the next call finds the
+   array's new address).  All calls share the one array, so calls that
+   overlap on the GPU (other streams, other host threads) race; every call
+   clears what must start at zero.  Inputs and outputs are still
+   caller-provided device buffers.  No counterpart in the reference. */
 MIA_API int mia_measure_static(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat,
                                const mia_result* res, void* stream);
 

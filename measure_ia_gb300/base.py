@@ -24,7 +24,7 @@ from __future__ import annotations
 
 import numpy as np
 
-from .output import norm_path, open_output
+from .output import norm_path, store_for
 
 
 class BaseHelpers:
@@ -109,7 +109,7 @@ class JackknifeCovariance:
         valid = ["w_g_plus", "multipoles_g_plus", "w_gg", "multipoles_gg"]
         if corr_type not in valid:
             raise ValueError("corr_type must be 'w_g_plus', 'w_gg', 'multipoles_g_plus' or 'multipoles_gg'.")
-        store = open_output(self.output_file_name)
+        store = store_for(self)
         reals = []
         for name in dataset_names:
             grp = norm_path(self.snap_group, corr_type, f"{name}_jk{num_box}")
@@ -142,7 +142,7 @@ class JackknifeCovariance:
         d0, d1, d2 = dataset_names[0], dataset_names[1], dataset_names[2]
         for a, b in ((d0, d1), (d0, d2), (d1, d2)):
             self.measure_covariance_multiple_datasets(corr_type=corr_type, dataset_names=[a, b], num_box=num_box)
-        store = open_output(self.output_file_name)
+        store = store_for(self)
         grp = norm_path(self.snap_group, corr_type)
         rd = lambda name: np.asarray(store.read(norm_path(grp, name)))
         cov_xx = rd(f"{d0}_jackknife_cov_{num_box}")

@@ -4,11 +4,28 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <mutex>
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "mia_internal.cuh"
+
+// NVTX ranges around the enqueue of each stage (prep, pairs, re-test, post),
+// so that a profiler's timeline and `ncu --nvtx --nvtx-include` can select a
+// stage; they mark host enqueue time, the kernels run asynchronously.
+namespace {
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+};
+}  // namespace
+
+// Streams on which a batch's per-catalogue preparation (memsets, labels, cell
+// list, work units: ~20 short launches each) runs side by side, forked from
+// and joined back into the caller's stream with events, so that the small
+// catalogues of a batch do not wait for each other.
+constexpr int kPrepStreams = 4;
 
 struct mia_context {
   int device;
@@ -17,7 +34,33 @@ struct mia_context {
   // pair-kernel launch timing (mia_profile_pairs): a ring of event pairs
   std::vector<cudaEvent_t> prof_start, prof_stop;
   long long prof_count = 0;  // launches recorded since enabling
+  // preparation streams and their fork / join events (created by mia_batch_prepare)
+  cudaStream_t prep[kPrepStreams] = {};
+  cudaEvent_t fork = nullptr, join[kPrepStreams] = {};
+  bool prep_ready = false;
 };
+
+static void free_prep_streams(mia_context* c) {
+  if (!c->prep_ready) return;
+  for (int k = 0; k < kPrepStreams; ++k) {
+    cudaStreamDestroy(c->prep[k]);
+    cudaEventDestroy(c->join[k]);
+  }
+  cudaEventDestroy(c->fork);
+  c->prep_ready = false;
+}
+
+static cudaError_t make_prep_streams(mia_context* c) {
+  if (c->prep_ready) return cudaSuccess;
+  cudaError_t e = cudaEventCreateWithFlags(&c->fork, cudaEventDisableTiming);
+  for (int k = 0; k < kPrepStreams && e == cudaSuccess; ++k) {
+    e = cudaStreamCreateWithFlags(&c->prep[k], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join[k], cudaEventDisableTiming);
+  }
+  if (e != cudaSuccess) return e;
+  c->prep_ready = true;
+  return cudaSuccess;
+}
 
 static void free_profile_events(mia_context* c) {
   for (cudaEvent_t e : c->prof_start) cudaEventDestroy(e);
@@ -180,7 +223,8 @@ bool make_plan(const mia_config* cfg, long long n_pos, long long n_shape, Plan* 
   take(p.off_p32, mixed ? 4 * 7 * NP : 0);
   take(p.off_s64, 8 * 7 * NS);
   take(p.off_slab_s, 4 * NS);
-  take(p.off_s32, mixed ? 4 * 10 * NS : 0);
+  // (FP32 shape arrays 16-byte aligned each: a stride of a multiple of 4 floats)
+  take(p.off_s32, mixed ? 4 * 10 * ((NS + 3) & ~size_t(3)) : 0);
   take(p.off_wu, sizeof(WorkUnit) * (size_t)p.n_wu_max);
   take(p.off_reg, (size_t)(p.J + 1) * 48 + 64);
   take(p.off_edges, sizeof(int2) * (size_t)p.edge_capacity);
@@ -258,16 +302,17 @@ static void bind_arrays(const Plan& p, void* base, long long n_pos, long long n_
   w->se = s64 + 5 * NS;
   w->sws = s64 + 6 * NS;
   float* s32 = reinterpret_cast<float*>(b + p.off_s32);
+  const size_t NS4 = (NS + 3) & ~size_t(3);
   w->sxh = s32;
-  w->sxl = s32 + NS;
-  w->syh = s32 + 2 * NS;
-  w->syl = s32 + 3 * NS;
-  w->szh = s32 + 4 * NS;
-  w->szl = s32 + 5 * NS;
-  w->saxf = s32 + 6 * NS;
-  w->sayf = s32 + 7 * NS;
-  w->swef = s32 + 8 * NS;
-  w->swsf = s32 + 9 * NS;
+  w->sxl = s32 + NS4;
+  w->syh = s32 + 2 * NS4;
+  w->syl = s32 + 3 * NS4;
+  w->szh = s32 + 4 * NS4;
+  w->szl = s32 + 5 * NS4;
+  w->saxf = s32 + 6 * NS4;
+  w->sayf = s32 + 7 * NS4;
+  w->swef = s32 + 8 * NS4;
+  w->swsf = s32 + 9 * NS4;
 }
 
 static float f32_down(double v) {
@@ -370,7 +415,10 @@ int mia_create(int device, mia_context** out) {
 }
 
 int mia_destroy(mia_context* ctx) {
-  if (ctx) free_profile_events(ctx);
+  if (ctx) {
+    free_profile_events(ctx);
+    free_prep_streams(ctx);
+  }
   delete ctx;
   return MIA_OK;
 }
@@ -580,6 +628,18 @@ void make_params(const mia_config* cfg, const Plan& plan, const Tables& T, int l
   P.range_los = plan.range_los;
   P.n_cells = plan.n_cells;
   P.shapes_per_unit = plan.shapes_per_unit;
+  // the most jackknife regions (sub-boxes per dimension, multiplied) the fine
+  // cells of a shape cell's neighbourhood can touch: work units per run
+  P.reg_slots = 1;
+  if (plan.J > 0) {
+    for (int k = 0; k < 3; ++k) {
+      const int cps = plan.nf[k] / plan.n_sub;
+      const int span = plan.full[k] ? plan.nf[k] : plan.m[k] + 2 * plan.Rf[k];
+      int m = (span + cps - 1) / cps + 1;
+      if (m > plan.n_sub) m = plan.n_sub;
+      P.reg_slots *= m;
+    }
+  }
   P.lut32_base = lut_base;
   const double p0 = cfg->p_edges[0], p1 = cfg->p_edges[cfg->n_p];
   P.p_lo32 = (float)p0;
@@ -665,6 +725,7 @@ int mia_batch_prepare(mia_context* ctx, const mia_config* cfg, int n, const mia_
     if (!results[i].out || !results[i].npairs) return fail(ctx, MIA_ERR_ARG, "null result buffer");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   MIA_CUDA(cudaSetDevice(ctx->device));
+  if (n > 1) MIA_CUDA(make_prep_streams(ctx));
   mia_layout lay;
   mia_output_layout(cfg, &lay);
   unsigned char* b = static_cast<unsigned char*>(workspace);
@@ -706,21 +767,39 @@ int mia_batch_enqueue(mia_context* ctx, const mia_config* cfg, int n, const mia_
   unsigned long long* prefix = reinterpret_cast<unsigned long long*>(b + bp.prefix_off);
   MIA_CUDA(cudaMemsetAsync(hdr, 0, sizeof(BatchHeader), st));
   const size_t nb = (size_t)bp.plans[0].nb, J1 = (size_t)bp.plans[0].J + 1;
+  {
+  NvtxRange r("mia/prep");
+  // catalogues of a batch prepare side by side on the context's streams
+  // (forked from and joined back into `st`; mia_batch_prepare made them)
+  const bool fan = n > 1 && ctx->prep_ready;
+  if (fan) {
+    MIA_CUDA(cudaEventRecord(ctx->fork, st));
+    for (int k = 0; k < kPrepStreams; ++k) MIA_CUDA(cudaStreamWaitEvent(ctx->prep[k], ctx->fork, 0));
+  }
   for (int i = 0; i < n; ++i) {
     const Plan& pl = bp.plans[i];
     unsigned char* base = b + bp.off[i];
+    cudaStream_t sp = fan ? ctx->prep[i % kPrepStreams] : st;
     Dataset d;
     make_dataset(pl, base, cats[i], results[i], lay, &d);
-    MIA_CUDA(cudaMemsetAsync(base + pl.off_status, 0, sizeof(Status), st));
-    MIA_CUDA(cudaMemsetAsync(&d.w.status->bad_index, 0xFF, sizeof(unsigned long long), st));
-    MIA_CUDA(cudaMemsetAsync(base + pl.off_pcount, 0, pl.off_tiles - pl.off_pcount, st));
-    MIA_CUDA(cudaMemsetAsync(base + pl.off_reg, 0, (size_t)(pl.J + 1) * 48 + 64, st));
-    MIA_CUDA(cudaMemsetAsync(base + pl.off_acc, 0, acc_bytes(pl), st));
-    MIA_CUDA(cudaMemsetAsync(results[i].out, 0, sizeof(double) * (size_t)lay.total, st));
-    MIA_CUDA(cudaMemsetAsync(results[i].npairs, 0, sizeof(unsigned long long) * J1 * nb, st));
-    MIA_CUDA(launch_prep(pl, P, cats[i], d.w, st));
+    MIA_CUDA(cudaMemsetAsync(base + pl.off_status, 0, sizeof(Status), sp));
+    MIA_CUDA(cudaMemsetAsync(&d.w.status->bad_index, 0xFF, sizeof(unsigned long long), sp));
+    MIA_CUDA(cudaMemsetAsync(base + pl.off_pcount, 0, pl.off_tiles - pl.off_pcount, sp));
+    MIA_CUDA(cudaMemsetAsync(base + pl.off_reg, 0, (size_t)(pl.J + 1) * 48 + 64, sp));
+    MIA_CUDA(cudaMemsetAsync(base + pl.off_acc, 0, acc_bytes(pl), sp));
+    MIA_CUDA(cudaMemsetAsync(results[i].out, 0, sizeof(double) * (size_t)lay.total, sp));
+    MIA_CUDA(cudaMemsetAsync(results[i].npairs, 0, sizeof(unsigned long long) * J1 * nb, sp));
+    MIA_CUDA(launch_prep(pl, P, cats[i], d.w, sp));
   }
-  MIA_CUDA(launch_batch_prefix(ds_dev, n, prefix, st));
+  if (fan) {
+    for (int k = 0; k < kPrepStreams; ++k) {
+      MIA_CUDA(cudaEventRecord(ctx->join[k], ctx->prep[k]));
+      MIA_CUDA(cudaStreamWaitEvent(st, ctx->join[k], 0));
+    }
+  }
+  MIA_CUDA(launch_batch_prefix(ds_dev, n, P.reg_slots, prefix, st));
+  }
+  NvtxRange r_pairs("mia/pairs");
   const long long slot = ctx->prof_start.empty() ? -1 : ctx->prof_count % (long long)ctx->prof_start.size();
   if (slot >= 0) MIA_CUDA(cudaEventRecord(ctx->prof_start[slot], st));
   MIA_CUDA(launch_pairs(bp.plans[0], P, ds_dev, n, prefix, &hdr->wu_next, st, ctx->num_sms));
@@ -731,7 +810,11 @@ int mia_batch_enqueue(mia_context* ctx, const mia_config* cfg, int n, const mia_
   for (int i = 0; i < n; ++i) {
     Dataset d;
     make_dataset(bp.plans[i], b + bp.off[i], cats[i], results[i], lay, &d);
-    if (P.precision == MIA_MIXED) MIA_CUDA(launch_edge_retest(P, d.w, d.o, st, ctx->num_sms));
+    if (P.precision == MIA_MIXED) {
+      NvtxRange r("mia/edge_retest");
+      MIA_CUDA(launch_edge_retest(P, d.w, d.o, st, ctx->num_sms));
+    }
+    NvtxRange r("mia/post");
     MIA_CUDA(launch_fixed_out(P, d.w, d.o, st));  // exact fixed-point sums -> the output doubles
     MIA_CUDA(launch_post(P, d.w, lay, results[i].out, cfg->volume, cats[i].n_pos, cats[i].n_shape, st));
   }
@@ -758,6 +841,8 @@ int mia_batch_status(mia_context* ctx, int n, void* workspace, void* stream) {
              hh.first_bad, (unsigned long long)hh.bad_index);
     return fail(ctx, MIA_ERR_RANGE, buf);
   }
+  if (hh.flags & kStatusStall)
+    return fail(ctx, MIA_ERR_CUDA, "a bounded device wait ran out (an asynchronous copy did not complete)");
   if (hh.flags & kStatusOverflow)
     return fail(ctx, MIA_ERR_OVERFLOW, "edge re-test queue overflow; rerun in the FP64 form");
   ctx->err.clear();
@@ -786,48 +871,37 @@ int mia_measure(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat,
 // whole GPU memory budget, or a loop where cudaMalloc's implicit device
 // synchronisation is not allowed), mia_measure_static runs mia_measure on a
 // scratch array compiled into this module.  In host code `g_static_scratch`
-// is only a host-side handle; its device address is looked up once per
-// device, with that device current, and then passed on as the workspace.
-// Every call shares the array: mia_measure zeroes what must start at zero,
-// and calls that overlap on the GPU race.
+// is only a host-side handle: every call looks up its device address with
+// cudaGetSymbolAddress, with the context's device current, and passes that on
+// as the workspace (a device's first call also loads this module there; after
+// a cudaDeviceReset the next call finds the array's new address).  Every call
+// shares the array: mia_measure zeroes what must start at zero, and calls
+// that overlap on the GPU race.
 
 static __device__ __align__(256) unsigned char g_static_scratch[MIA_STATIC_SCRATCH_BYTES];
-
-namespace {
-constexpr int kMaxStaticDevices = 64;
-void* g_static_ptr[kMaxStaticDevices] = {};
-std::mutex g_static_mutex;
-}  // namespace
 
 int mia_measure_static(mia_context* ctx, const mia_config* cfg, const mia_catalog* cat, const mia_result* res,
                        void* stream) {
   if (!ctx) return MIA_ERR_ARG;
-  if (!cfg || !cat || !res) return fail(ctx, MIA_ERR_ARG, "null argument");
-  size_t need = 0;
-  if (mia_workspace_size(cfg, cat->n_pos, cat->n_shape, &need) != MIA_OK) return fail(ctx, MIA_ERR_ARG, "invalid configuration");
-  if (need > (size_t)MIA_STATIC_SCRATCH_BYTES) {
+  if (!cfg || !cat || !res || !res->out || !res->npairs) return fail(ctx, MIA_ERR_ARG, "null argument");
+  // the same checks and messages as mia_measure, then the size test
+  BatchPlan bp;
+  std::string why;
+  if (!make_batch(cfg, 1, cat, &bp, &why)) return fail(ctx, MIA_ERR_ARG, why);
+  if (bp.total > (size_t)MIA_STATIC_SCRATCH_BYTES) {
     char buf[256];
     snprintf(buf, sizeof(buf),
              "mia_measure_static: this measurement needs %zu bytes of scratch but the static scratch holds %llu; "
              "use mia_measure with a caller-provided workspace",
-             need, (unsigned long long)MIA_STATIC_SCRATCH_BYTES);
+             bp.total, (unsigned long long)MIA_STATIC_SCRATCH_BYTES);
     return fail(ctx, MIA_ERR_WORKSPACE, buf);
   }
-  if (ctx->device < 0 || ctx->device >= kMaxStaticDevices)
-    return fail(ctx, MIA_ERR_ARG, "mia_measure_static: device index out of range");
   void* base = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_static_mutex);
-    base = g_static_ptr[ctx->device];
-    if (!base) {
-      cudaError_t e = cudaSetDevice(ctx->device);
-      if (e == cudaSuccess) e = cudaGetSymbolAddress(&base, g_static_scratch);
-      if (e != cudaSuccess || !base)
-        return fail(ctx, MIA_ERR_CUDA,
-                    std::string("mia_measure_static: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
-      g_static_ptr[ctx->device] = base;
-    }
-  }
+  cudaError_t e = cudaSetDevice(ctx->device);
+  if (e == cudaSuccess) e = cudaGetSymbolAddress(&base, g_static_scratch);
+  if (e != cudaSuccess || !base)
+    return fail(ctx, MIA_ERR_CUDA,
+                std::string("mia_measure_static: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
   return mia_measure(ctx, cfg, cat, base, (size_t)MIA_STATIC_SCRATCH_BYTES, res, stream);
 }
 

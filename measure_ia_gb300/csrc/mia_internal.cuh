@@ -15,7 +15,6 @@ constexpr int kThreads = 256;            // pair-kernel block size
 constexpr int kLutBits = 11;             // 2048-bucket logarithmic lookup table (32 octaves)
 constexpr int kLut = 1 << kLutBits;
 constexpr int kLutMantBits = 6;          // 64 buckets per octave of q
-constexpr int kMaxSlots = 12;            // jackknife regions a work unit can touch in shared memory
 constexpr int kMaxRows = 1024;           // neighbour rows per pass of a work unit
 constexpr int kMaxSegs = 2 * kMaxRows;   // a row wraps into at most 2 contiguous segments
 constexpr int kScanTile = 2048;
@@ -24,6 +23,7 @@ constexpr int kScanTile = 2048;
 constexpr unsigned kStatusRange = 1u;      // input coordinate outside [0, L) or NaN
 constexpr unsigned kStatusOverflow = 2u;   // edge queue overflow
 constexpr unsigned kStatusNoSlot = 4u;     // (informational) global-atomic fallback used
+constexpr unsigned kStatusStall = 8u;      // a bounded device wait ran out (a copy that never completed)
 
 // --------------------------------------------------------------------------
 // Device-visible status block (first bytes of the workspace)
@@ -270,6 +270,7 @@ struct Params {
   double range_proj, range_los;
   long long n_cells;
   int shapes_per_unit;
+  int reg_slots;                // work units per run of shapes: the most jackknife regions a neighbourhood touches
   // mixed-form guards and tables
   int lut32_base;               // bucket of the first lut32 entry
   float p_lo32, p_inv32;        // Pi/mu: t = (v - p_lo) * p_inv, bin = floor(t)
@@ -436,7 +437,8 @@ cudaError_t launch_pairs(const Plan& plan, const Params& P, const Dataset* ds_de
                          const unsigned long long* wu_prefix, unsigned long long* wu_next, cudaStream_t st,
                          int num_sms);
 cudaError_t launch_edge_retest(const Params& P, const Work& w, const Out& o, cudaStream_t st, int num_sms);
-cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, unsigned long long* wu_prefix, cudaStream_t st);
+cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, int reg_slots, unsigned long long* wu_prefix,
+                                cudaStream_t st);
 cudaError_t launch_post(const Params& P, const Work& w, const mia_layout& lay, double* out, double volume,
                         long long n_pos, long long n_shape, cudaStream_t st);
 cudaError_t launch_fixed_out(const Params& P, const Work& w, const Out& o, cudaStream_t st);

@@ -7,15 +7,22 @@
 // the KD-tree candidate search that feeds them (:577-580) and the Pool.map over
 // shape chunks (:765-780).
 //
-// Work decomposition: one work unit = up to `shapes_per_unit` shapes of one
-// cell that share a jackknife label a.  A block takes a unit from a global
-// counter, stages the shapes in shared memory, and streams every position of
-// the neighbouring cells (rows of cells along d0 are contiguous in the sorted
-// position arrays); each thread owns one position at a time and loops over the
-// unit's shapes.  Pair contributions go to block-private shared histograms,
-// one per jackknife region b of the positions ("slot"), flushed at the end of
-// the unit into the global histograms of all pairs, of region a and of region
-// b != a (the attribution rule of measure_w_box_jk.py:625-644).
+// Work decomposition: a run is up to `shapes_per_unit` shapes of one cell
+// that share a jackknife label a; a work unit is one run together with one
+// jackknife region b of the positions around it (the regions a run's
+// neighbourhood touches are enumerated per unit; without a jackknife every
+// run is one unit).  A block takes a unit from a global counter, stages the
+// shapes in shared memory, and streams the positions of region b in the
+// neighbouring cells (rows of cells along d0 are contiguous in the sorted
+// position arrays; cells refine the sub-box grid, so a row clipped to b's
+// range is one index range); each thread owns one position at a time and
+// loops over the unit's shapes.  Pair contributions go to one block-private
+// shared histogram, which each lane of a warp updates in its own copy, and
+// are flushed at the end of the unit into the global histograms of all
+// pairs, of region a and of region b != a (the attribution rule of
+// measure_w_box_jk.py:625-644).  A position whose label is not b (a point on
+// a sub-box face carries label 0 wherever it is) adds its pairs to the
+// global sums directly.
 //
 // Sums are exact integers in both forms, so no result depends on the order in
 // which blocks meet the pairs: the mixed form adds FP32 terms as 64-bit fixed
@@ -26,6 +33,17 @@
 
 #include "mia_internal.cuh"
 
+// 1: the mixed form's pair loop runs in two phases (range test, then binning of
+// the survivors with full warps); 0: every lane bins its own pair
+#ifndef MIA_COMPACT
+#define MIA_COMPACT 0
+#endif
+// 1: the mixed form stages a unit's shapes with 1-D TMA bulk copies
+// (cp.async.bulk) into shared memory; 0: with plain loads
+#ifndef MIA_TMA_SHAPES
+#define MIA_TMA_SHAPES 0
+#endif
+
 namespace mia {
 
 namespace {
@@ -35,8 +53,12 @@ constexpr int kRowsPerPass = 256;
 constexpr int kSegsPerPass = 2 * kRowsPerPass;
 
 struct SmemLayout {
-  size_t tables, slot_of, slot_region, shapes, seg_begin, seg_pref, seg_shift, hist, total;
+  size_t tables, shapes, seg_begin, seg_pref, seg_shift, wpos, ring, hist, total;
 };
+
+// Mixed form, per warp: the lanes' current positions (two float4 each) and a
+// ring of kRing candidate pairs (shape << 5 | lane) that passed the range test.
+constexpr int kRing = 64;
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
@@ -61,15 +83,11 @@ struct TablesSmem {
   unsigned short lut32[kLut];
 };
 
-__host__ __device__ inline SmemLayout smem_layout(int J, int spu, int hw, int knb, int mixed, int var) {
+__host__ __device__ inline SmemLayout smem_layout(int spu, int hw, int knb, int mixed, int var) {
   SmemLayout L;
   size_t o = 0;
   L.tables = o;
   o = align16(o + sizeof(TablesSmem));
-  L.slot_of = o;
-  o = align16(o + sizeof(int) * (size_t)(J + 1));
-  L.slot_region = o;
-  o = align16(o + sizeof(int) * kMaxSlots);
   L.shapes = o;
   o = align16(o + (size_t)spu * (mixed ? 48 : 60));
   L.seg_begin = o;
@@ -78,6 +96,10 @@ __host__ __device__ inline SmemLayout smem_layout(int J, int spu, int hw, int kn
   o = align16(o + sizeof(int) * (kSegsPerPass + 1));
   L.seg_shift = o;
   o = align16(o + sizeof(unsigned char) * kSegsPerPass);
+  L.wpos = o;
+  o = align16(o + (mixed ? sizeof(float4) * 2 * kThreads : 0));
+  L.ring = o;
+  o = align16(o + (mixed ? sizeof(unsigned short) * kRing * (kThreads / 32) : 0));
   L.hist = o;
   o = align16(o + sizeof(unsigned) * hist_u32_words(hw, knb, mixed, var) + 16);
   L.total = o;
@@ -191,7 +213,7 @@ struct MixedPos {
 };
 
 __device__ __forceinline__ void load_mixed_pos(const Params& P, const Work& w, const int* seg_begin,
-                                               const int* seg_pref, const unsigned char* seg_shift, const int* slot_of, int nb,
+                                               const int* seg_pref, const unsigned char* seg_shift, int region,
                                                int t, int total, int& seg, MixedPos& p) {
   p.valid = t < total;
   int pidx = 0;
@@ -202,10 +224,10 @@ __device__ __forceinline__ void load_mixed_pos(const Params& P, const Work& w, c
     code = seg_shift[seg];
   }
   p.idx = pidx;
-  p.lab = p.valid ? w.plab_s[pidx] : 0;
-  p.slot = slot_of[p.lab];
-  p.base = p.slot * nb;
-  p.hbase = p.base;
+  p.lab = p.valid ? w.plab_s[pidx] : region;
+  p.slot = p.lab == region ? 0 : -1;
+  p.base = 0;
+  p.hbase = 0;
   p.xh = w.pxh[pidx]; p.xl = w.pxl[pidx];
   p.yh = w.pyh[pidx]; p.yl = w.pyl[pidx];
   p.zh = w.pzh[pidx]; p.zl = w.pzl[pidx];
@@ -360,38 +382,119 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
   }
 }
 
+// The range test of mixed_pair alone: false when the pair is surely beyond
+// the binned line-of-sight range (w) or the last binned separation.  The
+// survivors are exactly the pairs that mixed_pair does not drop before its
+// bin lookups.
+template <int KIND, int FULL>
+__device__ __forceinline__ bool in_range(const Params& P, const float4& a, const float4& b, const MixedPos& p) {
+  float dz = (a.z - p.zh) + (b.z - p.zl);
+  if (FULL && KIND == MIA_KIND_W && P.full[2]) {
+    if (dz > P.halfLf) dz -= P.Lf_hi;
+    else if (dz < -P.halfLf) dz += P.Lf_hi;
+  }
+  if (KIND == MIA_KIND_W && fabsf(dz) > P.los_cut) return false;
+  const float dx = (a.x - p.xh) + (b.x - p.xl);
+  const float dy = (a.y - p.yh) + (b.y - p.yl);
+  const float qp = fmaf(dx, dx, dy * dy);
+  const float q = KIND == MIA_KIND_W ? qp : fmaf(dz, dz, qp);
+  return !(q > P.q_cut);
+}
+
+// ---- TMA bulk copies (1-D) with an mbarrier ------------------------------------
+
+__device__ __forceinline__ unsigned smem_addr(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+               : "memory");
+}
+
+// global -> shared, `bytes` (a multiple of 16, both addresses 16-byte aligned),
+// completion counted on the mbarrier
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
+      "l"(src), "r"(bytes), "r"(smem_addr(bar))
+      : "memory");
+}
+
+// Wait for the mbarrier phase of parity `parity` with a bounded number of
+// polls; false when the limit was reached.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int limit) {
+  for (int k = 0; k < limit; ++k) {
+    unsigned done;
+    asm volatile(
+        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
+        : "=r"(done)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // ---- the persistent pair kernel ----------------------------------------------
 
 // (a minimum-blocks bound of 4 gives the same 61 registers but code that
 // runs 8% slower on the 4M/1M w step; the register count alone allows 4)
+// Sub-boxes (jackknife regions along one cell dimension) that the fine cells
+// lo..hi (unwrapped, periodic) fall in, ascending by first appearance; their
+// number.  cps = fine cells per sub-box.
+__device__ __forceinline__ int subbox_set(int lo, int hi, int nf, int cps, int n_sub, int* set) {
+  int cnt = 0;
+  for (int u = lo; u <= hi && cnt < n_sub;) {
+    const int cc = ((u % nf) + nf) % nf;
+    const int sb = cc / cps;
+    bool seen = false;
+    for (int j = 0; j < cnt; ++j) seen |= set[j] == sb;
+    if (!seen) set[cnt++] = sb;
+    u += cps - cc % cps;  // the first cell of the next sub-box
+  }
+  return cnt;
+}
+
 template <int MIXED, int VAR, int KIND, int FULL>
 __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __restrict__ ds, int n_ds,
                                                      const unsigned long long* __restrict__ wu_prefix,
-                                                     unsigned long long* wu_next, int K, int HW) {
+                                                     unsigned long long* wu_next, int HW) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int tid = threadIdx.x;
   const int nb = P.nb;
-  const SmemLayout SL = smem_layout(P.J, P.shapes_per_unit, HW, K * P.nb, MIXED, VAR);
+  const SmemLayout SL = smem_layout(P.shapes_per_unit, HW, P.nb, MIXED, VAR);
   TablesSmem& T = *reinterpret_cast<TablesSmem*>(smem + SL.tables);
-  int* slot_of = reinterpret_cast<int*>(smem + SL.slot_of);
-  int* slot_region = reinterpret_cast<int*>(smem + SL.slot_region);
   int* seg_begin = reinterpret_cast<int*>(smem + SL.seg_begin);
   int* seg_pref = reinterpret_cast<int*>(smem + SL.seg_pref);
   unsigned char* seg_shift = reinterpret_cast<unsigned char*>(smem + SL.seg_shift);
   unsigned* hist = reinterpret_cast<unsigned*>(smem + SL.hist);
+  float4* wpos = reinterpret_cast<float4*>(smem + SL.wpos);
+  unsigned short* ring = reinterpret_cast<unsigned short*>(smem + SL.ring);
   const int KB = HW;  // >= K * nb
 
-  __shared__ int s_wu;
+  __shared__ long long s_wu;
   __shared__ int s_ds;
   __shared__ Dataset s_data;        // the current unit's dataset (workspace and outputs)
   __shared__ double s_twoR;
   __shared__ Scales s_sc;
-  __shared__ int s_nslots;
+  __shared__ int s_region;          // jackknife region b of the unit's positions (-1: none, skip the unit)
+  __shared__ int s_sub[3];          // b's sub-box along d0, d1, d2
   __shared__ int s_copies;
   __shared__ int s_stride;
   __shared__ int s_scan[32];
   __shared__ int s_total;
   __shared__ float s_box[4];  // the unit's shape cell in d0, d1, widened (see the window below)
+#if MIA_TMA_SHAPES
+  __shared__ __align__(8) unsigned long long s_bar;  // completion of a unit's shape copies
+  unsigned bar_phase = 0;
+  if (MIXED && tid == 0) mbar_init(&s_bar, 1);
+#endif
 
   // tables -> shared (the same binning for every dataset of a batch)
   {
@@ -408,11 +511,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
     }
     if (MIXED)
       for (int i = tid; i < kLut; i += blockDim.x) T.lut32[i] = G.lut32[i];
-    for (int i = tid; i <= P.J; i += blockDim.x) slot_of[i] = -1;
-    if (tid == 0) {
-      s_nslots = 0;
-      s_ds = -1;
-    }
+    if (tid == 0) s_ds = -1;
   }
   const unsigned long long n_wu_all = wu_prefix[n_ds];
   __syncthreads();
@@ -428,7 +527,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
     sx_lo = hist + 3 * KB;
     if (VAR) vr_lo = hist + 4 * KB;
     int* hi = reinterpret_cast<int*>(hist + (4 + VAR) * KB);
-    const int knb = K * nb;
+    const int knb = nb;
     dd_hi = hi;
     sp_hi = hi + knb;
     sx_hi = hi + 2 * knb;
@@ -442,7 +541,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
     sx_q = base + 4 * KB;
     if (VAR) vr_q = base + 6 * KB;
   }
-  const int hist_u32 = MIXED ? (int)hist_u32_words(KB, K * nb, 1, VAR)
+  const int hist_u32 = MIXED ? (int)hist_u32_words(KB, nb, 1, VAR)
                              : (int)(align16(sizeof(unsigned) * (size_t)KB) / 4) + KB * 4 * (3 + VAR);
 
   // rows of position cells: fine-grid extents along d1 and d2 around a shape cell
@@ -464,7 +563,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
           const int mid = (lo + hi + 1) >> 1;
           if (wu_prefix[mid] <= g) lo = mid; else hi = mid - 1;
         }
-        s_wu = (int)(g - wu_prefix[lo]);
+        s_wu = (long long)(g - wu_prefix[lo]);  // run * reg_slots + region slot
         if (lo != s_ds) {
           s_ds = lo;
           s_data = ds[lo];
@@ -475,14 +574,21 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
       }
     }
     __syncthreads();
-    const int wi = s_wu;
+    const long long wi = s_wu;
     if (wi < 0) break;
+    // a catalogue with coordinates outside [0, L) or not finite ends in
+    // MIA_ERR_RANGE: its units are skipped (nothing of it would be used)
+    if (*reinterpret_cast<volatile const unsigned*>(&s_data.w.status->flags) & kStatusRange) {
+      __syncthreads();
+      continue;
+    }
     const Work& w = s_data.w;
     const Out& o = s_data.o;
     const double twoR = s_twoR;
     const Scales& sc = s_sc;
     unsigned long long my_binned = 0;
-    const WorkUnit u = w.wu[wi];
+    const WorkUnit u = w.wu[wi / P.reg_slots];
+    const int rslot = (int)(wi % P.reg_slots);
     int c[3];
     {
       long long t = u.cell;
@@ -501,59 +607,53 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
       s_box[2] = (float)(c[1] * P.s[1] - m);
       s_box[3] = (float)((c[1] + 1) * P.s[1] + m);
     }
-    // -- slot map for the jackknife regions around this cell
+    // -- the unit's position region: slot rslot of the regions that the
+    // neighbourhood's fine cells touch (sub-boxes per dimension, all
+    // combinations); a slot past their number leaves nothing to do
     if (tid == 0) {
-      for (int k = 0; k < s_nslots; ++k) slot_of[slot_region[k]] = -1;
-      int ns = 0;
-      if (P.J == 0) {
-        slot_of[0] = 0;
-        slot_region[0] = 0;
-        ns = 1;
-      } else {
-        int sets[3][16];
-        int cnt[3] = {0, 0, 0};
+      int reg = 0;
+      s_sub[0] = s_sub[1] = s_sub[2] = 0;
+      if (P.J > 0) {
+        int sets[3][16], cnt[3];
         for (int k = 0; k < 3; ++k) {
-          const bool all = P.full[k] || 2 * P.R[k] + 1 >= P.n[k];
-          int lo = all ? -(P.n[k] / 2) : -P.R[k];
-          int N = all ? P.n[k] : 2 * P.R[k] + 1;
-          for (int d = 0; d < N && cnt[k] < 16; ++d) {
-            int cc = wrapi(((c[k] + lo + d) % P.n[k] + P.n[k]) % P.n[k], P.n[k]);
-            int sb = (int)((long long)cc * P.n_sub / P.n[k]);
-            bool seen = false;
-            for (int j = 0; j < cnt[k]; ++j) seen |= sets[k][j] == sb;
-            if (!seen) sets[k][cnt[k]++] = sb;
-          }
+          const int f = c[k] * P.m[k];
+          const int lo = P.full[k] ? 0 : f - P.Rf[k];
+          const int hi = P.full[k] ? P.nf[k] - 1 : f + P.m[k] - 1 + P.Rf[k];
+          cnt[k] = subbox_set(lo, hi, P.nf[k], P.nf[k] / P.n_sub, P.n_sub, sets[k]);
         }
-        for (int i0 = 0; i0 < cnt[0]; ++i0)
-          for (int i1 = 0; i1 < cnt[1]; ++i1)
-            for (int i2 = 0; i2 < cnt[2]; ++i2) {
-              int sub[3];
-              sub[P.axis[0]] = sets[0][i0];
-              sub[P.axis[1]] = sets[1][i1];
-              sub[P.axis[2]] = sets[2][i2];
-              int reg = (sub[0] * P.n_sub + sub[1]) * P.n_sub + sub[2];
-              if (slot_of[reg] < 0 && ns < K) {
-                slot_of[reg] = ns;
-                slot_region[ns++] = reg;
-              }
-            }
-        // positions on a sub-box face carry region 0 wherever they are
-        if (slot_of[0] < 0 && ns < K) {
-          slot_of[0] = ns;
-          slot_region[ns++] = 0;
+        if (rslot >= cnt[0] * cnt[1] * cnt[2]) {
+          reg = -1;
+        } else {
+          const int i0 = rslot % cnt[0], i1 = (rslot / cnt[0]) % cnt[1], i2 = rslot / (cnt[0] * cnt[1]);
+          s_sub[0] = sets[0][i0];
+          s_sub[1] = sets[1][i1];
+          s_sub[2] = sets[2][i2];
+          int sub[3];
+          sub[P.axis[0]] = s_sub[0];
+          sub[P.axis[1]] = s_sub[1];
+          sub[P.axis[2]] = s_sub[2];
+          reg = (sub[0] * P.n_sub + sub[1]) * P.n_sub + sub[2];
         }
+      } else if (rslot > 0) {
+        reg = -1;
       }
-      s_nslots = ns;
-      // private copies of the unit's histograms (mixed form): lanes holding
+      s_region = reg;
+      // private copies of the unit's histogram (mixed form): lanes holding
       // neighbouring positions hit the same bin against a shape, and shared
       // atomics on one address serialise, so lane l adds into copy l mod R;
       // the odd stride puts the R copies of a bin in R distinct banks
       int R = 1;
-      const int stride = (ns * nb) | 1;
+      const int stride = nb | 1;
       if (MIXED)
         while (R < 32 && (2 * R) * stride <= HW) R *= 2;
       s_copies = R;
-      s_stride = R > 1 ? stride : ns * nb;
+      s_stride = R > 1 ? stride : nb;
+    }
+    __syncthreads();
+    const int region = s_region;
+    if (region < 0) {
+      __syncthreads();
+      continue;
     }
     for (int i = tid; i < hist_u32; i += blockDim.x) hist[i] = 0u;
     // -- shapes of the unit -> shared
@@ -571,12 +671,50 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
       float2 rc = make_float2(0.f, 0.f);
       float z = 0.f;
       const int g = u.begin + tid;
+#if MIA_TMA_SHAPES
+      // the ten FP32 shape arrays' slices [b4, b4 + n4) (16-byte aligned: the
+      // arrays' stride is a multiple of 4 floats) -> the per-warp position
+      // area, free until the pair loop
+      const int b4 = u.begin & ~3, n4 = ((u.begin + S + 3) & ~3) - b4, rs = (n4 + 3) & ~3;
+      float* raw = reinterpret_cast<float*>(wpos);
+      if (10 * rs <= 2 * kThreads * 4) {
+        // every thread's earlier accesses to the area (generic proxy) before
+        // the copies (async proxy) write it
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+          mbar_expect(&s_bar, 10u * 4u * (unsigned)n4);
+          const float* src[10] = {w.sxh, w.syh, w.szh, w.swsf, w.sxl, w.syl, w.szl, w.swef, w.saxf, w.sayf};
+          for (int k = 0; k < 10; ++k) bulk_g2s(raw + k * rs, src[k] + b4, 4u * (unsigned)n4, &s_bar);
+        }
+        const bool ok = mbar_wait(&s_bar, bar_phase, 1 << 22);
+        bar_phase ^= 1u;
+        if (__syncthreads_or(!ok)) {  // a copy that never landed: flag it, give it time, stop
+          if (tid == 0) atomicOr(&w.status->flags, kStatusStall);
+          mbar_wait(&s_bar, bar_phase ^ 1u, 1 << 22);
+          return;
+        }
+        if (tid < S) {
+          const int j = tid + (u.begin - b4);
+          ra = make_float4(raw[j], raw[rs + j], raw[2 * rs + j], raw[3 * rs + j] * sc.sc_dd);
+          rb = make_float4(raw[4 * rs + j], raw[5 * rs + j], raw[6 * rs + j], raw[7 * rs + j] * sc.sc_sp);
+          rc = make_float2(raw[8 * rs + j], raw[9 * rs + j]);
+        }
+      } else if (tid < S) {
+        ra = make_float4(w.sxh[g], w.syh[g], w.szh[g], w.swsf[g] * sc.sc_dd);
+        rb = make_float4(w.sxl[g], w.syl[g], w.szl[g], w.swef[g] * sc.sc_sp);
+        rc = make_float2(w.saxf[g], w.sayf[g]);
+      }
+      if (tid < S) {
+#else
       if (tid < S) {
         // weights times the (power-of-two) fixed-point scales: exact
         ra = make_float4(w.sxh[g], w.syh[g], w.szh[g], w.swsf[g] * sc.sc_dd);
         rb = make_float4(w.sxl[g], w.syl[g], w.szl[g], w.swef[g] * sc.sc_sp);
         rc = make_float2(w.saxf[g], w.sayf[g]);
+#endif
         z = ra.z + rb.z;
+        if (!(z == z)) z = INFINITY;  // the ranks below must form a permutation
         zs[tid] = z;
       }
       __syncthreads();
@@ -603,6 +741,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
       float z = 0.f;
       if (tid < S) {
         z = (float)w.sz[g];
+        if (!(z == z)) z = INFINITY;  // the ranks below must form a permutation
         zs[tid] = z;
       }
       __syncthreads();
@@ -647,10 +786,14 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
             rem = r2proj - gap1 * gap1 - gap2 * gap2;
             ok = rem >= 0.0;
           }
+          const int cc1 = wrapi(u1, P.nf[1]), cc2 = wrapi(u2, P.nf[2]);
+          // only the cells of the unit's position region
+          if (P.J > 0 && ((long long)cc1 * P.n_sub / P.nf[1] != s_sub[1] ||
+                          (long long)cc2 * P.n_sub / P.nf[2] != s_sub[2]))
+            ok = false;
           if (ok) {
             const int sh1d = u1 < 0 ? -1 : (u1 >= P.nf[1] ? 1 : 0);
             const int sh2d = u2 < 0 ? -1 : (u2 >= P.nf[2] ? 1 : 0);
-            const int cc1 = wrapi(u1, P.nf[1]), cc2 = wrapi(u2, P.nf[2]);
             const int f0 = c[0] * P.m[0];
             int a0, a1;
             if (P.full[0]) {
@@ -664,24 +807,43 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
             }
             const long long rowbase = ((long long)cc2 * P.nf[1] + cc1) * P.nf[0];
             const int code_yz = 3 * (sh1d + 1) + 9 * (sh2d + 1);
+            // the row's cells as at most two wrapped ranges [x0, x1] (d0 shift -1, 0 or +1),
+            // each clipped to the unit's region along d0
+            int x0a, x1a, x0b = 0, x1b = -1;
             if (a0 < 0) {
-              b0 = w.pstart[rowbase + a0 + P.nf[0]];
-              len0 = w.pstart[rowbase + P.nf[0]] - b0;
+              x0a = a0 + P.nf[0];
+              x1a = P.nf[0] - 1;
               sh0 = code_yz + 0;  // d0 shift -1
-              b1 = w.pstart[rowbase];
-              len1 = w.pstart[rowbase + a1 + 1] - b1;
+              x0b = 0;
+              x1b = a1;
               sh1 = code_yz + 1;
             } else if (a1 >= P.nf[0]) {
-              b0 = w.pstart[rowbase + a0];
-              len0 = w.pstart[rowbase + P.nf[0]] - b0;
+              x0a = a0;
+              x1a = P.nf[0] - 1;
               sh0 = code_yz + 1;
-              b1 = w.pstart[rowbase];
-              len1 = w.pstart[rowbase + a1 - P.nf[0] + 1] - b1;
+              x0b = 0;
+              x1b = a1 - P.nf[0];
               sh1 = code_yz + 2;  // d0 shift +1
             } else {
-              b0 = w.pstart[rowbase + a0];
-              len0 = w.pstart[rowbase + a1 + 1] - b0;
+              x0a = a0;
+              x1a = a1;
               sh0 = code_yz + 1;
+            }
+            if (P.J > 0) {
+              const int cps = P.nf[0] / P.n_sub;
+              const int r0 = s_sub[0] * cps, r1 = r0 + cps - 1;
+              x0a = max(x0a, r0);
+              x1a = min(x1a, r1);
+              x0b = max(x0b, r0);
+              x1b = min(x1b, r1);
+            }
+            if (x0a <= x1a) {
+              b0 = w.pstart[rowbase + x0a];
+              len0 = w.pstart[rowbase + x1a + 1] - b0;
+            }
+            if (x0b <= x1b) {
+              b1 = w.pstart[rowbase + x0b];
+              len1 = w.pstart[rowbase + x1b + 1] - b1;
             }
           }
         }
@@ -743,7 +905,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
         // agree on one shape range
         for (int tb = 0; tb < total; tb += blockDim.x) {
           MixedPos p0;
-          load_mixed_pos(P, w, seg_begin, seg_pref, seg_shift, slot_of, nb, tb + tid, total, seg, p0);
+          load_mixed_pos(P, w, seg_begin, seg_pref, seg_shift, region, tb + tid, total, seg, p0);
           p0.base += copy_off;
           int i_lo = S, i_hi = 0;
           if (p0.valid) {
@@ -777,6 +939,62 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
           // and every lane then reads the same staged shape in each iteration
           const int wlo = __reduce_min_sync(0xffffffffu, i_lo);
           const int whi = __reduce_max_sync(0xffffffffu, i_hi);
+#if MIA_COMPACT
+          // Two phases.  (1) Every lane tests its own pair with the shape of
+          // the iteration (the cheap range test); the warp's survivors go to
+          // its ring as (shape, lane).  (2) Whenever 32 are waiting, each lane
+          // takes one and bins and accumulates it (mixed_pair) with the
+          // position of the lane that found it.  A third of the pairs fail the
+          // range test, and without the ring a lane holding one would idle
+          // through the whole binning path of its warp-mates.
+          const int lane = tid & 31;
+          float4* WP = wpos + 2 * (tid & ~31);
+          unsigned short* Q = ring + kRing * (tid >> 5);
+          // this lane's position for the others (idx, or ~idx for a position
+          // whose label is not the unit's region)
+          WP[2 * lane] = make_float4(p0.xh, p0.xl, p0.yh, p0.yl);
+          WP[2 * lane + 1] = make_float4(p0.zh, p0.zl, p0.w, __int_as_float(p0.slot >= 0 ? p0.idx : ~p0.idx));
+          __syncwarp();
+          auto bin_entry = [&](unsigned e) {
+            const int i = (int)(e >> 5), src = (int)(e & 31u);
+            const float4 pa = WP[2 * src], pb = WP[2 * src + 1];
+            MixedPos q;
+            q.xh = pa.x; q.xl = pa.y; q.yh = pa.z; q.yl = pa.w;
+            q.zh = pb.x; q.zl = pb.y; q.w = pb.z;
+            const int v = __float_as_int(pb.w);
+            q.valid = true;
+            q.base = copy_off;
+            q.hbase = 0;
+            if (v >= 0) {
+              q.idx = v;
+              q.slot = 0;
+              q.lab = region;
+            } else {
+              q.idx = ~v;
+              q.slot = -1;
+              q.lab = w.plab_s[q.idx];
+            }
+            mixed_pair<KIND, FULL, VAR>(P, T, A[i], B[i], C, I, i, q, hv, w, o, sc, twoR, u.label, my_binned);
+          };
+          const unsigned below = (1u << lane) - 1u;
+          unsigned head = 0, tail = 0;  // warp-uniform ring counters
+          for (int i = wlo; i < whi; ++i) {
+            const bool pass = p0.valid && in_range<KIND, FULL>(P, A[i], B[i], p0);
+            const unsigned m = __ballot_sync(0xffffffffu, pass);
+            if (pass) Q[(tail + __popc(m & below)) & (kRing - 1)] = (unsigned short)((i << 5) | lane);
+            tail += __popc(m);
+            if (tail - head >= 32) {
+              __syncwarp();
+              const unsigned e = Q[(head + lane) & (kRing - 1)];
+              head += 32;
+              bin_entry(e);
+              __syncwarp();
+            }
+          }
+          __syncwarp();
+          if ((unsigned)lane < tail - head) bin_entry(Q[(head + lane) & (kRing - 1)]);
+          __syncwarp();
+#else
           if (p0.valid && wlo < whi) {
             // the next shape is in flight while this pair is processed (index S
             // at most: still inside the staging area); two register sets take
@@ -792,6 +1010,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
               if (++i >= whi) break;
             }
           }
+#endif
         }
       } else {
         int seg = 0;
@@ -807,9 +1026,9 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
             pidx = seg_begin[seg] + (t - seg_pref[seg]);
             code = seg_shift[seg];
           }
-          const int plab = t < total ? w.plab_s[pidx] : 0;
-          const int slot = slot_of[plab];
-          const int base = slot * nb;
+          const int plab = t < total ? w.plab_s[pidx] : region;
+          const int slot = plab == region ? 0 : -1;
+          const int base = 0;
           const double qx = w.px[pidx], qy = w.py[pidx], qz = w.pz[pidx], pw = w.pw[pidx];
           // the shapes that can bin with this position: the same conservative
           // FP32 window over the line-of-sight order as the mixed form (the
@@ -872,17 +1091,16 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
       __syncthreads();
     }
 
-    // -- flush the unit's histograms
-    const int ns = s_nslots;
+    // -- flush the unit's histogram
     const int a = u.label;
+    const int b = region;
     const int copies = s_copies, stride = s_stride;
-    for (int idx = tid; idx < ns * nb; idx += blockDim.x) {
-      const int k = idx / nb, bin = idx - k * nb;
+    for (int idx = tid; idx < nb; idx += blockDim.x) {
+      const int bin = idx;
       unsigned cnt = 0;
       for (int c = 0; c < copies; ++c) cnt += h_cnt[c * stride + idx];
       if (cnt == 0) continue;
       my_binned += cnt;
-      const int b = slot_region[k];
       if (MIXED) {
         // the unit's exact partial of this (slot, bin): the high word plus the
         // copies' signed low words, added to the dataset's 64-bit sums
@@ -950,6 +1168,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
 // FP64 re-test of the pairs the mixed kernel could not decide in FP32; their
 // FP64 terms join the dataset's fixed-point sums at the same scales.
 __global__ void k_edge_retest(Params P, Work w, Out o) {
+  if (w.status->flags & kStatusRange) return;  // the measurement ends in MIA_ERR_RANGE
   const unsigned long long n_raw = w.status->edge_count;
   const unsigned long long n = n_raw < (unsigned long long)w.edge_capacity ? n_raw : (unsigned long long)w.edge_capacity;
   const double twoR = dataset_twoR(w.reg, P.J);
@@ -1006,12 +1225,12 @@ __global__ void k_fixed_out(Params P, Work w, Out o) {
   }
 }
 
-// Histogram words per array for the mixed form: K slots of nb bins at least,
-// and as much more (for private copies, up to 32 copies of one slot) as fits
-// without lowering the blocks per SM that the registers allow.
+// Histogram words per array for the mixed form: nb bins at least, and as
+// much more (for private copies, up to 32) as fits without lowering the
+// blocks per SM that the registers allow.
 template <int MIXED, int VAR, int KIND, int FULL>
-cudaError_t hist_words_for(const Params& P, int K, int& hw) {
-  hw = K * P.nb;
+cudaError_t hist_words_for(const Params& P, int& hw) {
+  hw = P.nb;
   if (!MIXED) return cudaSuccess;
   auto kern = k_pairs<MIXED, VAR, KIND, FULL>;
   int dev = 0, smem_sm = 0, smem_blk = 0, reserved = 0, b_reg = 0;
@@ -1023,13 +1242,16 @@ cudaError_t hist_words_for(const Params& P, int K, int& hw) {
   cudaFuncAttributes fa;
   if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, kern);
   if (e != cudaSuccess) return e;
+#ifdef MIA_MAX_BLOCKS_PER_SM
+  if (b_reg > MIA_MAX_BLOCKS_PER_SM) b_reg = MIA_MAX_BLOCKS_PER_SM;
+#endif
   if (b_reg < 1) return cudaSuccess;
   long long room = (long long)smem_sm / b_reg - reserved - (long long)fa.sharedSizeBytes;
   if (room > smem_blk - (long long)fa.sharedSizeBytes) room = smem_blk - (long long)fa.sharedSizeBytes;
   const int hw_max = 32 * (P.nb | 1);
   int best = hw;
   for (int c = hw_max; c > hw; c -= 16)
-    if ((long long)smem_layout(P.J, P.shapes_per_unit, c, K * P.nb, MIXED, VAR).total <= room) {
+    if ((long long)smem_layout(P.shapes_per_unit, c, P.nb, MIXED, VAR).total <= room) {
       best = c;
       break;
     }
@@ -1039,22 +1261,25 @@ cudaError_t hist_words_for(const Params& P, int K, int& hw) {
 
 template <int MIXED, int VAR, int KIND, int FULL>
 cudaError_t launch_one(const Params& P, const Dataset* ds, int n_ds, const unsigned long long* wu_prefix,
-                       unsigned long long* wu_next, cudaStream_t st, int num_sms, int K) {
+                       unsigned long long* wu_next, cudaStream_t st, int num_sms) {
   int hw = 0;
-  cudaError_t e = hist_words_for<MIXED, VAR, KIND, FULL>(P, K, hw);
+  cudaError_t e = hist_words_for<MIXED, VAR, KIND, FULL>(P, hw);
   if (e != cudaSuccess) return e;
   auto kern = k_pairs<MIXED, VAR, KIND, FULL>;
-  const int hw0 = K * P.nb;
+  const int hw0 = P.nb;
   int per_sm = 0, per_sm0 = 0;
-  size_t smem = smem_layout(P.J, P.shapes_per_unit, hw0, hw0, MIXED, VAR).total;
+  size_t smem = smem_layout(P.shapes_per_unit, hw0, hw0, MIXED, VAR).total;
   e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm0, kern, kThreads, smem);
   if (e != cudaSuccess) return e;
+#ifdef MIA_MAX_BLOCKS_PER_SM
+  if (per_sm0 > MIA_MAX_BLOCKS_PER_SM) per_sm0 = MIA_MAX_BLOCKS_PER_SM;
+#endif
   per_sm = per_sm0;
   // the copies must not cost a block per SM
   while (hw > hw0) {
-    const size_t s1 = smem_layout(P.J, P.shapes_per_unit, hw, hw0, MIXED, VAR).total;
+    const size_t s1 = smem_layout(P.shapes_per_unit, hw, hw0, MIXED, VAR).total;
     e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s1);
     if (e != cudaSuccess) return e;
     int b = 0;
@@ -1062,7 +1287,7 @@ cudaError_t launch_one(const Params& P, const Dataset* ds, int n_ds, const unsig
     if (e != cudaSuccess) return e;
     if (b >= per_sm0) {
       smem = s1;
-      per_sm = b;
+      per_sm = per_sm0;
       break;
     }
     hw = hw - 16 > hw0 ? hw - 16 : hw0;
@@ -1072,27 +1297,29 @@ cudaError_t launch_one(const Params& P, const Dataset* ds, int n_ds, const unsig
     if (e != cudaSuccess) return e;
   }
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  kern<<<num_sms * per_sm, kThreads, smem, st>>>(P, ds, n_ds, wu_prefix, wu_next, K, hw);
+  kern<<<num_sms * per_sm, kThreads, smem, st>>>(P, ds, n_ds, wu_prefix, wu_next, hw);
   return cudaGetLastError();
 }
 
 template <int MIXED, int VAR>
 cudaError_t launch_kind(const Params& P, const Dataset* ds, int n_ds, const unsigned long long* wu_prefix,
-                        unsigned long long* wu_next, cudaStream_t st, int num_sms, int K) {
+                        unsigned long long* wu_next, cudaStream_t st, int num_sms) {
   const bool full = P.full[0] || P.full[1] || P.full[2];
   if (P.kind == MIA_KIND_W)
-    return full ? launch_one<MIXED, VAR, MIA_KIND_W, 1>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms, K)
-                : launch_one<MIXED, VAR, MIA_KIND_W, 0>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms, K);
-  return full ? launch_one<MIXED, VAR, MIA_KIND_MULTIPOLES, 1>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms, K)
-              : launch_one<MIXED, VAR, MIA_KIND_MULTIPOLES, 0>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms, K);
+    return full ? launch_one<MIXED, VAR, MIA_KIND_W, 1>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms)
+                : launch_one<MIXED, VAR, MIA_KIND_W, 0>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms);
+  return full ? launch_one<MIXED, VAR, MIA_KIND_MULTIPOLES, 1>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms)
+              : launch_one<MIXED, VAR, MIA_KIND_MULTIPOLES, 0>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms);
 }
 
-__global__ void k_batch_prefix(const Dataset* ds, int n, unsigned long long* prefix) {
+// Global work-unit index of each dataset's first unit: a dataset has n_wu
+// runs times reg_slots region slots.
+__global__ void k_batch_prefix(const Dataset* ds, int n, int reg_slots, unsigned long long* prefix) {
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     unsigned long long acc = 0;
     for (int i = 0; i < n; ++i) {
       prefix[i] = acc;
-      acc += ds[i].w.status->n_wu;
+      acc += ds[i].w.status->n_wu * (unsigned long long)reg_slots;
     }
     prefix[n] = acc;
   }
@@ -1100,12 +1327,13 @@ __global__ void k_batch_prefix(const Dataset* ds, int n, unsigned long long* pre
 
 }  // namespace
 
-size_t pair_smem_bytes(int J, int spu, int K, int nb, int mixed, int var) {
-  return smem_layout(J, spu, K * nb, K * nb, mixed, var).total;
+size_t pair_smem_bytes(int spu, int nb, int mixed, int var) {
+  return smem_layout(spu, nb, nb, mixed, var).total;
 }
 
-cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, unsigned long long* wu_prefix, cudaStream_t st) {
-  k_batch_prefix<<<1, 32, 0, st>>>(ds_dev, n_ds, wu_prefix);
+cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, int reg_slots, unsigned long long* wu_prefix,
+                                cudaStream_t st) {
+  k_batch_prefix<<<1, 32, 0, st>>>(ds_dev, n_ds, reg_slots, wu_prefix);
   return cudaGetLastError();
 }
 
@@ -1124,32 +1352,12 @@ cudaError_t launch_edge_retest(const Params& P, const Work& w, const Out& o, cud
 cudaError_t launch_pairs(const Plan& plan, const Params& P, const Dataset* ds_dev, int n_ds,
                          const unsigned long long* wu_prefix, unsigned long long* wu_next, cudaStream_t st,
                          int num_sms) {
-  // slots: as many regions as a neighbourhood can touch, within the shared-memory budget
-  int K = plan.J > 0 ? kMaxSlots : 1;
-  {
-    int need = 1;
-    if (plan.J > 0) {
-      need = 1;
-      for (int k = 0; k < 3; ++k) {
-        int span = plan.full[k] ? plan.n[k] : 2 * plan.R[k] + 1;
-        int per_sub = plan.n[k] / plan.n_sub;
-        int m = (span + per_sub - 1) / per_sub + 1;
-        if (m > plan.n_sub) m = plan.n_sub;
-        need *= m;
-      }
-      need += 1;
-    }
-    if (need < K) K = need;
-    const size_t budget = 200 * 1024;
-    while (K > 1 && pair_smem_bytes(plan.J, P.shapes_per_unit, K, P.nb, P.precision == MIA_MIXED, P.want_variance) >
-                        budget)
-      --K;
-  }
+  (void)plan;
   if (P.precision == MIA_MIXED)
-    return P.want_variance ? launch_kind<1, 1>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms, K)
-                           : launch_kind<1, 0>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms, K);
-  return P.want_variance ? launch_kind<0, 1>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms, K)
-                         : launch_kind<0, 0>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms, K);
+    return P.want_variance ? launch_kind<1, 1>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms)
+                           : launch_kind<1, 0>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms);
+  return P.want_variance ? launch_kind<0, 1>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms)
+                         : launch_kind<0, 0>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms);
 }
 
 }  // namespace mia

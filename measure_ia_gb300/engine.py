@@ -381,17 +381,8 @@ class BatchCounter:
 
     def capture(self):
         """Record ``enqueue`` in a CUDA graph (after ``prepare``)."""
-        import torch
-        s = torch.cuda.Stream(self.pc.device)
-        s.wait_stream(torch.cuda.current_stream(self.pc.device))
-        with torch.cuda.stream(s):  # one eager run on the capture stream first
-            self.enqueue(s)
-        s.synchronize()
-        g = torch.cuda.CUDAGraph()
-        with torch.cuda.graph(g, stream=s, capture_error_mode="relaxed"):
-            self.enqueue(s)
-        self.graph = g
-        return g
+        self.graph = capture_batches([self])
+        return self.graph
 
     def replay(self):
         self.graph.replay()
@@ -421,3 +412,23 @@ class BatchCounter:
         import torch
         reals = torch.cat([self.realisations(i, key) for i in range(self.n)], dim=1)
         return jackknife_cross_cov(reals, None, device=self.pc.device)
+
+
+def capture_batches(batches):
+    """One CUDA graph that runs every batch's ``enqueue`` (e.g. the w and the
+    multipole measurement of the same catalogues), after each batch's
+    ``prepare``.  Replaying it re-measures all of them; ``status()`` of each
+    batch then reports its errors."""
+    import torch
+    dev = batches[0].pc.device
+    s = torch.cuda.Stream(dev)
+    s.wait_stream(torch.cuda.current_stream(dev))
+    with torch.cuda.stream(s):  # one eager run on the capture stream first
+        for b in batches:
+            b.enqueue(s)
+    s.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=s, capture_error_mode="relaxed"):
+        for b in batches:
+            b.enqueue(s)
+    return g

@@ -36,7 +36,7 @@ from . import _lib as L
 from . import binning as B
 from .base import BaseHelpers, JackknifeCovariance
 from .cosmology import comoving_radial_distance, default_cosmology
-from .output import norm_path, open_output
+from .output import norm_path, store_for
 
 
 def _centres(edges):
@@ -401,7 +401,7 @@ class MeasureIALightcone(BaseHelpers, JackknifeCovariance):
         chi = lambda z: comoving_radial_distance(cosmology, 1 / (1 + z)) * (h if over_h else 1.0)
         run = _Run(self, kind, est, d, corr_type, data, rnd, chi, h, over_h, rp_cut, masks, jk_patches if measure_cov
                    else None)
-        store = open_output(self.output_file_name)
+        store = store_for(self)
         try:
             run.full_and_realisations(ns)
         finally:

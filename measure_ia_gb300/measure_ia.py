@@ -17,8 +17,10 @@ Backend choice mirrors the reference's dispatch (measure_IA.py:103-161):
 The temporary file the reference writes is not needed: catalogues stay in
 device memory.  Extra keyword arguments: ``precision`` ('fp64' for the plain
 FP64 form, 'mixed' for FP32 pair arithmetic with FP64 edge re-tests),
-``device`` and ``autotune`` (search the launch knobs on first use of a
-workload shape; results are identical, only speed changes).
+``device``, ``autotune`` (search the launch knobs on first use of a
+workload shape; results are identical, only speed changes) and
+``launch_knobs`` (fixed knobs instead: a dict with any of ``cell_size``,
+``cell_refine``, ``shapes_per_unit``, ``cell_size_los``, ``cell_refine_los``).
 """
 
 from __future__ import annotations
@@ -29,7 +31,7 @@ import numpy as np
 
 from ._lib import MIA_ERR_OVERFLOW, MiaError
 from .engine import PairCounter
-from .output import norm_path, open_output
+from .output import norm_path, store_for
 from .base import BaseHelpers, JackknifeCovariance
 from .sim_info import SimInfo
 
@@ -59,7 +61,7 @@ class MeasureIABox(SimInfo, BaseHelpers, JackknifeCovariance):
 
     def __init__(self, data, output_file_name, simulation=None, snapshot=None, separation_limits=[0.1, 20.0],
                  num_bins_r=8, num_bins_pi=20, pi_max=None, boxsize=None, periodicity=True, num_nodes=1,
-                 precision="fp64", device=0, autotune=False):
+                 precision="fp64", device=0, autotune=False, launch_knobs=None):
         SimInfo.__init__(self, simulation, snapshot, boxsize)
         self.data = data
         self.output_file_name = output_file_name
@@ -68,6 +70,7 @@ class MeasureIABox(SimInfo, BaseHelpers, JackknifeCovariance):
         self.precision = precision
         self.device = device
         self.autotune = autotune
+        self.launch_knobs = dict(launch_knobs or {})
         try:
             self.Num_position = len(data["Position"])
             self.Num_shape = len(data["Position_shape_sample"])
@@ -172,7 +175,7 @@ class MeasureIABox(SimInfo, BaseHelpers, JackknifeCovariance):
                     precision=precision, membership="brute" if layout == "brute" else "tree",
                     ellipticity=ellipticity, want_variance=(layout == "brute" and L_sub > 0),
                     volume=self.boxsize ** 3, rp_cut=0.0 if rp_cut is None else rp_cut, device=self.device)
-        counter = PairCounter(kind, **args)
+        counter = PairCounter(kind, **args, **self.launch_knobs)
         dcat = counter.to_device(cat)
         if self.autotune:
             counter = counter.tuned(dcat)
@@ -187,7 +190,7 @@ class MeasureIABox(SimInfo, BaseHelpers, JackknifeCovariance):
                 raise
             warnings.warn("mixed form: edge re-test queue overflow, measuring in the FP64 form", RuntimeWarning)
             del bufs
-            counter = PairCounter(kind, **{**args, "precision": "fp64"})
+            counter = PairCounter(kind, **{**args, "precision": "fp64"}, **self.launch_knobs)
             bufs = counter.allocate(n_pos, n_shape)
             counter.run(dcat, bufs)
         meas = counter.fetch(bufs)
@@ -213,7 +216,7 @@ class MeasureIABox(SimInfo, BaseHelpers, JackknifeCovariance):
     def _write(self, kind, d, corr_type, num_jk, meas, layout):
         """Datasets in the reference's groups (measure_w_box_jk.py:816-854,
         measure_m_box_jk.py:857-894, measure_IA_base.py:454-668)."""
-        f = open_output(self.output_file_name)
+        f = store_for(self)
         sg = self.snap_group
         a = meas.arrays
         J = meas.J

@@ -10,6 +10,12 @@ already in the file (earlier runs, other processes) are read first and kept,
 as h5py's append mode keeps them; a file the built-in reader cannot parse is
 left untouched and the write raises.  Paths are normalised the way HDF5
 resolves them ('Snapshot_99//w/xi_gg/' == 'Snapshot_99/w/xi_gg').
+
+A store of a named file lives only while it holds datasets not yet written:
+``flush`` writes the file and releases the store, and the next
+``open_output`` of that name reads the file again.  Without a file name
+(``output_file_name=None``) the products stay in an in-memory store owned by
+the measuring object (``store_for``), never shared between objects.
 """
 
 from __future__ import annotations
@@ -26,7 +32,8 @@ try:  # pragma: no cover - depends on the host
 except Exception:
     HAVE_H5PY = False
 
-_STORES: dict[str, "OutputFile"] = {}
+# stores of named files with datasets not yet flushed, by absolute path
+_OPEN: dict[str, "OutputFile"] = {}
 
 
 def norm_path(*parts):
@@ -45,13 +52,20 @@ class OutputFile:
         if self._loaded:
             return
         self._loaded = True
-        if self.name is None or self.use_h5py or not os.path.exists(self.name):
+        if self.name is None or not os.path.exists(self.name):
             return
-        try:
-            old = hdf5.read_file(self.name)
-        except (ValueError, NotImplementedError) as exc:
-            raise RuntimeError(f"{self.name} exists but cannot be read without h5py ({exc}); "
-                               "remove it or install h5py") from exc
+        if self.use_h5py:
+            import h5py
+            old = {}
+            with h5py.File(self.name, "r") as f:
+                f.visititems(lambda path, obj: old.__setitem__(path, obj[()]) if isinstance(obj, h5py.Dataset)
+                             else None)
+        else:
+            try:
+                old = hdf5.read_file(self.name)
+            except (ValueError, NotImplementedError) as exc:
+                raise RuntimeError(f"{self.name} exists but cannot be read without h5py ({exc}); "
+                                   "remove it or install h5py") from exc
         self.data = {**old, **self.data}
 
     def write(self, group, dataset, value):
@@ -67,7 +81,8 @@ class OutputFile:
         return sorted(self.data)
 
     def flush(self):
-        """Write the datasets to ``output_file_name``."""
+        """Write the datasets to ``output_file_name`` and release the store
+        (a later ``open_output`` of the name reads the file)."""
         if self.name is None:
             return
         if self.use_h5py:
@@ -77,19 +92,39 @@ class OutputFile:
                     if path in f:
                         del f[path]
                     f.create_dataset(path, data=v)
-            return
-        d = os.path.dirname(os.path.abspath(self.name))
-        if os.path.isdir(d):
+        else:
+            d = os.path.dirname(os.path.abspath(self.name))
+            if not os.path.isdir(d):  # nowhere to write: the datasets stay in this store
+                return
             self._load()
             hdf5.write_file(self.name, self.data)
+        key = os.path.abspath(self.name)
+        if _OPEN.get(key) is self:
+            del _OPEN[key]
 
 
 def open_output(name) -> OutputFile:
-    """The store behind ``output_file_name`` (created on first use)."""
-    key = os.path.abspath(name) if name is not None else None
-    if key not in _STORES:
-        _STORES[key] = OutputFile(name)
-    return _STORES[key]
+    """The store behind ``output_file_name``: the open one with unflushed
+    datasets, else a new one that reads the file on first use.  ``None`` gives
+    a new in-memory store (use ``store_for`` to keep one per object)."""
+    if name is None:
+        return OutputFile(None)
+    key = os.path.abspath(name)
+    if key not in _OPEN:
+        _OPEN[key] = OutputFile(name)
+    return _OPEN[key]
+
+
+def store_for(obj) -> OutputFile:
+    """The output store of a measuring object: its file's store, or, without a
+    file name, an in-memory store kept on the object itself."""
+    if obj.output_file_name is not None:
+        return open_output(obj.output_file_name)
+    st = getattr(obj, "_memory_store", None)
+    if st is None:
+        st = OutputFile(None)
+        obj._memory_store = st
+    return st
 
 
 def read_output(name) -> dict:

@@ -288,15 +288,26 @@ class Counts:
     npairs_jk: np.ndarray | None = None
 
 
+def position_tree(kind, b: Binning, los, pos):
+    """The periodic KD-tree over the positions that the tree backends query:
+    2-D over the projected plane for (r_p, Pi), 3-D for (r, mu_r)
+    (measure_w_box_jk.py:764, measure_m_box_jk.py:804)."""
+    return KDTree(pos[:, _not_los(los)] if kind == "w" else pos, boxsize=b.boxsize)
+
+
 def count_pairs(kind, b: Binning, los, pos, w, spos, axis, e, ws, R, lab_pos=None, lab_shape=None,
-                n_box=0, membership="tree", rp_cut=0.0, chunk=2000, periodic=True, shape_range=None):
+                n_box=0, membership="tree", rp_cut=0.0, chunk=2000, periodic=True, shape_range=None,
+                pos_tree=None):
     """Histograms DD, S+D, SxD (+ jackknife parts) over all binned pairs.
 
     Follows ``_measure_xi_rp_pi_box_jk_batch`` (measure_w_box_jk.py:543-646)
     for ``kind='w'`` and ``_measure_xi_r_mur_box_jk_batch``
     (measure_m_box_jk.py:570-682) for ``kind='m'``; ``membership='brute'``
     follows the brute variants (measure_w_box_jk.py:157-211,
-    measure_m_box_jk.py:164-223), which also accumulate the S+D variance."""
+    measure_m_box_jk.py:164-223), which also accumulate the S+D variance.
+    ``pos_tree`` (from ``position_tree``) is reused when given, as the
+    reference's Pool workers reuse the parent's ``self.pos_tree``; ``chunk``
+    bounds the shapes whose candidate pairs are held in memory at once."""
     nr, npi = b.num_bins_r, b.num_bins_pi
     nb = nr * npi
     DD = np.zeros(nb); SP = np.zeros(nb); SX = np.zeros(nb); VAR = np.zeros(nb)
@@ -305,9 +316,8 @@ def count_pairs(kind, b: Binning, los, pos, w, spos, axis, e, ws, R, lab_pos=Non
     if jk:
         DDj = np.zeros(n_box * nb); SPj = np.zeros(n_box * nb); CNTj = np.zeros(n_box * nb, dtype=np.int64)
     nl = _not_los(los)
-    pos_tree = None
-    if membership == "tree":
-        pos_tree = KDTree(pos[:, nl] if kind == "w" else pos, boxsize=b.boxsize)
+    if membership == "tree" and pos_tree is None:
+        pos_tree = position_tree(kind, b, los, pos)
     s_lo, s_hi = (0, len(spos)) if shape_range is None else shape_range
     for c0 in range(s_lo, s_hi, chunk):
         c1 = min(s_hi, c0 + chunk)
@@ -463,7 +473,7 @@ def _sub(a, b):
 
 
 def measure(kind, b: Binning, data, dataset_name, corr_type="both", num_jk=0, masks=None,
-            ellipticity="distortion", layout="multiprocessing", rp_cut=0.0, chunk=2000):
+            ellipticity="distortion", layout="multiprocessing", rp_cut=0.0, chunk=2000, processes=1):
     """Whole measurement as ``MeasureIABox.measure_xi_w`` (kind='w') or
     ``measure_xi_multipoles`` (kind='m') writes it (measure_IA.py:68-262):
     returns {hdf5 path: array} with the reference's dataset names, plus
@@ -471,7 +481,9 @@ def measure(kind, b: Binning, data, dataset_name, corr_type="both", num_jk=0, ma
 
     ``layout`` selects the backend whose datasets are mirrored:
     'multiprocessing' (num_nodes > 1), 'tree' (num_nodes == 1) or 'brute'
-    (temp_file_path=False)."""
+    (temp_file_path=False).  ``processes > 1`` counts the pairs of a tree
+    layout in a spawned process pool (``count_pairs_parallel``; large
+    catalogues), with ``chunk`` shapes per task."""
     if corr_type not in ("both", "g+", "gg"):
         raise KeyError("Unknown value for corr_type. Choose from [g+, gg, both]")
     L_sub = 0
@@ -490,7 +502,11 @@ def measure(kind, b: Binning, data, dataset_name, corr_type="both", num_jk=0, ma
         lab_p = jackknife_labels(pos, b.L_0p5, L_sub)
         lab_s = jackknife_labels(spos, b.L_0p5, L_sub)
     membership = "brute" if layout == "brute" else "tree"
-    c = count_pairs(kind, b, los, pos, w, spos, axis, e, ws, R, lab_p, lab_s, n_box, membership, rp_cut, chunk)
+    if processes > 1 and membership == "tree" and rp_cut == 0.0:
+        c, _ = count_pairs_parallel(kind, b, los, pos, w, spos, axis, e, ws, R, lab_p, lab_s, n_box,
+                                    (0, n_shape), processes=processes, chunk=chunk, context="spawn")
+    else:
+        c = count_pairs(kind, b, los, pos, w, spos, axis, e, ws, R, lab_p, lab_s, n_box, membership, rp_cut, chunk)
     out = {"__counts__": c}
     sg = b.snap_group
     top = "w" if kind == "w" else "multipoles"
@@ -580,29 +596,57 @@ def _worker(args):
     c0, c1 = args
     g = _G
     return count_pairs(g["kind"], g["b"], g["los"], g["pos"], g["w"], g["spos"], g["axis"], g["e"], g["ws"],
-                       g["R"], g["lab_p"], g["lab_s"], g["n_box"], "tree", 0.0, 1000, True, (c0, c1))
+                       g["R"], g["lab_p"], g["lab_s"], g["n_box"], "tree", 0.0, g["sub_chunk"], True, (c0, c1),
+                       pos_tree=g["tree"])
+
+
+def _init_spawned(state):
+    """Pool initializer of a spawned worker: the inputs, and its own copy of
+    the position tree (a spawned process shares nothing with the parent)."""
+    _G.update(state)
+    _G["tree"] = position_tree(state["kind"], state["b"], state["los"], state["pos"])
 
 
 def count_pairs_parallel(kind, b, los, pos, w, spos, axis, e, ws, R, lab_p, lab_s, n_box, shape_range,
-                         processes=None, chunk=1000):
-    """Pool over chunks of ``chunk`` shapes, summing the partial histograms in
-    the parent.  Uses a fork pool started before any GPU work, or a
-    single-process loop when ``processes == 1``."""
+                         processes=None, chunk=1000, sub_chunk=4, context="fork"):
+    """The reference's multiprocessing driver (measure_w_box_jk.py:764-780,
+    measure_m_box_jk.py:804-820): the position tree is built once, in the
+    parent, then a fork Pool maps chunks of ``chunk`` shapes (the reference's
+    ``chunk_size``) over ``processes`` workers that query that tree, and the
+    parent sums the partial histograms.  Inside a chunk, ``sub_chunk`` shapes
+    at a time hold their candidate pairs in memory (the reference loops shape
+    by shape).  A fork Pool must start before any GPU work; ``context =
+    'spawn'`` (for callers that already use the GPU) starts fresh workers that
+    each build the tree once; ``processes == 1`` runs in this process.
+    Returns (Counts, seconds the parent spent building the tree)."""
     import multiprocessing as mp
+    import time
     processes = processes or os.cpu_count()
-    _G.update(kind=kind, b=b, los=los, pos=pos, w=w, spos=spos, axis=axis, e=e, ws=ws, R=R,
-              lab_p=lab_p, lab_s=lab_s, n_box=n_box)
+    state = dict(kind=kind, b=b, los=los, pos=pos, w=w, spos=spos, axis=axis, e=e, ws=ws, R=R,
+                 lab_p=lab_p, lab_s=lab_s, n_box=n_box, sub_chunk=sub_chunk)
     lo, hi = shape_range
     jobs = [(c, min(hi, c + chunk)) for c in range(lo, hi, chunk)]
-    if processes == 1:
-        parts = [_worker(j) for j in jobs]
-    else:
-        ctx = mp.get_context("fork")
-        with ctx.Pool(processes) as pool:
-            parts = pool.map(_worker, jobs)
+    t_tree = 0.0
+    try:
+        if context == "spawn" and processes > 1:
+            ctx = mp.get_context("spawn")
+            with ctx.Pool(processes, initializer=_init_spawned, initargs=(state,)) as pool:
+                parts = pool.map(_worker, jobs)
+        else:
+            t0 = time.perf_counter()
+            tree = position_tree(kind, b, los, pos)
+            t_tree = time.perf_counter() - t0
+            _G.update(state, tree=tree)
+            if processes == 1:
+                parts = [_worker(j) for j in jobs]
+            else:
+                with mp.get_context("fork").Pool(processes) as pool:
+                    parts = pool.map(_worker, jobs)
+    finally:
+        _G.clear()
     tot = parts[0]
     for p in parts[1:]:
         tot.DD += p.DD; tot.SplusD += p.SplusD; tot.ScrossD += p.ScrossD; tot.npairs += p.npairs
         if n_box:
             tot.DD_jk += p.DD_jk; tot.SplusD_jk += p.SplusD_jk; tot.npairs_jk += p.npairs_jk
-    return tot
+    return tot, t_tree

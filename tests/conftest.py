@@ -25,3 +25,15 @@ def pytest_collection_modifyitems(config, items):
     for item in items:
         if "gpu" in item.keywords:
             item.add_marker(skip)
+
+
+def pytest_terminal_summary(terminalreporter):
+    """How many fixture cases had their floats checked against the oracle on
+    this host instead of the fixture (whose bins follow the build host's
+    numpy log10)."""
+    mod = sys.modules.get("test_gpu_parity")
+    if mod is None or not getattr(mod, "CHECKED", None):
+        return
+    fb = mod.FALLBACKS
+    terminalreporter.write_line(f"parity: {len(fb)} of {len(mod.CHECKED)} fixture case(s) compared against the "
+                                f"host oracle (fixture bins differ on this host){': ' + ', '.join(fb) if fb else ''}")

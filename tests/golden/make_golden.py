@@ -5,7 +5,7 @@ GPU host and never from the test suite.  Two kinds of fixture:
 
 1. ``ref_<case>.npz`` -- the reference's own ``MeasureIABox.measure_xi_w`` /
    ``measure_xi_multipoles`` run on small seeded catalogues.  The reference
-   is imported from ``/root/reference/src`` with stand-ins for modules that
+   is imported from ``$MIA_REFERENCE_ROOT/src`` with stand-ins for modules that
    are absent here and unused by the box path (kmeans_radec, astropy,
    pathos, pyccl), an in-memory replacement for h5py, and ``lpmn`` mapped to
    ``scipy.special.assoc_legendre_p`` (scipy 1.18 removed ``lpmn``).  Each
@@ -30,7 +30,7 @@ GPU host and never from the test suite.  Two kinds of fixture:
    replay them exactly.  pathos's pool is replaced by a serial map (the
    pooled realisation driver runs unchanged, one patch after another).
 
-Usage:  python tests/golden/make_golden.py
+Usage:  MIA_REFERENCE_ROOT=<reference checkout> python tests/golden/make_golden.py
 """
 
 from __future__ import annotations
@@ -43,7 +43,8 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = "/root/reference"
+# the reference's source tree (MarloesvL/measure_IA), e.g. a clone of it
+REF = os.environ.get("MIA_REFERENCE_ROOT", "")
 sys.path.insert(0, os.path.join(HERE, "..", ".."))
 
 
@@ -477,6 +478,8 @@ def extract_reference_golden_files():
 
 
 if __name__ == "__main__":
+    if not REF or not os.path.isdir(os.path.join(REF, "src", "measureia")):
+        sys.exit("set MIA_REFERENCE_ROOT to a checkout of the reference (with src/measureia)")
     sys.path.insert(0, HERE)
     install_shims()
     import io, contextlib

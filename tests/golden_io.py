@@ -9,6 +9,17 @@ import numpy as np
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
+def reference_file(rel):
+    """A file of the reference's source tree, found under the directory that
+    ``MIA_REFERENCE_ROOT`` names; None when the variable is unset or the file
+    is absent (tests that need it skip)."""
+    root = os.environ.get("MIA_REFERENCE_ROOT")
+    if not root:
+        return None
+    p = os.path.join(root, rel)
+    return p if os.path.exists(p) else None
+
+
 def case_names():
     return sorted(os.path.basename(p)[4:-4] for p in glob.glob(os.path.join(GOLDEN, "ref_*.npz")))
 

@@ -59,6 +59,13 @@ def oracle_counts(meta, inputs, call):
     return res
 
 
+# cases whose floats were compared with the oracle on this host because the
+# x86-made fixture's counts differ from the host oracle's (numpy's log10 is
+# host dependent); reported at the end of the session
+FALLBACKS = []
+CHECKED = []
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("name", case_names())
 def test_cases_match_reference(name, precision, tmp_path):
@@ -66,11 +73,15 @@ def test_cases_match_reference(name, precision, tmp_path):
     produced, meas = run_product(meta, inputs, precision, str(tmp_path / f"{name}_{precision}.hdf5"))
     assert set(produced) == set(outs), sorted(set(produced) ^ set(outs))[:10]
     rtol = FP64_RTOL if precision == "fp64" else MIXED_RTOL
+    CHECKED.append(f"{name}/{precision}")
     # integer counts: bit-exact against the oracle run on this host (same log10 as the bin tables),
     # and against the reference's unit-weight DD wherever the host oracle agrees with it
     host_agrees = True
+    host_outs = {}
     for call, m in meas:
-        c = oracle_counts(meta, inputs, call)["__counts__"]
+        res = oracle_counts(meta, inputs, call)
+        c = res.pop("__counts__")
+        host_outs.update(res)
         np.testing.assert_array_equal(m.npairs[0], c.npairs, err_msg=f"{call}")
         for i in range(call["num_jk"]):
             np.testing.assert_array_equal(m.npairs[0] - m.npairs[1 + i], c.npairs - c.npairs_jk[i])
@@ -80,10 +91,16 @@ def test_cases_match_reference(name, precision, tmp_path):
         host_agrees &= np.array_equal(c.npairs, ref_tot)
         if host_agrees:
             np.testing.assert_array_equal(m.npairs[0], ref_tot)
-    for path, ref in outs.items():
-        got = produced[path]
-        if host_agrees:
-            assert_close(got, ref, rtol, path)
+    if host_agrees:
+        for path, ref in outs.items():
+            assert_close(produced[path], ref, rtol, path)
+    else:
+        # the fixture's bin assignment is not this host's: every float dataset
+        # against the oracle run here on the same inputs instead
+        FALLBACKS.append(f"{name}/{precision}")
+        assert set(host_outs) == set(outs), sorted(set(host_outs) ^ set(outs))[:10]
+        for path, ref in host_outs.items():
+            assert_close(produced[path], ref, rtol, path)
 
 
 def test_config0_against_oracle():

@@ -102,3 +102,54 @@ def test_mixed_form_is_bitwise_reproducible():
     np.testing.assert_array_equal(a.npairs, b.npairs)
     for k in a.arrays:
         np.testing.assert_array_equal(a[k], b[k], err_msg=k)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("where,value", [("Position", 205.0), ("Position", -1e-9), ("Position", float("nan")),
+                                         ("Position_shape_sample", float("nan")),
+                                         ("Position_shape_sample", 205.0 + 1e-12)])
+def test_coordinates_outside_the_box_raise(where, value, precision, tmp_path):
+    """A coordinate at exactly L, a negative one or a NaN (positions or shape
+    positions) is refused on the device: the preparation kernels flag it,
+    the pair kernel skips the catalogue, and MeasureIABox raises ValueError
+    with the first offending index (the reference's periodic KD-tree,
+    ``KDTree(..., boxsize=L)`` at measure_w_box_jk.py:764, raises ValueError
+    for such data).  The library stays usable: the next measurement of a valid
+    catalogue equals one made before the error."""
+    from measure_ia_gb300 import MeasureIABox
+    from measure_ia_gb300.catalogs import neyman_scott_catalog
+    data = neyman_scott_catalog(200, 205.0, 3000, 21, mean_children=30, sigma=1.0)
+    kw = dict(separation_limits=[0.1, 20.0], num_bins_r=10, num_bins_pi=8, pi_max=20.0, boxsize=205.0,
+              precision=precision)
+    good = MeasureIABox({k: np.array(v) if k != "LOS" else v for k, v in data.items()}, None, **kw)
+    good.measure_xi_w("ok", "both", 27, temp_file_path=str(tmp_path))
+    before = good.last_measurement
+    bad = {k: np.array(v) if k != "LOS" else v for k, v in data.items()}
+    idx = 137
+    bad[where][idx, 1] = value
+    box = MeasureIABox(bad, None, **kw)
+    with pytest.raises(ValueError, match=rf"outside \[0, boxsize\) or not finite.*first offending index {idx}"):
+        box.measure_xi_w("bad", "both", 27, temp_file_path=str(tmp_path))
+    again = MeasureIABox({k: np.array(v) if k != "LOS" else v for k, v in data.items()}, None, **kw)
+    again.measure_xi_w("ok", "both", 27, temp_file_path=str(tmp_path))
+    after = again.last_measurement
+    np.testing.assert_array_equal(after.npairs, before.npairs)
+    for key in ("proj_gp", "proj_gg", "cov_gp", "DD_all", "Splus_all"):
+        np.testing.assert_array_equal(after[key], before[key])
+
+
+def test_batch_reports_the_catalogue_with_bad_coordinates():
+    """In a batch, the catalogue whose positions leave the box is named in the
+    error, and the other catalogues' products are those of single runs."""
+    from measure_ia_gb300.catalogs import neyman_scott_catalog
+    from measure_ia_gb300.engine import BatchCounter
+    pc = _counter("mixed")
+    cats = [neyman_scott_catalog(150, 205.0, 2000, 30 + i, mean_children=30, sigma=1.0) for i in range(3)]
+    cats[1]["Position"][5, 0] = float("nan")
+    dcats = [pc.to_device(c) for c in cats]
+    batch = BatchCounter(pc, dcats)
+    batch.prepare()
+    with pytest.raises(ValueError, match=r"catalogue 1, first offending index 5"):
+        batch.run()
+    for i in (0, 2):
+        np.testing.assert_array_equal(batch.fetch(i).npairs, pc.measure(cats[i]).npairs)

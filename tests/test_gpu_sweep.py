@@ -77,7 +77,7 @@ def draw_case(i):
         pi_max = float(min(L / 2.0, r_max * rng.uniform(0.3, 2.0)))
     case = dict(L=L, kind=kind, r_min=r_min, r_max=r_max, pi_max=pi_max,
                 n_r=int(rng.integers(1, 16)), n_p=int(rng.integers(1, 13)),
-                num_jk=int(rng.choice([0, 8, 27, 64])), los=int(rng.integers(0, 3)),
+                num_jk=int(rng.choice([0, 8, 27, 64, 125])), los=int(rng.integers(0, 3)),
                 corr_type=str(rng.choice(["both", "g+", "gg"])),
                 ellipticity=str(rng.choice(["distortion", "ellipticity"])),
                 layout=str(rng.choice(["tree", "multiprocessing", "brute"])))
@@ -254,3 +254,37 @@ def test_nan_axis_directions(precision, tmp_path):
     store = open_output(out)
     for path, v in ref.items():
         _close(store.read(path), v, FP64_RTOL, path)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("kind", ["w", "m"])
+def test_large_box_geometry_jk125(kind, precision, tmp_path):
+    """The large-box configuration's geometry scaled down: a 1000 Mpc/h box,
+    15 log r bins 0.1-60, 20 Pi bins over |Pi| <= 60 (or 20 mu_r bins), 125
+    jackknife regions (5 x 5 x 5 sub-boxes, measure_IA_base.py:404-452, and
+    the RR_jk loop of measure_w_box_jk.py:798-807), on a clustered catalogue
+    of ~24,000 positions and 6,000 shapes.  At 125 regions a work unit's
+    neighbourhood spans more regions than at 27.  Every dataset against the
+    oracle: counts per (bin, region) bit-exact, values as in the sweep."""
+    from measure_ia_gb300 import MeasureIABox, open_output
+    from measure_ia_gb300.catalogs import neyman_scott_catalog
+    L = 1000.0
+    data = neyman_scott_catalog(600, L, 6000, 125, mean_children=40, sigma=1.5)
+    r_min, r_max, n_r, n_p, pi_max = 0.1, 60.0, 15, 20, 60.0
+    b = O.Binning(boxsize=L, r_min=r_min, r_max=r_max, num_bins_r=n_r, num_bins_pi=n_p, pi_max=pi_max)
+    ref = dict(O.measure(kind, b, _copy(data), "big", "both", 125, None, "distortion", "multiprocessing"))
+    c = ref.pop("__counts__")
+    out = str(tmp_path / "big.hdf5")
+    box = MeasureIABox(_copy(data), out, None, None, [r_min, r_max], n_r, n_p, pi_max, boxsize=L, num_nodes=4,
+                       precision=precision)
+    fn = box.measure_xi_w if kind == "w" else box.measure_xi_multipoles
+    fn("big", "both", 125, temp_file_path=str(tmp_path))
+    m = box.last_measurement
+    assert c.npairs.sum() > 10000
+    np.testing.assert_array_equal(m.npairs[0], c.npairs)
+    np.testing.assert_array_equal(m.npairs[1:], c.npairs_jk)
+    store = open_output(out)
+    assert set(store.keys()) == set(ref)
+    rtol = FP64_RTOL if precision == "fp64" else MIXED_RTOL
+    for path, v in ref.items():
+        _close(store.read(path), v, rtol, path)

@@ -18,6 +18,7 @@ import pytest
 
 from measure_ia_gb300 import hdf5
 from measure_ia_gb300.output import OutputFile
+from golden_io import reference_file
 
 sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
 import h5read  # noqa: E402
@@ -28,7 +29,7 @@ H5PY_1D = [(0x1, 0, "01010100000000000a000000000000000a00000000000000"),
            (0x3, 1, "11203f000800000000004000340b0034ff03000000000000"),
            (0x5, 1, "0202020100000000")]
 H5PY_2D_SPACE = "01020100000000000a000000000000000a000000000000000a000000000000000a00000000000000"
-GOLDEN_H5 = "/root/reference/tests/data/processed/TNG300/mock_IA_TNG300.hdf5"
+GOLDEN_H5 = reference_file("tests/data/processed/TNG300/mock_IA_TNG300.hdf5")
 
 
 def _sample(rng):
@@ -132,7 +133,7 @@ def test_writer_rejects_what_it_cannot_store(tmp_path):
     assert not os.path.exists(str(tmp_path / "b.hdf5"))
 
 
-@pytest.mark.skipif(not os.path.exists(GOLDEN_H5), reason="the reference's golden file is not on this host")
+@pytest.mark.skipif(GOLDEN_H5 is None, reason="MIA_REFERENCE_ROOT unset or without the golden file")
 def test_reader_on_h5py_files():
     x, y = hdf5.read_file(GOLDEN_H5), h5read.read_all(GOLDEN_H5)
     assert set(x) == set(y) and len(x) > 700

@@ -11,9 +11,10 @@ import pytest
 
 from measure_ia_gb300 import hdf5
 from measure_ia_gb300.read_data import ReadData
+from golden_io import reference_file
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-GOLDEN_H5 = "/root/reference/tests/data/processed/TNG300/mock_IA_TNG300.hdf5"
+GOLDEN_H5 = reference_file("tests/data/processed/TNG300/mock_IA_TNG300.hdf5")
 
 
 def _multi(tmp_path, stem, group, per_file, chunked=(1,), missing=()):
@@ -111,7 +112,7 @@ def test_read_measureia_output(tmp_path):
         ReadData("TNG300", "mock", 50, data_path=str(tmp_path)).read_MeasureIA_output("All", 8)
 
 
-@pytest.mark.skipif(not os.path.exists(GOLDEN_H5), reason="the reference's golden file is not on this host")
+@pytest.mark.skipif(GOLDEN_H5 is None, reason="MIA_REFERENCE_ROOT unset or without the golden file")
 def test_read_measureia_output_h5py_file():
     out = _golden_outputs()
     rd = ReadData("TNG300", "mock_IA_TNG300", 99, data_path=os.path.dirname(GOLDEN_H5))
