@@ -29,7 +29,7 @@ import os
 
 KNOBS = ("cell_size", "cell_refine", "shapes_per_unit", "cell_size_los", "cell_refine_los")
 DEFAULT = {"cell_size": 0.0, "cell_refine": 0, "shapes_per_unit": 0, "cell_size_los": 0.0, "cell_refine_los": 0}
-_VERSION = "g4"  # geometry search with separate line-of-sight cells
+_VERSION = "g5"  # per-region work units (the best geometry moved)
 
 
 def cache_path():

@@ -654,6 +654,8 @@ void make_params(const mia_config* cfg, const Plan& plan, const Tables& T, int l
     double ev = cfg->kind == MIA_KIND_W ? vmax * u : vmax * 6e-7;
     double et = (ev + fabs(p0) * u * 0.5 + (vmax + fabs(p0)) * u * 0.5) * inv + cfg->n_p * u;
     P.p_guard = (float)fmin(0.25, fmax(4.0 * et, 1.0 / 1048576.0));
+    P.p_half_in = 0.5f - P.p_guard;
+    P.p_off32 = (float)(-p0 * inv);
   }
   P.c_guard = 1e-12f;
   P.wrap_guard = (float)(cfg->boxsize * 1e-5);
@@ -663,6 +665,9 @@ void make_params(const mia_config* cfg, const Plan& plan, const Tables& T, int l
   P.range_los32 = f32_down(plan.range_los);
   const int nq = cfg->n_qbreak;
   P.q_cut = (nq > 0 && cfg->q_bin[nq] < 0) ? T.q_hi32[nq - 1] : INFINITY;
+  // each coordinate rounded to FP32 (2^-24 L), their difference and L - |d|
+  // (2^-24 L each): 2^-22 L in all, taken four times over
+  P.pre_margin = (float)(cfg->boxsize * (1.0 / 1048576.0));
   P.edge_capacity = plan.edge_capacity;
 }
 
@@ -841,8 +846,6 @@ int mia_batch_status(mia_context* ctx, int n, void* workspace, void* stream) {
              hh.first_bad, (unsigned long long)hh.bad_index);
     return fail(ctx, MIA_ERR_RANGE, buf);
   }
-  if (hh.flags & kStatusStall)
-    return fail(ctx, MIA_ERR_CUDA, "a bounded device wait ran out (an asynchronous copy did not complete)");
   if (hh.flags & kStatusOverflow)
     return fail(ctx, MIA_ERR_OVERFLOW, "edge re-test queue overflow; rerun in the FP64 form");
   ctx->err.clear();

@@ -23,7 +23,6 @@ constexpr int kScanTile = 2048;
 constexpr unsigned kStatusRange = 1u;      // input coordinate outside [0, L) or NaN
 constexpr unsigned kStatusOverflow = 2u;   // edge queue overflow
 constexpr unsigned kStatusNoSlot = 4u;     // (informational) global-atomic fallback used
-constexpr unsigned kStatusStall = 8u;      // a bounded device wait ran out (a copy that never completed)
 
 // --------------------------------------------------------------------------
 // Device-visible status block (first bytes of the workspace)
@@ -274,13 +273,16 @@ struct Params {
   // mixed-form guards and tables
   int lut32_base;               // bucket of the first lut32 entry
   float p_lo32, p_inv32;        // Pi/mu: t = (v - p_lo) * p_inv, bin = floor(t)
+  float p_off32;                // -p_lo * p_inv: t = fma(v, p_inv, p_off)
   float p_guard;                // fraction of a bin treated as ambiguous at each edge
+  float p_half_in;              // 0.5 - p_guard: |frac(t) - 0.5| above it is an edge
   float c_guard;                // sin^2(phi) below which the exact FP64 cos(phi) decides
   float wrap_guard;
   float los_cut;                // |Pi| above this is surely outside the Pi bins (w)
   float zwin;                   // half-width of the line-of-sight window over the LOS-sorted shapes
   float range_los32;            // range_los in FP32: zwin - range_los32 is the window's slack
   float q_cut;                  // q above this is surely beyond the last binned separation
+  float pre_margin;             // FP64 form: bound on the FP32 error of a separation from single floats
   long long edge_capacity;
 };
 
@@ -378,7 +380,8 @@ struct PairResult {
 
 // Shape s, position p: coordinates in cell-dimension order (d0, d1 projected,
 // d2 line of sight).  `perm_r2` selects the original-axis order of the 3-D sum.
-__device__ __forceinline__ PairResult pair_exact(const Params& P, const Tables& T, double sx, double sy,
+template <class Tab>  // Tables in global memory, or the kernel's shared-memory copy of its keys and bins
+__device__ __forceinline__ PairResult pair_exact(const Params& P, const Tab& T, double sx, double sy,
                                                  double sz, double ax, double ay, double e, double qx, double qy,
                                                  double qz) {
   PairResult res;

@@ -33,15 +33,11 @@
 
 #include "mia_internal.cuh"
 
-// 1: the mixed form's pair loop runs in two phases (range test, then binning of
-// the survivors with full warps); 0: every lane bins its own pair
-#ifndef MIA_COMPACT
-#define MIA_COMPACT 0
-#endif
-// 1: the mixed form stages a unit's shapes with 1-D TMA bulk copies
-// (cp.async.bulk) into shared memory; 0: with plain loads
-#ifndef MIA_TMA_SHAPES
-#define MIA_TMA_SHAPES 0
+// 1: the mixed form stages a unit's shapes by projected quadrant of their cell
+// (2 x 2), each quadrant in line-of-sight order, and a position meets only the
+// quadrants within reach; 0: one line-of-sight order for the whole cell
+#ifndef MIA_QUADS
+#define MIA_QUADS 0
 #endif
 
 namespace mia {
@@ -56,8 +52,8 @@ struct SmemLayout {
   size_t tables, shapes, seg_begin, seg_pref, seg_shift, wpos, ring, hist, total;
 };
 
-// Mixed form, per warp: the lanes' current positions (two float4 each) and a
-// ring of kRing candidate pairs (shape << 5 | lane) that passed the range test.
+// FP64 form, per warp: a ring of kRing candidate pairs (shape << 5 | lane)
+// that passed the range test.
 constexpr int kRing = 64;
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
@@ -89,17 +85,19 @@ __host__ __device__ inline SmemLayout smem_layout(int spu, int hw, int knb, int 
   L.tables = o;
   o = align16(o + sizeof(TablesSmem));
   L.shapes = o;
-  o = align16(o + (size_t)spu * (mixed ? 48 : 60));
+  o = align16(o + (size_t)spu * (mixed ? 48 : 68));
   L.seg_begin = o;
   o = align16(o + sizeof(int) * kSegsPerPass);
   L.seg_pref = o;
   o = align16(o + sizeof(int) * (kSegsPerPass + 1));
   L.seg_shift = o;
   o = align16(o + sizeof(unsigned char) * kSegsPerPass);
+  // FP64 form, two-phase loop: the lanes' positions (two double2 and a label
+  // each) and the survivor rings
   L.wpos = o;
-  o = align16(o + (mixed ? sizeof(float4) * 2 * kThreads : 0));
+  o = align16(o + (mixed ? 0 : sizeof(double2) * 2 * kThreads + sizeof(int) * kThreads));
   L.ring = o;
-  o = align16(o + (mixed ? sizeof(unsigned short) * kRing * (kThreads / 32) : 0));
+  o = align16(o + (mixed ? 0 : sizeof(unsigned short) * kRing * (kThreads / 32)));
   L.hist = o;
   o = align16(o + sizeof(unsigned) * hist_u32_words(hw, knb, mixed, var) + 16);
   L.total = o;
@@ -259,7 +257,9 @@ __device__ __forceinline__ void z_window(const float* Z, int S, float z, float w
 // Everything one (shape i, position p) pair contributes in the mixed form:
 // FP32 separations, guarded bin decisions, e+/ex, fixed-point accumulation; a
 // pair near any decision edge is queued for the FP64 re-test instead.
-template <int KIND, int FULL, int VAR>
+// SLOTS: 1 when every position of the warp belongs to the unit's region (no
+// per-pair check of the position's slot), 0 otherwise.
+template <int KIND, int FULL, int VAR, int SLOTS>
 __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T, const float4& a, const float4& b,
                                            const float2* C, const int* I, int i, const MixedPos& p,
                                            const HistView& h, const Work& w, const Out& o,
@@ -325,18 +325,19 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
       }
       v = dz * rsqrtf(q);
     }
-    const float t2 = (v - P.p_lo32) * P.p_inv32;
+    // t = (v - p_lo) n / (p_hi - p_lo) as one FMA; its fraction within 4x
+    // its error bound of 0 or 1 is an edge
+    const float t2 = fmaf(v, P.p_inv32, P.p_off32);
     const float fl = floorf(t2);
-    const float fr = t2 - fl;
     jb = (int)fl;
-    if (fr < P.p_guard || fr > 1.0f - P.p_guard) edge = true;
-    if (jb < 0 || jb >= P.n_p) jb = -1;
+    if (fabsf((t2 - fl) - 0.5f) > P.p_half_in) edge = true;
   }
-  if (!edge && jb < 0) return;
+  if (!edge && (unsigned)jb >= (unsigned)P.n_p) return;
   const float2 cxy = C[i];
   const float dot = fmaf(dx, cxy.x, dy * cxy.y);
   const float crs = fmaf(dx, cxy.y, -dy * cxy.x);
-  if (crs * crs < P.c_guard * qp) edge = true;
+  const float crs2 = crs * crs;
+  if (crs2 < P.c_guard * qp) edge = true;
   if (edge) {
     const unsigned long long k = atomicAdd(&w.status->edge_count, 1ULL);
     if (k < (unsigned long long)w.edge_capacity) w.edges[k] = make_int2(I[i], p.idx);
@@ -344,13 +345,12 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
     return;
   }
   const int bin = ib * P.n_p + jb;
-  const float inv = __fdividef(1.0f, qp);
-  const float cos2 = (dot * dot - crs * crs) * inv;
-  const float sin2 = 2.0f * dot * fabsf(crs) * inv;
-  const float ww = p.w * a.w;   // scaled by sc_dd
-  const float we = p.w * b.w;   // scaled by sc_sp
-  const float tp = we * cos2, tx = we * sin2;
-  if (p.slot >= 0) {  // (binned pairs in the shared histograms are counted at the flush)
+  // e+ w = w e cos 2phi = w e (dot^2 - crs^2) / r_p^2, ex w = w e 2 dot |crs| / r_p^2
+  const float ww = p.w * a.w;                  // scaled by sc_dd
+  const float s = __fdividef(p.w * b.w, qp);   // w_p w_s e / r_p^2, scaled by sc_sp
+  const float tp = fmaf(dot, dot, -crs2) * s;
+  const float tx = (dot * fabsf(crs)) * (s + s);
+  if (SLOTS || p.slot >= 0) {  // (binned pairs in the shared histograms are counted at the flush)
     const int k = p.base + bin;
     const int vd = __float2int_rn(ww);
     const int vp = __float2int_rn(tp);
@@ -382,63 +382,42 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
   }
 }
 
-// The range test of mixed_pair alone: false when the pair is surely beyond
-// the binned line-of-sight range (w) or the last binned separation.  The
-// survivors are exactly the pairs that mixed_pair does not drop before its
-// bin lookups.
-template <int KIND, int FULL>
-__device__ __forceinline__ bool in_range(const Params& P, const float4& a, const float4& b, const MixedPos& p) {
-  float dz = (a.z - p.zh) + (b.z - p.zl);
-  if (FULL && KIND == MIA_KIND_W && P.full[2]) {
-    if (dz > P.halfLf) dz -= P.Lf_hi;
-    else if (dz < -P.halfLf) dz += P.Lf_hi;
+// FP64 form, the two-phase loop's range test from single-float coordinates:
+// the minimum-image gap per axis less `m` (a bound on the FP32 error), so that
+// a pair it drops is beyond the binned range in the exact arithmetic too.
+__device__ __forceinline__ float fp32_gap(float d, float L, float m) {
+  const float a = fabsf(d);
+  return fmaxf(fminf(a, L - a) - m, 0.0f);
+}
+
+template <int KIND>
+__device__ __forceinline__ bool in_range_fp64(const Params& P, float sx, float sy, float sz, float px, float py,
+                                              float pz) {
+  const float m = P.pre_margin, L = P.Lf_hi;
+  const float gx = fp32_gap(sx - px, L, m), gy = fp32_gap(sy - py, L, m), gz = fp32_gap(sz - pz, L, m);
+  if (KIND == MIA_KIND_W) return !(gz > P.los_cut) && !(fmaf(gx, gx, gy * gy) > P.q_cut);
+  return !(fmaf(gz, gz, fmaf(gx, gx, gy * gy)) > P.q_cut);
+}
+
+// One position against the staged shapes [wlo, whi): the next shape is in
+// flight while this pair is processed (index whi at most: still inside the
+// staging area); two register sets take turns, so the prefetched shape is
+// never copied.
+template <int KIND, int FULL, int VAR, int SLOTS>
+__device__ __forceinline__ void shape_loop(const Params& P, const TablesSmem& T, const float4* A, const float4* B,
+                                           const float2* C, const int* I, int wlo, int whi, const MixedPos& p0,
+                                           const HistView& hv, const Work& w, const Out& o, const Scales& sc,
+                                           double twoR, int label_a, unsigned long long& my_binned) {
+  float4 a0 = A[wlo], b0 = B[wlo];
+  for (int i = wlo;;) {
+    const float4 a1 = A[i + 1], b1 = B[i + 1];
+    mixed_pair<KIND, FULL, VAR, SLOTS>(P, T, a0, b0, C, I, i, p0, hv, w, o, sc, twoR, label_a, my_binned);
+    if (++i >= whi) break;
+    a0 = A[i + 1];
+    b0 = B[i + 1];
+    mixed_pair<KIND, FULL, VAR, SLOTS>(P, T, a1, b1, C, I, i, p0, hv, w, o, sc, twoR, label_a, my_binned);
+    if (++i >= whi) break;
   }
-  if (KIND == MIA_KIND_W && fabsf(dz) > P.los_cut) return false;
-  const float dx = (a.x - p.xh) + (b.x - p.xl);
-  const float dy = (a.y - p.yh) + (b.y - p.yl);
-  const float qp = fmaf(dx, dx, dy * dy);
-  const float q = KIND == MIA_KIND_W ? qp : fmaf(dz, dz, qp);
-  return !(q > P.q_cut);
-}
-
-// ---- TMA bulk copies (1-D) with an mbarrier ------------------------------------
-
-__device__ __forceinline__ unsigned smem_addr(const void* p) {
-  return (unsigned)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
-  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_expect(unsigned long long* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
-               : "memory");
-}
-
-// global -> shared, `bytes` (a multiple of 16, both addresses 16-byte aligned),
-// completion counted on the mbarrier
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_addr(dst)),
-      "l"(src), "r"(bytes), "r"(smem_addr(bar))
-      : "memory");
-}
-
-// Wait for the mbarrier phase of parity `parity` with a bounded number of
-// polls; false when the limit was reached.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int limit) {
-  for (int k = 0; k < limit; ++k) {
-    unsigned done;
-    asm volatile(
-        "{ .reg .pred p; mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2; selp.u32 %0, 1, 0, p; }"
-        : "=r"(done)
-        : "r"(smem_addr(bar)), "r"(parity)
-        : "memory");
-    if (done) return true;
-  }
-  return false;
 }
 
 // ---- the persistent pair kernel ----------------------------------------------
@@ -462,7 +441,12 @@ __device__ __forceinline__ int subbox_set(int lo, int hi, int nf, int cps, int n
 }
 
 template <int MIXED, int VAR, int KIND, int FULL>
-__global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __restrict__ ds, int n_ds,
+#ifdef MIA_MINB  // (launch-bound experiments: blocks per SM the registers must allow)
+__global__ void __launch_bounds__(kThreads, MIA_MINB) k_pairs(
+#else
+__global__ void __launch_bounds__(kThreads) k_pairs(
+#endif
+    Params P, const Dataset* __restrict__ ds, int n_ds,
                                                      const unsigned long long* __restrict__ wu_prefix,
                                                      unsigned long long* wu_next, int HW) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -490,11 +474,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
   __shared__ int s_scan[32];
   __shared__ int s_total;
   __shared__ float s_box[4];  // the unit's shape cell in d0, d1, widened (see the window below)
-#if MIA_TMA_SHAPES
-  __shared__ __align__(8) unsigned long long s_bar;  // completion of a unit's shape copies
-  unsigned bar_phase = 0;
-  if (MIXED && tid == 0) mbar_init(&s_bar, 1);
-#endif
+  __shared__ int s_qn[5];     // shapes per projected quadrant of the cell, then their starts (MIA_QUADS)
 
   // tables -> shared (the same binning for every dataset of a batch)
   {
@@ -671,58 +651,51 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
       float2 rc = make_float2(0.f, 0.f);
       float z = 0.f;
       const int g = u.begin + tid;
-#if MIA_TMA_SHAPES
-      // the ten FP32 shape arrays' slices [b4, b4 + n4) (16-byte aligned: the
-      // arrays' stride is a multiple of 4 floats) -> the per-warp position
-      // area, free until the pair loop
-      const int b4 = u.begin & ~3, n4 = ((u.begin + S + 3) & ~3) - b4, rs = (n4 + 3) & ~3;
-      float* raw = reinterpret_cast<float*>(wpos);
-      if (10 * rs <= 2 * kThreads * 4) {
-        // every thread's earlier accesses to the area (generic proxy) before
-        // the copies (async proxy) write it
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        __syncthreads();
-        if (tid == 0) {
-          mbar_expect(&s_bar, 10u * 4u * (unsigned)n4);
-          const float* src[10] = {w.sxh, w.syh, w.szh, w.swsf, w.sxl, w.syl, w.szl, w.swef, w.saxf, w.sayf};
-          for (int k = 0; k < 10; ++k) bulk_g2s(raw + k * rs, src[k] + b4, 4u * (unsigned)n4, &s_bar);
-        }
-        const bool ok = mbar_wait(&s_bar, bar_phase, 1 << 22);
-        bar_phase ^= 1u;
-        if (__syncthreads_or(!ok)) {  // a copy that never landed: flag it, give it time, stop
-          if (tid == 0) atomicOr(&w.status->flags, kStatusStall);
-          mbar_wait(&s_bar, bar_phase ^ 1u, 1 << 22);
-          return;
-        }
-        if (tid < S) {
-          const int j = tid + (u.begin - b4);
-          ra = make_float4(raw[j], raw[rs + j], raw[2 * rs + j], raw[3 * rs + j] * sc.sc_dd);
-          rb = make_float4(raw[4 * rs + j], raw[5 * rs + j], raw[6 * rs + j], raw[7 * rs + j] * sc.sc_sp);
-          rc = make_float2(raw[8 * rs + j], raw[9 * rs + j]);
-        }
-      } else if (tid < S) {
-        ra = make_float4(w.sxh[g], w.syh[g], w.szh[g], w.swsf[g] * sc.sc_dd);
-        rb = make_float4(w.sxl[g], w.syl[g], w.szl[g], w.swef[g] * sc.sc_sp);
-        rc = make_float2(w.saxf[g], w.sayf[g]);
-      }
-      if (tid < S) {
-#else
       if (tid < S) {
         // weights times the (power-of-two) fixed-point scales: exact
         ra = make_float4(w.sxh[g], w.syh[g], w.szh[g], w.swsf[g] * sc.sc_dd);
         rb = make_float4(w.sxl[g], w.syl[g], w.szl[g], w.swef[g] * sc.sc_sp);
         rc = make_float2(w.saxf[g], w.sayf[g]);
-#endif
         z = ra.z + rb.z;
         if (!(z == z)) z = INFINITY;  // the ranks below must form a permutation
         zs[tid] = z;
       }
+#if MIA_QUADS
+      // quadrant of the shape in the cell's projected box (split at the box's
+      // middle, FP32; the quadrant boxes below are widened by the box margin)
+      int* qs = seg_pref;  // free until the segments are built
+      int qd = 0;
+      if (tid < 4) s_qn[tid] = 0;
       __syncthreads();
+      if (tid < S) {
+        const float mx = 0.5f * (s_box[0] + s_box[1]), my = 0.5f * (s_box[2] + s_box[3]);
+        qd = ((ra.x + rb.x) > mx ? 1 : 0) + ((ra.y + rb.y) > my ? 2 : 0);
+        qs[tid] = qd;
+        atomicAdd(&s_qn[qd], 1);
+      }
+      __syncthreads();
+      if (tid == 0) {  // counts -> starts (s_qn[4] = S)
+        int acc = 0;
+        for (int k = 0; k < 4; ++k) {
+          const int c = s_qn[k];
+          s_qn[k] = acc;
+          acc += c;
+        }
+        s_qn[4] = acc;
+      }
+#else
+      __syncthreads();
+#endif
       if (tid < S) {
         int rank = 0;
         for (int j = 0; j < S; ++j) {
           const float zj = zs[j];
+#if MIA_QUADS
+          const int qj = qs[j];
+          rank += (qj < qd || (qj == qd && (zj < z || (zj == z && j < tid)))) ? 1 : 0;
+#else
           rank += (zj < z || (zj == z && j < tid)) ? 1 : 0;
+#endif
         }
         A[rank] = ra;
         B[rank] = rb;
@@ -759,6 +732,8 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
         D[5 * M + rank] = w.se[g];
         D[6 * M + rank] = w.sws[g];
         Z[rank] = z;
+        Z[M + rank] = (float)w.sx[g];
+        Z[2 * M + rank] = (float)w.sy[g];
       }
     }
     __syncthreads();
@@ -907,6 +882,47 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
           MixedPos p0;
           load_mixed_pos(P, w, seg_begin, seg_pref, seg_shift, region, tb + tid, total, seg, p0);
           p0.base += copy_off;
+          // positions of the unit's region only (all but points on sub-box
+          // faces): no per-pair slot check
+          const bool all_in = __all_sync(0xffffffffu, !p0.valid || p0.slot >= 0);
+#if MIA_QUADS
+          if (!FULL) {
+            // each projected quadrant of the cell in turn: its box (half the
+            // cell's, widened by the same margin) bounds the gap to its shapes
+            const float px = p0.xh + p0.xl, py = p0.yh + p0.yl, pz = p0.zh + p0.zl;
+            const float mx = 0.5f * (s_box[0] + s_box[1]), my = 0.5f * (s_box[2] + s_box[3]);
+            const float mg = 0.5f * (s_box[1] - s_box[0]) - 0.5f * (float)P.s[0];  // the box margin
+            for (int qd = 0; qd < 4; ++qd) {
+              const int q0 = s_qn[qd], qn = s_qn[qd + 1] - q0;
+              if (qn == 0) continue;
+              const float x0 = (qd & 1) ? mx - mg : s_box[0], x1 = (qd & 1) ? s_box[1] : mx + mg;
+              const float y0 = (qd & 2) ? my - mg : s_box[2], y1 = (qd & 2) ? s_box[3] : my + mg;
+              int lo = qn, hi = 0;
+              if (p0.valid) {
+                const float gx = fmaxf(0.0f, fmaxf(x0 - px, px - x1));
+                const float gy = fmaxf(0.0f, fmaxf(y0 - py, py - y1));
+                const float g2 = fmaf(gx, gx, gy * gy);
+                if (!(g2 > P.q_cut)) {
+                  float win = P.zwin;
+                  if (KIND == MIA_KIND_MULTIPOLES)
+                    win = fminf(win, sqrtf(fmaxf(P.q_cut - g2, 0.0f) + 1e-4f * P.q_cut) + P.zwin - P.range_los32);
+                  z_window(Z + q0, qn, pz, win, lo, hi);
+                }
+              }
+              const int wlo = __reduce_min_sync(0xffffffffu, lo) + q0;
+              const int whi = __reduce_max_sync(0xffffffffu, hi) + q0;
+              if (p0.valid && wlo < whi) {
+                if (all_in)
+                  shape_loop<KIND, FULL, VAR, 1>(P, T, A, B, C, I, wlo, whi, p0, hv, w, o, sc, twoR, u.label,
+                                                 my_binned);
+                else
+                  shape_loop<KIND, FULL, VAR, 0>(P, T, A, B, C, I, wlo, whi, p0, hv, w, o, sc, twoR, u.label,
+                                                 my_binned);
+              }
+            }
+            continue;
+          }
+#endif
           int i_lo = S, i_hi = 0;
           if (p0.valid) {
             if (FULL && P.full[2]) {
@@ -939,78 +955,12 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
           // and every lane then reads the same staged shape in each iteration
           const int wlo = __reduce_min_sync(0xffffffffu, i_lo);
           const int whi = __reduce_max_sync(0xffffffffu, i_hi);
-#if MIA_COMPACT
-          // Two phases.  (1) Every lane tests its own pair with the shape of
-          // the iteration (the cheap range test); the warp's survivors go to
-          // its ring as (shape, lane).  (2) Whenever 32 are waiting, each lane
-          // takes one and bins and accumulates it (mixed_pair) with the
-          // position of the lane that found it.  A third of the pairs fail the
-          // range test, and without the ring a lane holding one would idle
-          // through the whole binning path of its warp-mates.
-          const int lane = tid & 31;
-          float4* WP = wpos + 2 * (tid & ~31);
-          unsigned short* Q = ring + kRing * (tid >> 5);
-          // this lane's position for the others (idx, or ~idx for a position
-          // whose label is not the unit's region)
-          WP[2 * lane] = make_float4(p0.xh, p0.xl, p0.yh, p0.yl);
-          WP[2 * lane + 1] = make_float4(p0.zh, p0.zl, p0.w, __int_as_float(p0.slot >= 0 ? p0.idx : ~p0.idx));
-          __syncwarp();
-          auto bin_entry = [&](unsigned e) {
-            const int i = (int)(e >> 5), src = (int)(e & 31u);
-            const float4 pa = WP[2 * src], pb = WP[2 * src + 1];
-            MixedPos q;
-            q.xh = pa.x; q.xl = pa.y; q.yh = pa.z; q.yl = pa.w;
-            q.zh = pb.x; q.zl = pb.y; q.w = pb.z;
-            const int v = __float_as_int(pb.w);
-            q.valid = true;
-            q.base = copy_off;
-            q.hbase = 0;
-            if (v >= 0) {
-              q.idx = v;
-              q.slot = 0;
-              q.lab = region;
-            } else {
-              q.idx = ~v;
-              q.slot = -1;
-              q.lab = w.plab_s[q.idx];
-            }
-            mixed_pair<KIND, FULL, VAR>(P, T, A[i], B[i], C, I, i, q, hv, w, o, sc, twoR, u.label, my_binned);
-          };
-          const unsigned below = (1u << lane) - 1u;
-          unsigned head = 0, tail = 0;  // warp-uniform ring counters
-          for (int i = wlo; i < whi; ++i) {
-            const bool pass = p0.valid && in_range<KIND, FULL>(P, A[i], B[i], p0);
-            const unsigned m = __ballot_sync(0xffffffffu, pass);
-            if (pass) Q[(tail + __popc(m & below)) & (kRing - 1)] = (unsigned short)((i << 5) | lane);
-            tail += __popc(m);
-            if (tail - head >= 32) {
-              __syncwarp();
-              const unsigned e = Q[(head + lane) & (kRing - 1)];
-              head += 32;
-              bin_entry(e);
-              __syncwarp();
-            }
-          }
-          __syncwarp();
-          if ((unsigned)lane < tail - head) bin_entry(Q[(head + lane) & (kRing - 1)]);
-          __syncwarp();
-#else
           if (p0.valid && wlo < whi) {
-            // the next shape is in flight while this pair is processed (index S
-            // at most: still inside the staging area); two register sets take
-            // turns, so the prefetched shape is never copied
-            float4 a0 = A[wlo], b0 = B[wlo];
-            for (int i = wlo;;) {
-              const float4 a1 = A[i + 1], b1 = B[i + 1];
-              mixed_pair<KIND, FULL, VAR>(P, T, a0, b0, C, I, i, p0, hv, w, o, sc, twoR, u.label, my_binned);
-              if (++i >= whi) break;
-              a0 = A[i + 1];
-              b0 = B[i + 1];
-              mixed_pair<KIND, FULL, VAR>(P, T, a1, b1, C, I, i, p0, hv, w, o, sc, twoR, u.label, my_binned);
-              if (++i >= whi) break;
-            }
+            if (all_in)
+              shape_loop<KIND, FULL, VAR, 1>(P, T, A, B, C, I, wlo, whi, p0, hv, w, o, sc, twoR, u.label, my_binned);
+            else
+              shape_loop<KIND, FULL, VAR, 0>(P, T, A, B, C, I, wlo, whi, p0, hv, w, o, sc, twoR, u.label, my_binned);
           }
-#endif
         }
       } else {
         int seg = 0;
@@ -1057,12 +1007,13 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
           }
           const int wlo = __reduce_min_sync(0xffffffffu, i_lo);
           const int whi = __reduce_max_sync(0xffffffffu, i_hi);
-          if (t >= total) continue;
-          for (int i = wlo; i < whi; ++i) {
-            PairResult r = pair_exact(P, *w.tables, D[i], D[M + i], D[2 * M + i], D[3 * M + i], D[4 * M + i],
-                                      D[5 * M + i], qx, qy, qz);
-            if (r.bin < 0) continue;
-            const double ww = __dmul_rn(pw, D[6 * M + i]);
+          // one pair in the exact FP64 arithmetic, into the unit's histogram
+          auto exact_pair = [&](int i, double x, double y, double z, double wp, int lab) {
+            const PairResult r = pair_exact(P, T, D[i], D[M + i], D[2 * M + i], D[3 * M + i], D[4 * M + i],
+                                            D[5 * M + i], x, y, z);
+            if (r.bin < 0) return;
+            const int sl = lab == region ? 0 : -1;
+            const double ww = __dmul_rn(wp, D[6 * M + i]);
             const double sp = __dmul_rn(ww, r.ep);
             const double sx = __dmul_rn(ww, r.ex);
             double tv = 0.0;
@@ -1073,7 +1024,7 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
             ok &= to_fix128(sp, sc.e128, fp);
             ok &= to_fix128(sx, sc.e128, fx);
             if (VAR) ok &= to_fix128(vr, sc.e128v, fv);
-            if (slot >= 0 && ok) {
+            if (sl >= 0 && ok) {
               const int hi = base + r.bin;
               atomicAdd(&h_cnt[hi], 1u);
               add_fix128(dd_q + 2 * hi, fd);
@@ -1081,11 +1032,58 @@ __global__ void __launch_bounds__(kThreads) k_pairs(Params P, const Dataset* __r
               add_fix128(sx_q + 2 * hi, fx);
               if (VAR) add_fix128(vr_q + 2 * hi, fv);
             } else {
-              acc_global(w, o, sc, nb, P.J, u.label, plab, r.bin, ww, sp, sx, vr, VAR);
-              if (slot < 0) atomicOr(&w.status->flags, kStatusNoSlot);
+              acc_global(w, o, sc, nb, P.J, u.label, lab, r.bin, ww, sp, sx, vr, VAR);
+              if (sl < 0) atomicOr(&w.status->flags, kStatusNoSlot);
               ++my_binned;
             }
+          };
+          // Two phases.  (1) Every lane tests its own pair with the shape of
+          // the iteration: an FP32 range test from single floats, with a margin
+          // for their rounding; the warp's survivors go to its ring as (shape,
+          // lane).  (2) Whenever 32 are waiting, each lane takes one and runs
+          // the exact FP64 arithmetic with the position of the lane that found
+          // it.  A third of the candidates fail the range test; without the
+          // ring the FP64 pipe would spend their share of every warp
+          // instruction on idle lanes (1.35x on the 4M / 1M w step).  (The
+          // mixed form does better without it: its binning is cheap enough
+          // that the scattered shared-memory reads of phase (2) cost more than
+          // the idle lanes.)
+          (void)slot;
+          const int lane = tid & 31;
+          double2* WD = reinterpret_cast<double2*>(wpos) + 2 * (tid & ~31);
+          int* WL = reinterpret_cast<int*>(reinterpret_cast<double2*>(wpos) + 2 * kThreads) + (tid & ~31);
+          unsigned short* Q = ring + kRing * (tid >> 5);
+          const bool valid = t < total;
+          WD[2 * lane] = make_double2(qx, qy);
+          WD[2 * lane + 1] = make_double2(qz, pw);
+          WL[lane] = plab;
+          __syncwarp();
+          const float* XF = Z + M;
+          const float* YF = Z + 2 * M;
+          const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
+          auto bin_entry = [&](unsigned e) {
+            const int i = (int)(e >> 5), src = (int)(e & 31u);
+            const double2 a = WD[2 * src], b = WD[2 * src + 1];
+            exact_pair(i, a.x, a.y, b.x, b.y, WL[src]);
+          };
+          const unsigned below = (1u << lane) - 1u;
+          unsigned head = 0, tail = 0;  // warp-uniform ring counters
+          for (int i = wlo; i < whi; ++i) {
+            const bool pass = valid && in_range_fp64<KIND>(P, XF[i], YF[i], Z[i], fx, fy, fz);
+            const unsigned m = __ballot_sync(0xffffffffu, pass);
+            if (pass) Q[(tail + __popc(m & below)) & (kRing - 1)] = (unsigned short)((i << 5) | lane);
+            tail += __popc(m);
+            if (tail - head >= 32) {
+              __syncwarp();
+              const unsigned e = Q[(head + lane) & (kRing - 1)];
+              head += 32;
+              bin_entry(e);
+              __syncwarp();
+            }
           }
+          __syncwarp();
+          if ((unsigned)lane < tail - head) bin_entry(Q[(head + lane) & (kRing - 1)]);
+          __syncwarp();
         }
       }
       __syncthreads();
