@@ -29,7 +29,7 @@ import os
 
 KNOBS = ("cell_size", "cell_refine", "shapes_per_unit", "cell_size_los", "cell_refine_los")
 DEFAULT = {"cell_size": 0.0, "cell_refine": 0, "shapes_per_unit": 0, "cell_size_los": 0.0, "cell_refine_los": 0}
-_VERSION = "g5"  # per-region work units (the best geometry moved)
+_VERSION = "g6"  # per-region work units, two descent rounds
 
 
 def cache_path():
@@ -141,11 +141,15 @@ def tune(make_counter, dcat, range_proj, range_los=None, key=None, path=None, lo
     best = min(({**cubic, "cell_size": s} for s in sides[:3]), key=time_one)
     best = min([best] + [{**best, "cell_size": s, "cell_size_los": rl, "cell_refine_los": los_refine(rl, 6)}
                          for s in sides[1:]], key=time_one)
-    if best["cell_size_los"] > 0.0:
-        best = min([best] + [{**best, "cell_size_los": ls, "cell_refine_los": los_refine(ls, d)}
-                             for ls in los_sides for d in (3, 6, 10)], key=time_one)
-    best = min([best] + [{**best, "cell_refine": m} for m in refines], key=time_one)
-    best = min([best] + [{**best, "shapes_per_unit": u} for u in units], key=time_one)
+    # two rounds over the axes: the best side in the plane depends on the
+    # line-of-sight geometry, the refinement and the unit size found after it
+    for _ in range(2):
+        if best["cell_size_los"] > 0.0:
+            best = min([best] + [{**best, "cell_size_los": ls, "cell_refine_los": los_refine(ls, d)}
+                                 for ls in los_sides for d in (3, 6, 10)], key=time_one)
+        best = min([best] + [{**best, "cell_refine": m} for m in refines], key=time_one)
+        best = min([best] + [{**best, "shapes_per_unit": u} for u in units], key=time_one)
+        best = min([best] + [{**best, "cell_size": s} for s in sides], key=time_one)
     if not math.isfinite(time_one(best)):
         raise failures[-1]
     out = dict(norm(best))

@@ -33,12 +33,6 @@
 
 #include "mia_internal.cuh"
 
-// 1: the mixed form stages a unit's shapes by projected quadrant of their cell
-// (2 x 2), each quadrant in line-of-sight order, and a position meets only the
-// quadrants within reach; 0: one line-of-sight order for the whole cell
-#ifndef MIA_QUADS
-#define MIA_QUADS 0
-#endif
 
 namespace mia {
 
@@ -474,7 +468,6 @@ __global__ void __launch_bounds__(kThreads) k_pairs(
   __shared__ int s_scan[32];
   __shared__ int s_total;
   __shared__ float s_box[4];  // the unit's shape cell in d0, d1, widened (see the window below)
-  __shared__ int s_qn[5];     // shapes per projected quadrant of the cell, then their starts (MIA_QUADS)
 
   // tables -> shared (the same binning for every dataset of a batch)
   {
@@ -660,42 +653,12 @@ __global__ void __launch_bounds__(kThreads) k_pairs(
         if (!(z == z)) z = INFINITY;  // the ranks below must form a permutation
         zs[tid] = z;
       }
-#if MIA_QUADS
-      // quadrant of the shape in the cell's projected box (split at the box's
-      // middle, FP32; the quadrant boxes below are widened by the box margin)
-      int* qs = seg_pref;  // free until the segments are built
-      int qd = 0;
-      if (tid < 4) s_qn[tid] = 0;
       __syncthreads();
-      if (tid < S) {
-        const float mx = 0.5f * (s_box[0] + s_box[1]), my = 0.5f * (s_box[2] + s_box[3]);
-        qd = ((ra.x + rb.x) > mx ? 1 : 0) + ((ra.y + rb.y) > my ? 2 : 0);
-        qs[tid] = qd;
-        atomicAdd(&s_qn[qd], 1);
-      }
-      __syncthreads();
-      if (tid == 0) {  // counts -> starts (s_qn[4] = S)
-        int acc = 0;
-        for (int k = 0; k < 4; ++k) {
-          const int c = s_qn[k];
-          s_qn[k] = acc;
-          acc += c;
-        }
-        s_qn[4] = acc;
-      }
-#else
-      __syncthreads();
-#endif
       if (tid < S) {
         int rank = 0;
         for (int j = 0; j < S; ++j) {
           const float zj = zs[j];
-#if MIA_QUADS
-          const int qj = qs[j];
-          rank += (qj < qd || (qj == qd && (zj < z || (zj == z && j < tid)))) ? 1 : 0;
-#else
           rank += (zj < z || (zj == z && j < tid)) ? 1 : 0;
-#endif
         }
         A[rank] = ra;
         B[rank] = rb;
@@ -885,44 +848,6 @@ __global__ void __launch_bounds__(kThreads) k_pairs(
           // positions of the unit's region only (all but points on sub-box
           // faces): no per-pair slot check
           const bool all_in = __all_sync(0xffffffffu, !p0.valid || p0.slot >= 0);
-#if MIA_QUADS
-          if (!FULL) {
-            // each projected quadrant of the cell in turn: its box (half the
-            // cell's, widened by the same margin) bounds the gap to its shapes
-            const float px = p0.xh + p0.xl, py = p0.yh + p0.yl, pz = p0.zh + p0.zl;
-            const float mx = 0.5f * (s_box[0] + s_box[1]), my = 0.5f * (s_box[2] + s_box[3]);
-            const float mg = 0.5f * (s_box[1] - s_box[0]) - 0.5f * (float)P.s[0];  // the box margin
-            for (int qd = 0; qd < 4; ++qd) {
-              const int q0 = s_qn[qd], qn = s_qn[qd + 1] - q0;
-              if (qn == 0) continue;
-              const float x0 = (qd & 1) ? mx - mg : s_box[0], x1 = (qd & 1) ? s_box[1] : mx + mg;
-              const float y0 = (qd & 2) ? my - mg : s_box[2], y1 = (qd & 2) ? s_box[3] : my + mg;
-              int lo = qn, hi = 0;
-              if (p0.valid) {
-                const float gx = fmaxf(0.0f, fmaxf(x0 - px, px - x1));
-                const float gy = fmaxf(0.0f, fmaxf(y0 - py, py - y1));
-                const float g2 = fmaf(gx, gx, gy * gy);
-                if (!(g2 > P.q_cut)) {
-                  float win = P.zwin;
-                  if (KIND == MIA_KIND_MULTIPOLES)
-                    win = fminf(win, sqrtf(fmaxf(P.q_cut - g2, 0.0f) + 1e-4f * P.q_cut) + P.zwin - P.range_los32);
-                  z_window(Z + q0, qn, pz, win, lo, hi);
-                }
-              }
-              const int wlo = __reduce_min_sync(0xffffffffu, lo) + q0;
-              const int whi = __reduce_max_sync(0xffffffffu, hi) + q0;
-              if (p0.valid && wlo < whi) {
-                if (all_in)
-                  shape_loop<KIND, FULL, VAR, 1>(P, T, A, B, C, I, wlo, whi, p0, hv, w, o, sc, twoR, u.label,
-                                                 my_binned);
-                else
-                  shape_loop<KIND, FULL, VAR, 0>(P, T, A, B, C, I, wlo, whi, p0, hv, w, o, sc, twoR, u.label,
-                                                 my_binned);
-              }
-            }
-            continue;
-          }
-#endif
           int i_lo = S, i_hi = 0;
           if (p0.valid) {
             if (FULL && P.full[2]) {
