@@ -29,7 +29,7 @@ import os
 
 KNOBS = ("cell_size", "cell_refine", "shapes_per_unit", "cell_size_los", "cell_refine_los")
 DEFAULT = {"cell_size": 0.0, "cell_refine": 0, "shapes_per_unit": 0, "cell_size_los": 0.0, "cell_refine_los": 0}
-_VERSION = "g6"  # per-region work units, two descent rounds
+_VERSION = "g7"  # per-region work units, two descent rounds, long-cell family
 
 
 def cache_path():
@@ -150,6 +150,12 @@ def tune(make_counter, dcat, range_proj, range_los=None, key=None, path=None, lo
         best = min([best] + [{**best, "cell_refine": m} for m in refines], key=time_one)
         best = min([best] + [{**best, "shapes_per_unit": u} for u in units], key=time_one)
         best = min([best] + [{**best, "cell_size": s} for s in sides], key=time_one)
+    # the long-cell family as a whole (two line-of-sight ranges deep, fine
+    # position cells along it, the largest units): coordinate descent changes
+    # one axis at a time and can stop short of it
+    best = min([best] + [{"cell_size": s, "cell_refine": m, "shapes_per_unit": units[-1], "cell_size_los": 2 * rl,
+                          "cell_refine_los": los_refine(2 * rl, 10)} for s in sides[1:5] for m in (1, 2)],
+               key=time_one)
     if not math.isfinite(time_one(best)):
         raise failures[-1]
     out = dict(norm(best))
