@@ -29,7 +29,7 @@ import os
 
 KNOBS = ("cell_size", "cell_refine", "shapes_per_unit", "cell_size_los", "cell_refine_los")
 DEFAULT = {"cell_size": 0.0, "cell_refine": 0, "shapes_per_unit": 0, "cell_size_los": 0.0, "cell_refine_los": 0}
-_VERSION = "g7"  # per-region work units, two descent rounds, long-cell family
+_VERSION = "g8"  # per-region work units, two descent rounds, long-cell family
 
 
 def cache_path():
@@ -69,7 +69,9 @@ def store(key, choice, path=None):
 def candidates(range_proj, range_los=None):
     """Search axes: projected sides, line-of-sight sides, refinements, unit sizes."""
     range_los = range_proj if range_los is None else range_los
-    sides = [range_proj / k for k in (2.0, 3.0, 4.0, 5.0, 6.0, 8.0)]
+    # (cells as wide as the reach or 2/3 of it: a small catalogue with one or
+    # two shapes per cell loses more to per-unit work than to extra candidates)
+    sides = [range_proj / k for k in (1.0, 1.5, 2.0, 3.0, 4.0, 5.0, 6.0, 8.0)]
     los_sides = [range_los * f for f in (0.5, 1.0, 2.0)]
     return sides, los_sides, (1, 2, 3), (64, 128, 256)
 
@@ -138,9 +140,9 @@ def tune(make_counter, dcat, range_proj, range_los=None, key=None, path=None, lo
     # around the best so far
     cubic = {"cell_size": range_proj / 3.0, "cell_refine": 2, "shapes_per_unit": 128, "cell_size_los": 0.0,
              "cell_refine_los": 0}
-    best = min(({**cubic, "cell_size": s} for s in sides[:3]), key=time_one)
+    best = min(({**cubic, "cell_size": s} for s in sides[:5]), key=time_one)
     best = min([best] + [{**best, "cell_size": s, "cell_size_los": rl, "cell_refine_los": los_refine(rl, 6)}
-                         for s in sides[1:]], key=time_one)
+                         for s in sides[3:]], key=time_one)
     # two rounds over the axes: the best side in the plane depends on the
     # line-of-sight geometry, the refinement and the unit size found after it
     for _ in range(2):
@@ -154,7 +156,7 @@ def tune(make_counter, dcat, range_proj, range_los=None, key=None, path=None, lo
     # position cells along it, the largest units): coordinate descent changes
     # one axis at a time and can stop short of it
     best = min([best] + [{"cell_size": s, "cell_refine": m, "shapes_per_unit": units[-1], "cell_size_los": 2 * rl,
-                          "cell_refine_los": los_refine(2 * rl, 10)} for s in sides[1:5] for m in (1, 2)],
+                          "cell_refine_los": los_refine(2 * rl, 10)} for s in sides[3:7] for m in (1, 2)],
                key=time_one)
     if not math.isfinite(time_one(best)):
         raise failures[-1]

@@ -393,6 +393,22 @@ __device__ __forceinline__ bool in_range_fp64(const Params& P, float sx, float s
   return !(fmaf(gz, gz, fmaf(gx, gx, gy * gy)) > P.q_cut);
 }
 
+// Sub-boxes (jackknife regions along one cell dimension) that the fine cells
+// lo..hi (unwrapped, periodic) fall in, ascending by first appearance; their
+// number.  cps = fine cells per sub-box.
+__device__ __forceinline__ int subbox_set(int lo, int hi, int nf, int cps, int n_sub, int* set) {
+  int cnt = 0;
+  for (int u = lo; u <= hi && cnt < n_sub;) {
+    const int cc = ((u % nf) + nf) % nf;
+    const int sb = cc / cps;
+    bool seen = false;
+    for (int j = 0; j < cnt; ++j) seen |= set[j] == sb;
+    if (!seen) set[cnt++] = sb;
+    u += cps - cc % cps;  // the first cell of the next sub-box
+  }
+  return cnt;
+}
+
 // One position against the staged shapes [wlo, whi): the next shape is in
 // flight while this pair is processed (index whi at most: still inside the
 // staging area); two register sets take turns, so the prefetched shape is
@@ -418,28 +434,13 @@ __device__ __forceinline__ void shape_loop(const Params& P, const TablesSmem& T,
 
 // (a minimum-blocks bound of 4 gives the same 61 registers but code that
 // runs 8% slower on the 4M/1M w step; the register count alone allows 4)
-// Sub-boxes (jackknife regions along one cell dimension) that the fine cells
-// lo..hi (unwrapped, periodic) fall in, ascending by first appearance; their
-// number.  cps = fine cells per sub-box.
-__device__ __forceinline__ int subbox_set(int lo, int hi, int nf, int cps, int n_sub, int* set) {
-  int cnt = 0;
-  for (int u = lo; u <= hi && cnt < n_sub;) {
-    const int cc = ((u % nf) + nf) % nf;
-    const int sb = cc / cps;
-    bool seen = false;
-    for (int j = 0; j < cnt; ++j) seen |= set[j] == sb;
-    if (!seen) set[cnt++] = sb;
-    u += cps - cc % cps;  // the first cell of the next sub-box
-  }
-  return cnt;
-}
-
 template <int MIXED, int VAR, int KIND, int FULL>
-#ifdef MIA_MINB  // (launch-bound experiments: blocks per SM the registers must allow)
-__global__ void __launch_bounds__(kThreads, MIA_MINB) k_pairs(
-#else
-__global__ void __launch_bounds__(kThreads) k_pairs(
-#endif
+// (4 blocks of 256 threads per SM need 64 registers: asked of the multipole
+// and FP64 variants, which the compiler otherwise takes to 80 or beyond --
+// mixed multipoles 104.0 against 112.7 ms on the 4M/1M step; the mixed w
+// kernel reaches 64 unbounded)
+#define MIA_PAIR_MINB (MIXED ? (KIND == MIA_KIND_W ? 0 : 4) : 4)
+__global__ void __launch_bounds__(kThreads, MIA_PAIR_MINB) k_pairs(
     Params P, const Dataset* __restrict__ ds, int n_ds,
                                                      const unsigned long long* __restrict__ wu_prefix,
                                                      unsigned long long* wu_next, int HW) {
@@ -525,18 +526,24 @@ __global__ void __launch_bounds__(kThreads) k_pairs(
   const double r2los = P.range_los * P.range_los;
 
   while (true) {
+    // -- the next unit with work, found by one thread: global unit g is slot
+    // rslot of run g / reg_slots of its dataset, and that slot is one of the
+    // jackknife regions the run's neighbourhood touches (sub-boxes per
+    // dimension, all combinations), or past their number (nothing to do, and
+    // the thread takes the next unit at once); a catalogue with coordinates
+    // outside [0, L) or not finite ends in MIA_ERR_RANGE, so its units are
+    // skipped as well
     if (tid == 0) {
-      const unsigned long long g = atomicAdd(wu_next, 1ULL);
-      if (g >= n_wu_all) {
-        s_wu = -1;
-      } else {
+      long long found = -1;
+      while (true) {
+        const unsigned long long g = atomicAdd(wu_next, 1ULL);
+        if (g >= n_wu_all) break;
         // dataset of global unit g: largest d with wu_prefix[d] <= g
         int lo = 0, hi = n_ds - 1;
         while (lo < hi) {
           const int mid = (lo + hi + 1) >> 1;
           if (wu_prefix[mid] <= g) lo = mid; else hi = mid - 1;
         }
-        s_wu = (long long)(g - wu_prefix[lo]);  // run * reg_slots + region slot
         if (lo != s_ds) {
           s_ds = lo;
           s_data = ds[lo];
@@ -544,59 +551,29 @@ __global__ void __launch_bounds__(kThreads) k_pairs(
           s_twoR = dataset_twoR(wd.reg, P.J);
           s_sc = dataset_scales(wd.status, s_twoR);
         }
-      }
-    }
-    __syncthreads();
-    const long long wi = s_wu;
-    if (wi < 0) break;
-    // a catalogue with coordinates outside [0, L) or not finite ends in
-    // MIA_ERR_RANGE: its units are skipped (nothing of it would be used)
-    if (*reinterpret_cast<volatile const unsigned*>(&s_data.w.status->flags) & kStatusRange) {
-      __syncthreads();
-      continue;
-    }
-    const Work& w = s_data.w;
-    const Out& o = s_data.o;
-    const double twoR = s_twoR;
-    const Scales& sc = s_sc;
-    unsigned long long my_binned = 0;
-    const WorkUnit u = w.wu[wi / P.reg_slots];
-    const int rslot = (int)(wi % P.reg_slots);
-    int c[3];
-    {
-      long long t = u.cell;
-      c[0] = (int)(t % P.n[0]);
-      t /= P.n[0];
-      c[1] = (int)(t % P.n[1]);
-      c[2] = (int)(t / P.n[1]);
-    }
-    // -- the shape cell's projected box, widened by 1e-3 r_max + 1e-5 L: more
-    // than the FP32 error of a position's coordinates, so a gap measured to
-    // it never exceeds the true gap to any of the cell's shapes
-    if (tid == 0) {
-      const double m = 1e-3 * P.range_proj + 1e-5 * P.L;
-      s_box[0] = (float)(c[0] * P.s[0] - m);
-      s_box[1] = (float)((c[0] + 1) * P.s[0] + m);
-      s_box[2] = (float)(c[1] * P.s[1] - m);
-      s_box[3] = (float)((c[1] + 1) * P.s[1] + m);
-    }
-    // -- the unit's position region: slot rslot of the regions that the
-    // neighbourhood's fine cells touch (sub-boxes per dimension, all
-    // combinations); a slot past their number leaves nothing to do
-    if (tid == 0) {
-      int reg = 0;
-      s_sub[0] = s_sub[1] = s_sub[2] = 0;
-      if (P.J > 0) {
-        int sets[3][16], cnt[3];
-        for (int k = 0; k < 3; ++k) {
-          const int f = c[k] * P.m[k];
-          const int lo = P.full[k] ? 0 : f - P.Rf[k];
-          const int hi = P.full[k] ? P.nf[k] - 1 : f + P.m[k] - 1 + P.Rf[k];
-          cnt[k] = subbox_set(lo, hi, P.nf[k], P.nf[k] / P.n_sub, P.n_sub, sets[k]);
+        if (*reinterpret_cast<volatile const unsigned*>(&s_data.w.status->flags) & kStatusRange) continue;
+        const long long wi = (long long)(g - wu_prefix[lo]);
+        const WorkUnit u = s_data.w.wu[wi / P.reg_slots];
+        const int rslot = (int)(wi % P.reg_slots);
+        int c[3];
+        {
+          long long t = u.cell;
+          c[0] = (int)(t % P.n[0]);
+          t /= P.n[0];
+          c[1] = (int)(t % P.n[1]);
+          c[2] = (int)(t / P.n[1]);
         }
-        if (rslot >= cnt[0] * cnt[1] * cnt[2]) {
-          reg = -1;
-        } else {
+        int reg = 0;
+        s_sub[0] = s_sub[1] = s_sub[2] = 0;
+        if (P.J > 0) {
+          int sets[3][16], cnt[3];
+          for (int k = 0; k < 3; ++k) {
+            const int f = c[k] * P.m[k];
+            const int a0 = P.full[k] ? 0 : f - P.Rf[k];
+            const int a1 = P.full[k] ? P.nf[k] - 1 : f + P.m[k] - 1 + P.Rf[k];
+            cnt[k] = subbox_set(a0, a1, P.nf[k], P.nf[k] / P.n_sub, P.n_sub, sets[k]);
+          }
+          if (rslot >= cnt[0] * cnt[1] * cnt[2]) continue;
           const int i0 = rslot % cnt[0], i1 = (rslot / cnt[0]) % cnt[1], i2 = rslot / (cnt[0] * cnt[1]);
           s_sub[0] = sets[0][i0];
           s_sub[1] = sets[1][i1];
@@ -606,29 +583,61 @@ __global__ void __launch_bounds__(kThreads) k_pairs(
           sub[P.axis[1]] = s_sub[1];
           sub[P.axis[2]] = s_sub[2];
           reg = (sub[0] * P.n_sub + sub[1]) * P.n_sub + sub[2];
+        } else if (rslot > 0) {
+          continue;
         }
-      } else if (rslot > 0) {
-        reg = -1;
+        found = wi;
+        s_region = reg;
+        // the shape cell's projected box, widened by 1e-3 r_max + 1e-5 L: more
+        // than the FP32 error of a position's coordinates, so a gap measured
+        // to it never exceeds the true gap to any of the cell's shapes
+        const double m = 1e-3 * P.range_proj + 1e-5 * P.L;
+        s_box[0] = (float)(c[0] * P.s[0] - m);
+        s_box[1] = (float)((c[0] + 1) * P.s[0] + m);
+        s_box[2] = (float)(c[1] * P.s[1] - m);
+        s_box[3] = (float)((c[1] + 1) * P.s[1] + m);
+        // private copies of the unit's histogram (mixed form): lanes holding
+        // neighbouring positions hit the same bin against a shape, and shared
+        // atomics on one address serialise, so lane l adds into copy l mod R;
+        // the odd stride puts the R copies of a bin in R distinct banks.  No
+        // more copies than the unit has shapes: each copy is zeroed and read
+        // back once per unit
+        int R = 1;
+        const int stride = nb | 1;
+        if (MIXED)
+          while (R < 32 && R < u.count && (2 * R) * stride <= HW) R *= 2;
+        s_copies = R;
+        s_stride = R > 1 ? stride : nb;
+        break;
       }
-      s_region = reg;
-      // private copies of the unit's histogram (mixed form): lanes holding
-      // neighbouring positions hit the same bin against a shape, and shared
-      // atomics on one address serialise, so lane l adds into copy l mod R;
-      // the odd stride puts the R copies of a bin in R distinct banks
-      int R = 1;
-      const int stride = nb | 1;
-      if (MIXED)
-        while (R < 32 && (2 * R) * stride <= HW) R *= 2;
-      s_copies = R;
-      s_stride = R > 1 ? stride : nb;
+      s_wu = found;
     }
     __syncthreads();
-    const int region = s_region;
-    if (region < 0) {
-      __syncthreads();
-      continue;
+    const long long wi = s_wu;
+    if (wi < 0) break;
+    const Work& w = s_data.w;
+    const Out& o = s_data.o;
+    const double twoR = s_twoR;
+    const Scales& sc = s_sc;
+    unsigned long long my_binned = 0;
+    const WorkUnit u = w.wu[wi / P.reg_slots];
+    int c[3];
+    {
+      long long t = u.cell;
+      c[0] = (int)(t % P.n[0]);
+      t /= P.n[0];
+      c[1] = (int)(t % P.n[1]);
+      c[2] = (int)(t / P.n[1]);
     }
-    for (int i = tid; i < hist_u32; i += blockDim.x) hist[i] = 0u;
+    const int region = s_region;
+    if (MIXED) {
+      // the copies in use of the replicated words, and the high words
+      const int used = s_copies * s_stride;
+      for (int i = tid; i < (4 + VAR) * KB + (3 + VAR) * nb; i += blockDim.x)
+        if (i >= (4 + VAR) * KB || i % KB < used) hist[i] = 0u;
+    } else {
+      for (int i = tid; i < hist_u32; i += blockDim.x) hist[i] = 0u;
+    }
     // -- shapes of the unit -> shared
     const int S = u.count;
     if (MIXED) {

@@ -156,7 +156,7 @@ def test_autotune_cache_roundtrip(tmp_path, monkeypatch):
     assert autotune.load_cache()[k1]["cell_refine"] == 2
     assert set(autotune.KNOBS) <= set(autotune.load_cache()[k1])
     sides, los_sides, refines, units = autotune.candidates(20.0, 40.0)
-    assert len(sides) == 6 and 40.0 in los_sides and 2 in refines and 128 in units
+    assert len(sides) == 8 and 40.0 in los_sides and 2 in refines and 128 in units
 
 
 @pytest.mark.parametrize("key,value", [("q", np.nan), ("weight", np.inf), ("weight_shape_sample", np.nan)])
