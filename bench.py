@@ -386,8 +386,10 @@ def run_batch48(args, local):
     pcs = {"w": PairCounter("w", p_bins=PI_BINS, **common),
            "m": PairCounter("m", p_bins=np.linspace(-1.0, 1.0, 21), **common)}
     dcats = [pcs["w"].to_device(c) for c in cats]
-    big = int(np.argmax(sizes))
-    pcs = {k: _pick(pc, dcats[big], args) for k, pc in pcs.items()}  # launch knobs of the largest catalogue
+    if args.knobs or args.no_tune:
+        pcs = {k: _pick(pc, dcats[0], args) for k, pc in pcs.items()}
+    else:  # launch knobs tuned on the batch as a whole (outside the timed region; cached per batch shape)
+        pcs = {k: BatchCounter(pc, dcats).tuned().pc for k, pc in pcs.items()}
     stream = torch.cuda.current_stream(local)
     out = {}
     batches = {}

@@ -76,11 +76,14 @@ def candidates(range_proj, range_los=None):
     return sides, los_sides, (1, 2, 3), (64, 128, 256)
 
 
-def tune(make_counter, dcat, range_proj, range_los=None, key=None, path=None, log=None):
+def tune(make_counter, dcat, range_proj, range_los=None, key=None, path=None, log=None, run=None):
     """Return the fastest knob set (a dict over KNOBS, plus its time in 'ms').
 
     ``make_counter(**knobs)`` builds a PairCounter for the knobs; ``dcat`` is
-    the device-resident catalogue.  With ``key`` the result is cached."""
+    the device-resident catalogue.  ``run(**knobs)``, when given, replaces the
+    single measurement as the thing timed: it returns a callable that runs
+    the whole job once (e.g. a batch of catalogues).  With ``key`` the result
+    is cached."""
     import torch
 
     from ._lib import MiaError
@@ -89,27 +92,33 @@ def tune(make_counter, dcat, range_proj, range_los=None, key=None, path=None, lo
         hit = load_cache(path).get(key)
         if hit and all(k in hit for k in KNOBS):
             return hit
-    n_pos = dcat["Position"].shape[0]
-    n_shape = dcat["Position_shape_sample"].shape[0]
     timings = {}
     failures = []
 
     def norm(knobs):
         return tuple((k, float(knobs[k]) if k.startswith("cell_size") else int(knobs[k])) for k in KNOBS)
 
+    def job(knobs):
+        if run is not None:
+            return run(**knobs)
+        n_pos = dcat["Position"].shape[0]
+        n_shape = dcat["Position_shape_sample"].shape[0]
+        pc = make_counter(**knobs)
+        bufs = pc.allocate(n_pos, n_shape)
+        return lambda: pc.run(dcat, bufs)
+
     def time_one(knobs):
         tkey = norm(knobs)
         if tkey in timings:
             return timings[tkey]
-        bufs = None
+        go = None
         try:
-            pc = make_counter(**knobs)
-            bufs = pc.allocate(n_pos, n_shape)
-            pc.run(dcat, bufs)
+            go = job(knobs)
+            go()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             torch.cuda.synchronize()
             e0.record()
-            pc.run(dcat, bufs)
+            go()
             e1.record()
             torch.cuda.synchronize()
             ms = e0.elapsed_time(e1)
@@ -123,7 +132,7 @@ def tune(make_counter, dcat, range_proj, range_los=None, key=None, path=None, lo
             if log:
                 log(f"autotune {dict(tkey)} -> skipped ({exc})")
         timings[tkey] = ms
-        del bufs
+        del go
         return ms
 
     sides, los_sides, refines, units = candidates(range_proj, range_los)

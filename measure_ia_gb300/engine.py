@@ -345,6 +345,31 @@ class BatchCounter:
             self.res[i].npairs = self.cnts[i].data_ptr()
         self.graph = None
 
+    def tuned(self, cache=True, log=None):
+        """A batch of the same catalogues with launch knobs autotuned on the
+        batch as a whole (the time of one batched run per candidate; cached per
+        batch shape): the best geometry for many small catalogues differs from
+        that of the largest one."""
+        import torch
+        from . import autotune
+        pc = self.pc
+        rp, rl = pc.search_ranges()
+        key = None
+        if cache:
+            sizes = [(d["Position"].shape[0], d["Position_shape_sample"].shape[0]) for d in self.dcats]
+            key = autotune.workload_key(pc.kind, pc.precision, sum(a for a, _ in sizes), sum(b for _, b in sizes),
+                                        float(pc._args["boxsize"]), pc.n_r, pc.n_p, rp, rl,
+                                        int(pc._args["l_subboxes"]), pc.membership,
+                                        torch.cuda.get_device_name(pc.device)) + f"|batch{self.n}"
+
+        def run(**knobs):
+            b = BatchCounter(pc.with_knobs(**knobs), self.dcats)
+            b.prepare()
+            return lambda: (b.enqueue(), b.status())
+
+        best = autotune.tune(pc.with_knobs, None, rp, rl, key=key, log=log, run=run)
+        return BatchCounter(pc.with_knobs(**{k: best[k] for k in autotune.KNOBS}), self.dcats)
+
     def _call(self, name, stream):
         import torch
         lib = L.load()

@@ -107,3 +107,22 @@ def test_w_and_multipoles_in_one_graph():
                 np.testing.assert_array_equal(got.npairs, ref.npairs)
                 for k in ("proj_gp", "proj_gg", "cov_gp"):
                     assert_close(got[k], ref[k], 1e-12, f"{name} catalogue {i}: {k}")
+
+
+def test_batch_tuned_on_the_whole_batch(tmp_path, monkeypatch):
+    """Launch knobs tuned on a batch as a whole change its speed, never its
+    products: the tuned batch's counts equal the single measurements'."""
+    from measure_ia_gb300.engine import BatchCounter, PairCounter
+    monkeypatch.setenv("MIA_TUNE_CACHE", str(tmp_path / "tune.json"))
+    pc = PairCounter("w", boxsize=205.0, r_bins=np.logspace(-1, np.log10(20.0), 11), r_min=0.1, r_max=20.0,
+                     p_bins=np.linspace(-20.0, 20.0, 9), l_subboxes=3, precision="mixed")
+    dcats = [pc.to_device(c) for c in _catalogues()[:3]]
+    tuned = BatchCounter(pc, dcats).tuned()
+    import json
+    assert len(json.load(open(tmp_path / "tune.json"))) == 1  # the choice is cached per batch shape
+    tuned.prepare()
+    tuned.run()
+    for i, d in enumerate(dcats):
+        ref = pc.measure({k: v for k, v in d.items()})
+        np.testing.assert_array_equal(tuned.fetch(i).npairs, ref.npairs)
+        assert_close(tuned.fetch(i)["proj_gp"], ref["proj_gp"], 1e-12, f"tuned batch {i}")
