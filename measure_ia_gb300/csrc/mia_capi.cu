@@ -807,7 +807,7 @@ int mia_batch_enqueue(mia_context* ctx, const mia_config* cfg, int n, const mia_
   NvtxRange r_pairs("mia/pairs");
   const long long slot = ctx->prof_start.empty() ? -1 : ctx->prof_count % (long long)ctx->prof_start.size();
   if (slot >= 0) MIA_CUDA(cudaEventRecord(ctx->prof_start[slot], st));
-  MIA_CUDA(launch_pairs(bp.plans[0], P, ds_dev, n, prefix, &hdr->wu_next, st, ctx->num_sms));
+  MIA_CUDA(launch_pairs(P, ds_dev, n, prefix, &hdr->wu_next, st, ctx->num_sms));
   if (slot >= 0) {
     MIA_CUDA(cudaEventRecord(ctx->prof_stop[slot], st));
     ++ctx->prof_count;

@@ -15,8 +15,6 @@ constexpr int kThreads = 256;            // pair-kernel block size
 constexpr int kLutBits = 11;             // 2048-bucket logarithmic lookup table (32 octaves)
 constexpr int kLut = 1 << kLutBits;
 constexpr int kLutMantBits = 6;          // 64 buckets per octave of q
-constexpr int kMaxRows = 1024;           // neighbour rows per pass of a work unit
-constexpr int kMaxSegs = 2 * kMaxRows;   // a row wraps into at most 2 contiguous segments
 constexpr int kScanTile = 2048;
 
 // status word bits
@@ -436,9 +434,8 @@ void bind_work(const Plan& plan, void* base, Work* w);
 
 // Stage launchers (mia_prep.cu, mia_pairs.cu, mia_post.cu)
 cudaError_t launch_prep(const Plan& plan, const Params& P, const mia_catalog& cat, const Work& w, cudaStream_t st);
-cudaError_t launch_pairs(const Plan& plan, const Params& P, const Dataset* ds_dev, int n_ds,
-                         const unsigned long long* wu_prefix, unsigned long long* wu_next, cudaStream_t st,
-                         int num_sms);
+cudaError_t launch_pairs(const Params& P, const Dataset* ds_dev, int n_ds, const unsigned long long* wu_prefix,
+                         unsigned long long* wu_next, cudaStream_t st, int num_sms);
 cudaError_t launch_edge_retest(const Params& P, const Work& w, const Out& o, cudaStream_t st, int num_sms);
 cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, int reg_slots, unsigned long long* wu_prefix,
                                 cudaStream_t st);

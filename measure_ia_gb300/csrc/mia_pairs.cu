@@ -1259,10 +1259,6 @@ __global__ void k_batch_prefix(const Dataset* ds, int n, int reg_slots, unsigned
 
 }  // namespace
 
-size_t pair_smem_bytes(int spu, int nb, int mixed, int var) {
-  return smem_layout(spu, nb, nb, mixed, var).total;
-}
-
 cudaError_t launch_batch_prefix(const Dataset* ds_dev, int n_ds, int reg_slots, unsigned long long* wu_prefix,
                                 cudaStream_t st) {
   k_batch_prefix<<<1, 32, 0, st>>>(ds_dev, n_ds, reg_slots, wu_prefix);
@@ -1281,10 +1277,8 @@ cudaError_t launch_edge_retest(const Params& P, const Work& w, const Out& o, cud
   return cudaGetLastError();
 }
 
-cudaError_t launch_pairs(const Plan& plan, const Params& P, const Dataset* ds_dev, int n_ds,
-                         const unsigned long long* wu_prefix, unsigned long long* wu_next, cudaStream_t st,
-                         int num_sms) {
-  (void)plan;
+cudaError_t launch_pairs(const Params& P, const Dataset* ds_dev, int n_ds, const unsigned long long* wu_prefix,
+                         unsigned long long* wu_next, cudaStream_t st, int num_sms) {
   if (P.precision == MIA_MIXED)
     return P.want_variance ? launch_kind<1, 1>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms)
                            : launch_kind<1, 0>(P, ds_dev, n_ds, wu_prefix, wu_next, st, num_sms);
