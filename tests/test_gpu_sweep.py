@@ -263,14 +263,19 @@ def test_large_box_geometry_jk125(kind, precision, tmp_path):
     15 log r bins 0.1-60, 20 Pi bins over |Pi| <= 60 (or 20 mu_r bins), 125
     jackknife regions (5 x 5 x 5 sub-boxes, measure_IA_base.py:404-452, and
     the RR_jk loop of measure_w_box_jk.py:798-807), on a clustered catalogue
-    of ~24,000 positions and 6,000 shapes.  At 125 regions a work unit's
-    neighbourhood spans more regions than at 27.  Every dataset against the
-    oracle: counts per (bin, region) bit-exact, values as in the sweep."""
+    of ~24,000 positions and 6,000 shapes, plus 600 pairs placed on bin
+    edges (r_p or Pi equal to an edge up to the FP64 subtraction, r_max = 60
+    and |Pi| = 60 among them): in this box the FP64 form's FP32 range test has
+    its largest absolute margin.  At 125 regions a work unit's neighbourhood
+    spans more regions than at 27.  Every dataset against the oracle: counts
+    per (bin, region) bit-exact, values as in the sweep."""
     from measure_ia_gb300 import MeasureIABox, open_output
-    from measure_ia_gb300.catalogs import neyman_scott_catalog
+    from measure_ia_gb300.catalogs import add_edge_pairs, neyman_scott_catalog
     L = 1000.0
-    data = neyman_scott_catalog(600, L, 6000, 125, mean_children=40, sigma=1.5)
     r_min, r_max, n_r, n_p, pi_max = 0.1, 60.0, 15, 20, 60.0
+    data = neyman_scott_catalog(600, L, 6000, 125, mean_children=40, sigma=1.5)
+    data = add_edge_pairs(data, L, 126, np.logspace(np.log10(r_min), np.log10(r_max), n_r + 1),
+                          np.linspace(-pi_max, pi_max, n_p + 1), 600)
     b = O.Binning(boxsize=L, r_min=r_min, r_max=r_max, num_bins_r=n_r, num_bins_pi=n_p, pi_max=pi_max)
     ref = dict(O.measure(kind, b, _copy(data), "big", "both", 125, None, "distortion", "multiprocessing"))
     c = ref.pop("__counts__")
