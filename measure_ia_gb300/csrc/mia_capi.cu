@@ -374,6 +374,7 @@ static void build_tables(const mia_config* cfg, Tables* T, int* lut_base) {
     memcpy(&hi, &hi_bits, 4);
     if (!(lo < INFINITY)) {  // beyond the float range: walk
       T->lut32[b] = 0x8000;
+      T->lutw[b] = 0x8000;
       continue;
     }
     int iv = 0;
@@ -382,7 +383,13 @@ static void build_tables(const mia_config* cfg, Tables* T, int* lut_base) {
     // clean bucket: the bin itself (+1, 0 = not binned); otherwise the first
     // breakpoint to compare against, flagged
     T->lut32[b] = clean ? (unsigned short)(T->q_bin[iv] + 1) : (unsigned short)(iv | 0x8000);
+    T->lutw[b] = clean ? (unsigned short)(T->q_bin[iv] >= 0 ? T->q_bin[iv] * cfg->n_p : kLutReject)
+                       : (unsigned short)(iv | 0x8000);
   }
+  // (clamped indices: bucket 0 lies an octave below the first guard band, so
+  // every q under it has bin q_bin[0]; a q over the last bucket is walked from
+  // that bucket's entry, or takes q_bin[n] when the bucket is clean and past
+  // every band)
 }
 
 }  // namespace mia
@@ -656,6 +663,16 @@ void make_params(const mia_config* cfg, const Plan& plan, const Tables& T, int l
     P.p_guard = (float)fmin(0.25, fmax(4.0 * et, 1.0 / 1048576.0));
     P.p_half_in = 0.5f - P.p_guard;
     P.p_off32 = (float)(-p0 * inv);
+    // short w path: t = fma(z_lo, inv, fma(z_hi, inv, off_p)) from the shape's
+    // hi/lo line-of-sight coordinate and the position's offset off_p = -(p_lo
+    // + z_p) inv rounded to FP32.  Errors, in bins: the FP32 inverse width
+    // ((n_p + 1) 2^-24 over the binned range), off_p's rounding (|off_p| <=
+    // (L + 2 reach + |p_lo|) inv, 2^-24 of it) and the two FMA roundings
+    // ((n_p + 1) 2^-24 each); taken four times over
+    P.p_off_d = -p0 * inv;
+    const double lmax = (cfg->boxsize + 2.0 * plan.range_los + fabs(p0)) * inv;
+    const double ew = (3.0 * (cfg->n_p + 1) + lmax) * (u * 0.5);
+    P.p_guard_w = (float)fmin(0.25, fmax(4.0 * ew, 1.0 / 1048576.0));
   }
   P.c_guard = 1e-12f;
   P.wrap_guard = (float)(cfg->boxsize * 1e-5);

@@ -16,6 +16,8 @@ constexpr int kLutBits = 11;             // 2048-bucket logarithmic lookup table
 constexpr int kLut = 1 << kLutBits;
 constexpr int kLutMantBits = 6;          // 64 buckets per octave of q
 constexpr int kScanTile = 2048;
+constexpr int kLutReject = 0x7FFF;       // lutw: clean bucket whose q is not binned
+constexpr int kHistShort = 1920;         // u32 words per replicated histogram array, short w path
 
 // status word bits
 constexpr unsigned kStatusRange = 1u;      // input coordinate outside [0, L) or NaN
@@ -53,6 +55,12 @@ struct Tables {
   // lookup tables: bucket -> bin + 1, or first breakpoint index | 0x8000
   // (the bucket touches a guard band)
   unsigned short lut32[kLut];
+  // the same buckets for the w kernel's short pair path: a clean bucket holds
+  // ib * n_p (kLutReject when not binned), a bucket touching a guard band the
+  // first breakpoint to compare against | 0x8000; the kernel clamps bucket
+  // indices to [0, kLut), so entry 0 and entry kLut - 1 also hold for every q
+  // below and above the table
+  unsigned short lutw[kLut];
   // bin edges (r_bins; pi_bins or mu_r_bins)
   double r_edges[MIA_MAX_BINS_R + 1];
   double p_edges[MIA_MAX_BINS_P + 1];
@@ -274,6 +282,8 @@ struct Params {
   float p_off32;                // -p_lo * p_inv: t = fma(v, p_inv, p_off)
   float p_guard;                // fraction of a bin treated as ambiguous at each edge
   float p_half_in;              // 0.5 - p_guard: |frac(t) - 0.5| above it is an edge
+  double p_off_d;               // -p_lo * n_p / (p_hi - p_lo) in FP64 (per-position offset of the short w path)
+  float p_guard_w;              // short w path: |t - rint(t)| below it is an edge (t from the shape's hi/lo z)
   float c_guard;                // sin^2(phi) below which the exact FP64 cos(phi) decides
   float wrap_guard;
   float los_cut;                // |Pi| above this is surely outside the Pi bins (w)

@@ -200,6 +200,8 @@ struct HistView {
 // One position in FP32 hi/lo form, moved to the periodic image of its row.
 struct MixedPos {
   float xh, xl, yh, yl, zh, zl, w;
+  float loff;  // short w path: -(p_lo + z) n_p / (p_hi - p_lo)
+  float2 nh, nl, w2;  // short w path: -(x_hi, y_hi), -(x_lo, y_lo), (w, w) as register pairs
   int idx, lab, slot, base, hbase;
   bool valid;
 };
@@ -376,6 +378,93 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
   }
 }
 
+// The w kernel's short pair path (mixed form, local neighbourhoods, no
+// variance terms): the same decisions as mixed_pair in fewer instructions.
+//  * Pi bin: t = (Pi - p_lo) n_p / (p_hi - p_lo) from two FMAs on the shape's
+//    hi/lo line-of-sight coordinate and the position's offset p.loff, bin =
+//    floor(t); t within p_guard_w of an integer is an edge.  No separate
+//    line-of-sight cut: a pair outside the Pi range has its bin outside
+//    [0, n_p).
+//  * r bin: the lutw bucket of q (indices clamped to the table) holds
+//    ib * n_p, kLutReject, or a breakpoint to walk from; one test covers a
+//    reject, a walk and a Pi bin outside the range.
+//  * Histogram words sit kHistShort words apart, so one address serves the
+//    four atomics.  `hk` is the lane's copy of the unit's histogram, `hh` the
+//    high words.
+//  * Paired FP32 instructions (FADD2, FMUL2) where both halves have the same
+//    operation: the staged shape is a = (x_hi, y_hi, x_lo, y_lo), b = (z_hi,
+//    z_lo, w_s, w_s e) (scaled weights), so (dx, dy) and the two weight
+//    products come out of register pairs; each half rounds as the scalar
+//    operation would.
+template <int SLOTS>
+__device__ __forceinline__ void mixed_pair_short(const Params& P, const TablesSmem& T, const float4& a,
+                                                 const float4& b, const float2* C, const int* I, int i,
+                                                 const MixedPos& p, unsigned* hk, int* hh, const Work& w,
+                                                 const Out& o, int label_a, unsigned long long& my_binned) {
+  const float t = fmaf(b.y, P.p_inv32, fmaf(b.x, P.p_inv32, p.loff));
+  const float2 d = __fadd2_rn(__fadd2_rn(make_float2(a.x, a.y), p.nh), __fadd2_rn(make_float2(a.z, a.w), p.nl));
+  const float dx = d.x, dy = d.y;
+  const float qp = fmaf(dx, dx, dy * dy);
+  const int bucket = min(max((int)(__float_as_uint(qp) >> (23 - kLutMantBits)) - P.lut32_base, 0), kLut - 1);
+  int e = T.lut32[bucket];
+  const int jb = __float2int_rd(t);
+  const bool pi_edge = fabsf(t - rintf(t)) < P.p_guard_w;
+  bool edge = pi_edge;
+  if ((e >= kLutReject) | ((unsigned)jb >= (unsigned)P.n_p)) {
+    // Pi surely outside the bins (an edge at 0 or n_p goes on to the re-test)
+    if ((unsigned)jb >= (unsigned)P.n_p && ((unsigned)jb + 1u > (unsigned)P.n_p + 1u || !pi_edge)) return;
+    if (e == kLutReject) return;
+    if (e & 0x8000) {
+      int iv = e & 0x7fff;
+      while (iv < P.n_qbreak && qp >= T.q_hi32[iv]) ++iv;
+      const bool q_edge = iv < P.n_qbreak && qp >= T.q_lo32[iv];
+      const int ib = T.q_bin[iv];
+      if (ib < 0 && !q_edge) return;
+      edge |= q_edge;
+      e = ib * P.n_p;  // (not used when ib < 0: the pair is an edge)
+    }
+  }
+  const float2 cxy = C[i];
+  const float dot = fmaf(dx, cxy.x, dy * cxy.y);
+  const float crs = fmaf(dx, cxy.y, -dy * cxy.x);
+  const float crs2 = crs * crs;
+  if (crs2 < P.c_guard * qp) edge = true;
+  if (edge) {
+    const unsigned long long k = atomicAdd(&w.status->edge_count, 1ULL);
+    if (k < (unsigned long long)w.edge_capacity) w.edges[k] = make_int2(I[i], p.idx);
+    else atomicOr(&w.status->flags, kStatusOverflow);
+    return;
+  }
+  const int bin = e + jb;
+  const float2 pw = __fmul2_rn(make_float2(b.z, b.w), p.w2);  // (w_p w_s, w_p w_s e), scaled
+  const float ww = pw.x;
+  const float s = __fdividef(pw.y, qp);
+  const float2 tt = __fmul2_rn(make_float2(fmaf(dot, dot, -crs2), dot * fabsf(crs)), make_float2(s, s + s));
+  const float tp = tt.x, tx = tt.y;
+  if (SLOTS || p.slot >= 0) {
+    const int vd = __float2int_rn(ww);
+    const int vp = __float2int_rn(tp);
+    const int vx = __float2int_rn(tx);
+    unsigned* h = hk + bin;
+    const unsigned od = atomicAdd(h + kHistShort, (unsigned)vd);
+    const unsigned op = atomicAdd(h + 2 * kHistShort, (unsigned)vp);
+    const unsigned ox = atomicAdd(h + 3 * kHistShort, (unsigned)vx);
+    atomicAdd(h, 1u);
+    const int fd = overflow_of(od, vd), fp = overflow_of(op, vp), fx = overflow_of(ox, vx);
+    if ((fd | fp | fx) < 0) {
+      int* g = hh + bin;
+      if (fd < 0) atomicAdd(g, (vd >> 31) | 1);
+      if (fp < 0) atomicAdd(g + P.nb, (vp >> 31) | 1);
+      if (fx < 0) atomicAdd(g + 2 * P.nb, (vx >> 31) | 1);
+    }
+  } else {
+    acc_global_fixed(w, o, P.nb, P.J, label_a, p.lab, bin, __float2ll_rn(ww), __float2ll_rn(tp), __float2ll_rn(tx),
+                     0, 0);
+    atomicOr(&w.status->flags, kStatusNoSlot);
+    ++my_binned;
+  }
+}
+
 // FP64 form, the two-phase loop's range test from single-float coordinates:
 // the minimum-image gap per axis less `m` (a bound on the FP32 error), so that
 // a pair it drops is beyond the binned range in the exact arithmetic too.
@@ -413,19 +502,28 @@ __device__ __forceinline__ int subbox_set(int lo, int hi, int nf, int cps, int n
 // flight while this pair is processed (index whi at most: still inside the
 // staging area); two register sets take turns, so the prefetched shape is
 // never copied.
-template <int KIND, int FULL, int VAR, int SLOTS>
+template <int KIND, int FULL, int VAR, int SLOTS, int SHORT>
 __device__ __forceinline__ void shape_loop(const Params& P, const TablesSmem& T, const float4* A, const float4* B,
                                            const float2* C, const int* I, int wlo, int whi, const MixedPos& p0,
                                            const HistView& hv, const Work& w, const Out& o, const Scales& sc,
                                            double twoR, int label_a, unsigned long long& my_binned) {
+  // (short path: the lane's copy of the histogram and the high words)
+  unsigned* const hk = hv.cnt + p0.base;
+  int* const hh = hv.dd_hi + p0.hbase;
+  auto pair = [&](const float4& a, const float4& b, int i) {
+    if (SHORT)
+      mixed_pair_short<SLOTS>(P, T, a, b, C, I, i, p0, hk, hh, w, o, label_a, my_binned);
+    else
+      mixed_pair<KIND, FULL, VAR, SLOTS>(P, T, a, b, C, I, i, p0, hv, w, o, sc, twoR, label_a, my_binned);
+  };
   float4 a0 = A[wlo], b0 = B[wlo];
   for (int i = wlo;;) {
     const float4 a1 = A[i + 1], b1 = B[i + 1];
-    mixed_pair<KIND, FULL, VAR, SLOTS>(P, T, a0, b0, C, I, i, p0, hv, w, o, sc, twoR, label_a, my_binned);
+    pair(a0, b0, i);
     if (++i >= whi) break;
     a0 = A[i + 1];
     b0 = B[i + 1];
-    mixed_pair<KIND, FULL, VAR, SLOTS>(P, T, a1, b1, C, I, i, p0, hv, w, o, sc, twoR, label_a, my_binned);
+    pair(a1, b1, i);
     if (++i >= whi) break;
   }
 }
@@ -434,7 +532,7 @@ __device__ __forceinline__ void shape_loop(const Params& P, const TablesSmem& T,
 
 // (a minimum-blocks bound of 4 gives the same 61 registers but code that
 // runs 8% slower on the 4M/1M w step; the register count alone allows 4)
-template <int MIXED, int VAR, int KIND, int FULL>
+template <int MIXED, int VAR, int KIND, int FULL, int SHORT>
 // (4 blocks of 256 threads per SM need 64 registers: asked of the multipole
 // and FP64 variants, which the compiler otherwise takes to 80 or beyond --
 // mixed multipoles 104.0 against 112.7 ms on the 4M/1M step; the mixed w
@@ -455,7 +553,7 @@ __global__ void __launch_bounds__(kThreads, MIA_PAIR_MINB) k_pairs(
   unsigned* hist = reinterpret_cast<unsigned*>(smem + SL.hist);
   float4* wpos = reinterpret_cast<float4*>(smem + SL.wpos);
   unsigned short* ring = reinterpret_cast<unsigned short*>(smem + SL.ring);
-  const int KB = HW;  // >= K * nb
+  const int KB = SHORT ? kHistShort : HW;  // words per replicated array (the short path's stride is fixed)
 
   __shared__ long long s_wu;
   __shared__ int s_ds;
@@ -484,7 +582,7 @@ __global__ void __launch_bounds__(kThreads, MIA_PAIR_MINB) k_pairs(
       T.p_bin[i] = G.p_bin[i];
     }
     if (MIXED)
-      for (int i = tid; i < kLut; i += blockDim.x) T.lut32[i] = G.lut32[i];
+      for (int i = tid; i < kLut; i += blockDim.x) T.lut32[i] = SHORT ? G.lutw[i] : G.lut32[i];
     if (tid == 0) s_ds = -1;
   }
   const unsigned long long n_wu_all = wu_prefix[n_ds];
@@ -654,11 +752,17 @@ __global__ void __launch_bounds__(kThreads, MIA_PAIR_MINB) k_pairs(
       float z = 0.f;
       const int g = u.begin + tid;
       if (tid < S) {
-        // weights times the (power-of-two) fixed-point scales: exact
-        ra = make_float4(w.sxh[g], w.syh[g], w.szh[g], w.swsf[g] * sc.sc_dd);
-        rb = make_float4(w.sxl[g], w.syl[g], w.szl[g], w.swef[g] * sc.sc_sp);
+        // weights times the (power-of-two) fixed-point scales: exact; the
+        // short path pairs (x, y) hi, (x, y) lo, (z hi, z lo) and the weights
+        if (SHORT) {
+          ra = make_float4(w.sxh[g], w.syh[g], w.sxl[g], w.syl[g]);
+          rb = make_float4(w.szh[g], w.szl[g], w.swsf[g] * sc.sc_dd, w.swef[g] * sc.sc_sp);
+        } else {
+          ra = make_float4(w.sxh[g], w.syh[g], w.szh[g], w.swsf[g] * sc.sc_dd);
+          rb = make_float4(w.sxl[g], w.syl[g], w.szl[g], w.swef[g] * sc.sc_sp);
+        }
         rc = make_float2(w.saxf[g], w.sayf[g]);
-        z = ra.z + rb.z;
+        z = SHORT ? rb.x + rb.y : ra.z + rb.z;
         if (!(z == z)) z = INFINITY;  // the ranks below must form a permutation
         zs[tid] = z;
       }
@@ -854,6 +958,12 @@ __global__ void __launch_bounds__(kThreads, MIA_PAIR_MINB) k_pairs(
           MixedPos p0;
           load_mixed_pos(P, w, seg_begin, seg_pref, seg_shift, region, tb + tid, total, seg, p0);
           p0.base += copy_off;
+          if (SHORT) {
+            p0.loff = (float)(P.p_off_d - ((double)p0.zh + (double)p0.zl) * (double)P.p_inv32);
+            p0.nh = make_float2(-p0.xh, -p0.yh);
+            p0.nl = make_float2(-p0.xl, -p0.yl);
+            p0.w2 = make_float2(p0.w, p0.w);
+          }
           // positions of the unit's region only (all but points on sub-box
           // faces): no per-pair slot check
           const bool all_in = __all_sync(0xffffffffu, !p0.valid || p0.slot >= 0);
@@ -891,9 +1001,11 @@ __global__ void __launch_bounds__(kThreads, MIA_PAIR_MINB) k_pairs(
           const int whi = __reduce_max_sync(0xffffffffu, i_hi);
           if (p0.valid && wlo < whi) {
             if (all_in)
-              shape_loop<KIND, FULL, VAR, 1>(P, T, A, B, C, I, wlo, whi, p0, hv, w, o, sc, twoR, u.label, my_binned);
+              shape_loop<KIND, FULL, VAR, 1, SHORT>(P, T, A, B, C, I, wlo, whi, p0, hv, w, o, sc, twoR, u.label,
+                                                    my_binned);
             else
-              shape_loop<KIND, FULL, VAR, 0>(P, T, A, B, C, I, wlo, whi, p0, hv, w, o, sc, twoR, u.label, my_binned);
+              shape_loop<KIND, FULL, VAR, 0, SHORT>(P, T, A, B, C, I, wlo, whi, p0, hv, w, o, sc, twoR, u.label,
+                                                    my_binned);
           }
         }
       } else {
@@ -1164,7 +1276,7 @@ template <int MIXED, int VAR, int KIND, int FULL>
 cudaError_t hist_words_for(const Params& P, int& hw) {
   hw = P.nb;
   if (!MIXED) return cudaSuccess;
-  auto kern = k_pairs<MIXED, VAR, KIND, FULL>;
+  auto kern = k_pairs<MIXED, VAR, KIND, FULL, 0>;
   int dev = 0, smem_sm = 0, smem_blk = 0, reserved = 0, b_reg = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
@@ -1191,13 +1303,34 @@ cudaError_t hist_words_for(const Params& P, int& hw) {
   return cudaSuccess;
 }
 
+// The short w path: histogram arrays of kHistShort words (as many copies as
+// they hold), the blocks per SM that this leaves.
+cudaError_t launch_short(const Params& P, const Dataset* ds, int n_ds, const unsigned long long* wu_prefix,
+                         unsigned long long* wu_next, cudaStream_t st, int num_sms) {
+  auto kern = k_pairs<1, 0, MIA_KIND_W, 0, 1>;
+  const size_t smem = smem_layout(P.shapes_per_unit, kHistShort, P.nb, 1, 0).total;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int per_sm = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem);
+  if (e != cudaSuccess) return e;
+#ifdef MIA_MAX_BLOCKS_PER_SM
+  if (per_sm > MIA_MAX_BLOCKS_PER_SM) per_sm = MIA_MAX_BLOCKS_PER_SM;
+#endif
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  kern<<<num_sms * per_sm, kThreads, smem, st>>>(P, ds, n_ds, wu_prefix, wu_next, kHistShort);
+  return cudaGetLastError();
+}
+
 template <int MIXED, int VAR, int KIND, int FULL>
 cudaError_t launch_one(const Params& P, const Dataset* ds, int n_ds, const unsigned long long* wu_prefix,
                        unsigned long long* wu_next, cudaStream_t st, int num_sms) {
+  if (MIXED && !VAR && KIND == MIA_KIND_W && !FULL && (P.nb | 1) <= kHistShort)
+    return launch_short(P, ds, n_ds, wu_prefix, wu_next, st, num_sms);
   int hw = 0;
   cudaError_t e = hist_words_for<MIXED, VAR, KIND, FULL>(P, hw);
   if (e != cudaSuccess) return e;
-  auto kern = k_pairs<MIXED, VAR, KIND, FULL>;
+  auto kern = k_pairs<MIXED, VAR, KIND, FULL, 0>;
   const int hw0 = P.nb;
   int per_sm = 0, per_sm0 = 0;
   size_t smem = smem_layout(P.shapes_per_unit, hw0, hw0, MIXED, VAR).total;
