@@ -29,7 +29,7 @@ import os
 
 KNOBS = ("cell_size", "cell_refine", "shapes_per_unit", "cell_size_los", "cell_refine_los")
 DEFAULT = {"cell_size": 0.0, "cell_refine": 0, "shapes_per_unit": 0, "cell_size_los": 0.0, "cell_refine_los": 0}
-_VERSION = "g8"  # per-region work units, two descent rounds, long-cell family
+_VERSION = "g9"  # short pair path (fixed histogram stride), per-region work units, long-cell family
 
 
 def cache_path():

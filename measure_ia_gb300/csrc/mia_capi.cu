@@ -386,10 +386,10 @@ static void build_tables(const mia_config* cfg, Tables* T, int* lut_base) {
     T->lutw[b] = clean ? (unsigned short)(T->q_bin[iv] >= 0 ? T->q_bin[iv] * cfg->n_p : kLutReject)
                        : (unsigned short)(iv | 0x8000);
   }
-  // (clamped indices: bucket 0 lies an octave below the first guard band, so
-  // every q under it has bin q_bin[0]; a q over the last bucket is walked from
-  // that bucket's entry, or takes q_bin[n] when the bucket is clean and past
-  // every band)
+  // the short path's wrapped index: bucket 0 lies an octave below the first
+  // guard band, so every q under the table has bin q_bin[0]
+  T->lutw[kLut - 1] = (unsigned short)(n > 0 && T->q_bin[0] >= 0 ? T->q_bin[0] * cfg->n_p
+                                                                   : (n > 0 ? kLutReject : T->lutw[kLut - 1]));
 }
 
 }  // namespace mia
@@ -664,14 +664,14 @@ void make_params(const mia_config* cfg, const Plan& plan, const Tables& T, int l
     P.p_half_in = 0.5f - P.p_guard;
     P.p_off32 = (float)(-p0 * inv);
     // short w path: t = fma(z_lo, inv, fma(z_hi, inv, off_p)) from the shape's
-    // hi/lo line-of-sight coordinate and the position's offset off_p = -(p_lo
-    // + z_p) inv rounded to FP32.  Errors, in bins: the FP32 inverse width
-    // ((n_p + 1) 2^-24 over the binned range), off_p's rounding (|off_p| <=
-    // (L + 2 reach + |p_lo|) inv, 2^-24 of it) and the two FMA roundings
-    // ((n_p + 1) 2^-24 each); taken four times over
-    P.p_off_d = -p0 * inv;
+    // hi/lo line-of-sight coordinate and the position's offset off_p =
+    // fma(-z_lo, inv, fma(-z_hi, inv, -p_lo inv)) in FP32.  Errors, in bins:
+    // the FP32 inverse width ((n_p + 1) 2^-24 over the binned range), the
+    // rounding of -p_lo inv (|p_lo| inv 2^-24), off_p's two FMA roundings
+    // (|off_p| <= (L + 2 reach + |p_lo|) inv, 2^-24 of it each) and the two
+    // FMA roundings of t ((n_p + 1) 2^-24 each); taken four times over
     const double lmax = (cfg->boxsize + 2.0 * plan.range_los + fabs(p0)) * inv;
-    const double ew = (3.0 * (cfg->n_p + 1) + lmax) * (u * 0.5);
+    const double ew = (3.0 * (cfg->n_p + 1) + 2.0 * lmax + fabs(p0) * inv) * (u * 0.5);
     P.p_guard_w = (float)fmin(0.25, fmax(4.0 * ew, 1.0 / 1048576.0));
   }
   P.c_guard = 1e-12f;
@@ -682,6 +682,13 @@ void make_params(const mia_config* cfg, const Plan& plan, const Tables& T, int l
   P.range_los32 = f32_down(plan.range_los);
   const int nq = cfg->n_qbreak;
   P.q_cut = (nq > 0 && cfg->q_bin[nq] < 0) ? T.q_hi32[nq - 1] : INFINITY;
+  // the short pair path looks up q <= q_cut only, in a bucket below the last one
+  P.short_ok = 0;
+  if (P.q_cut < INFINITY) {
+    unsigned qb;
+    memcpy(&qb, &P.q_cut, 4);
+    P.short_ok = (qb >> (23 - kLutMantBits)) - (unsigned)lut_base < (unsigned)(kLut - 1) ? 1 : 0;
+  }
   // each coordinate rounded to FP32 (2^-24 L), their difference and L - |d|
   // (2^-24 L each): 2^-22 L in all, taken four times over
   P.pre_margin = (float)(cfg->boxsize * (1.0 / 1048576.0));

@@ -57,9 +57,10 @@ struct Tables {
   unsigned short lut32[kLut];
   // the same buckets for the w kernel's short pair path: a clean bucket holds
   // ib * n_p (kLutReject when not binned), a bucket touching a guard band the
-  // first breakpoint to compare against | 0x8000; the kernel clamps bucket
-  // indices to [0, kLut), so entry 0 and entry kLut - 1 also hold for every q
-  // below and above the table
+  // first breakpoint to compare against | 0x8000.  That path only looks up
+  // q <= q_cut, which lies below the last bucket, and an index below the
+  // table wraps (unsigned) to the last bucket: it holds the bin under the
+  // first breakpoint
   unsigned short lutw[kLut];
   // bin edges (r_bins; pi_bins or mu_r_bins)
   double r_edges[MIA_MAX_BINS_R + 1];
@@ -282,8 +283,8 @@ struct Params {
   float p_off32;                // -p_lo * p_inv: t = fma(v, p_inv, p_off)
   float p_guard;                // fraction of a bin treated as ambiguous at each edge
   float p_half_in;              // 0.5 - p_guard: |frac(t) - 0.5| above it is an edge
-  double p_off_d;               // -p_lo * n_p / (p_hi - p_lo) in FP64 (per-position offset of the short w path)
   float p_guard_w;              // short w path: |t - rint(t)| below it is an edge (t from the shape's hi/lo z)
+  int short_ok;                 // the short pair path applies (finite q_cut inside the lookup table)
   float c_guard;                // sin^2(phi) below which the exact FP64 cos(phi) decides
   float wrap_guard;
   float los_cut;                // |Pi| above this is surely outside the Pi bins (w)

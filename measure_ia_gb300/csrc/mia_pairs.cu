@@ -396,19 +396,33 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
 //    z_lo, w_s, w_s e) (scaled weights), so (dx, dy) and the two weight
 //    products come out of register pairs; each half rounds as the scalar
 //    operation would.
-template <int SLOTS>
+//  * Multipoles: the same, with mu = Pi rsqrt(r^2) and the generic form's
+//    bin coordinate and guard; r_p > rp_cut as the generic form decides it.
+template <int KIND, int SLOTS>
 __device__ __forceinline__ void mixed_pair_short(const Params& P, const TablesSmem& T, const float4& a,
                                                  const float4& b, const float2* C, const int* I, int i,
                                                  const MixedPos& p, unsigned* hk, int* hh, const Work& w,
                                                  const Out& o, int label_a, unsigned long long& my_binned) {
-  const float t = fmaf(b.y, P.p_inv32, fmaf(b.x, P.p_inv32, p.loff));
   const float2 d = __fadd2_rn(__fadd2_rn(make_float2(a.x, a.y), p.nh), __fadd2_rn(make_float2(a.z, a.w), p.nl));
   const float dx = d.x, dy = d.y;
   const float qp = fmaf(dx, dx, dy * dy);
-  const int bucket = min(max((int)(__float_as_uint(qp) >> (23 - kLutMantBits)) - P.lut32_base, 0), kLut - 1);
+  float t, q, dz = 0.0f;
+  if (KIND == MIA_KIND_W) {
+    t = fmaf(b.y, P.p_inv32, fmaf(b.x, P.p_inv32, p.loff));
+    q = qp;
+  } else {
+    dz = (b.x - p.zh) + (b.y - p.zl);
+    q = fmaf(dz, dz, qp);
+  }
+  // surely beyond the last binned separation (whole warps leave here often)
+  if (q > P.q_cut) return;
+  // (q <= q_cut lies in the table; a q below it wraps to the last entry,
+  // which holds the bin under the first breakpoint)
+  const unsigned bucket = min((__float_as_uint(q) >> (23 - kLutMantBits)) - (unsigned)P.lut32_base, (unsigned)kLut - 1u);
   int e = T.lut32[bucket];
+  if (KIND != MIA_KIND_W) t = fmaf(dz * rsqrtf(q), P.p_inv32, P.p_off32);
   const int jb = __float2int_rd(t);
-  const bool pi_edge = fabsf(t - rintf(t)) < P.p_guard_w;
+  const bool pi_edge = fabsf(t - rintf(t)) < (KIND == MIA_KIND_W ? P.p_guard_w : P.p_guard);
   bool edge = pi_edge;
   if ((e >= kLutReject) | ((unsigned)jb >= (unsigned)P.n_p)) {
     // Pi surely outside the bins (an edge at 0 or n_p goes on to the re-test)
@@ -416,12 +430,24 @@ __device__ __forceinline__ void mixed_pair_short(const Params& P, const TablesSm
     if (e == kLutReject) return;
     if (e & 0x8000) {
       int iv = e & 0x7fff;
-      while (iv < P.n_qbreak && qp >= T.q_hi32[iv]) ++iv;
-      const bool q_edge = iv < P.n_qbreak && qp >= T.q_lo32[iv];
+      while (iv < P.n_qbreak && q >= T.q_hi32[iv]) ++iv;
+      const bool q_edge = iv < P.n_qbreak && q >= T.q_lo32[iv];
       const int ib = T.q_bin[iv];
       if (ib < 0 && !q_edge) return;
       edge |= q_edge;
       e = ib * P.n_p;  // (not used when ib < 0: the pair is an edge)
+    }
+  }
+  if (KIND != MIA_KIND_W) {
+    if (P.rp_cut2 == 0.0) {
+      if (!(qp > 0.0f) && !edge) return;  // r_p > rp_cut = 0 (measure_m_box_jk.py:637)
+    } else {
+      const float rc2 = (float)P.rp_cut2;
+      if (qp < rc2 * (1.0f - 1e-5f)) {
+        if (!edge) return;
+      } else if (qp <= rc2 * (1.0f + 1e-5f)) {
+        edge = true;
+      }
     }
   }
   const float2 cxy = C[i];
@@ -512,7 +538,7 @@ __device__ __forceinline__ void shape_loop(const Params& P, const TablesSmem& T,
   int* const hh = hv.dd_hi + p0.hbase;
   auto pair = [&](const float4& a, const float4& b, int i) {
     if (SHORT)
-      mixed_pair_short<SLOTS>(P, T, a, b, C, I, i, p0, hk, hh, w, o, label_a, my_binned);
+      mixed_pair_short<KIND, SLOTS>(P, T, a, b, C, I, i, p0, hk, hh, w, o, label_a, my_binned);
     else
       mixed_pair<KIND, FULL, VAR, SLOTS>(P, T, a, b, C, I, i, p0, hv, w, o, sc, twoR, label_a, my_binned);
   };
@@ -527,6 +553,7 @@ __device__ __forceinline__ void shape_loop(const Params& P, const TablesSmem& T,
     if (++i >= whi) break;
   }
 }
+
 
 // ---- the persistent pair kernel ----------------------------------------------
 
@@ -959,7 +986,7 @@ __global__ void __launch_bounds__(kThreads, MIA_PAIR_MINB) k_pairs(
           load_mixed_pos(P, w, seg_begin, seg_pref, seg_shift, region, tb + tid, total, seg, p0);
           p0.base += copy_off;
           if (SHORT) {
-            p0.loff = (float)(P.p_off_d - ((double)p0.zh + (double)p0.zl) * (double)P.p_inv32);
+            if (KIND == MIA_KIND_W) p0.loff = fmaf(-p0.zl, P.p_inv32, fmaf(-p0.zh, P.p_inv32, P.p_off32));
             p0.nh = make_float2(-p0.xh, -p0.yh);
             p0.nl = make_float2(-p0.xl, -p0.yl);
             p0.w2 = make_float2(p0.w, p0.w);
@@ -1305,9 +1332,10 @@ cudaError_t hist_words_for(const Params& P, int& hw) {
 
 // The short w path: histogram arrays of kHistShort words (as many copies as
 // they hold), the blocks per SM that this leaves.
+template <int KIND>
 cudaError_t launch_short(const Params& P, const Dataset* ds, int n_ds, const unsigned long long* wu_prefix,
                          unsigned long long* wu_next, cudaStream_t st, int num_sms) {
-  auto kern = k_pairs<1, 0, MIA_KIND_W, 0, 1>;
+  auto kern = k_pairs<1, 0, KIND, 0, 1>;
   const size_t smem = smem_layout(P.shapes_per_unit, kHistShort, P.nb, 1, 0).total;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -1325,8 +1353,8 @@ cudaError_t launch_short(const Params& P, const Dataset* ds, int n_ds, const uns
 template <int MIXED, int VAR, int KIND, int FULL>
 cudaError_t launch_one(const Params& P, const Dataset* ds, int n_ds, const unsigned long long* wu_prefix,
                        unsigned long long* wu_next, cudaStream_t st, int num_sms) {
-  if (MIXED && !VAR && KIND == MIA_KIND_W && !FULL && (P.nb | 1) <= kHistShort)
-    return launch_short(P, ds, n_ds, wu_prefix, wu_next, st, num_sms);
+  if (MIXED && !VAR && !FULL && P.short_ok && (P.nb | 1) <= kHistShort)
+    return launch_short<KIND>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms);
   int hw = 0;
   cudaError_t e = hist_words_for<MIXED, VAR, KIND, FULL>(P, hw);
   if (e != cudaSuccess) return e;
