@@ -327,7 +327,7 @@ static float f32_up(double v) {
 }
 
 // Host-side construction of the device tables from the configuration.
-static void build_tables(const mia_config* cfg, Tables* T, int* lut_base) {
+static void build_tables(const mia_config* cfg, Tables* T, int* lut_base, bool* short_tables) {
   memset(T, 0, sizeof(Tables));
   const double g = 1.0 / 524288.0;  // 2^-19 relative guard band on q
   for (int j = 0; j < MIA_MAX_BREAKS; ++j) {
@@ -366,15 +366,17 @@ static void build_tables(const mia_config* cfg, Tables* T, int* lut_base) {
   }
   *lut_base = base;
   const int n = cfg->n_qbreak;
+  int n_dirty = 0;
+  *short_tables = true;
   for (int b = 0; b < kLut; ++b) {
     unsigned lo_bits = (unsigned)(b + base) << (23 - kLutMantBits);
     unsigned hi_bits = (unsigned)(b + base + 1) << (23 - kLutMantBits);
     float lo, hi;
     memcpy(&lo, &lo_bits, 4);
     memcpy(&hi, &hi_bits, 4);
-    if (!(lo < INFINITY)) {  // beyond the float range: walk
+    if (!(lo < INFINITY)) {  // beyond the float range: walk (the short path never gets here)
       T->lut32[b] = 0x8000;
-      T->lutw[b] = 0x8000;
+      T->lutw[b] = kLutReject;
       continue;
     }
     int iv = 0;
@@ -383,8 +385,30 @@ static void build_tables(const mia_config* cfg, Tables* T, int* lut_base) {
     // clean bucket: the bin itself (+1, 0 = not binned); otherwise the first
     // breakpoint to compare against, flagged
     T->lut32[b] = clean ? (unsigned short)(T->q_bin[iv] + 1) : (unsigned short)(iv | 0x8000);
-    T->lutw[b] = clean ? (unsigned short)(T->q_bin[iv] >= 0 ? T->q_bin[iv] * cfg->n_p : kLutReject)
-                       : (unsigned short)(iv | 0x8000);
+    auto code = [&](int bin) { return bin >= 0 ? bin * cfg->n_p : kLutReject; };
+    if (clean) {
+      T->lutw[b] = (unsigned short)code(T->q_bin[iv]);
+    } else {
+      // the guard bands that meet this bucket, iv .. last, as one band
+      int last = iv;
+      while (last + 1 < n && T->q_lo32[last + 1] < hi) ++last;
+      const float lo_band = T->q_lo32[iv], hi_band = T->q_hi32[last];
+      const int below = code(T->q_bin[iv]), above = code(T->q_bin[last + 1]);
+      int d = 0;
+      while (d < n_dirty && !(T->qdirty[d].x == lo_band && T->qdirty[d].y == hi_band)) ++d;
+      if (d == n_dirty) {
+        if (n_dirty == MIA_MAX_BREAKS) {
+          *short_tables = false;  // (too many: the generic path walks the breakpoints)
+          d = 0;
+        } else {
+          float fb, fa;
+          memcpy(&fb, &below, 4);
+          memcpy(&fa, &above, 4);
+          T->qdirty[n_dirty++] = make_float4(lo_band, hi_band, fb, fa);
+        }
+      }
+      T->lutw[b] = (unsigned short)(d | 0x8000);
+    }
   }
   // the short path's wrapped index: bucket 0 lies an octave below the first
   // guard band, so every q under the table has bin q_bin[0]
@@ -663,15 +687,15 @@ void make_params(const mia_config* cfg, const Plan& plan, const Tables& T, int l
     P.p_guard = (float)fmin(0.25, fmax(4.0 * et, 1.0 / 1048576.0));
     P.p_half_in = 0.5f - P.p_guard;
     P.p_off32 = (float)(-p0 * inv);
-    // short w path: t = fma(z_lo, inv, fma(z_hi, inv, off_p)) from the shape's
-    // hi/lo line-of-sight coordinate and the position's offset off_p =
-    // fma(-z_lo, inv, fma(-z_hi, inv, -p_lo inv)) in FP32.  Errors, in bins:
-    // the FP32 inverse width ((n_p + 1) 2^-24 over the binned range), the
-    // rounding of -p_lo inv (|p_lo| inv 2^-24), off_p's two FMA roundings
-    // (|off_p| <= (L + 2 reach + |p_lo|) inv, 2^-24 of it each) and the two
-    // FMA roundings of t ((n_p + 1) 2^-24 each); taken four times over
+    // short w path: t = z_s + off_p, with the shape's z_s = fma(z_hi, inv,
+    // z_lo inv) and the position's off_p = fma(-z_lo, inv, fma(-z_hi, inv,
+    // -p_lo inv)) in FP32.  Errors, in bins: the FP32 inverse width ((n_p +
+    // 1) 2^-24 over the binned range), the rounding of -p_lo inv (|p_lo| inv
+    // 2^-24), z_s's and off_p's FMA roundings (|z_s|, |off_p| <= (L + 2 reach
+    // + |p_lo|) inv, 2^-24 of it each, three in all) and the rounding of t
+    // ((n_p + 1) 2^-24); taken four times over
     const double lmax = (cfg->boxsize + 2.0 * plan.range_los + fabs(p0)) * inv;
-    const double ew = (3.0 * (cfg->n_p + 1) + 2.0 * lmax + fabs(p0) * inv) * (u * 0.5);
+    const double ew = (2.0 * (cfg->n_p + 1) + 3.0 * lmax + fabs(p0) * inv) * (u * 0.5);
     P.p_guard_w = (float)fmin(0.25, fmax(4.0 * ew, 1.0 / 1048576.0));
   }
   P.c_guard = 1e-12f;
@@ -761,7 +785,8 @@ int mia_batch_prepare(mia_context* ctx, const mia_config* cfg, int n, const mia_
   static thread_local Tables host_tables;
   static thread_local std::vector<Dataset> host_ds;
   int lut_base = 0;
-  build_tables(cfg, &host_tables, &lut_base);
+  bool short_tables = true;
+  build_tables(cfg, &host_tables, &lut_base, &short_tables);
   host_ds.resize(n);
   for (int i = 0; i < n; ++i) {
     make_dataset(bp.plans[i], b + bp.off[i], cats[i], results[i], lay, &host_ds[i]);
@@ -788,9 +813,11 @@ int mia_batch_enqueue(mia_context* ctx, const mia_config* cfg, int n, const mia_
   unsigned char* b = static_cast<unsigned char*>(workspace);
   int lut_base = 0;
   static thread_local Tables tq;  // host copy: only the guard values enter the launch parameters
-  build_tables(cfg, &tq, &lut_base);
+  bool short_tables = true;
+  build_tables(cfg, &tq, &lut_base, &short_tables);
   Params P;
   make_params(cfg, bp.plans[0], tq, lut_base, &P);
+  if (!short_tables) P.short_ok = 0;
   BatchHeader* hdr = reinterpret_cast<BatchHeader*>(b);
   const Dataset* ds_dev = reinterpret_cast<const Dataset*>(b + bp.ds_off);
   unsigned long long* prefix = reinterpret_cast<unsigned long long*>(b + bp.prefix_off);

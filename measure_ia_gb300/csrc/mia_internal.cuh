@@ -55,13 +55,19 @@ struct Tables {
   // lookup tables: bucket -> bin + 1, or first breakpoint index | 0x8000
   // (the bucket touches a guard band)
   unsigned short lut32[kLut];
-  // the same buckets for the w kernel's short pair path: a clean bucket holds
-  // ib * n_p (kLutReject when not binned), a bucket touching a guard band the
-  // first breakpoint to compare against | 0x8000.  That path only looks up
+  // the same buckets for the short pair path: a clean bucket holds ib * n_p
+  // (kLutReject when not binned), a bucket touching a guard band its qdirty
+  // entry | 0x8000.  That path only looks up
   // q <= q_cut, which lies below the last bucket, and an index below the
   // table wraps (unsigned) to the last bucket: it holds the bin under the
   // first breakpoint
   unsigned short lutw[kLut];
+  // short path, buckets touching a guard band (lutw entry 0x8000 | index):
+  // (band_lo, band_hi, code below, code above) -- the union of the guard
+  // bands that meet the bucket; a q below it takes the code below (ib * n_p
+  // or kLutReject, as int bits), above it the code above, inside it is an
+  // edge
+  float4 qdirty[MIA_MAX_BREAKS];
   // bin edges (r_bins; pi_bins or mu_r_bins)
   double r_edges[MIA_MAX_BINS_R + 1];
   double p_edges[MIA_MAX_BINS_P + 1];

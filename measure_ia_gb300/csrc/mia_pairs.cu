@@ -64,11 +64,16 @@ __host__ __device__ inline size_t hist_u32_words(int hw, int knb, int mixed, int
 }
 
 struct TablesSmem {
-  long long q_key[MIA_MAX_BREAKS];
+  union {
+    struct {  // FP64 form: the breakpoint keys
+      long long q_key[MIA_MAX_BREAKS];
+      long long p_key[MIA_MAX_BREAKS];
+    };
+    float4 qdirty[MIA_MAX_BREAKS];  // short mixed path: the guard bands of lutw's buckets
+  };
   int q_bin[MIA_MAX_BREAKS + 1];
   float q_lo32[MIA_MAX_BREAKS];
   float q_hi32[MIA_MAX_BREAKS];
-  long long p_key[MIA_MAX_BREAKS];
   int p_bin[MIA_MAX_BREAKS + 1];
   unsigned short lut32[kLut];
 };
@@ -380,20 +385,21 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
 
 // The w kernel's short pair path (mixed form, local neighbourhoods, no
 // variance terms): the same decisions as mixed_pair in fewer instructions.
-//  * Pi bin: t = (Pi - p_lo) n_p / (p_hi - p_lo) from two FMAs on the shape's
-//    hi/lo line-of-sight coordinate and the position's offset p.loff, bin =
+//  * Pi bin: t = (Pi - p_lo) n_p / (p_hi - p_lo) as the shape's staged
+//    z n_p / (p_hi - p_lo) plus the position's offset p.loff, bin =
 //    floor(t); t within p_guard_w of an integer is an edge.  No separate
 //    line-of-sight cut: a pair outside the Pi range has its bin outside
 //    [0, n_p).
-//  * r bin: the lutw bucket of q (indices clamped to the table) holds
-//    ib * n_p, kLutReject, or a breakpoint to walk from; one test covers a
-//    reject, a walk and a Pi bin outside the range.
+//  * r bin: the lutw bucket of q holds ib * n_p, kLutReject, or (for a
+//    bucket touching a guard band) that band with the codes below and above
+//    it; one test covers a reject, a band and a Pi bin outside the range.
 //  * Histogram words sit kHistShort words apart, so one address serves the
 //    four atomics.  `hk` is the lane's copy of the unit's histogram, `hh` the
 //    high words.
 //  * Paired FP32 instructions (FADD2, FMUL2) where both halves have the same
-//    operation: the staged shape is a = (x_hi, y_hi, x_lo, y_lo), b = (z_hi,
-//    z_lo, w_s, w_s e) (scaled weights), so (dx, dy) and the two weight
+//    operation: the staged shape is a = (x_hi, y_hi, x_lo, y_lo), b = (z
+//    term, z_lo, w_s, w_s e) (scaled weights; the z term is z n_p / (p_hi -
+//    p_lo) for w, z_hi for multipoles), so (dx, dy) and the two weight
 //    products come out of register pairs; each half rounds as the scalar
 //    operation would.
 //  * Multipoles: the same, with mu = Pi rsqrt(r^2) and the generic form's
@@ -408,7 +414,7 @@ __device__ __forceinline__ void mixed_pair_short(const Params& P, const TablesSm
   const float qp = fmaf(dx, dx, dy * dy);
   float t, q, dz = 0.0f;
   if (KIND == MIA_KIND_W) {
-    t = fmaf(b.y, P.p_inv32, fmaf(b.x, P.p_inv32, p.loff));
+    t = b.x + p.loff;
     q = qp;
   } else {
     dz = (b.x - p.zh) + (b.y - p.zl);
@@ -427,16 +433,13 @@ __device__ __forceinline__ void mixed_pair_short(const Params& P, const TablesSm
   if ((e >= kLutReject) | ((unsigned)jb >= (unsigned)P.n_p)) {
     // Pi surely outside the bins (an edge at 0 or n_p goes on to the re-test)
     if ((unsigned)jb >= (unsigned)P.n_p && ((unsigned)jb + 1u > (unsigned)P.n_p + 1u || !pi_edge)) return;
-    if (e == kLutReject) return;
-    if (e & 0x8000) {
-      int iv = e & 0x7fff;
-      while (iv < P.n_qbreak && q >= T.q_hi32[iv]) ++iv;
-      const bool q_edge = iv < P.n_qbreak && q >= T.q_lo32[iv];
-      const int ib = T.q_bin[iv];
-      if (ib < 0 && !q_edge) return;
-      edge |= q_edge;
-      e = ib * P.n_p;  // (not used when ib < 0: the pair is an edge)
+    if (e & 0x8000) {  // a bucket touching a guard band: below, inside (an edge) or above the band
+      const float* D = reinterpret_cast<const float*>(&T.qdirty[e & 0x7fff]);
+      const bool below = q < D[0], above = q >= D[1];
+      e = below ? __float_as_int(D[2]) : (above ? __float_as_int(D[3]) : 0);
+      edge |= !(below || above);
     }
+    if (e == kLutReject) return;
   }
   if (KIND != MIA_KIND_W) {
     if (P.rp_cut2 == 0.0) {
@@ -599,10 +602,14 @@ __global__ void __launch_bounds__(kThreads, MIA_PAIR_MINB) k_pairs(
   {
     const Tables& G = *ds[0].w.tables;
     for (int i = tid; i < MIA_MAX_BREAKS; i += blockDim.x) {
-      T.q_key[i] = G.q_key[i];
+      if (SHORT) {
+        T.qdirty[i] = G.qdirty[i];
+      } else {
+        T.q_key[i] = G.q_key[i];
+        T.p_key[i] = G.p_key[i];
+      }
       T.q_lo32[i] = G.q_lo32[i];
       T.q_hi32[i] = G.q_hi32[i];
-      T.p_key[i] = G.p_key[i];
     }
     for (int i = tid; i < MIA_MAX_BREAKS + 1; i += blockDim.x) {
       T.q_bin[i] = G.q_bin[i];
@@ -782,14 +789,18 @@ __global__ void __launch_bounds__(kThreads, MIA_PAIR_MINB) k_pairs(
         // weights times the (power-of-two) fixed-point scales: exact; the
         // short path pairs (x, y) hi, (x, y) lo, (z hi, z lo) and the weights
         if (SHORT) {
+          // (w: the line-of-sight coordinate times n_p / (p_hi - p_lo) in one
+          // float, the shape's share of the Pi bin coordinate)
           ra = make_float4(w.sxh[g], w.syh[g], w.sxl[g], w.syl[g]);
-          rb = make_float4(w.szh[g], w.szl[g], w.swsf[g] * sc.sc_dd, w.swef[g] * sc.sc_sp);
+          const float zh = w.szh[g], zl = w.szl[g];
+          rb = make_float4(KIND == MIA_KIND_W ? fmaf(zh, P.p_inv32, zl * P.p_inv32) : zh, zl,
+                           w.swsf[g] * sc.sc_dd, w.swef[g] * sc.sc_sp);
         } else {
           ra = make_float4(w.sxh[g], w.syh[g], w.szh[g], w.swsf[g] * sc.sc_dd);
           rb = make_float4(w.sxl[g], w.syl[g], w.szl[g], w.swef[g] * sc.sc_sp);
         }
         rc = make_float2(w.saxf[g], w.sayf[g]);
-        z = SHORT ? rb.x + rb.y : ra.z + rb.z;
+        z = SHORT ? w.szh[g] + w.szl[g] : ra.z + rb.z;
         if (!(z == z)) z = INFINITY;  // the ranks below must form a permutation
         zs[tid] = z;
       }
