@@ -293,3 +293,37 @@ def test_large_box_geometry_jk125(kind, precision, tmp_path):
     rtol = FP64_RTOL if precision == "fp64" else MIXED_RTOL
     for path, v in ref.items():
         _close(store.read(path), v, rtol, path)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("kind", ["w", "m"])
+def test_narrow_r_bins(kind, precision, tmp_path):
+    """60 log r bins over 1.0-1.2 Mpc/h: adjacent breakpoints of q = r^2 lie
+    0.6% apart, so a 1/64-octave bucket of the mixed form's lookup table can
+    hold the guard bands of two of them, and r_min / r_max coincide with the
+    first and last bin edges (tree membership).  The short pair path merges
+    the bands that meet a bucket into one; a q inside it goes to the FP64
+    re-test.  Counts per (bin, region) bit-exact against the oracle, values as
+    in the sweep."""
+    from measure_ia_gb300 import MeasureIABox, open_output
+    from measure_ia_gb300.catalogs import neyman_scott_catalog
+    L = 60.0
+    r_min, r_max, n_r, n_p, pi_max = 1.0, 1.2, 60, 4, 3.0
+    data = neyman_scott_catalog(600, L, 8000, 61, mean_children=60, sigma=1.0)
+    b = O.Binning(boxsize=L, r_min=r_min, r_max=r_max, num_bins_r=n_r, num_bins_pi=n_p, pi_max=pi_max)
+    ref = dict(O.measure(kind, b, _copy(data), "nb", "both", 8, None, "distortion", "tree"))
+    c = ref.pop("__counts__")
+    out = str(tmp_path / "nb.hdf5")
+    box = MeasureIABox(_copy(data), out, None, None, [r_min, r_max], n_r, n_p, pi_max, boxsize=L, num_nodes=1,
+                       precision=precision)
+    fn = box.measure_xi_w if kind == "w" else box.measure_xi_multipoles
+    fn("nb", "both", 8, temp_file_path=str(tmp_path))
+    m = box.last_measurement
+    assert c.npairs.sum() > 20000
+    np.testing.assert_array_equal(m.npairs[0], c.npairs)
+    np.testing.assert_array_equal(m.npairs[1:], c.npairs_jk)
+    store = open_output(out)
+    assert set(store.keys()) == set(ref)
+    rtol = FP64_RTOL if precision == "fp64" else MIXED_RTOL
+    for path, v in ref.items():
+        _close(store.read(path), v, rtol, path)
