@@ -547,7 +547,8 @@ def run_large(args, local):
                 "accuracy_mixed_vs_fp64": _errors(m64, m, (("proj_gp", "w_g+"), ("proj_gg", "w_gg")))}
     return {"metric": "binned pairs/s, w_gg+w_g+ 125JK, 1000 Mpc/h box, mixed form",
             "value": m.stats["binned_pairs"] / (ms / 1e3), "unit": "binned pairs/s", "ms_per_step": ms,
-            "step_ms": per, "binned_pairs_per_step": m.stats["binned_pairs"], "knobs": pc.knobs, "fp64_form": fp64,
+            "step_ms": per, "binned_pairs_per_step": m.stats["binned_pairs"],
+            "edge_pairs_retested": m.stats.get("edge_pairs"), "knobs": pc.knobs, "fp64_form": fp64,
             "config": {"workload": "25M positions / 5M shapes, 1000 Mpc/h, 15x20 bins, 125 jackknife (config 4)",
                        "n_positions": int(len(data["Position"])), "n_shapes": int(len(data["Position_shape_sample"]))}}
 

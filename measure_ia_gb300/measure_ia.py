@@ -36,6 +36,21 @@ from .base import BaseHelpers, JackknifeCovariance
 from .sim_info import SimInfo
 
 
+def _all_finite(a) -> bool:
+    """No NaN or infinity in ``a``: the dot product of ``a`` with itself is
+    finite when every element is (one BLAS pass, no temporary array); only a
+    non-finite result, which large finite elements can also give by
+    overflowing, needs the element-wise test."""
+    if hasattr(a, "is_cuda"):  # a torch tensor
+        import torch
+        return bool(torch.isfinite(a).all())
+    a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+    with np.errstate(over="ignore", invalid="ignore"):
+        if np.isfinite(np.dot(a, a)):
+            return True
+    return bool(np.all(np.isfinite(a)))
+
+
 def _cube_root_exact(n):
     """(root, exact) like sympy.integer_nthroot(n, 3)."""
     r = int(round(n ** (1.0 / 3.0)))
@@ -159,12 +174,12 @@ class MeasureIABox(SimInfo, BaseHelpers, JackknifeCovariance):
         L_sub, layout = self._validate(corr_type, num_jk, temp_file_path)
         cat = self._select(masks)
         for key in ("weight", "weight_shape_sample", "q"):
-            if not np.all(np.isfinite(np.asarray(cat[key], dtype=np.float64))):
+            if not _all_finite(cat[key]):
                 # the reference carries these into NaN sums (a NaN q or shape
                 # weight makes its responsivity, and so every S+D bin, NaN)
                 raise ValueError(f"'{key}' values must be finite")
         precision = self.precision
-        if precision == "mixed" and not np.all(np.isfinite(np.asarray(cat["Axis_Direction"], dtype=np.float64))):
+        if precision == "mixed" and not _all_finite(cat["Axis_Direction"]):
             # a non-finite axis gives e+ = ex = 0 in the reference (NaN -> 0,
             # measure_w_box_jk.py:599-600); the FP64 form repeats that exactly
             warnings.warn("mixed form: non-finite Axis_Direction, measuring in the FP64 form", RuntimeWarning)
