@@ -383,8 +383,9 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
   }
 }
 
-// The w kernel's short pair path (mixed form, local neighbourhoods, no
-// variance terms): the same decisions as mixed_pair in fewer instructions.
+// The short pair path of the mixed form (local neighbourhoods, no variance
+// terms; w and multipoles): the same decisions as mixed_pair in fewer
+// instructions.
 //  * Pi bin: t = (Pi - p_lo) n_p / (p_hi - p_lo) as the shape's staged
 //    z n_p / (p_hi - p_lo) plus the position's offset p.loff, bin =
 //    floor(t); t within p_guard_w of an integer is an edge.  No separate

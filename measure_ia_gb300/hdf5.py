@@ -26,6 +26,7 @@ built on, so chunked files have only been read back by this module.
 
 from __future__ import annotations
 
+import functools
 import mmap
 import os
 import struct
@@ -176,26 +177,35 @@ def _write_chunked(img: _Image, v: np.ndarray, dt: np.dtype, chunk_rows: int, le
     return addr
 
 
+@functools.lru_cache(maxsize=256)
+def _contiguous_header(shape, dtype_str):
+    """Object header of a contiguous dataset of this shape and type, with the
+    layout message's address and size left to fill in: (bytes, offset of the
+    address field).  Datasets of one shape and type share everything else."""
+    dt = np.dtype(dtype_str)
+    hdr = _object_header([
+        _message(_MSG_DATASPACE, _dataspace(shape)),
+        _message(_MSG_DATATYPE, _datatype(dt), flags=1),
+        _message(_MSG_FILL, bytes([2, 2, 2, 1]) + struct.pack("<I", 0), flags=1),
+        _message(_MSG_LAYOUT, struct.pack("<BBQQ", 3, 1, UNDEF, 0))])
+    # the layout message is last: its data (version, class, address, size) ends
+    # the header after 6 bytes of padding to 8
+    return hdr, len(hdr) - 6 - 16
+
+
 def _write_dataset(img: _Image, value: np.ndarray, chunks=None) -> int:
     v = np.asarray(value)
     if v.dtype.kind == "b":
         raise TypeError("boolean datasets are not supported by the HDF5 writer")
     dt = v.dtype.newbyteorder("<") if v.dtype.byteorder != "|" else v.dtype
-    _datatype(np.dtype(dt))
+    hdr, at = _contiguous_header(tuple(int(d) for d in v.shape), np.dtype(dt).str)
     if chunks:
         return _write_chunked(img, v, np.dtype(dt), chunks, 4)
     raw = np.ascontiguousarray(v, dtype=dt).tobytes()
-
-    def header(data_at):
-        return _object_header([
-            _message(_MSG_DATASPACE, _dataspace(v.shape)),
-            _message(_MSG_DATATYPE, _datatype(np.dtype(dt)), flags=1),
-            _message(_MSG_FILL, bytes([2, 2, 2, 1]) + struct.pack("<I", 0), flags=1),
-            _message(_MSG_LAYOUT, struct.pack("<BBQQ", 3, 1, data_at, len(raw)))])
-
-    addr = img.alloc(len(header(UNDEF)))
+    addr = img.alloc(len(hdr))
     data_at = img.alloc(len(raw)) if raw else UNDEF   # an empty dataset has no storage
-    img.put(addr, header(data_at))
+    img.put(addr, hdr)
+    struct.pack_into("<QQ", img.b, addr + at, data_at, len(raw))
     if raw:
         img.put(data_at, raw)
     return addr

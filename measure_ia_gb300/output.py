@@ -35,6 +35,19 @@ except Exception:
 # stores of named files with datasets not yet flushed, by absolute path
 _OPEN: dict[str, "OutputFile"] = {}
 
+# the datasets of the last file this process wrote with the built-in writer:
+# (absolute path, (size, mtime_ns) of the file just after the write, copies of
+# the datasets).  A store opened on that file while it is still unchanged
+# takes them instead of parsing the file again (measuring into one file over
+# and over re-reads nothing); any other write to the file changes its size or
+# time and the file is read
+_LAST_WRITTEN: list = []
+
+
+def _stamp(name):
+    st = os.stat(name)
+    return (st.st_size, st.st_mtime_ns)
+
 
 def norm_path(*parts):
     return "/".join(p for part in parts for p in str(part).split("/") if p)
@@ -61,6 +74,10 @@ class OutputFile:
                 f.visititems(lambda path, obj: old.__setitem__(path, obj[()]) if isinstance(obj, h5py.Dataset)
                              else None)
         else:
+            key = os.path.abspath(self.name)
+            if _LAST_WRITTEN and _LAST_WRITTEN[0] == key and _LAST_WRITTEN[1] == _stamp(self.name):
+                self.data = {**_LAST_WRITTEN[2], **self.data}
+                return
             try:
                 old = hdf5.read_file(self.name)
             except (ValueError, NotImplementedError) as exc:
@@ -98,6 +115,8 @@ class OutputFile:
                 return
             self._load()
             hdf5.write_file(self.name, self.data)
+            _LAST_WRITTEN[:] = [os.path.abspath(self.name), _stamp(self.name),
+                                {k: np.array(v, copy=True) for k, v in self.data.items()}]
         key = os.path.abspath(self.name)
         if _OPEN.get(key) is self:
             del _OPEN[key]
