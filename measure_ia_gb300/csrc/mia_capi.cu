@@ -695,7 +695,18 @@ void make_params(const mia_config* cfg, const Plan& plan, const Tables& T, int l
     // + |p_lo|) inv, 2^-24 of it each, three in all) and the rounding of t
     // ((n_p + 1) 2^-24); taken four times over
     const double lmax = (cfg->boxsize + 2.0 * plan.range_los + fabs(p0)) * inv;
-    const double ew = (2.0 * (cfg->n_p + 1) + 3.0 * lmax + fabs(p0) * inv) * (u * 0.5);
+    double ew = (2.0 * (cfg->n_p + 1) + 3.0 * lmax + fabs(p0) * inv) * (u * 0.5);
+    // a line-of-sight reach that spans the box: t is brought to the minimum
+    // image by adding or subtracting L n_p / (p_hi - p_lo) (its rounding and
+    // that of the add); the wrap points -L/2 and L/2 are the Pi range's ends
+    // or lie beyond them, so a pair near one is an edge or out of range
+    const double L_t = cfg->boxsize * inv;
+    P.short_wrap = cfg->kind == MIA_KIND_W && plan.full[2] && !plan.full[0] && !plan.full[1] &&
+                   p0 >= -0.5 * cfg->boxsize && p1 <= 0.5 * cfg->boxsize;
+    if (P.short_wrap) ew += 2.0 * L_t * (u * 0.5);
+    P.t_wrap_lo = (float)((-0.5 * cfg->boxsize - p0) * inv);
+    P.t_wrap_hi = (float)((0.5 * cfg->boxsize - p0) * inv);
+    P.L_t = (float)L_t;
     P.p_guard_w = (float)fmin(0.25, fmax(4.0 * ew, 1.0 / 1048576.0));
   }
   P.c_guard = 1e-12f;

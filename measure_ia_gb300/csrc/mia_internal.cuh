@@ -291,6 +291,10 @@ struct Params {
   float p_half_in;              // 0.5 - p_guard: |frac(t) - 0.5| above it is an edge
   float p_guard_w;              // short w path: |t - rint(t)| below it is an edge (t from the shape's hi/lo z)
   int short_ok;                 // the short pair path applies (finite q_cut inside the lookup table)
+  int short_wrap;               // w whose line-of-sight reach spans the box, Pi range inside [-L/2, L/2]:
+                                // the short path with a per-pair minimum image along the line of sight
+  float t_wrap_lo, t_wrap_hi;   // that path: Pi bin coordinates of -L/2 and L/2 (the wrap points)
+  float L_t;                    // that path: L in bin-coordinate units, L n_p / (p_hi - p_lo)
   float c_guard;                // sin^2(phi) below which the exact FP64 cos(phi) decides
   float wrap_guard;
   float los_cut;                // |Pi| above this is surely outside the Pi bins (w)

@@ -405,7 +405,11 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
 //    operation would.
 //  * Multipoles: the same, with mu = Pi rsqrt(r^2) and the generic form's
 //    bin coordinate and guard; r_p > rp_cut as the generic form decides it.
-template <int KIND, int SLOTS>
+//  * WRAP (w whose line-of-sight reach spans the box, as with the default
+//    pi_max = L/2): t is brought to the minimum image along the line of sight
+//    by adding or subtracting L in bin units beyond the wrap points; those
+//    coincide with the Pi range's ends (edges) or lie outside it.
+template <int KIND, int SLOTS, int WRAP>
 __device__ __forceinline__ void mixed_pair_short(const Params& P, const TablesSmem& T, const float4& a,
                                                  const float4& b, const float2* C, const int* I, int i,
                                                  const MixedPos& p, unsigned* hk, int* hh, const Work& w,
@@ -416,6 +420,7 @@ __device__ __forceinline__ void mixed_pair_short(const Params& P, const TablesSm
   float t, q, dz = 0.0f;
   if (KIND == MIA_KIND_W) {
     t = b.x + p.loff;
+    if (WRAP) t = t >= P.t_wrap_hi ? t - P.L_t : (t < P.t_wrap_lo ? t + P.L_t : t);
     q = qp;
   } else {
     dz = (b.x - p.zh) + (b.y - p.zl);
@@ -542,7 +547,7 @@ __device__ __forceinline__ void shape_loop(const Params& P, const TablesSmem& T,
   int* const hh = hv.dd_hi + p0.hbase;
   auto pair = [&](const float4& a, const float4& b, int i) {
     if (SHORT)
-      mixed_pair_short<KIND, SLOTS>(P, T, a, b, C, I, i, p0, hk, hh, w, o, label_a, my_binned);
+      mixed_pair_short<KIND, SLOTS, SHORT == 2>(P, T, a, b, C, I, i, p0, hk, hh, w, o, label_a, my_binned);
     else
       mixed_pair<KIND, FULL, VAR, SLOTS>(P, T, a, b, C, I, i, p0, hv, w, o, sc, twoR, label_a, my_binned);
   };
@@ -1031,7 +1036,14 @@ __global__ void __launch_bounds__(kThreads, MIA_PAIR_MINB) k_pairs(
                   win = fminf(win, sqrtf(fmaxf(P.q_cut - g2, 0.0f) + 1e-4f * P.q_cut) + P.zwin - P.range_los32);
                 }
               }
-              if (win >= 0.0f) z_window(Z, S, p0.zh + p0.zl, win, i_lo, i_hi);
+              if (win >= 0.0f) {
+                if (SHORT == 2) {  // (the line-of-sight reach spans the box: every staged shape)
+                  i_lo = 0;
+                  i_hi = S;
+                } else {
+                  z_window(Z, S, p0.zh + p0.zl, win, i_lo, i_hi);
+                }
+              }
             }
           }
           // the union over the warp is barely wider (neighbouring positions),
@@ -1344,10 +1356,10 @@ cudaError_t hist_words_for(const Params& P, int& hw) {
 
 // The short w path: histogram arrays of kHistShort words (as many copies as
 // they hold), the blocks per SM that this leaves.
-template <int KIND>
+template <int KIND, int SHORT>
 cudaError_t launch_short(const Params& P, const Dataset* ds, int n_ds, const unsigned long long* wu_prefix,
                          unsigned long long* wu_next, cudaStream_t st, int num_sms) {
-  auto kern = k_pairs<1, 0, KIND, 0, 1>;
+  auto kern = k_pairs<1, 0, KIND, 0, SHORT>;
   const size_t smem = smem_layout(P.shapes_per_unit, kHistShort, P.nb, 1, 0).total;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
@@ -1365,8 +1377,6 @@ cudaError_t launch_short(const Params& P, const Dataset* ds, int n_ds, const uns
 template <int MIXED, int VAR, int KIND, int FULL>
 cudaError_t launch_one(const Params& P, const Dataset* ds, int n_ds, const unsigned long long* wu_prefix,
                        unsigned long long* wu_next, cudaStream_t st, int num_sms) {
-  if (MIXED && !VAR && !FULL && P.short_ok && (P.nb | 1) <= kHistShort)
-    return launch_short<KIND>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms);
   int hw = 0;
   cudaError_t e = hist_words_for<MIXED, VAR, KIND, FULL>(P, hw);
   if (e != cudaSuccess) return e;
@@ -1410,6 +1420,14 @@ template <int MIXED, int VAR>
 cudaError_t launch_kind(const Params& P, const Dataset* ds, int n_ds, const unsigned long long* wu_prefix,
                         unsigned long long* wu_next, cudaStream_t st, int num_sms) {
   const bool full = P.full[0] || P.full[1] || P.full[2];
+  // the short path: local neighbourhoods, or (w) a line-of-sight reach that
+  // spans the box with the plane local
+  if (MIXED && !VAR && P.short_ok && (P.nb | 1) <= kHistShort) {
+    if (!full)
+      return P.kind == MIA_KIND_W ? launch_short<MIA_KIND_W, 1>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms)
+                                  : launch_short<MIA_KIND_MULTIPOLES, 1>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms);
+    if (P.short_wrap) return launch_short<MIA_KIND_W, 2>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms);
+  }
   if (P.kind == MIA_KIND_W)
     return full ? launch_one<MIXED, VAR, MIA_KIND_W, 1>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms)
                 : launch_one<MIXED, VAR, MIA_KIND_W, 0>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms);
