@@ -206,7 +206,8 @@ struct HistView {
 struct MixedPos {
   float xh, xl, yh, yl, zh, zl, w;
   float loff;  // short w path: -(p_lo + z) n_p / (p_hi - p_lo)
-  float2 nh, nl, w2;  // short w path: -(x_hi, y_hi), -(x_lo, y_lo), (w, w) as register pairs
+  float2 nh, nl, w2;  // short path: -(x_hi, y_hi), -(x_lo, y_lo), (w, w) as register pairs
+  float2 nz;          // short multipole path: -(z_hi, z_lo)
   int idx, lab, slot, base, hbase;
   bool valid;
 };
@@ -423,7 +424,8 @@ __device__ __forceinline__ void mixed_pair_short(const Params& P, const TablesSm
     if (WRAP) t = t >= P.t_wrap_hi ? t - P.L_t : (t < P.t_wrap_lo ? t + P.L_t : t);
     q = qp;
   } else {
-    dz = (b.x - p.zh) + (b.y - p.zl);
+    const float2 zz = __fadd2_rn(make_float2(b.x, b.y), p.nz);  // (z_hi, z_lo) differences
+    dz = zz.x + zz.y;
     q = fmaf(dz, dz, qp);
   }
   // surely beyond the last binned separation (whole warps leave here often)
@@ -1007,6 +1009,7 @@ __global__ void __launch_bounds__(kThreads, MIA_PAIR_MINB) k_pairs(
             p0.nh = make_float2(-p0.xh, -p0.yh);
             p0.nl = make_float2(-p0.xl, -p0.yl);
             p0.w2 = make_float2(p0.w, p0.w);
+            if (KIND != MIA_KIND_W) p0.nz = make_float2(-p0.zh, -p0.zl);
           }
           // positions of the unit's region only (all but points on sub-box
           // faces): no per-pair slot check
