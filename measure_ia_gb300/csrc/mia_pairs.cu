@@ -428,12 +428,15 @@ __device__ __forceinline__ void mixed_pair_short(const Params& P, const TablesSm
     dz = zz.x + zz.y;
     q = fmaf(dz, dz, qp);
   }
-  // surely beyond the last binned separation (whole warps leave here often)
-  if (q > P.q_cut) return;
   // (q <= q_cut lies in the table; a q below it wraps to the last entry,
-  // which holds the bin under the first breakpoint)
+  // which holds the bin under the first breakpoint; a q above q_cut, whose
+  // entry is not used, is clamped to the table too.  The load is issued
+  // before the exit below, so its latency overlaps the branch: 89.9 -> 88.7 ms
+  // on the 4M / 1M w step)
   const unsigned bucket = min((__float_as_uint(q) >> (23 - kLutMantBits)) - (unsigned)P.lut32_base, (unsigned)kLut - 1u);
   int e = T.lut32[bucket];
+  // surely beyond the last binned separation (whole warps leave here often)
+  if (q > P.q_cut) return;
   if (KIND != MIA_KIND_W) t = fmaf(dz * rsqrtf(q), P.p_inv32, P.p_off32);
   const int jb = __float2int_rd(t);
   const bool pi_edge = fabsf(t - rintf(t)) < (KIND == MIA_KIND_W ? P.p_guard_w : P.p_guard);
