@@ -1267,9 +1267,26 @@ __global__ void __launch_bounds__(kThreads, MIA_PAIR_MINB) k_pairs(
 }
 
 // FP64 re-test of the pairs the mixed kernel could not decide in FP32; their
-// FP64 terms join the dataset's fixed-point sums at the same scales.
-__global__ void k_edge_retest(Params P, Work w, Out o) {
+// FP64 terms join the dataset's fixed-point sums at the same scales.  Every
+// re-tested pair adds to one of the nb all-pairs sums, so a block first sums
+// those in shared memory (64-bit integer atomics, flushed once per block);
+// the per-region sums, spread over (1 + J) nb words, go to global memory
+// directly.  (With 2.4M pairs on a few hundred words, global atomics alone
+// serialised on their L2 lines.)
+__global__ void k_edge_retest(Params P, Work w, Out o, int agg) {
+  extern __shared__ __align__(8) unsigned long long rt_smem[];
   if (w.status->flags & kStatusRange) return;  // the measurement ends in MIA_ERR_RANGE
+  typedef unsigned long long u64;
+  const int nb = P.nb;
+  const int want_var = P.want_variance;
+  u64* s_cnt = rt_smem;          // nb each: count, w, S+D, SxD (, variance terms)
+  u64* s_dd = s_cnt + nb;
+  u64* s_sp = s_dd + nb;
+  u64* s_sx = s_sp + nb;
+  u64* s_vr = s_sx + nb;
+  const int words = agg ? (4 + want_var) * nb : 0;  // (agg = 0: too many bins for shared memory)
+  for (int i = threadIdx.x; i < words; i += blockDim.x) rt_smem[i] = 0ull;
+  __syncthreads();
   const unsigned long long n_raw = w.status->edge_count;
   const unsigned long long n = n_raw < (unsigned long long)w.edge_capacity ? n_raw : (unsigned long long)w.edge_capacity;
   const double twoR = dataset_twoR(w.reg, P.J);
@@ -1286,13 +1303,49 @@ __global__ void k_edge_retest(Params P, Work w, Out o) {
     const double sp = __dmul_rn(ww, r.ep);
     const double sx = __dmul_rn(ww, r.ex);
     const double tv = __ddiv_rn(sp, twoR);
-    acc_global_fixed(w, o, P.nb, P.J, w.slab_s[si], w.plab_s[pi], r.bin, __double2ll_rn(ww * sc.sd_dd),
-                     __double2ll_rn(sp * sc.sd_sp), __double2ll_rn(sx * sc.sd_sp),
-                     P.want_variance ? __double2ll_rn(tv * tv * sc.sd_vr) : 0, P.want_variance);
+    const long long vd = __double2ll_rn(ww * sc.sd_dd), vp = __double2ll_rn(sp * sc.sd_sp),
+                    vx = __double2ll_rn(sx * sc.sd_sp), vv = want_var ? __double2ll_rn(tv * tv * sc.sd_vr) : 0;
+    const int bin = r.bin;
+    if (agg) {
+      atomicAdd(&s_cnt[bin], 1ull);
+      atomicAdd(&s_dd[bin], (u64)vd);
+      atomicAdd(&s_sp[bin], (u64)vp);
+      atomicAdd(&s_sx[bin], (u64)vx);
+      if (want_var) atomicAdd(&s_vr[bin], (u64)vv);
+    } else {
+      atomicAdd(&o.npairs[bin], 1ULL);
+      atomicAdd(reinterpret_cast<u64*>(&w.acc_dd[bin]), (u64)vd);
+      atomicAdd(reinterpret_cast<u64*>(&w.acc_sp[bin]), (u64)vp);
+      atomicAdd(reinterpret_cast<u64*>(&w.acc_sx[bin]), (u64)vx);
+      if (want_var) atomicAdd(reinterpret_cast<u64*>(&w.acc_vr[bin]), (u64)vv);
+    }
+    if (P.J > 0) {
+      const int a = w.slab_s[si], b = w.plab_s[pi];
+      const size_t ia = (size_t)(1 + a) * nb + bin;
+      atomicAdd(&o.npairs[ia], 1ULL);
+      atomicAdd(reinterpret_cast<u64*>(&w.acc_dd[ia]), (u64)vd);
+      atomicAdd(reinterpret_cast<u64*>(&w.acc_sp[ia]), (u64)vp);
+      if (b != a) {
+        const size_t ib = (size_t)(1 + b) * nb + bin;
+        atomicAdd(&o.npairs[ib], 1ULL);
+        atomicAdd(reinterpret_cast<u64*>(&w.acc_dd[ib]), (u64)vd);
+        atomicAdd(reinterpret_cast<u64*>(&w.acc_sp[ib]), (u64)vp);
+      }
+    }
     ++binned;
   }
   for (int of = 16; of > 0; of >>= 1) binned += __shfl_down_sync(0xffffffffu, binned, of);
   if ((threadIdx.x & 31) == 0 && binned) atomicAdd(&w.status->binned, binned);
+  __syncthreads();
+  for (int bin = threadIdx.x; agg && bin < nb; bin += blockDim.x) {
+    const u64 c = s_cnt[bin];
+    if (!c) continue;
+    atomicAdd(&o.npairs[bin], c);
+    atomicAdd(reinterpret_cast<u64*>(&w.acc_dd[bin]), s_dd[bin]);
+    atomicAdd(reinterpret_cast<u64*>(&w.acc_sp[bin]), s_sp[bin]);
+    atomicAdd(reinterpret_cast<u64*>(&w.acc_sx[bin]), s_sx[bin]);
+    if (want_var) atomicAdd(reinterpret_cast<u64*>(&w.acc_vr[bin]), s_vr[bin]);
+  }
 }
 
 // The dataset's exact fixed-point sums into the output doubles (w and S+D per
@@ -1470,7 +1523,11 @@ cudaError_t launch_fixed_out(const Params& P, const Work& w, const Out& o, cudaS
 }
 
 cudaError_t launch_edge_retest(const Params& P, const Work& w, const Out& o, cudaStream_t st, int num_sms) {
-  k_edge_retest<<<num_sms * 4, 256, 0, st>>>(P, w, o);
+  // the all-pairs sums in shared memory when they fit in 48 KB (nb <= 1228)
+  size_t smem = sizeof(unsigned long long) * (size_t)(4 + (P.want_variance ? 1 : 0)) * P.nb;
+  const int agg = smem <= 48 * 1024 ? 1 : 0;
+  if (!agg) smem = 0;
+  k_edge_retest<<<num_sms * 4, 256, smem, st>>>(P, w, o, agg);
   return cudaGetLastError();
 }
 
