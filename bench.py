@@ -37,12 +37,13 @@ L_BOX = 205.0
 R_BINS = np.logspace(-1, np.log10(20.0), 11)
 PI_BINS = np.linspace(-20.0, 20.0, 9)
 LANE_OPS_PER_PAIR = 32          # FP32 lane-ops per binned (r_p, Pi) pair (fixed recipe)
-# FP64 operations per binned (r_p, Pi) pair in the plain FP64 form (fixed recipe,
-# the reference's sequence): separations 3, squares 3, r_p^2 1, r_p = sqrt 8,
-# dx/r_p and dy/r_p 2 x 8, c = two products and a sum 3, c^2 1, 2c^2 - 1 2,
-# (1 - c)(1 + c) 3, its sqrt 8, sin 2phi 2, e cos / e sin 2, weight products 3;
-# a square root or a division counted as 8 (its Newton steps)
-FP64_OPS_PER_PAIR = 55
+# FP64 operations per binned (r_p, Pi) pair in the plain FP64 form (fixed recipe):
+# separations 3, squares 2, r_p^2 1, dot and crs against the axis 2 x 2, crs^2 1,
+# the sin^2 phi guard 1, e / r_p^2 8 (a division counted as 8, its Newton steps),
+# e cos 2phi 2, e sin 2phi 3, weight products 3.  (The reference's arccos route,
+# with two square roots and two more divisions, runs only for near-collinear
+# pairs.)
+FP64_OPS_PER_PAIR = 28
 
 
 def make_catalog(seed=2026, n_centres=80000, n_shape=1_000_000, n_edge=2000):
@@ -937,9 +938,10 @@ def main():
         fp64_form.update({"fp64_ops_per_binned_pair": FP64_OPS_PER_PAIR, "achieved_fp64_tops": fp64_ops,
                           "dgemm_tflops_measured": dgemm, "dgemm_fma_rate_tops": dgemm / 2,
                           "frac_of_dgemm_fma_rate": fp64_ops / (dgemm / 2),
-                          "note": "plain FP64 form: an FP32 range test, then the reference's FP64 operation "
-                                  "sequence for the survivors with all lanes busy; ops per pair from the fixed "
-                                  "recipe in bench.py (a sqrt or a division counted as 8)"})
+                          "note": "plain FP64 form: an FP32 range test, then the reference's FP64 separations "
+                                  "and bin decisions for the survivors with all lanes busy, the S+D terms from "
+                                  "a short FP64 chain; ops per pair from the fixed recipe in bench.py (a "
+                                  "division counted as 8)"})
     if rank != 0:
         return
     launches_per_step = 22  # prep 16 (prep 2, scans 9, scatter 2, responsivity sums 1, work units 2), work prefix 1, pairs 1, edge re-test 1, fixed-point sums 1, post 1, status 1

@@ -425,18 +425,33 @@ __device__ __forceinline__ PairResult pair_exact(const Params& P, const Tab& T, 
   int ib = T.q_bin[count_le(T.q_key, P.n_qbreak, __double_as_longlong(q))];
   if (ib < 0) return res;
   int jb;
-  double rp = __dsqrt_rn(qp);
   if (P.kind == MIA_KIND_W) {
     jb = T.p_bin[count_le(T.p_key, P.n_pbreak, order_key(dz))];
   } else {
-    if (!(rp > P.rp_cut)) return res;
+    // r_p > rp_cut (for rp_cut = 0 that is r_p^2 > 0, no square root needed)
+    if (P.rp_cut == 0.0 ? !(qp > 0.0) : !(__dsqrt_rn(qp) > P.rp_cut)) return res;
     double r = __dsqrt_rn(q);
     double mu = __ddiv_rn(dz, r);
     jb = T.p_bin[count_le(T.p_key, P.n_pbreak, order_key(mu))];
   }
   if (jb < 0) return res;
   res.bin = ib * P.n_p + jb;
-  // phi = arccos(sdir . a) with sdir = proj / r_p (measure_w_box_jk.py:590-596)
+  // phi = arccos(sdir . a) with sdir = proj / r_p (measure_w_box_jk.py:590-596),
+  // e+ = e cos 2phi, ex = e sin 2phi.  With the unit axis a, dot = d . a and
+  // crs = d x a: cos 2phi = (dot^2 - crs^2) / r_p^2, sin 2phi = 2 dot |crs| /
+  // r_p^2, a short chain within a few ulps of the reference's arccos route.
+  // That route runs as written where it is ill-conditioned or takes its NaN
+  // rule: sin^2 phi below 1e-6 (c near +-1, where (1 - c)(1 + c) cancels and
+  // |c| > 1 can occur), r_p = 0, a NaN axis (the comparison below is false).
+  const double dot = fma(dx, ax, dy * ay), crs = fma(dx, ay, -(dy * ax));
+  const double s2 = crs * crs;
+  if (s2 >= 1e-6 * qp && qp > 0.0) {
+    const double f = e / qp;
+    res.ep = fma(dot, dot, -s2) * f;
+    res.ex = 2.0 * dot * fabs(crs) * f;
+    return res;
+  }
+  const double rp = __dsqrt_rn(qp);
   double c = __dadd_rn(__dmul_rn(__ddiv_rn(dx, rp), ax), __dmul_rn(__ddiv_rn(dy, rp), ay));
   if (c >= -1.0 && c <= 1.0) {  // arccos of |c| > 1 (or NaN) is NaN -> e_+ = e_x = 0
     double c2 = __dmul_rn(c, c);
