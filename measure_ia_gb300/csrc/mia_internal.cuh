@@ -17,7 +17,8 @@ constexpr int kLut = 1 << kLutBits;
 constexpr int kLutMantBits = 6;          // 64 buckets per octave of q
 constexpr int kScanTile = 2048;
 constexpr int kLutReject = 0x7FFF;       // lutw: clean bucket whose q is not binned
-constexpr int kHistShort = 1920;         // u32 words per replicated histogram array, short w path
+constexpr int kHistShort = 1920;         // u32 words per replicated histogram array, short pair path
+constexpr int kHistShortVar = 1536;      // the same with variance terms (five arrays)
 
 // status word bits
 constexpr unsigned kStatusRange = 1u;      // input coordinate outside [0, L) or NaN

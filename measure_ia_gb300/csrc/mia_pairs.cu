@@ -384,9 +384,9 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
   }
 }
 
-// The short pair path of the mixed form (local neighbourhoods, no variance
-// terms; w and multipoles): the same decisions as mixed_pair in fewer
-// instructions.
+// The short pair path of the mixed form (local neighbourhoods; w and
+// multipoles, with or without variance terms): the same decisions as
+// mixed_pair in fewer instructions.
 //  * Pi bin: t = (Pi - p_lo) n_p / (p_hi - p_lo) as the shape's staged
 //    z n_p / (p_hi - p_lo) plus the position's offset p.loff, bin =
 //    floor(t); t within p_guard_w of an integer is an edge.  No separate
@@ -395,8 +395,8 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
 //  * r bin: the lutw bucket of q holds ib * n_p, kLutReject, or (for a
 //    bucket touching a guard band) that band with the codes below and above
 //    it; one test covers a reject, a band and a Pi bin outside the range.
-//  * Histogram words sit kHistShort words apart, so one address serves the
-//    four atomics.  `hk` is the lane's copy of the unit's histogram, `hh` the
+//  * Histogram words sit kHistShort (kHistShortVar with variance terms) words
+//    apart, so one address serves the four (five) atomics.  `hk` is the lane's copy of the unit's histogram, `hh` the
 //    high words.
 //  * Paired FP32 instructions (FADD2, FMUL2) where both halves have the same
 //    operation: the staged shape is a = (x_hi, y_hi, x_lo, y_lo), b = (z
@@ -410,11 +410,13 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
 //    pi_max = L/2): t is brought to the minimum image along the line of sight
 //    by adding or subtracting L in bin units beyond the wrap points; those
 //    coincide with the Pi range's ends (edges) or lie outside it.
-template <int KIND, int SLOTS, int WRAP>
+template <int KIND, int SLOTS, int WRAP, int VAR>
 __device__ __forceinline__ void mixed_pair_short(const Params& P, const TablesSmem& T, const float4& a,
                                                  const float4& b, const float2* C, const int* I, int i,
                                                  const MixedPos& p, unsigned* hk, int* hh, const Work& w,
-                                                 const Out& o, int label_a, unsigned long long& my_binned) {
+                                                 const Out& o, const Scales& sc, int label_a,
+                                                 unsigned long long& my_binned) {
+  constexpr int KS = VAR ? kHistShortVar : kHistShort;
   const float2 d = __fadd2_rn(__fadd2_rn(make_float2(a.x, a.y), p.nh), __fadd2_rn(make_float2(a.z, a.w), p.nl));
   const float dx = d.x, dy = d.y;
   const float qp = fmaf(dx, dx, dy * dy);
@@ -485,21 +487,27 @@ __device__ __forceinline__ void mixed_pair_short(const Params& P, const TablesSm
     const int vd = __float2int_rn(ww);
     const int vp = __float2int_rn(tp);
     const int vx = __float2int_rn(tx);
+    int vv = 0;
+    if (VAR) vv = __float2int_rn(tp * tp * sc.c_vr);
     unsigned* h = hk + bin;
-    const unsigned od = atomicAdd(h + kHistShort, (unsigned)vd);
-    const unsigned op = atomicAdd(h + 2 * kHistShort, (unsigned)vp);
-    const unsigned ox = atomicAdd(h + 3 * kHistShort, (unsigned)vx);
+    const unsigned od = atomicAdd(h + KS, (unsigned)vd);
+    const unsigned op = atomicAdd(h + 2 * KS, (unsigned)vp);
+    const unsigned ox = atomicAdd(h + 3 * KS, (unsigned)vx);
+    unsigned ov = 0;
+    if (VAR) ov = atomicAdd(h + 4 * KS, (unsigned)vv);
     atomicAdd(h, 1u);
     const int fd = overflow_of(od, vd), fp = overflow_of(op, vp), fx = overflow_of(ox, vx);
-    if ((fd | fp | fx) < 0) {
+    const int fv = VAR ? overflow_of(ov, vv) : 0;
+    if ((fd | fp | fx | fv) < 0) {
       int* g = hh + bin;
       if (fd < 0) atomicAdd(g, (vd >> 31) | 1);
       if (fp < 0) atomicAdd(g + P.nb, (vp >> 31) | 1);
       if (fx < 0) atomicAdd(g + 2 * P.nb, (vx >> 31) | 1);
+      if (VAR && fv < 0) atomicAdd(g + 3 * P.nb, (vv >> 31) | 1);
     }
   } else {
     acc_global_fixed(w, o, P.nb, P.J, label_a, p.lab, bin, __float2ll_rn(ww), __float2ll_rn(tp), __float2ll_rn(tx),
-                     0, 0);
+                     VAR ? __float2ll_rn(tp * tp * sc.c_vr) : 0, VAR);
     atomicOr(&w.status->flags, kStatusNoSlot);
     ++my_binned;
   }
@@ -552,7 +560,7 @@ __device__ __forceinline__ void shape_loop(const Params& P, const TablesSmem& T,
   int* const hh = hv.dd_hi + p0.hbase;
   auto pair = [&](const float4& a, const float4& b, int i) {
     if (SHORT)
-      mixed_pair_short<KIND, SLOTS, SHORT == 2>(P, T, a, b, C, I, i, p0, hk, hh, w, o, label_a, my_binned);
+      mixed_pair_short<KIND, SLOTS, SHORT == 2, VAR>(P, T, a, b, C, I, i, p0, hk, hh, w, o, sc, label_a, my_binned);
     else
       mixed_pair<KIND, FULL, VAR, SLOTS>(P, T, a, b, C, I, i, p0, hv, w, o, sc, twoR, label_a, my_binned);
   };
@@ -594,7 +602,8 @@ __global__ void __launch_bounds__(kThreads, MIA_PAIR_MINB) k_pairs(
   unsigned* hist = reinterpret_cast<unsigned*>(smem + SL.hist);
   float4* wpos = reinterpret_cast<float4*>(smem + SL.wpos);
   unsigned short* ring = reinterpret_cast<unsigned short*>(smem + SL.ring);
-  const int KB = SHORT ? kHistShort : HW;  // words per replicated array (the short path's stride is fixed)
+  // words per replicated array (the short path's stride is fixed)
+  const int KB = SHORT ? (VAR ? kHistShortVar : kHistShort) : HW;
 
   __shared__ long long s_wu;
   __shared__ int s_ds;
@@ -1413,13 +1422,14 @@ cudaError_t hist_words_for(const Params& P, int& hw) {
   return cudaSuccess;
 }
 
-// The short w path: histogram arrays of kHistShort words (as many copies as
-// they hold), the blocks per SM that this leaves.
-template <int KIND, int SHORT>
+// The short pair path: histogram arrays of kHistShort (kHistShortVar) words,
+// as many copies as they hold, and the blocks per SM that this leaves.
+template <int KIND, int SHORT, int VAR>
 cudaError_t launch_short(const Params& P, const Dataset* ds, int n_ds, const unsigned long long* wu_prefix,
                          unsigned long long* wu_next, cudaStream_t st, int num_sms) {
-  auto kern = k_pairs<1, 0, KIND, 0, SHORT>;
-  const size_t smem = smem_layout(P.shapes_per_unit, kHistShort, P.nb, 1, 0).total;
+  auto kern = k_pairs<1, VAR, KIND, 0, SHORT>;
+  constexpr int KS = VAR ? kHistShortVar : kHistShort;
+  const size_t smem = smem_layout(P.shapes_per_unit, KS, P.nb, 1, VAR).total;
   cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int per_sm = 0;
@@ -1429,7 +1439,7 @@ cudaError_t launch_short(const Params& P, const Dataset* ds, int n_ds, const uns
   if (per_sm > MIA_MAX_BLOCKS_PER_SM) per_sm = MIA_MAX_BLOCKS_PER_SM;
 #endif
   if (per_sm < 1) return cudaErrorInvalidConfiguration;
-  kern<<<num_sms * per_sm, kThreads, smem, st>>>(P, ds, n_ds, wu_prefix, wu_next, kHistShort);
+  kern<<<num_sms * per_sm, kThreads, smem, st>>>(P, ds, n_ds, wu_prefix, wu_next, KS);
   return cudaGetLastError();
 }
 
@@ -1481,11 +1491,12 @@ cudaError_t launch_kind(const Params& P, const Dataset* ds, int n_ds, const unsi
   const bool full = P.full[0] || P.full[1] || P.full[2];
   // the short path: local neighbourhoods, or (w) a line-of-sight reach that
   // spans the box with the plane local
-  if (MIXED && !VAR && P.short_ok && (P.nb | 1) <= kHistShort) {
+  if (MIXED && P.short_ok && (P.nb | 1) <= (VAR ? kHistShortVar : kHistShort)) {
     if (!full)
-      return P.kind == MIA_KIND_W ? launch_short<MIA_KIND_W, 1>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms)
-                                  : launch_short<MIA_KIND_MULTIPOLES, 1>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms);
-    if (P.short_wrap) return launch_short<MIA_KIND_W, 2>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms);
+      return P.kind == MIA_KIND_W ? launch_short<MIA_KIND_W, 1, VAR>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms)
+                                  : launch_short<MIA_KIND_MULTIPOLES, 1, VAR>(P, ds, n_ds, wu_prefix, wu_next, st,
+                                                                             num_sms);
+    if (P.short_wrap) return launch_short<MIA_KIND_W, 2, VAR>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms);
   }
   if (P.kind == MIA_KIND_W)
     return full ? launch_one<MIXED, VAR, MIA_KIND_W, 1>(P, ds, n_ds, wu_prefix, wu_next, st, num_sms)
