@@ -193,11 +193,16 @@ def _contiguous_header(shape, dtype_str):
     return hdr, len(hdr) - 6 - 16
 
 
-def _write_dataset(img: _Image, value: np.ndarray, chunks=None) -> int:
+def _le(dtype):
+    """The little-endian form of a dataset's type (the file's byte order)."""
+    return dtype.newbyteorder("<") if dtype.byteorder != "|" else dtype
+
+
+def _write_dataset(img: _Image, value: np.ndarray, chunks=None, slots=None, path=None) -> int:
     v = np.asarray(value)
     if v.dtype.kind == "b":
         raise TypeError("boolean datasets are not supported by the HDF5 writer")
-    dt = v.dtype.newbyteorder("<") if v.dtype.byteorder != "|" else v.dtype
+    dt = _le(v.dtype)
     hdr, at = _contiguous_header(tuple(int(d) for d in v.shape), np.dtype(dt).str)
     if chunks:
         return _write_chunked(img, v, np.dtype(dt), chunks, 4)
@@ -208,22 +213,25 @@ def _write_dataset(img: _Image, value: np.ndarray, chunks=None) -> int:
     struct.pack_into("<QQ", img.b, addr + at, data_at, len(raw))
     if raw:
         img.put(data_at, raw)
+        if slots is not None:
+            slots.append((path, data_at, len(raw)))
     return addr
 
 
-def _write_group(img: _Image, children: dict, chunks=None) -> tuple[int, int, int]:
+def _write_group(img: _Image, children: dict, chunks=None, slots=None, prefix=()) -> tuple[int, int, int]:
     """Writes a group and (recursively) its members; returns the addresses
-    of its object header, B-tree root and local heap."""
+    of its object header, B-tree root and local heap.  ``slots`` collects
+    (member path, data address, bytes) of every contiguous dataset."""
     names = sorted(children, key=lambda s: s.encode())
     # member objects first, so that their entries can be filled in
     entries = {}
     for n in names:
         c = children[n]
         if isinstance(c, dict):
-            h, bt, hp = _write_group(img, c, chunks)
+            h, bt, hp = _write_group(img, c, chunks, slots, prefix + (n,))
             entries[n] = (h, (bt, hp))
         else:
-            entries[n] = (_write_dataset(img, c, chunks), None)
+            entries[n] = (_write_dataset(img, c, chunks, slots, prefix + (n,)), None)
     # local heap: "" at offset 0, the names, then one free block
     heap_data = bytearray(b"\0" * 8)
     offs = {}
@@ -293,19 +301,56 @@ def _tree(datasets: dict) -> dict:
     return root
 
 
+# file images of recent contiguous writes, by their layout key: every byte of
+# the file but the datasets' data depends only on the member paths, shapes and
+# types, so a write of the same products again (a measurement repeated into
+# one file) copies the image and places the new data at the recorded addresses
+_IMAGES: dict = {}
+_IMAGES_MAX = 8
+
+
+def _image(datasets: dict, chunks):
+    if chunks:
+        img = _Image()
+        h, bt, hp = _write_group(img, _tree(datasets), chunks)
+        return _finish(img, h, bt, hp)
+    vals = {p: np.asarray(v) for p, v in datasets.items()}
+    key = tuple(sorted((p, v.shape, _le(v.dtype).str) for p, v in vals.items()))
+    hit = _IMAGES.get(key)
+    if hit is not None:
+        template, slots = hit
+        b = bytearray(template)
+        for p, at, n in slots:
+            v = vals[p]
+            b[at:at + n] = np.ascontiguousarray(v, dtype=_le(v.dtype)).tobytes()
+        return b
+    img = _Image()
+    slots = []
+    h, bt, hp = _write_group(img, _tree(vals), None, slots)
+    b = _finish(img, h, bt, hp)
+    flat = {tuple(q for q in p.split("/") if q): p for p in vals}
+    if len(_IMAGES) >= _IMAGES_MAX:
+        _IMAGES.pop(next(iter(_IMAGES)))
+    _IMAGES[key] = (bytes(b), [(flat[path], at, n) for path, at, n in slots])
+    return b
+
+
+def _finish(img: _Image, h, bt, hp) -> bytearray:
+    sb = SIGNATURE + bytes([0, 0, 0, 0, 0, 8, 8, 0]) + struct.pack("<HHI", LEAF_K, NODE_K, 0)
+    sb += struct.pack("<QQQQ", 0, UNDEF, len(img.b), UNDEF) + _entry(0, h, (bt, hp))
+    img.put(0, sb)
+    return img.b
+
+
 def write_file(path, datasets: dict, chunks=None) -> None:
     """Writes ``{'group/sub/name': array}`` as a new HDF5 file at ``path``
     (replacing it atomically: the file appears complete or not at all).
     ``chunks=n`` stores every non-scalar dataset in chunks of n rows,
     shuffled and deflate-compressed."""
-    img = _Image()
-    h, bt, hp = _write_group(img, _tree(datasets), chunks)
-    sb = SIGNATURE + bytes([0, 0, 0, 0, 0, 8, 8, 0]) + struct.pack("<HHI", LEAF_K, NODE_K, 0)
-    sb += struct.pack("<QQQQ", 0, UNDEF, len(img.b), UNDEF) + _entry(0, h, (bt, hp))
-    img.put(0, sb)
+    b = _image(datasets, chunks)
     tmp = f"{path}.tmp{os.getpid()}"
     with open(tmp, "wb") as f:
-        f.write(bytes(img.b))
+        f.write(b)
     os.replace(tmp, path)
 
 

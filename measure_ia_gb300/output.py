@@ -50,7 +50,10 @@ def _stamp(name):
 
 
 def norm_path(*parts):
-    return "/".join(p for part in parts for p in str(part).split("/") if p)
+    s = "/".join(map(str, parts))
+    if "//" in s or s[:1] == "/" or s[-1:] == "/":   # empty components: drop them
+        s = "/".join(p for p in s.split("/") if p)
+    return s
 
 
 class OutputFile:

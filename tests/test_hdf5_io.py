@@ -66,6 +66,36 @@ def test_round_trip_through_both_readers(tmp_path):
         np.testing.assert_array_equal(b[k], v)
 
 
+def test_repeated_layout_reuses_image(tmp_path):
+    """A second write of the same paths, shapes and types reuses the first
+    file's image with the new data placed in it: the bytes equal a fresh
+    write of the new values; a changed shape or type writes afresh."""
+    rng = np.random.default_rng(5)
+    d1 = _sample(rng)
+    d2 = {k: (np.asarray(v) + 1).astype(np.asarray(v).dtype) for k, v in d1.items()}
+    p1, p2 = str(tmp_path / "one.hdf5"), str(tmp_path / "two.hdf5")
+    hdf5._IMAGES.clear()
+    hdf5.write_file(p1, d1)
+    assert len(hdf5._IMAGES) == 1
+    hdf5.write_file(p2, d2)                                   # layout hit
+    assert len(hdf5._IMAGES) == 1
+    hdf5._IMAGES.clear()
+    fresh = str(tmp_path / "fresh.hdf5")
+    hdf5.write_file(fresh, d2)
+    assert open(p2, "rb").read() == open(fresh, "rb").read()
+    got = hdf5.read_file(p2)
+    for k, v in d2.items():
+        np.testing.assert_array_equal(got[k], v)
+    d3 = dict(d2, top=np.arange(6, dtype=np.int64))           # another shape
+    d4 = dict(d2, top=np.arange(5, dtype=np.int32))           # another type
+    for d in (d3, d4):
+        hdf5.write_file(p2, d)
+        got = hdf5.read_file(p2)
+        assert got["top"].shape == d["top"].shape and got["top"].dtype == d["top"].dtype
+        np.testing.assert_array_equal(got["top"], d["top"])
+    assert len(hdf5._IMAGES) == 3
+
+
 def test_layout_matches_h5py(tmp_path):
     rng = np.random.default_rng(1)
     path = str(tmp_path / "h.hdf5")
