@@ -173,6 +173,8 @@ class MeasureIABox(SimInfo, BaseHelpers, JackknifeCovariance):
             raise ValueError("Invalid value for ellipticity. Choose 'distortion' or 'ellipticity'.")
         L_sub, layout = self._validate(corr_type, num_jk, temp_file_path)
         cat = self._select(masks)
+        if len(cat["Position"]) == 0 or len(cat["Position_shape_sample"]) == 0:
+            raise ValueError("empty position or shape sample")
         for key in ("weight", "weight_shape_sample", "q"):
             if not _all_finite(cat[key]):
                 # the reference carries these into NaN sums (a NaN q or shape

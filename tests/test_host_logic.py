@@ -178,6 +178,28 @@ def test_box_rejects_non_finite_weights_and_q(key, value):
         box.measure_xi_w("a", "both", 0, temp_file_path="/tmp")
 
 
+@pytest.mark.parametrize("which", ["Position", "Position_shape_sample"])
+def test_box_rejects_empty_samples(which):
+    """A sample left empty by the masks is refused before any GPU work (the
+    reference divides by zero for an empty shape sample and returns NaN
+    correlations for an empty position sample)."""
+    from measure_ia_gb300 import MeasureIABox
+    rng = np.random.default_rng(0)
+    n = 50
+    pos = rng.uniform(0, 100.0, (n, 3))
+    ang = rng.uniform(0, np.pi, n)
+    data = {"Position": pos, "Position_shape_sample": pos.copy(), "Axis_Direction": np.c_[np.cos(ang), np.sin(ang)],
+            "q": rng.uniform(0.2, 1, n), "LOS": 2, "weight": np.ones(n), "weight_shape_sample": np.ones(n)}
+    keep = np.ones(n, dtype=bool)
+    masks = {"Position": keep.copy(), "Position_shape_sample": keep.copy(), "Axis_Direction": keep.copy(),
+             "q": keep.copy()}
+    for k in ((which,) if which == "Position" else ("Position_shape_sample", "Axis_Direction", "q")):
+        masks[k][:] = False
+    box = MeasureIABox(data, None, None, None, [0.1, 10.0], 6, 4, 10.0, boxsize=100.0)
+    with pytest.raises(ValueError, match="empty position or shape sample"):
+        box.measure_xi_w("a", "both", 0, temp_file_path="/tmp", masks=masks)
+
+
 def test_mixed_form_hands_nan_axes_to_fp64(monkeypatch):
     """A non-finite Axis_Direction: the mixed form's FP32 terms would not give
     the reference's e+ = ex = 0, so the measurement runs in the FP64 form,
