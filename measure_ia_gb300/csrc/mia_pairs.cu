@@ -396,88 +396,43 @@ __device__ __forceinline__ void mixed_pair(const Params& P, const TablesSmem& T,
 //    bucket touching a guard band) that band with the codes below and above
 //    it; one test covers a reject, a band and a Pi bin outside the range.
 //  * Histogram words sit kHistShort (kHistShortVar with variance terms) words
-//    apart, so one address serves the four (five) atomics.  `hk` is the lane's copy of the unit's histogram, `hh` the
-//    high words.
+//    apart, so one address serves the four (five) atomics.  `hk` is the lane's
+//    copy of the unit's histogram, `hh` the high words.
 //  * Paired FP32 instructions (FADD2, FMUL2) where both halves have the same
 //    operation: the staged shape is a = (x_hi, y_hi, x_lo, y_lo), b = (z
 //    term, z_lo, w_s, w_s e) (scaled weights; the z term is z n_p / (p_hi -
 //    p_lo) for w, z_hi for multipoles), so (dx, dy) and the two weight
 //    products come out of register pairs; each half rounds as the scalar
 //    operation would.
-//  * Multipoles: the same, with mu = Pi rsqrt(r^2) and the generic form's
-//    bin coordinate and guard; r_p > rp_cut as the generic form decides it.
+//  * w (mixed_pair_short_w): every rare decision (a reject, a guard-band
+//    bucket, a Pi bin outside the range, an edge) sits in one region, so that
+//    the common path has a single branch around it; one divergent region
+//    instead of three took the 4M / 1M w step's pair kernel from 88.7 to 87.2
+//    ms.  The same for multipoles ran 9% slower, so they keep the sequence of
+//    mixed_pair_short_m.
+//  * Multipoles (mixed_pair_short_m): mu = Pi rsqrt(r^2) and the generic
+//    form's bin coordinate and guard; r_p > rp_cut as the generic form decides
+//    it.
 //  * WRAP (w whose line-of-sight reach spans the box, as with the default
 //    pi_max = L/2): t is brought to the minimum image along the line of sight
 //    by adding or subtracting L in bin units beyond the wrap points; those
 //    coincide with the Pi range's ends (edges) or lie outside it.
-template <int KIND, int SLOTS, int WRAP, int VAR>
-__device__ __forceinline__ void mixed_pair_short(const Params& P, const TablesSmem& T, const float4& a,
-                                                 const float4& b, const float2* C, const int* I, int i,
-                                                 const MixedPos& p, unsigned* hk, int* hh, const Work& w,
-                                                 const Out& o, const Scales& sc, int label_a,
+
+// A pair that goes to the FP64 re-test.
+__device__ __forceinline__ void short_queue_edge(const Work& w, int shape, int pos) {
+  const unsigned long long k = atomicAdd(&w.status->edge_count, 1ULL);
+  if (k < (unsigned long long)w.edge_capacity) w.edges[k] = make_int2(shape, pos);
+  else atomicOr(&w.status->flags, kStatusOverflow);
+}
+
+// The binned pair's terms into the lane's histogram copy (or, without a slot
+// for the position's region, into the dataset's sums).
+template <int SLOTS, int VAR>
+__device__ __forceinline__ void short_accumulate(const Params& P, int bin, const float4& b, const MixedPos& p,
+                                                 float qp, float dot, float crs, float crs2, unsigned* hk, int* hh,
+                                                 const Work& w, const Out& o, const Scales& sc, int label_a,
                                                  unsigned long long& my_binned) {
   constexpr int KS = VAR ? kHistShortVar : kHistShort;
-  const float2 d = __fadd2_rn(__fadd2_rn(make_float2(a.x, a.y), p.nh), __fadd2_rn(make_float2(a.z, a.w), p.nl));
-  const float dx = d.x, dy = d.y;
-  const float qp = fmaf(dx, dx, dy * dy);
-  float t, q, dz = 0.0f;
-  if (KIND == MIA_KIND_W) {
-    t = b.x + p.loff;
-    if (WRAP) t = t >= P.t_wrap_hi ? t - P.L_t : (t < P.t_wrap_lo ? t + P.L_t : t);
-    q = qp;
-  } else {
-    const float2 zz = __fadd2_rn(make_float2(b.x, b.y), p.nz);  // (z_hi, z_lo) differences
-    dz = zz.x + zz.y;
-    q = fmaf(dz, dz, qp);
-  }
-  // (q <= q_cut lies in the table; a q below it wraps to the last entry,
-  // which holds the bin under the first breakpoint; a q above q_cut, whose
-  // entry is not used, is clamped to the table too.  The load is issued
-  // before the exit below, so its latency overlaps the branch: 89.9 -> 88.7 ms
-  // on the 4M / 1M w step)
-  const unsigned bucket = min((__float_as_uint(q) >> (23 - kLutMantBits)) - (unsigned)P.lut32_base, (unsigned)kLut - 1u);
-  int e = T.lut32[bucket];
-  // surely beyond the last binned separation (whole warps leave here often)
-  if (q > P.q_cut) return;
-  if (KIND != MIA_KIND_W) t = fmaf(dz * rsqrtf(q), P.p_inv32, P.p_off32);
-  const int jb = __float2int_rd(t);
-  const bool pi_edge = fabsf(t - rintf(t)) < (KIND == MIA_KIND_W ? P.p_guard_w : P.p_guard);
-  bool edge = pi_edge;
-  if ((e >= kLutReject) | ((unsigned)jb >= (unsigned)P.n_p)) {
-    // Pi surely outside the bins (an edge at 0 or n_p goes on to the re-test)
-    if ((unsigned)jb >= (unsigned)P.n_p && ((unsigned)jb + 1u > (unsigned)P.n_p + 1u || !pi_edge)) return;
-    if (e & 0x8000) {  // a bucket touching a guard band: below, inside (an edge) or above the band
-      const float* D = reinterpret_cast<const float*>(&T.qdirty[e & 0x7fff]);
-      const bool below = q < D[0], above = q >= D[1];
-      e = below ? __float_as_int(D[2]) : (above ? __float_as_int(D[3]) : 0);
-      edge |= !(below || above);
-    }
-    if (e == kLutReject) return;
-  }
-  if (KIND != MIA_KIND_W) {
-    if (P.rp_cut2 == 0.0) {
-      if (!(qp > 0.0f) && !edge) return;  // r_p > rp_cut = 0 (measure_m_box_jk.py:637)
-    } else {
-      const float rc2 = (float)P.rp_cut2;
-      if (qp < rc2 * (1.0f - 1e-5f)) {
-        if (!edge) return;
-      } else if (qp <= rc2 * (1.0f + 1e-5f)) {
-        edge = true;
-      }
-    }
-  }
-  const float2 cxy = C[i];
-  const float dot = fmaf(dx, cxy.x, dy * cxy.y);
-  const float crs = fmaf(dx, cxy.y, -dy * cxy.x);
-  const float crs2 = crs * crs;
-  if (crs2 < P.c_guard * qp) edge = true;
-  if (edge) {
-    const unsigned long long k = atomicAdd(&w.status->edge_count, 1ULL);
-    if (k < (unsigned long long)w.edge_capacity) w.edges[k] = make_int2(I[i], p.idx);
-    else atomicOr(&w.status->flags, kStatusOverflow);
-    return;
-  }
-  const int bin = e + jb;
   const float2 pw = __fmul2_rn(make_float2(b.z, b.w), p.w2);  // (w_p w_s, w_p w_s e), scaled
   const float ww = pw.x;
   const float s = __fdividef(pw.y, qp);
@@ -511,6 +466,105 @@ __device__ __forceinline__ void mixed_pair_short(const Params& P, const TablesSm
     atomicOr(&w.status->flags, kStatusNoSlot);
     ++my_binned;
   }
+}
+
+template <int SLOTS, int WRAP, int VAR>
+__device__ __forceinline__ void mixed_pair_short_w(const Params& P, const TablesSmem& T, const float4& a,
+                                                   const float4& b, const float2* C, const int* I, int i,
+                                                   const MixedPos& p, unsigned* hk, int* hh, const Work& w,
+                                                   const Out& o, const Scales& sc, int label_a,
+                                                   unsigned long long& my_binned) {
+  const float2 d = __fadd2_rn(__fadd2_rn(make_float2(a.x, a.y), p.nh), __fadd2_rn(make_float2(a.z, a.w), p.nl));
+  const float dx = d.x, dy = d.y;
+  const float qp = fmaf(dx, dx, dy * dy);
+  float t = b.x + p.loff;
+  if (WRAP) t = t >= P.t_wrap_hi ? t - P.L_t : (t < P.t_wrap_lo ? t + P.L_t : t);
+  // (q <= q_cut lies in the table; a q below it wraps to the last entry,
+  // which holds the bin under the first breakpoint; a q above q_cut, whose
+  // entry is not used, is clamped to the table too.  The load is issued
+  // before the exit below, so its latency overlaps the branch: 89.9 -> 88.7 ms
+  // on the 4M / 1M w step)
+  const unsigned bucket = min((__float_as_uint(qp) >> (23 - kLutMantBits)) - (unsigned)P.lut32_base, (unsigned)kLut - 1u);
+  int e = T.lut32[bucket];
+  // surely beyond the last binned separation (whole warps leave here often)
+  if (qp > P.q_cut) return;
+  const int jb = __float2int_rd(t);
+  const bool pi_edge = fabsf(t - rintf(t)) < P.p_guard_w;
+  const float2 cxy = C[i];
+  const float dot = fmaf(dx, cxy.x, dy * cxy.y);
+  const float crs = fmaf(dx, cxy.y, -dy * cxy.x);
+  const float crs2 = crs * crs;
+  const bool c_edge = crs2 < P.c_guard * qp;  // direction near the axis or its normal
+  if ((e >= kLutReject) | ((unsigned)jb >= (unsigned)P.n_p) | pi_edge | c_edge) {
+    // Pi surely outside the bins (an edge at 0 or n_p goes on to the re-test)
+    if ((unsigned)jb >= (unsigned)P.n_p && ((unsigned)jb + 1u > (unsigned)P.n_p + 1u || !pi_edge)) return;
+    bool edge = pi_edge | c_edge;
+    if (e & 0x8000) {  // a bucket touching a guard band: below, inside (an edge) or above the band
+      const float* D = reinterpret_cast<const float*>(&T.qdirty[e & 0x7fff]);
+      const bool below = qp < D[0], above = qp >= D[1];
+      e = below ? __float_as_int(D[2]) : (above ? __float_as_int(D[3]) : 0);
+      edge |= !(below || above);
+    }
+    if (e == kLutReject) return;
+    if (edge) {
+      short_queue_edge(w, I[i], p.idx);
+      return;
+    }
+  }
+  short_accumulate<SLOTS, VAR>(P, e + jb, b, p, qp, dot, crs, crs2, hk, hh, w, o, sc, label_a, my_binned);
+}
+
+template <int SLOTS, int VAR>
+__device__ __forceinline__ void mixed_pair_short_m(const Params& P, const TablesSmem& T, const float4& a,
+                                                   const float4& b, const float2* C, const int* I, int i,
+                                                   const MixedPos& p, unsigned* hk, int* hh, const Work& w,
+                                                   const Out& o, const Scales& sc, int label_a,
+                                                   unsigned long long& my_binned) {
+  const float2 d = __fadd2_rn(__fadd2_rn(make_float2(a.x, a.y), p.nh), __fadd2_rn(make_float2(a.z, a.w), p.nl));
+  const float dx = d.x, dy = d.y;
+  const float qp = fmaf(dx, dx, dy * dy);
+  const float2 zz = __fadd2_rn(make_float2(b.x, b.y), p.nz);  // (z_hi, z_lo) differences
+  const float dz = zz.x + zz.y;
+  const float q = fmaf(dz, dz, qp);
+  // (the table and the early exit as for w)
+  const unsigned bucket = min((__float_as_uint(q) >> (23 - kLutMantBits)) - (unsigned)P.lut32_base, (unsigned)kLut - 1u);
+  int e = T.lut32[bucket];
+  if (q > P.q_cut) return;
+  const float t = fmaf(dz * rsqrtf(q), P.p_inv32, P.p_off32);
+  const int jb = __float2int_rd(t);
+  const bool pi_edge = fabsf(t - rintf(t)) < P.p_guard;
+  bool edge = pi_edge;
+  if ((e >= kLutReject) | ((unsigned)jb >= (unsigned)P.n_p)) {
+    // mu surely outside the bins (an edge at 0 or n_p goes on to the re-test)
+    if ((unsigned)jb >= (unsigned)P.n_p && ((unsigned)jb + 1u > (unsigned)P.n_p + 1u || !pi_edge)) return;
+    if (e & 0x8000) {  // a bucket touching a guard band: below, inside (an edge) or above the band
+      const float* D = reinterpret_cast<const float*>(&T.qdirty[e & 0x7fff]);
+      const bool below = q < D[0], above = q >= D[1];
+      e = below ? __float_as_int(D[2]) : (above ? __float_as_int(D[3]) : 0);
+      edge |= !(below || above);
+    }
+    if (e == kLutReject) return;
+  }
+  if (P.rp_cut2 == 0.0) {
+    if (!(qp > 0.0f) && !edge) return;  // r_p > rp_cut = 0 (measure_m_box_jk.py:637)
+  } else {
+    const float rc2 = (float)P.rp_cut2;
+    if (qp < rc2 * (1.0f - 1e-5f)) {
+      if (!edge) return;
+    } else if (qp <= rc2 * (1.0f + 1e-5f)) {
+      edge = true;
+    }
+  }
+  const float2 cxy = C[i];
+  const float dot = fmaf(dx, cxy.x, dy * cxy.y);
+  const float crs = fmaf(dx, cxy.y, -dy * cxy.x);
+  const float crs2 = crs * crs;
+  if (crs2 < P.c_guard * qp) edge = true;
+  if (edge) {
+    short_queue_edge(w, I[i], p.idx);
+    return;
+  }
+  short_accumulate<SLOTS, VAR>(P, e + jb, b, p, qp, dot, crs, crs2, hk, hh, w, o, sc, label_a, my_binned);
 }
 
 // FP64 form, the two-phase loop's range test from single-float coordinates:
@@ -559,10 +613,14 @@ __device__ __forceinline__ void shape_loop(const Params& P, const TablesSmem& T,
   unsigned* const hk = hv.cnt + p0.base;
   int* const hh = hv.dd_hi + p0.hbase;
   auto pair = [&](const float4& a, const float4& b, int i) {
-    if (SHORT)
-      mixed_pair_short<KIND, SLOTS, SHORT == 2, VAR>(P, T, a, b, C, I, i, p0, hk, hh, w, o, sc, label_a, my_binned);
-    else
+    if (SHORT) {
+      if (KIND == MIA_KIND_W)
+        mixed_pair_short_w<SLOTS, SHORT == 2, VAR>(P, T, a, b, C, I, i, p0, hk, hh, w, o, sc, label_a, my_binned);
+      else
+        mixed_pair_short_m<SLOTS, VAR>(P, T, a, b, C, I, i, p0, hk, hh, w, o, sc, label_a, my_binned);
+    } else {
       mixed_pair<KIND, FULL, VAR, SLOTS>(P, T, a, b, C, I, i, p0, hv, w, o, sc, twoR, label_a, my_binned);
+    }
   };
   float4 a0 = A[wlo], b0 = B[wlo];
   for (int i = wlo;;) {
