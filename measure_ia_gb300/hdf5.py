@@ -30,6 +30,7 @@ import functools
 import mmap
 import os
 import struct
+import threading
 import zlib
 
 import numpy as np
@@ -307,6 +308,7 @@ def _tree(datasets: dict) -> dict:
 # one file) copies the image and places the new data at the recorded addresses
 _IMAGES: dict = {}
 _IMAGES_MAX = 8
+_IMAGES_LOCK = threading.Lock()
 
 
 def _image(datasets: dict, chunks):
@@ -316,7 +318,8 @@ def _image(datasets: dict, chunks):
         return _finish(img, h, bt, hp)
     vals = {p: np.asarray(v) for p, v in datasets.items()}
     key = tuple(sorted((p, v.shape, _le(v.dtype).str) for p, v in vals.items()))
-    hit = _IMAGES.get(key)
+    with _IMAGES_LOCK:
+        hit = _IMAGES.get(key)
     if hit is not None:
         template, slots = hit
         b = bytearray(template)
@@ -329,9 +332,11 @@ def _image(datasets: dict, chunks):
     h, bt, hp = _write_group(img, _tree(vals), None, slots)
     b = _finish(img, h, bt, hp)
     flat = {tuple(q for q in p.split("/") if q): p for p in vals}
-    if len(_IMAGES) >= _IMAGES_MAX:
-        _IMAGES.pop(next(iter(_IMAGES)))
-    _IMAGES[key] = (bytes(b), [(flat[path], at, n) for path, at, n in slots])
+    entry = (bytes(b), [(flat[path], at, n) for path, at, n in slots])
+    with _IMAGES_LOCK:
+        while len(_IMAGES) >= _IMAGES_MAX:
+            _IMAGES.pop(next(iter(_IMAGES)))
+        _IMAGES[key] = entry
     return b
 
 
