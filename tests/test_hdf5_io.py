@@ -145,6 +145,21 @@ def test_store_appends_and_replaces(tmp_path):
     np.testing.assert_array_equal(got["Snapshot_99/w/xi_gg/d_rp"], np.arange(2.0))
 
 
+@pytest.mark.parametrize("parts,want", [
+    (("Snapshot_99//w/xi_gg/",), "Snapshot_99/w/xi_gg"),
+    (("Snapshot_99", "w/xi_gg"), "Snapshot_99/w/xi_gg"),
+    (("", "w", "x"), "w/x"),
+    (("/a/", "/b/"), "a/b"),
+    (("a", ""), "a"),
+    (("", ""), ""),
+    (("a/b", "c_0_rp"), "a/b/c_0_rp"),
+    ((99, "w"), "99/w")])
+def test_paths_normalise_as_hdf5_resolves_them(parts, want):
+    """Empty components drop out, as HDF5 resolves 'a//b/' to 'a/b'."""
+    from measure_ia_gb300.output import norm_path
+    assert norm_path(*parts) == want
+
+
 def test_store_refuses_an_unreadable_file(tmp_path):
     path = str(tmp_path / "notes.hdf5")
     with open(path, "wb") as f:
