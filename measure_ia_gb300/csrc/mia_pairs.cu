@@ -494,7 +494,7 @@ __device__ __forceinline__ void mixed_pair_short_w(const Params& P, const Tables
   const float dot = fmaf(dx, cxy.x, dy * cxy.y);
   const float crs = fmaf(dx, cxy.y, -dy * cxy.x);
   const float crs2 = crs * crs;
-  const bool c_edge = crs2 < P.c_guard * qp;  // direction near the axis or its normal
+  const bool c_edge = crs2 < P.c_guard * qp;  // direction within the guard of the axis line
   if ((e >= kLutReject) | ((unsigned)jb >= (unsigned)P.n_p) | pi_edge | c_edge) {
     // Pi surely outside the bins (an edge at 0 or n_p goes on to the re-test)
     if ((unsigned)jb >= (unsigned)P.n_p && ((unsigned)jb + 1u > (unsigned)P.n_p + 1u || !pi_edge)) return;
